@@ -1,0 +1,340 @@
+#!/usr/bin/env python
+"""Benchmark of FFEA's per-timestep blob update on GB300.
+
+Workload (one "step" = one blob time step): a 40x40x40-cell Kuhn-split cube
+of side 200 nm (384,000 linear tets, 68,921 vertex nodes), seeded +-5% interior
+jitter, density 1500 kg/m^3, G = 5.7e8 Pa, K = 2.2e9 Pa, shear and bulk
+viscosity 1e-3 Pa s; NoMassCGSolver with CG tolerance 1e-10, dt = 1e-12 s,
+kT = 4.11e-21 J (thermal noise on, MRG32k3a stream 12345 x 6). Inputs are
+seeded synthetic meshes; there is no dataset.
+
+Metric: node-steps/s = vertex nodes x steps / time (whole job, all GPUs).
+Default arm: the mixed-precision GPU path (headline), with the plain FP64
+GPU path timed beside it. `--impl reference` times the reference algorithm on
+the host cores instead (the oracle's C restatement with OpenMP, since the
+reference sources are not on the benchmark machine).
+
+Timing: W untimed warm-up steps, then K steps each timed by CUDA events on
+the blob's stream, with 256 MiB of scratch written before every step outside
+the timed window (cold L2 for every step); max over ranks. Under torchrun each
+rank runs an independent replica on its own GPU (replicas only: a single blob
+does not shard), so the job's value is the sum of replica throughputs.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N_CELLS, SIDE = 40, 200.0
+PHYS = dict(solver="CG_nomass", dt=1e-12, kT=4.11e-21, epsilon=1e-10, max_iterations_cg=10000, calc_noise=1,
+            calc_stokes=0)
+FLUSH_BYTES = 256 << 20
+MESO_LENGTH = 1.7e-10
+
+
+def workload_config(n: int, precision: str) -> dict:
+    from ffea_ci_demo_gb300.mesh import counts
+
+    c = counts(n)
+    return {"workload": f"kuhn-cube-{n}: {c['T']} tets, {c['N']} nodes, NoMassCG eps=1e-10, dt=1e-12 s, "
+                        f"kT=4.11e-21 J", "cells_per_side": n, "tets": c["T"], "nodes": c["N"],
+            "matrix_nnz": c["nnz_linear"], "solver": "CG_nomass", "precision": precision,
+            "l2": "flushed before every timed step (256 MiB scratch write)"}
+
+
+def rank_info():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def pick_device(local: int) -> str:
+    vis = os.environ.get("CUDA_VISIBLE_DEVICES")
+    phys = vis.split(",")[local] if vis else str(local)
+    os.environ["CUDA_VISIBLE_DEVICES"] = phys
+    return phys
+
+
+class Clocks:
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: str):
+        self.gpu, self.lines, self.proc = gpu, [], None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                                          "-lms", "100", "-i", self.gpu], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+            threading.Thread(target=self._read, daemon=True).start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self) -> dict:
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 8:
+                continue
+            try:
+                sm.append(float(f[0]))
+                smax.append(float(f[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[4:8]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peak() -> tuple[float, str]:
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def profiled_traffic(precision: str):
+    """Per-launch DRAM bytes of cg_kernel from the committed ncu summary, if one exists."""
+    path = os.path.join(ROOT, "profiles", f"cg_kernel_{precision}_cube40.txt")
+    try:
+        for ln in open(path):
+            if ln.startswith("dram_bytes_per_launch_full_size"):
+                return float(ln.split("=")[1].split()[0])
+    except (OSError, ValueError, IndexError):
+        pass
+    return None
+
+
+def cg_bytes_per_iteration(n: int, p: int) -> float:
+    """Compulsory bytes of one CG iteration by the per-unit model: nnz (p + 4) + (R + 1) 4 + 8 R p."""
+    from ffea_ci_demo_gb300.mesh import counts
+
+    c = counts(n)
+    R = 3 * c["N"]
+    return c["nnz_linear"] * (p + 4) + (R + 1) * 4 + 8 * R * p
+
+
+def cg_format_bytes_per_iteration(blocks: int, nodes: int, p: int) -> float:
+    """Bytes the SELL 3x3-block matrix actually holds per SpMV (values + block columns + row data)
+    plus eight passes over padded 4-wide vectors."""
+    return blocks * (9 * p + 4) + nodes * 8 + 8 * nodes * 4 * p
+
+
+def run_gpu_arm(args, ws, rank, local) -> dict | None:
+    import numpy as np
+
+    from ffea_ci_demo_gb300 import build, lib
+    from ffea_ci_demo_gb300.mesh import apply_shear, counts, kuhn_cube
+
+    dist = None
+    if ws > 1:
+        import torch.distributed as dist  # noqa: F811
+
+        dist.init_process_group("gloo")
+    build.build()
+    n = args.cells
+    mesh = kuhn_cube(n, side=SIDE * n / N_CELLS, seed=12345)
+    N = counts(n)["N"]
+    gpu = os.environ.get("CUDA_VISIBLE_DEVICES", "0")
+
+    def barrier():
+        if dist:
+            dist.barrier()
+
+    def max_over_ranks(x: float) -> float:
+        if not dist:
+            return x
+        import torch
+
+        t = torch.tensor([x], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    out = {}
+    for prec in (["mixed", "fp64"] if args.precision == "both" else [args.precision]):
+        blob = lib.Blob(mesh, precision=prec, **PHYS)
+        blob.update(args.warmup)
+        it0 = blob.cg_iterations()[1]
+        l0 = lib.launch_count()
+        barrier()
+        steps = args.steps if prec == "mixed" or args.precision != "both" else max(3, args.steps // 4)
+        with Clocks(gpu) as clk:
+            t = blob.update_timed(steps, FLUSH_BYTES)
+        barrier()
+        launches = lib.launch_count() - l0
+        iters = blob.cg_iterations()[1] - it0
+        ms = max_over_ranks(t["ms"])
+        nl, ne, nb = blob.sizes()
+        out[prec] = {"ms": ms, "steps": steps, "value": ws * N * steps / (ms / 1e3), "phase_ms": t["phase_ms"],
+                     "cg_iters_per_step": iters / steps, "launches": launches, "clocks": clk.summary(),
+                     "blocks": nb}
+        if prec == args.headline:
+            # end to end through the C ABI: host positions in, one step, host positions out
+            pos_host = blob.pos()
+            k = max(3, steps // 2)
+            barrier()
+            t0 = time.perf_counter()
+            for _ in range(k):
+                blob.set_state(pos=pos_host)
+                blob.update(1)
+                pos_host = blob.pos()
+            t1 = time.perf_counter()
+            barrier()
+            e2e_s = max_over_ranks(t1 - t0)
+            out[prec]["e2e"] = {"value": ws * N * k / e2e_s, "unit": "node-steps/s", "h2d_bytes_per_step": 24 * N,
+                                "d2h_bytes_per_step": 24 * N, "steps": k}
+        blob.close()
+    # kT = 0 error of the mixed path against the FP64 path (same initial shear)
+    if args.precision == "both" and args.error_steps > 0:
+        p0 = apply_shear(mesh, 0.02, seed=3) * (mesh.scale / MESO_LENGTH)
+        res = {}
+        for prec in ("fp64", "mixed"):
+            b = lib.Blob(mesh, precision=prec, **dict(PHYS, kT=0.0, calc_noise=0))
+            b.set_state(pos=p0)
+            b.update(args.error_steps)
+            res[prec] = b.pos()
+            b.close()
+        d = np.abs(res["mixed"] - res["fp64"]).max() / np.abs(res["fp64"] - p0).max()
+        out["error"] = {"kT0_steps": args.error_steps, "max_abs_disp_err_rel_to_max_disp": float(d),
+                        "reference": "FP64 GPU path (bit-exact element math vs the reference; CG to rounding)"}
+    if dist:
+        dist.destroy_process_group()
+    return out if rank == 0 else None
+
+
+def cpu_sample(n: int, threads: int, budget_s: float, max_steps: int, warmup: int = 1):
+    """Time the oracle (reference algorithm, release optimisation, OpenMP) on the same workload."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle
+
+    from ffea_ci_demo_gb300.mesh import counts, kuhn_cube
+
+    pyoracle.build()
+    mesh = kuhn_cube(n, side=SIDE * n / N_CELLS, seed=12345)
+    o = pyoracle.OracleBlob(mesh, threads=threads, fast=True, **PHYS)
+    for _ in range(warmup):
+        o.step(1)
+    done, t0 = 0, time.perf_counter()
+    while done < max_steps:
+        if o.step(1) != 0:
+            break
+        done += 1
+        if time.perf_counter() - t0 > budget_s:
+            break
+    dt = time.perf_counter() - t0
+    N = counts(n)["N"]
+    return {"value": N * done / dt, "unit": "node-steps/s", "cores": threads, "kind": "port",
+            "sample": f"{done} full steps (after {warmup} warm-up) of the {n}^3-cell cube, {N} nodes, "
+                      f"{o.total_cg_iters() / max(1, done + warmup):.0f} CG iterations/step",
+            "seconds": dt, "steps": done}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=60)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--precision", choices=["both", "mixed", "fp64"], default="both")
+    ap.add_argument("--cells", type=int, default=N_CELLS)
+    ap.add_argument("--error-steps", type=int, default=100)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
+    args.headline = "fp64" if args.precision == "fp64" else "mixed"
+    ws, rank, local = rank_info()
+    threads = os.cpu_count() or 1
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        # each step is one full blob step of the same workload, run by the reference algorithm on all host
+        # cores; the number of timed steps is capped so that the run stays within a few minutes
+        r = cpu_sample(args.cells, threads, budget_s=150.0, max_steps=args.steps, warmup=min(args.warmup, 1))
+        line = {"metric": "node-steps/s", "value": r["value"], "unit": "node-steps/s", "n_gpus": args.gpus,
+                "steps": r["steps"], "warmup": min(args.warmup, 1), "ms_per_step": 1e3 * r["seconds"] / r["steps"],
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "data": "synthetic (seeded Kuhn cube)", "config": workload_config(args.cells, "fp64"),
+                "impl": "reference",
+                "cpu_baseline": {k: r[k] for k in ("value", "unit", "cores", "kind", "sample")},
+                "e2e": {"value": r["value"], "unit": "node-steps/s", "h2d_bytes_per_step": 0,
+                        "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
+        return
+
+    pick_device(local)
+    res = run_gpu_arm(args, ws, rank, local)
+    if rank != 0:
+        return
+    head = res[args.headline]
+    peak, peak_kind = measured_peak()
+    p = 4 if args.headline == "mixed" else 8
+    iters = head["cg_iters_per_step"]
+    cg_ms = head["phase_ms"]["cg"] / head["steps"]
+    model_bytes = iters * cg_bytes_per_iteration(args.cells, p)
+    fmt_bytes = iters * cg_format_bytes_per_iteration(head["blocks"], (args.cells + 1) ** 3, p)
+    achieved = model_bytes / (cg_ms / 1e3) / 1e9
+    roofline = {"bound": "hbm", "kernel": "cg_kernel", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "peak_source": peak_kind, "traffic": profiled_traffic(args.headline),
+                "bytes_per_launch_model": model_bytes, "bytes_per_launch_format": fmt_bytes,
+                "achieved_format": fmt_bytes / (cg_ms / 1e3) / 1e9, "ms_per_launch": cg_ms,
+                "cg_iters_per_launch": iters}
+    line = {"metric": "node-steps/s", "value": head["value"], "unit": "node-steps/s", "n_gpus": ws,
+            "steps": head["steps"], "warmup": args.warmup, "ms_per_step": head["ms"] / head["steps"],
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32+f64" if args.headline == "mixed" else "f64", "data": "synthetic (seeded Kuhn cube)",
+            "config": dict(workload_config(args.cells, args.headline), parallelism=f"replicas x{ws}"),
+            "clocks": head["clocks"], "e2e": head["e2e"], "gpu_launches": head["launches"],
+            "roofline": roofline, "phase_ms_per_step": {k: v / head["steps"] for k, v in head["phase_ms"].items()},
+            "cg_iters_per_step": iters}
+    if "fp64" in res and args.headline != "fp64":
+        f = res["fp64"]
+        line["fp64_path"] = {"value": f["value"], "ms_per_step": f["ms"] / f["steps"], "steps": f["steps"],
+                             "cg_iters_per_step": f["cg_iters_per_step"],
+                             "phase_ms_per_step": {k: v / f["steps"] for k, v in f["phase_ms"].items()}}
+        line["speedup_vs_fp64_path"] = head["value"] / f["value"]
+    if "error" in res:
+        line["error"] = res["error"]
+    if not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_sample(args.cells, os.cpu_count() or 1, budget_s=20.0, max_steps=3)
+        line["cpu_baseline"].pop("seconds")
+        line["cpu_baseline"].pop("steps")
+    print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

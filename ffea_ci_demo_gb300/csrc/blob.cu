@@ -1,0 +1,1132 @@
+// blob.cu -- host side of the GB300 blob-step engine and its C ABI.
+//
+// GpuBlob mirrors the reference's Blob (include/Blob.h:94-718) for the hot
+// path: it takes the structure a Blob holds after Blob::init, keeps only the
+// vertex ("linear") nodes on the device, builds the fixed 3x3-block sparsity
+// pattern of the viscosity matrix once, and runs
+//   element_kernel  -> update_internal_forces (src/Blob.cpp:400-491)
+//   assemble_kernel -> SparseMatrixFixedPattern::build + calc_inverse_diagonal
+//   gather_kernel   -> aggregate_forces_and_solve's gather (src/Blob.cpp:3147-3244)
+//   cg_kernel       -> NoMassCGSolver::solve / ConjugateGradientSolver::solve
+//   euler_kernel    -> euler_integrate (src/Blob.cpp:3249-3279)
+// per step on one CUDA stream. Host-side arithmetic (rest state, masses,
+// unit conversion) keeps the reference's evaluation order; this file is
+// compiled with -ffp-contract=off on the host side.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/ffea_gpu.h"
+#include "engine.h"
+
+namespace ffea {
+long long launch_count();
+}
+
+using namespace ffea;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int cuda_fail(cudaError_t e, const char *what) {
+    g_last_error = std::string(what) + ": " + cudaGetErrorString(e);
+    return e == cudaErrorMemoryAllocation ? FFEA_GPU_ENOMEM : FFEA_GPU_ECUDA;
+}
+
+#define CK(call)                                         \
+    do {                                                 \
+        cudaError_t e_ = (call);                         \
+        if (e_ != cudaSuccess) return cuda_fail(e_, #call); \
+    } while (0)
+
+// mesoDimensions, include/dimensions.h:30-41
+constexpr double MESO_LENGTH = 1.7e-10;
+constexpr double MESO_ENERGY = 4.141945559999999e-21;
+constexpr double MESO_MASS = 1.994307387553024e-26;
+constexpr double MESO_VOLUME = 4.913e-30;
+constexpr double MESO_TIME = 3.7302915560886126e-13;
+constexpr double MESO_PRESSURE = 8.4305832688784826e8;
+constexpr double FFEA_PI = 3.141592653589793238462643383279502884197169399375105820974944592307816406286208998628034825342117067982148;
+
+// ---------------------------------------------------------------------------
+// MRG32k3a transition-matrix powers (host)
+// ---------------------------------------------------------------------------
+struct Mat3 {
+    uint64_t m[3][3];
+};
+
+Mat3 mat_mul(const Mat3 &A, const Mat3 &B, uint64_t mod) {
+    Mat3 C{};
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) {
+            uint64_t s = 0;
+            for (int k = 0; k < 3; ++k) s = (s + (A.m[i][k] % mod) * (B.m[k][j] % mod) % mod) % mod;
+            C.m[i][j] = s;
+        }
+    return C;
+}
+
+Mat3 mat_pow(Mat3 A, uint64_t n, uint64_t mod) {
+    Mat3 R{};
+    for (int i = 0; i < 3; ++i) R.m[i][i] = 1;
+    while (n) {
+        if (n & 1) R = mat_mul(A, R, mod);
+        A = mat_mul(A, A, mod);
+        n >>= 1;
+    }
+    return R;
+}
+
+const Mat3 MRG_A1 = {{{0, 1, 0}, {0, 0, 1}, {MRG_M1 - 810728ull, 1403580ull, 0}}};
+const Mat3 MRG_A2 = {{{0, 1, 0}, {0, 0, 1}, {MRG_M2 - 1370589ull, 0, 527612ull}}};
+
+MrgJump to_jump(const Mat3 &a, const Mat3 &b) {
+    MrgJump J;
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) {
+            J.a[3 * i + j] = (uint32_t)a.m[i][j];
+            J.b[3 * i + j] = (uint32_t)b.m[i][j];
+        }
+    return J;
+}
+
+MrgJump jump_pow(uint64_t n) { return to_jump(mat_pow(MRG_A1, n, MRG_M1), mat_pow(MRG_A2, n, MRG_M2)); }
+
+// ---------------------------------------------------------------------------
+// device memory owned by a blob
+// ---------------------------------------------------------------------------
+struct Arena {
+    std::vector<void *> ptrs;
+    ~Arena() {
+        for (void *p : ptrs) cudaFree(p);
+    }
+    template <class T>
+    cudaError_t alloc(T **out, size_t n) {
+        void *p = nullptr;
+        cudaError_t e = cudaMalloc(&p, std::max<size_t>(n, 1) * sizeof(T));
+        if (e != cudaSuccess) return e;
+        ptrs.push_back(p);
+        *out = static_cast<T *>(p);
+        return cudaMemset(p, 0, std::max<size_t>(n, 1) * sizeof(T));
+    }
+    template <class T>
+    cudaError_t upload(T **out, const std::vector<T> &v) {
+        cudaError_t e = alloc(out, v.size());
+        if (e != cudaSuccess || v.empty()) return e;
+        return cudaMemcpy(*out, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice);
+    }
+};
+
+// ---------------------------------------------------------------------------
+// host description built once from the mesh
+// ---------------------------------------------------------------------------
+struct HostModel {
+    int n_all = 0, N = 0, T = 0;
+    std::vector<int> lin_of;       // n_all -> vertex index or -1
+    std::vector<int> node_of;      // N -> original node
+    std::vector<int> mid_nodes;    // original indices of midpoint nodes
+    std::vector<int> mid_a, mid_b; // their edge ends (vertex indices)
+    std::vector<int> tets10;       // original topology
+    std::vector<int> tet4;         // T*4 vertex indices
+    std::vector<double> pos;       // 3*N meso
+    std::vector<double> rho, A, B, G, E, vol0, last_det, jinv; // per element (jinv 9*T row-major)
+    std::vector<int> pinned;       // N flags
+    std::vector<int> pinned_all;   // n_all flags
+    std::vector<double> drag;      // N (stokes drag), empty if calc_stokes == 0
+    std::vector<double> drag_all;  // n_all
+    // incidence
+    std::vector<int> inc_ptr, inc;
+    // pattern (SELL-32 3x3 blocks)
+    int nslices = 0;
+    long long nslots = 0;
+    std::vector<int> slice_ptr, rowlen, bcol, diagk;
+    std::vector<std::vector<int>> nbr;  // sorted neighbours per vertex
+    std::vector<int> src_ptr;
+    std::vector<unsigned> src;
+    // mass matrix values (solver CG), SELL scalar over the same pattern; lumped inverse masses
+    std::vector<double> mass_sell, inv_mass;
+};
+
+// calc_shape_function_derivatives_and_volume's determinant and mat3_invert, in the reference's order
+void rest_state(HostModel &h) {
+    const int T = h.T;
+    h.vol0.assign(T, 0.0);
+    h.last_det.assign(T, 0.0);
+    h.jinv.assign(9 * (size_t)T, 0.0);
+    for (int e = 0; e < T; ++e) {
+        const int *t = &h.tet4[4 * (size_t)e];
+        double m[3][3];
+        for (int r = 0; r < 3; ++r)
+            for (int c = 0; c < 3; ++c) m[r][c] = h.pos[3 * (size_t)t[r + 1] + c] - h.pos[3 * (size_t)t[0] + c];
+        double *inv = &h.jinv[9 * (size_t)e];
+        inv[0] = m[2][2] * m[1][1] - m[2][1] * m[1][2];
+        inv[1] = m[2][1] * m[0][2] - m[2][2] * m[0][1];
+        inv[2] = m[1][2] * m[0][1] - m[1][1] * m[0][2];
+        inv[3] = m[2][0] * m[1][2] - m[2][2] * m[1][0];
+        inv[4] = m[2][2] * m[0][0] - m[2][0] * m[0][2];
+        inv[5] = m[1][0] * m[0][2] - m[1][2] * m[0][0];
+        inv[6] = m[2][1] * m[1][0] - m[2][0] * m[1][1];
+        inv[7] = m[2][0] * m[0][1] - m[2][1] * m[0][0];
+        inv[8] = m[1][1] * m[0][0] - m[1][0] * m[0][1];
+        double det = m[0][0] * inv[0] + m[1][0] * inv[1] + m[2][0] * inv[2];
+        // calc_shape_function_derivatives_and_volume stores this det as last_det and |det|/6 as vol
+        h.last_det[e] = det;
+        h.vol0[e] = (1.0 / 6.0) * fabs(det);
+        const double id = 1.0 / det;
+        for (int k = 0; k < 9; ++k) inv[k] *= id;
+    }
+}
+
+int build_model(const ffea_gpu_mesh *mesh, const ffea_gpu_params *p, HostModel &h) {
+    const int n = mesh->num_nodes, T = mesh->num_elements;
+    if (n <= 0 || T <= 0 || mesh->num_pinned < 0 || !mesh->pos || !mesh->tets || !mesh->rho || !mesh->A ||
+        !mesh->B || !mesh->G || !mesh->E) {
+        g_last_error = "empty mesh or missing arrays";
+        return FFEA_GPU_EINPUT;
+    }
+    if (T >= (1 << 28)) {
+        g_last_error = "too many elements (limit 2^28)";
+        return FFEA_GPU_EINPUT;
+    }
+    if (p->calc_stokes == 1 && p->calc_noise == 1) {
+        g_last_error = "Stokes noise (calc_stokes = 1 with calc_noise = 1) is not supported yet";
+        return FFEA_GPU_EINPUT;
+    }
+    if (p->calc_stokes == 1 && !mesh->stokes_radius) {
+        g_last_error = "calc_stokes needs stokes_radius";
+        return FFEA_GPU_EINPUT;
+    }
+    h.n_all = n;
+    h.T = T;
+    h.tets10.assign(mesh->tets, mesh->tets + 10 * (size_t)T);
+    std::vector<char> is_v(n, 0), is_m(n, 0);
+    for (int e = 0; e < T; ++e)
+        for (int s = 0; s < 10; ++s) {
+            const int x = h.tets10[10 * (size_t)e + s];
+            if (x < 0 || x >= n) {
+                g_last_error = "element references an out of bounds node index";
+                return FFEA_GPU_EINPUT;
+            }
+            (s < 4 ? is_v : is_m)[x] = 1;
+        }
+    h.lin_of.assign(n, -1);
+    for (int i = 0; i < n; ++i) {
+        if (is_v[i] && is_m[i]) {
+            g_last_error = "a node is both an element vertex and an edge midpoint (unsupported topology)";
+            return FFEA_GPU_EINPUT;
+        }
+        if (!is_v[i] && !is_m[i]) {
+            g_last_error = "a node belongs to no element";
+            return FFEA_GPU_EINPUT;
+        }
+        if (is_v[i]) {
+            h.lin_of[i] = (int)h.node_of.size();
+            h.node_of.push_back(i);
+        }
+    }
+    h.N = (int)h.node_of.size();
+    const int N = h.N;
+    // midpoints: ends from the first element holding them (linearise_element, src/tetra_element_linear.cpp:553-577)
+    static const int mid_pair[6][2] = {{0, 1}, {0, 2}, {0, 3}, {1, 2}, {1, 3}, {2, 3}};
+    std::vector<int> mid_seen(n, 0);
+    for (int e = 0; e < T; ++e)
+        for (int s = 4; s < 10; ++s) {
+            const int x = h.tets10[10 * (size_t)e + s];
+            if (mid_seen[x]) continue;
+            mid_seen[x] = 1;
+            h.mid_nodes.push_back(x);
+            h.mid_a.push_back(h.lin_of[h.tets10[10 * (size_t)e + mid_pair[s - 4][0]]]);
+            h.mid_b.push_back(h.lin_of[h.tets10[10 * (size_t)e + mid_pair[s - 4][1]]]);
+        }
+    h.tet4.resize(4 * (size_t)T);
+    for (int e = 0; e < T; ++e)
+        for (int s = 0; s < 4; ++s) h.tet4[4 * (size_t)e + s] = h.lin_of[h.tets10[10 * (size_t)e + s]];
+    h.pos.resize(3 * (size_t)N);
+    for (int k = 0; k < N; ++k)
+        for (int c = 0; c < 3; ++c) h.pos[3 * (size_t)k + c] = mesh->pos[3 * (size_t)h.node_of[k] + c];
+    h.rho.assign(mesh->rho, mesh->rho + T);
+    h.A.assign(mesh->A, mesh->A + T);
+    h.B.assign(mesh->B, mesh->B + T);
+    h.G.assign(mesh->G, mesh->G + T);
+    h.E.assign(mesh->E, mesh->E + T);
+    h.pinned_all.assign(n, 0);
+    h.pinned.assign(N, 0);
+    for (int k = 0; k < mesh->num_pinned; ++k) {
+        const int x = mesh->pinned[k];
+        if (x < 0 || x >= n) {
+            g_last_error = "pinned node index out of bounds";
+            return FFEA_GPU_EINPUT;
+        }
+        h.pinned_all[x] = 1;
+        if (h.lin_of[x] >= 0) h.pinned[h.lin_of[x]] = 1;
+    }
+    if (p->calc_stokes == 1) {
+        // Blob::init: stokes_drag = 6 pi eta r (src/Blob.cpp:262-268)
+        h.drag_all.resize(n);
+        for (int i = 0; i < n; ++i) h.drag_all[i] = 6.0 * FFEA_PI * p->stokes_visc * mesh->stokes_radius[i];
+        h.drag.resize(N);
+        for (int k = 0; k < N; ++k) h.drag[k] = h.drag_all[h.node_of[k]];
+    }
+    rest_state(h);
+    // incidence: element order, vertex slots (Blob::calculate_node_element_connectivity)
+    h.inc_ptr.assign(N + 1, 0);
+    for (int e = 0; e < T; ++e)
+        for (int s = 0; s < 4; ++s) h.inc_ptr[h.tet4[4 * (size_t)e + s] + 1]++;
+    for (int k = 0; k < N; ++k) h.inc_ptr[k + 1] += h.inc_ptr[k];
+    h.inc.resize(4 * (size_t)T);
+    {
+        std::vector<int> fill(N, 0);
+        for (int e = 0; e < T; ++e)
+            for (int s = 0; s < 4; ++s) {
+                const int a = h.tet4[4 * (size_t)e + s];
+                h.inc[h.inc_ptr[a] + fill[a]++] = 4 * e + s;
+            }
+    }
+    // neighbours: unpinned vertex pairs sharing an element; pinned rows keep only their diagonal
+    h.nbr.assign(N, {});
+    for (int e = 0; e < T; ++e) {
+        const int *t = &h.tet4[4 * (size_t)e];
+        for (int a = 0; a < 4; ++a) {
+            if (h.pinned[t[a]]) continue;
+            for (int b = 0; b < 4; ++b)
+                if (!h.pinned[t[b]]) h.nbr[t[a]].push_back(t[b]);
+        }
+    }
+    for (int k = 0; k < N; ++k) {
+        auto &v = h.nbr[k];
+        if (h.pinned[k]) v.assign(1, k);
+        std::sort(v.begin(), v.end());
+        v.erase(std::unique(v.begin(), v.end()), v.end());
+    }
+    // SELL-32 slices
+    h.nslices = (N + 31) / 32;
+    h.slice_ptr.assign(h.nslices + 1, 0);
+    h.rowlen.assign(N, 0);
+    h.diagk.assign(N, 0);
+    for (int s = 0; s < h.nslices; ++s) {
+        int w = 0;
+        for (int l = 0; l < 32 && 32 * s + l < N; ++l) w = std::max<int>(w, (int)h.nbr[32 * s + l].size());
+        h.slice_ptr[s + 1] = h.slice_ptr[s] + 32 * w;
+    }
+    h.nslots = h.slice_ptr[h.nslices];
+    if (h.nslots >= (1ll << 31)) {
+        g_last_error = "matrix too large for 32-bit slot indices";
+        return FFEA_GPU_EINPUT;
+    }
+    h.bcol.assign(h.nslots, 0);
+    for (int a = 0; a < N; ++a) {
+        const int s = a >> 5, lane = a & 31;
+        const auto &v = h.nbr[a];
+        h.rowlen[a] = (int)v.size();
+        const int w = (h.slice_ptr[s + 1] - h.slice_ptr[s]) / 32;
+        for (int k = 0; k < w; ++k) h.bcol[h.slice_ptr[s] + 32 * k + lane] = k < (int)v.size() ? v[k] : a;
+        h.diagk[a] = (int)(std::lower_bound(v.begin(), v.end(), a) - v.begin());
+    }
+    // assembly sources per slot, element order (the registration order of NoMassCGSolver::init)
+    auto slot_of = [&](int a, int b) -> long long {
+        const auto &v = h.nbr[a];
+        const int k = (int)(std::lower_bound(v.begin(), v.end(), b) - v.begin());
+        return (long long)h.slice_ptr[a >> 5] + 32 * k + (a & 31);
+    };
+    h.src_ptr.assign(h.nslots + 1, 0);
+    for (int e = 0; e < T; ++e) {
+        const int *t = &h.tet4[4 * (size_t)e];
+        for (int a = 0; a < 4; ++a) {
+            if (h.pinned[t[a]]) continue;
+            for (int b = 0; b < 4; ++b)
+                if (!h.pinned[t[b]]) h.src_ptr[slot_of(t[a], t[b]) + 1]++;
+        }
+    }
+    for (int a = 0; a < N; ++a)
+        if (h.pinned[a]) h.src_ptr[slot_of(a, a) + 1]++;
+    for (long long k = 0; k < h.nslots; ++k) h.src_ptr[k + 1] += h.src_ptr[k];
+    h.src.assign(h.src_ptr[h.nslots], 0u);
+    {
+        std::vector<int> fill(h.nslots, 0);
+        for (int a = 0; a < N; ++a)
+            if (h.pinned[a]) {
+                const long long k = slot_of(a, a);
+                h.src[h.src_ptr[k] + fill[k]++] = SRC_IDENTITY;
+            }
+        for (int e = 0; e < T; ++e) {
+            const int *t = &h.tet4[4 * (size_t)e];
+            for (int a = 0; a < 4; ++a) {
+                if (h.pinned[t[a]]) continue;
+                for (int b = 0; b < 4; ++b) {
+                    if (h.pinned[t[b]]) continue;
+                    const long long k = slot_of(t[a], t[b]);
+                    h.src[h.src_ptr[k] + fill[k]++] = ((unsigned)e << 4) | ((unsigned)a << 2) | (unsigned)b;
+                }
+            }
+        }
+    }
+    // ConjugateGradientSolver::init mass matrix (src/ConjugateGradientSolver.cpp:78-115), vertex rows
+    if (p->solver == FFEA_GPU_CG) {
+        h.mass_sell.assign(h.nslots, 0.0);
+        std::vector<char> set_one(h.nslots, 0);
+        for (int e = 0; e < T; ++e) {
+            const int *t = &h.tet4[4 * (size_t)e];
+            for (int i = 0; i < 4; ++i)
+                for (int j = 0; j < 4; ++j) {
+                    const int ni = t[i], nj = t[j];
+                    if (!h.pinned[ni] && !h.pinned[nj]) {
+                        const long long k = slot_of(ni, nj);
+                        if (i == j) h.mass_sell[k] += .1 * h.rho[e] * h.vol0[e];
+                        else h.mass_sell[k] += .05 * h.rho[e] * h.vol0[e];
+                    } else if (i == j) {
+                        h.mass_sell[slot_of(ni, nj)] = 1;
+                    }
+                }
+        }
+    }
+    // MassLumpedSolver::init (src/MassLumpedSolver.cpp:27-62)
+    if (p->solver == FFEA_GPU_MASSLUMPED) {
+        h.inv_mass.assign(N, 0.0);
+        for (int e = 0; e < T; ++e)
+            for (int s = 0; s < 4; ++s) h.inv_mass[h.tet4[4 * (size_t)e + s]] += .25 * h.rho[e] * h.vol0[e];
+        for (int a = 0; a < N; ++a) {
+            if (h.pinned[a]) h.inv_mass[a] = 1.0;
+            h.inv_mass[a] = 1.0 / h.inv_mass[a];
+        }
+    }
+    return FFEA_GPU_OK;
+}
+
+template <class R>
+std::vector<R> cast_vec(const std::vector<double> &v) {
+    return std::vector<R>(v.begin(), v.end());
+}
+
+// V[r][c] of the element viscosity matrix, same evaluation as the device's visc_entry
+double host_visc_entry(const double *dpsi, double A, double B, double vol, int r, int c) {
+    if (r > c) std::swap(r, c);
+    const int i = r >> 2, a = r & 3, j = c >> 2, b = c & 3;
+    if (i == j) {
+        const double t = dpsi[4 * i + a] * dpsi[4 * i + b] * (A + B);
+        const double d2 = (dpsi[a] * dpsi[b] + dpsi[4 + a] * dpsi[4 + b] + dpsi[8 + a] * dpsi[8 + b]);
+        return (t + d2 * A) * vol;
+    }
+    if (a == b) return ((B + A) * (dpsi[4 * i + a] * dpsi[4 * j + a])) * vol;
+    return (B * (dpsi[4 * i + a] * dpsi[4 * j + b]) + A * (dpsi[4 * i + b] * dpsi[4 * j + a])) * vol;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// the blob
+// ---------------------------------------------------------------------------
+struct ffea_gpu_blob {
+    virtual ~ffea_gpu_blob() = default;
+    HostModel h;
+    ffea_gpu_params p{};
+    uint32_t rng_host[6] = {12345, 12345, 12345, 12345, 12345, 12345};
+    virtual int init() = 0;
+    virtual int step(int nsteps, int *done) = 0;
+    virtual int step_timed(int nsteps, long long flush_bytes, int *done, double *step_ms, double *phase_ms) = 0;
+    virtual int get_state(double *pos, double *vel, double *force) = 0;
+    virtual int set_state(const double *pos, const double *vel) = 0;
+    virtual int set_rng(const uint32_t s[6]) = 0;
+    virtual int get_rng(uint32_t s[6]) = 0;
+    virtual int measure(double *se, double *ke) = 0;
+    virtual int cg_iters(int *last, long long *total) = 0;
+    virtual int get_elements(double *nf, double *vol, double *visc) = 0;
+    virtual int get_rhs(double *rhs) = 0;
+    virtual int get_matrix_values(std::vector<double> &val_sell) = 0;
+};
+
+namespace {
+
+template <class R>
+struct BlobImpl final : ffea_gpu_blob {
+    Arena mem;
+    cudaStream_t stream = nullptr;
+    int device = 0;
+    // device arrays
+    double *px, *py, *pz, *vx, *vy, *vz;
+    int4 *tet;
+    R *jinv, *G, *E, *A, *B, *vol0, *ef, *geom;
+    double *last_det;
+    int *inc_ptr, *inc, *pinned;
+    int *slice_ptr, *rowlen, *bcol, *diagk, *src_ptr;
+    unsigned *src;
+    double *drag = nullptr;
+    R *val, *dinv;
+    double *f;
+    R *x, *r, *pv, *q;
+    double *partials, *init_partials;
+    uint32_t *rng_state;
+    MrgJump *chunk_jump, *lane_jump, *step_jump;
+    DevStatus *st;
+    GridBarrier *gb;
+    int cg_grid = 0, gather_blocks = 0, partial_stride = 0;
+    cudaEvent_t ev[FFEA_GPU_NUM_PHASES + 1] = {};
+    bool record_phases = false;
+    double *staging = nullptr;  // pinned host buffer, 3*N doubles, for state copies
+
+    ~BlobImpl() override {
+        if (staging) cudaFreeHost(staging);
+        for (auto &e : ev)
+            if (e) cudaEventDestroy(e);
+        if (stream) cudaStreamDestroy(stream);
+    }
+
+    int mark(int k) {
+        if (record_phases) CK(cudaEventRecord(ev[k], stream));
+        return FFEA_GPU_OK;
+    }
+
+    int init() override {
+        CK(cudaGetDevice(&device));
+        int major = 0, minor = 0;
+        CK(cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, device));
+        CK(cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, device));
+        if (major != 10 || minor != 3) {
+            g_last_error = "this library is built for sm_103a (GB300) only";
+            return FFEA_GPU_ECUDA;
+        }
+        CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+        for (auto &e : ev) CK(cudaEventCreate(&e));
+        CK(cudaHostAlloc((void **)&staging, 3 * (size_t)std::max(h.N, 1) * sizeof(double), cudaHostAllocDefault));
+        const int N = h.N, T = h.T;
+        std::vector<double> tmp(N);
+        auto up3 = [&](double **dst, int c) -> cudaError_t {
+            for (int k = 0; k < N; ++k) tmp[k] = h.pos[3 * (size_t)k + c];
+            return mem.upload(dst, tmp);
+        };
+        CK(up3(&px, 0));
+        CK(up3(&py, 1));
+        CK(up3(&pz, 2));
+        CK(mem.alloc(&vx, N));
+        CK(mem.alloc(&vy, N));
+        CK(mem.alloc(&vz, N));
+        std::vector<int4> t4(T);
+        for (int e = 0; e < T; ++e)
+            t4[e] = make_int4(h.tet4[4 * (size_t)e], h.tet4[4 * (size_t)e + 1], h.tet4[4 * (size_t)e + 2],
+                              h.tet4[4 * (size_t)e + 3]);
+        CK(mem.upload(&tet, t4));
+        std::vector<R> js(9 * (size_t)T);
+        for (int e = 0; e < T; ++e)
+            for (int k = 0; k < 9; ++k) js[(size_t)k * T + e] = (R)h.jinv[9 * (size_t)e + k];
+        CK(mem.upload(&jinv, js));
+        CK(mem.upload(&G, cast_vec<R>(h.G)));
+        CK(mem.upload(&E, cast_vec<R>(h.E)));
+        CK(mem.upload(&A, cast_vec<R>(h.A)));
+        CK(mem.upload(&B, cast_vec<R>(h.B)));
+        CK(mem.upload(&vol0, cast_vec<R>(h.vol0)));
+        CK(mem.upload(&last_det, h.last_det));
+        CK(mem.alloc(&ef, 12 * (size_t)T));
+        CK(mem.alloc(&geom, 16 * (size_t)T));
+        CK(mem.upload(&inc_ptr, h.inc_ptr));
+        CK(mem.upload(&inc, h.inc));
+        CK(mem.upload(&pinned, h.pinned));
+        CK(mem.upload(&slice_ptr, h.slice_ptr));
+        CK(mem.upload(&rowlen, h.rowlen));
+        CK(mem.upload(&bcol, h.bcol));
+        CK(mem.upload(&diagk, h.diagk));
+        CK(mem.upload(&src_ptr, h.src_ptr));
+        CK(mem.upload(&src, h.src));
+        if (!h.drag.empty()) CK(mem.upload(&drag, h.drag));
+        const bool block3 = p.solver == FFEA_GPU_NOMASS_CG;
+        if (p.solver == FFEA_GPU_CG) {
+            CK(mem.upload(&val, cast_vec<R>(h.mass_sell)));
+        } else {
+            CK(mem.alloc(&val, (block3 ? 9 : 1) * (size_t)h.nslots));
+        }
+        // Jacobi preconditioner (CG solver: 1/diag of the constant mass matrix) or lumped inverse mass
+        std::vector<R> dv(4 * (size_t)N, (R)0);
+        if (p.solver == FFEA_GPU_CG) {
+            for (int a = 0; a < N; ++a) {
+                const int s = a >> 5, lane = a & 31;
+                const double d = h.mass_sell[h.slice_ptr[s] + 32 * h.diagk[a] + lane];
+                for (int c = 0; c < 3; ++c) dv[4 * (size_t)a + c] = (R)(1.0 / d);
+            }
+        } else if (p.solver == FFEA_GPU_MASSLUMPED) {
+            for (int a = 0; a < N; ++a)
+                for (int c = 0; c < 3; ++c) dv[4 * (size_t)a + c] = (R)h.inv_mass[a];
+        }
+        CK(mem.upload(&dinv, dv));
+        CK(mem.alloc(&f, 4 * (size_t)N));
+        CK(mem.alloc(&x, 4 * (size_t)N));
+        CK(mem.alloc(&r, 4 * (size_t)N));
+        CK(mem.alloc(&pv, 4 * (size_t)N));
+        CK(mem.alloc(&q, 4 * (size_t)N));
+        const int gthreads = Launch<R>::gather_threads();
+        gather_blocks = (N + gthreads - 1) / gthreads;
+        CK(mem.alloc(&init_partials, 2 * (size_t)gather_blocks));
+        const int maxg = Launch<R>::cg_max_grid(device);
+        if (maxg <= 0) {
+            g_last_error = "cg kernel cannot be made resident";
+            return FFEA_GPU_ECUDA;
+        }
+        cg_grid = std::max(1, std::min(maxg, (N + Launch<R>::cg_threads() - 1) / Launch<R>::cg_threads()));
+        partial_stride = cg_grid;
+        CK(mem.alloc(&partials, 3 * (size_t)partial_stride));
+        CK(mem.alloc(&st, 1));
+        CK(mem.alloc(&gb, 1));
+        // RNG jump tables: draws of element e start 7e after the step's state; a step consumes 7T
+        const int nchunks = (T + 31) / 32;
+        std::vector<MrgJump> cj(nchunks), lj(32);
+        const Mat3 A224a = mat_pow(MRG_A1, 224, MRG_M1), A224b = mat_pow(MRG_A2, 224, MRG_M2);
+        Mat3 ca{}, cb{};
+        for (int i = 0; i < 3; ++i) ca.m[i][i] = cb.m[i][i] = 1;
+        for (int c = 0; c < nchunks; ++c) {
+            cj[c] = to_jump(ca, cb);
+            ca = mat_mul(A224a, ca, MRG_M1);
+            cb = mat_mul(A224b, cb, MRG_M2);
+        }
+        for (int l = 0; l < 32; ++l) lj[l] = jump_pow(7ull * l);
+        CK(mem.upload(&chunk_jump, cj));
+        CK(mem.upload(&lane_jump, lj));
+        std::vector<MrgJump> sj(1, jump_pow(7ull * (uint64_t)T));
+        CK(mem.upload(&step_jump, sj));
+        std::vector<uint32_t> rs(rng_host, rng_host + 6);
+        CK(mem.upload(&rng_state, rs));
+        CK(cudaDeviceSynchronize());
+        return FFEA_GPU_OK;
+    }
+
+    int launch_step() {
+        const bool nomass = p.solver == FFEA_GPU_NOMASS_CG;
+        ElemArgs<R> ea{};
+        ea.T = h.T;
+        ea.nomass = nomass;
+        ea.calc_noise = p.calc_noise;
+        ea.kT = (R)p.kT;
+        ea.dt = (R)p.dt;
+        ea.tet = tet;
+        ea.px = px; ea.py = py; ea.pz = pz;
+        ea.vx = vx; ea.vy = vy; ea.vz = vz;
+        ea.jinv = jinv;
+        ea.G = G; ea.E = E; ea.A = A; ea.B = B; ea.vol0 = vol0;
+        ea.last_det = last_det;
+        ea.ef = ef;
+        ea.geom = geom;
+        ea.rng_state = rng_state;
+        ea.chunk_jump = chunk_jump;
+        ea.lane_jump = lane_jump;
+        ea.st = st;
+        int rc = mark(0);
+        if (rc) return rc;
+        CK(Launch<R>::element(ea, stream));
+        if ((rc = mark(1))) return rc;
+        if (nomass) {
+            AsmArgs<R> aa{};
+            aa.N = h.N;
+            aa.slice_ptr = slice_ptr; aa.rowlen = rowlen; aa.bcol = bcol; aa.diagk = diagk;
+            aa.src_ptr = src_ptr; aa.src = src;
+            aa.geom = geom; aa.A = A; aa.B = B;
+            aa.drag = (p.calc_stokes == 1) ? drag : nullptr;
+            aa.val = val; aa.dinv = dinv; aa.st = st;
+            CK(Launch<R>::assemble(aa, stream));
+        }
+        if ((rc = mark(2))) return rc;
+        GatherArgs<R> ga{};
+        ga.N = h.N;
+        ga.mode = p.solver == FFEA_GPU_MASSLUMPED ? 1 : 0;
+        ga.inc_ptr = inc_ptr; ga.inc = inc; ga.ef = ef; ga.pinned = pinned;
+        ga.drag = (!nomass && p.calc_stokes == 1) ? drag : nullptr;
+        ga.vx = vx; ga.vy = vy; ga.vz = vz;
+        ga.dinv = dinv; ga.f = f; ga.x = x; ga.r = r; ga.p = pv;
+        ga.partials = init_partials; ga.stride = gather_blocks; ga.st = st;
+        CK(Launch<R>::gather(ga, gather_blocks, stream));
+        if ((rc = mark(3))) return rc;
+        if (p.solver != FFEA_GPU_MASSLUMPED) {
+            CgArgs<R> ca{};
+            ca.N = h.N;
+            ca.block3 = nomass;
+            ca.check_last = nomass;
+            ca.slice_ptr = slice_ptr; ca.rowlen = rowlen; ca.bcol = bcol;
+            ca.val = val; ca.dinv = dinv;
+            ca.x = x; ca.r = r; ca.p = pv; ca.q = q;
+            ca.init_partials = init_partials; ca.n_init = gather_blocks; ca.init_stride = gather_blocks;
+            ca.partials = partials; ca.stride = partial_stride;
+            ca.gb = gb; ca.st = st;
+            ca.imax = p.max_iterations_cg;
+            ca.eps2 = p.epsilon2;
+            ca.limit_ns = 2000000000ull;
+            CK(Launch<R>::cg(ca, cg_grid, stream));
+        }
+        if ((rc = mark(4))) return rc;
+        EulerArgs<R> eu{};
+        eu.N = h.N; eu.nomass = nomass; eu.dt = p.dt; eu.x = x;
+        eu.px = px; eu.py = py; eu.pz = pz; eu.vx = vx; eu.vy = vy; eu.vz = vz;
+        eu.st = st;
+        CK(Launch<R>::euler(eu, stream));
+        CK(launch_finish_step(rng_state, step_jump, st, stream));
+        return mark(5);
+    }
+
+    int read_status(DevStatus &s) {
+        CK(cudaMemcpyAsync(&s, st, sizeof(DevStatus), cudaMemcpyDeviceToHost, stream));
+        CK(cudaStreamSynchronize(stream));
+        return FFEA_GPU_OK;
+    }
+
+    int status_code(const DevStatus &s) {
+        if (s.timeout) return FFEA_GPU_ETIMEOUT;
+        if (s.inversions) return FFEA_GPU_EINVERTED;
+        if (s.cg_fail) return FFEA_GPU_ECGMAXIT;
+        if (s.nonfinite) return FFEA_GPU_ENAN;
+        return FFEA_GPU_OK;
+    }
+
+    int step(int nsteps, int *done) override {
+        if (nsteps < 0) return FFEA_GPU_EINPUT;
+        DevStatus s{};
+        int rc = read_status(s);
+        if (rc) return rc;
+        // clear the per-call flags, keep the CG totals
+        s.inversions = s.cg_fail = s.nonfinite = s.timeout = s.abort = 0;
+        s.steps_done = 0;
+        CK(cudaMemcpyAsync(st, &s, sizeof(DevStatus), cudaMemcpyHostToDevice, stream));
+        for (int i = 0; i < nsteps; ++i) {
+            rc = launch_step();
+            if (rc) return rc;
+            // the non-finite flag is raised by euler_kernel after the positions moved; stop the step chain
+        }
+        rc = read_status(s);
+        if (rc) return rc;
+        if (done) *done = s.steps_done;
+        return status_code(s);
+    }
+
+    int step_timed(int nsteps, long long flush_bytes, int *done, double *step_ms, double *phase_ms) override {
+        if (nsteps < 0 || flush_bytes < 0) return FFEA_GPU_EINPUT;
+        DevStatus s{};
+        int rc = read_status(s);
+        if (rc) return rc;
+        s.inversions = s.cg_fail = s.nonfinite = s.timeout = s.abort = 0;
+        s.steps_done = 0;
+        CK(cudaMemcpyAsync(st, &s, sizeof(DevStatus), cudaMemcpyHostToDevice, stream));
+        void *scratch = nullptr;
+        if (flush_bytes > 0) CK(cudaMalloc(&scratch, (size_t)flush_bytes));
+        double tot = 0.0, ph[FFEA_GPU_NUM_PHASES] = {0};
+        record_phases = true;
+        for (int i = 0; i < nsteps && rc == FFEA_GPU_OK; ++i) {
+            if (scratch) {
+                cudaError_t e = cudaMemsetAsync(scratch, i & 0xff, (size_t)flush_bytes, stream);
+                if (e != cudaSuccess) { rc = cuda_fail(e, "flush"); break; }
+            }
+            rc = launch_step();
+            if (rc) break;
+            cudaError_t e = cudaEventSynchronize(ev[FFEA_GPU_NUM_PHASES]);
+            if (e != cudaSuccess) { rc = cuda_fail(e, "cudaEventSynchronize"); break; }
+            float ms = 0.f;
+            for (int k = 0; k < FFEA_GPU_NUM_PHASES; ++k) {
+                cudaEventElapsedTime(&ms, ev[k], ev[k + 1]);
+                ph[k] += ms;
+            }
+            cudaEventElapsedTime(&ms, ev[0], ev[FFEA_GPU_NUM_PHASES]);
+            tot += ms;
+        }
+        record_phases = false;
+        if (scratch) cudaFree(scratch);
+        if (rc) return rc;
+        rc = read_status(s);
+        if (rc) return rc;
+        if (done) *done = s.steps_done;
+        if (step_ms) *step_ms = tot;
+        if (phase_ms)
+            for (int k = 0; k < FFEA_GPU_NUM_PHASES; ++k) phase_ms[k] = ph[k];
+        return status_code(s);
+    }
+
+    int get_state(double *pos, double *vel, double *force) override {
+        const int N = h.N, n = h.n_all;
+        auto fill = [&](double *out, const double *dx, const double *dy, const double *dz, bool mids) -> int {
+            CK(cudaMemcpyAsync(staging, dx, N * sizeof(double), cudaMemcpyDeviceToHost, stream));
+            CK(cudaMemcpyAsync(staging + N, dy, N * sizeof(double), cudaMemcpyDeviceToHost, stream));
+            CK(cudaMemcpyAsync(staging + 2 * (size_t)N, dz, N * sizeof(double), cudaMemcpyDeviceToHost, stream));
+            CK(cudaStreamSynchronize(stream));
+            for (int i = 0; i < 3 * n; ++i) out[i] = 0.0;
+            for (int k = 0; k < N; ++k) {
+                const int i = h.node_of[k];
+                out[3 * (size_t)i] = staging[k];
+                out[3 * (size_t)i + 1] = staging[N + k];
+                out[3 * (size_t)i + 2] = staging[2 * (size_t)N + k];
+            }
+            if (mids)
+                for (size_t m = 0; m < h.mid_nodes.size(); ++m) {
+                    const int i = h.mid_nodes[m], a = h.node_of[h.mid_a[m]], b = h.node_of[h.mid_b[m]];
+                    for (int c = 0; c < 3; ++c)
+                        out[3 * (size_t)i + c] = .5 * (out[3 * (size_t)a + c] + out[3 * (size_t)b + c]);
+                }
+            return FFEA_GPU_OK;
+        };
+        int rc;
+        if (pos && (rc = fill(pos, px, py, pz, true))) return rc;
+        if (vel && (rc = fill(vel, vx, vy, vz, false))) return rc;
+        if (force) {
+            std::vector<R> hxv(4 * (size_t)N);
+            CK(cudaMemcpyAsync(hxv.data(), x, hxv.size() * sizeof(R), cudaMemcpyDeviceToHost, stream));
+            CK(cudaStreamSynchronize(stream));
+            for (int i = 0; i < 3 * n; ++i) force[i] = 0.0;
+            for (int k = 0; k < N; ++k)
+                for (int c = 0; c < 3; ++c) force[3 * (size_t)h.node_of[k] + c] = (double)hxv[4 * (size_t)k + c];
+        }
+        return FFEA_GPU_OK;
+    }
+
+    int set_state(const double *pos, const double *vel) override {
+        const int N = h.N;
+        auto put = [&](const double *in, double *dx, double *dy, double *dz) -> int {
+            for (int k = 0; k < N; ++k) {
+                const size_t i = 3 * (size_t)h.node_of[k];
+                staging[k] = in[i];
+                staging[N + k] = in[i + 1];
+                staging[2 * (size_t)N + k] = in[i + 2];
+            }
+            CK(cudaMemcpyAsync(dx, staging, N * sizeof(double), cudaMemcpyHostToDevice, stream));
+            CK(cudaMemcpyAsync(dy, staging + N, N * sizeof(double), cudaMemcpyHostToDevice, stream));
+            CK(cudaMemcpyAsync(dz, staging + 2 * (size_t)N, N * sizeof(double), cudaMemcpyHostToDevice, stream));
+            CK(cudaStreamSynchronize(stream));
+            return FFEA_GPU_OK;
+        };
+        int rc;
+        if (pos && (rc = put(pos, px, py, pz))) return rc;
+        if (vel && (rc = put(vel, vx, vy, vz))) return rc;
+        return FFEA_GPU_OK;
+    }
+
+    int set_rng(const uint32_t s[6]) override {
+        CK(cudaMemcpyAsync(rng_state, s, 6 * sizeof(uint32_t), cudaMemcpyHostToDevice, stream));
+        CK(cudaStreamSynchronize(stream));
+        return FFEA_GPU_OK;
+    }
+
+    int get_rng(uint32_t s[6]) override {
+        CK(cudaMemcpyAsync(s, rng_state, 6 * sizeof(uint32_t), cudaMemcpyDeviceToHost, stream));
+        CK(cudaStreamSynchronize(stream));
+        return FFEA_GPU_OK;
+    }
+
+    int cg_iters(int *last, long long *total) override {
+        DevStatus s{};
+        int rc = read_status(s);
+        if (rc) return rc;
+        if (last) *last = s.last_iters;
+        if (total) *total = s.total_iters;
+        return FFEA_GPU_OK;
+    }
+
+    int get_elements(double *nf, double *vol, double *visc) override {
+        const int T = h.T;
+        std::vector<R> he(12 * (size_t)T), hg(16 * (size_t)T);
+        CK(cudaMemcpyAsync(he.data(), ef, he.size() * sizeof(R), cudaMemcpyDeviceToHost, stream));
+        CK(cudaMemcpyAsync(hg.data(), geom, hg.size() * sizeof(R), cudaMemcpyDeviceToHost, stream));
+        CK(cudaStreamSynchronize(stream));
+        if (nf)
+            for (size_t i = 0; i < he.size(); ++i) nf[i] = (double)he[i];
+        if (vol)
+            for (int e = 0; e < T; ++e) vol[e] = (double)hg[16 * (size_t)e + 12];
+        if (visc)
+            for (int e = 0; e < T; ++e) {
+                double d[12];
+                for (int k = 0; k < 12; ++k) d[k] = (double)hg[16 * (size_t)e + k];
+                const double v = (double)hg[16 * (size_t)e + 12];
+                for (int rr = 0; rr < 12; ++rr)
+                    for (int cc = 0; cc < 12; ++cc)
+                        visc[144 * (size_t)e + 12 * rr + cc] =
+                            host_visc_entry(d, (double)(R)h.A[e], (double)(R)h.B[e], v, rr, cc);
+            }
+        return FFEA_GPU_OK;
+    }
+
+    int get_rhs(double *rhs) override {
+        const int N = h.N;
+        std::vector<double> hf(4 * (size_t)N);
+        CK(cudaMemcpyAsync(hf.data(), f, hf.size() * sizeof(double), cudaMemcpyDeviceToHost, stream));
+        CK(cudaStreamSynchronize(stream));
+        for (int i = 0; i < 3 * h.n_all; ++i) rhs[i] = 0.0;
+        for (int k = 0; k < N; ++k)
+            for (int c = 0; c < 3; ++c) rhs[3 * (size_t)h.node_of[k] + c] = hf[4 * (size_t)k + c];
+        return FFEA_GPU_OK;
+    }
+
+    int get_matrix_values(std::vector<double> &out) override {
+        const bool block3 = p.solver == FFEA_GPU_NOMASS_CG;
+        std::vector<R> hv((block3 ? 9 : 1) * (size_t)h.nslots);
+        CK(cudaMemcpyAsync(hv.data(), val, hv.size() * sizeof(R), cudaMemcpyDeviceToHost, stream));
+        CK(cudaStreamSynchronize(stream));
+        out.assign(hv.begin(), hv.end());
+        return FFEA_GPU_OK;
+    }
+
+    // Blob::make_measurements energies (src/Blob.cpp:1066-1125), evaluated on the host from device state
+    int measure(double *se, double *ke) override {
+        const int N = h.N, T = h.T;
+        std::vector<double> P(3 * (size_t)h.n_all), V(3 * (size_t)h.n_all);
+        int rc = get_state(P.data(), V.data(), nullptr);
+        if (rc) return rc;
+        double kenergy = 0.0, senergy = 0.0;
+        for (int e = 0; e < T; ++e) {
+            const int *t = &h.tets10[10 * (size_t)e];
+            double J[3][3];
+            for (int rr = 0; rr < 3; ++rr)
+                for (int c = 0; c < 3; ++c) J[rr][c] = P[3 * (size_t)t[rr + 1] + c] - P[3 * (size_t)t[0] + c];
+            double d1 = J[2][2] * J[1][1] - J[2][1] * J[1][2];
+            double d2 = J[2][1] * J[0][2] - J[2][2] * J[0][1];
+            double d3 = J[1][2] * J[0][1] - J[1][1] * J[0][2];
+            const double det = J[0][0] * d1 + J[1][0] * d2 + J[2][0] * d3;
+            const double vol = (1.0 / 6.0) * fabs(det);
+            const double *Ji = &h.jinv[9 * (size_t)e];
+            double F[3][3];
+            for (int i = 0; i < 3; ++i)
+                for (int j = 0; j < 3; ++j) {
+                    F[i][j] = 0;
+                    for (int k = 0; k < 3; ++k) F[i][j] += J[k][i] * Ji[3 * j + k];
+                }
+            if (p.solver != FFEA_GPU_NOMASS_CG) {
+                double v[12], tmp[12] = {0};
+                for (int a = 0; a < 4; ++a)
+                    for (int i = 0; i < 3; ++i) v[4 * i + a] = V[3 * (size_t)t[a] + i];
+                for (int k = 0; k < 12; k += 4)
+                    for (int i = 0; i < 4; ++i)
+                        for (int j = 0; j < 4; ++j) tmp[i + k] += (i == j ? .1 : .05) * v[j + k];
+                for (int i = 0; i < 12; ++i) tmp[i] = tmp[i] * (h.vol0[e] * h.rho[e]);
+                double s = 0;
+                for (int i = 0; i < 12; ++i) s += v[i] * tmp[i];
+                kenergy += s;
+            }
+            const double C = h.E[e] - (2.0 / 3.0) * h.G[e];
+            const double t1 = vol / h.vol0[e];
+            const double ff = F[0][0] * F[0][0] + F[1][1] * F[1][1] + F[2][2] * F[2][2] + F[0][1] * F[0][1] +
+                              F[1][0] * F[1][0] + F[0][2] * F[0][2] + F[2][0] * F[2][0] + F[1][2] * F[1][2] +
+                              F[2][1] * F[2][1];
+            senergy += h.vol0[e] * (h.G[e] * (ff - 3) + 0.5 * C * (t1 * t1 - 1) - (C + 2 * h.G[e]) * log(t1));
+        }
+        (void)N;
+        if (ke) *ke = kenergy * 0.5;
+        if (se) *se = senergy * 0.5;
+        return FFEA_GPU_OK;
+    }
+};
+
+bool valid_seed(const uint32_t s[6]) {
+    for (int i = 0; i < 3; ++i)
+        if (s[i] >= MRG_M1) return false;
+    for (int i = 3; i < 6; ++i)
+        if (s[i] >= MRG_M2) return false;
+    if (s[0] == 0 && s[1] == 0 && s[2] == 0) return false;
+    if (s[3] == 0 && s[4] == 0 && s[5] == 0) return false;
+    return true;
+}
+
+int check_params(const ffea_gpu_params *p) {
+    if (!p) return FFEA_GPU_EINPUT;
+    if (p->solver < 0 || p->solver > 2 || (p->precision != FFEA_GPU_FP64 && p->precision != FFEA_GPU_MIXED) ||
+        p->max_iterations_cg < 0 || !(p->dt > 0)) {
+        g_last_error = "invalid parameters";
+        return FFEA_GPU_EINPUT;
+    }
+    return FFEA_GPU_OK;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------
+extern "C" {
+
+int ffea_gpu_params_default(ffea_gpu_params *p) {
+    if (!p) return FFEA_GPU_EINPUT;
+    std::memset(p, 0, sizeof(*p));
+    p->dt = 1e-14 / MESO_TIME;
+    p->kT = 4.11e-21 / MESO_ENERGY;
+    p->epsilon2 = 0.01;
+    p->stokes_visc = 1e-3 / (MESO_PRESSURE * MESO_TIME);
+    p->max_iterations_cg = 1000;
+    p->calc_noise = 1;
+    p->calc_stokes = 1;
+    p->solver = FFEA_GPU_NOMASS_CG;
+    p->precision = FFEA_GPU_FP64;
+    return FFEA_GPU_OK;
+}
+
+int ffea_gpu_material_from_si(int n, const double *mat6, double *rho, double *A, double *B, double *G, double *E) {
+    if (n < 0 || (n > 0 && !mat6)) return FFEA_GPU_EINPUT;
+    for (int e = 0; e < n; ++e) {
+        const double *m = mat6 + 6 * (size_t)e;
+        if (rho) rho[e] = m[0] * MESO_VOLUME / MESO_MASS;
+        if (A) A[e] = m[1] / (MESO_PRESSURE * MESO_TIME);
+        if (B) B[e] = m[2] / (MESO_PRESSURE * MESO_TIME) - (2.0 / 3.0) * m[1];
+        if (G) G[e] = m[3] / MESO_PRESSURE;
+        if (E) E[e] = m[4] / MESO_PRESSURE;
+    }
+    return FFEA_GPU_OK;
+}
+
+int ffea_gpu_blob_create(const ffea_gpu_mesh *mesh, const ffea_gpu_params *params, ffea_gpu_blob **out) {
+    if (!out || !mesh) return FFEA_GPU_EINPUT;
+    *out = nullptr;
+    int rc = check_params(params);
+    if (rc) return rc;
+    ffea_gpu_blob *b = nullptr;
+    try {
+        if (params->precision == FFEA_GPU_MIXED) b = new BlobImpl<float>();
+        else b = new BlobImpl<double>();
+    } catch (std::bad_alloc &) {
+        return FFEA_GPU_ENOMEM;
+    }
+    b->p = *params;
+    try {
+        rc = build_model(mesh, params, b->h);
+    } catch (std::bad_alloc &) {
+        rc = FFEA_GPU_ENOMEM;
+    }
+    if (!rc) rc = b->init();
+    if (rc) {
+        delete b;
+        return rc;
+    }
+    *out = b;
+    return FFEA_GPU_OK;
+}
+
+void ffea_gpu_blob_destroy(ffea_gpu_blob *blob) { delete blob; }
+
+int ffea_gpu_blob_set_rng_state(ffea_gpu_blob *b, const uint32_t s[6]) {
+    if (!b || !s || !valid_seed(s)) return FFEA_GPU_EINPUT;
+    return b->set_rng(s);
+}
+
+int ffea_gpu_blob_get_rng_state(ffea_gpu_blob *b, uint32_t s[6]) {
+    if (!b || !s) return FFEA_GPU_EINPUT;
+    return b->get_rng(s);
+}
+
+int ffea_gpu_blob_step(ffea_gpu_blob *b, int nsteps, int *done) {
+    if (!b) return FFEA_GPU_EINPUT;
+    return b->step(nsteps, done);
+}
+
+int ffea_gpu_blob_step_timed(ffea_gpu_blob *b, int nsteps, long long flush_bytes, int *done, double *step_ms,
+                             double *phase_ms) {
+    if (!b) return FFEA_GPU_EINPUT;
+    return b->step_timed(nsteps, flush_bytes, done, step_ms, phase_ms);
+}
+
+int ffea_gpu_blob_get_state(ffea_gpu_blob *b, double *pos, double *vel, double *force) {
+    if (!b) return FFEA_GPU_EINPUT;
+    return b->get_state(pos, vel, force);
+}
+
+int ffea_gpu_blob_set_state(ffea_gpu_blob *b, const double *pos, const double *vel) {
+    if (!b) return FFEA_GPU_EINPUT;
+    return b->set_state(pos, vel);
+}
+
+int ffea_gpu_blob_measure(ffea_gpu_blob *b, double *se, double *ke) {
+    if (!b) return FFEA_GPU_EINPUT;
+    return b->measure(se, ke);
+}
+
+int ffea_gpu_blob_cg_iterations(ffea_gpu_blob *b, int *last, long long *total) {
+    if (!b) return FFEA_GPU_EINPUT;
+    return b->cg_iters(last, total);
+}
+
+int ffea_gpu_blob_sizes(ffea_gpu_blob *b, int *nl, int *ne, long long *nb) {
+    if (!b) return FFEA_GPU_EINPUT;
+    if (nl) *nl = b->h.N;
+    if (ne) *ne = b->h.T;
+    if (nb) {
+        long long s = 0;
+        for (int a = 0; a < b->h.N; ++a) s += b->h.rowlen[a];
+        *nb = s;
+    }
+    return FFEA_GPU_OK;
+}
+
+int ffea_gpu_blob_get_pattern(ffea_gpu_blob *b, int *key, int *col, double *val, int *nsrc, long long *nnz) {
+    if (!b) return FFEA_GPU_EINPUT;
+    const HostModel &h = b->h;
+    if (b->p.solver != FFEA_GPU_NOMASS_CG) return FFEA_GPU_EINPUT;
+    const int n = h.n_all;
+    // rows of the reference: vertex rows carry 3 entries per neighbour block, others one diagonal entry
+    std::vector<int> len(n, 1);
+    for (int k = 0; k < h.N; ++k)
+        if (!h.pinned[k]) len[h.node_of[k]] = 3 * h.rowlen[k];
+    long long total = 0;
+    for (int i = 0; i < n; ++i) total += 3ll * len[i];
+    if (nnz) *nnz = total;
+    if (!col && !key && !val && !nsrc) return FFEA_GPU_OK;
+    std::vector<double> vals;
+    if (val) {
+        int rc = b->get_matrix_values(vals);
+        if (rc) return rc;
+    }
+    long long pos = 0;
+    for (int i = 0; i < n; ++i)
+        for (int c = 0; c < 3; ++c) {
+            if (key) key[3 * (size_t)i + c] = (int)pos;
+            const int k = h.lin_of[i];
+            if (k >= 0 && !h.pinned[k]) {
+                const int s = k >> 5, lane = k & 31;
+                for (int m = 0; m < h.rowlen[k]; ++m) {
+                    const long long slot = (long long)h.slice_ptr[s] + 32 * m + lane;
+                    const int bcolv = h.bcol[slot];
+                    const int nsource = h.src_ptr[slot + 1] - h.src_ptr[slot];
+                    for (int j = 0; j < 3; ++j) {
+                        if (col) col[pos] = 3 * h.node_of[bcolv] + j;
+                        if (val) val[pos] = vals[9 * (size_t)h.slice_ptr[s] + 32 * (9 * m + 3 * c + j) + lane];
+                        if (nsrc) nsrc[pos] = nsource + ((m == h.diagk[k] && c == j && b->p.calc_stokes == 1) ? 1 : 0);
+                        ++pos;
+                    }
+                }
+            } else {
+                // pinned vertex or midpoint: the identity `one` (+ Stokes drag on unpinned midpoints)
+                const bool stokes = b->p.calc_stokes == 1 && !h.pinned_all[i];
+                if (col) col[pos] = 3 * i + c;
+                if (val) val[pos] = 1.0 + (stokes ? h.drag_all[i] : 0.0);
+                if (nsrc) nsrc[pos] = 1 + (stokes ? 1 : 0);
+                ++pos;
+            }
+        }
+    if (key) key[3 * (size_t)n] = (int)pos;
+    return FFEA_GPU_OK;
+}
+
+int ffea_gpu_blob_get_connectivity(ffea_gpu_blob *b, int *ptr, int *es, long long *count) {
+    if (!b) return FFEA_GPU_EINPUT;
+    const HostModel &h = b->h;
+    const int n = h.n_all, T = h.T;
+    std::vector<int> cnt(n + 1, 0);
+    for (int e = 0; e < T; ++e)
+        for (int s = 0; s < 10; ++s) cnt[h.tets10[10 * (size_t)e + s] + 1]++;
+    for (int i = 0; i < n; ++i) cnt[i + 1] += cnt[i];
+    if (count) *count = cnt[n];
+    if (ptr) std::memcpy(ptr, cnt.data(), sizeof(int) * (n + 1));
+    if (es) {
+        std::vector<int> fill(n, 0);
+        for (int e = 0; e < T; ++e)
+            for (int s = 0; s < 10; ++s) {
+                const int x = h.tets10[10 * (size_t)e + s];
+                es[cnt[x] + fill[x]++] = 10 * e + s;
+            }
+    }
+    return FFEA_GPU_OK;
+}
+
+int ffea_gpu_blob_get_elements(ffea_gpu_blob *b, double *nf, double *vol, double *visc) {
+    if (!b) return FFEA_GPU_EINPUT;
+    return b->get_elements(nf, vol, visc);
+}
+
+int ffea_gpu_blob_get_rhs(ffea_gpu_blob *b, double *rhs) {
+    if (!b || !rhs) return FFEA_GPU_EINPUT;
+    return b->get_rhs(rhs);
+}
+
+const char *ffea_gpu_last_error(void) { return g_last_error.c_str(); }
+
+long long ffea_gpu_launch_count(void) { return ffea::launch_count(); }
+
+}  // extern "C"

@@ -1,0 +1,203 @@
+// common.cuh -- device-side building blocks of the blob-step engine.
+//
+//  * DevStatus: the per-blob status word that kernels set instead of trapping
+//    (inversion count, CG non-convergence, non-finite output, barrier timeout).
+//  * grid_sync: a grid-wide barrier for cooperatively launched kernels whose
+//    wait is bounded by %globaltimer; on timeout it records FFEA_GPU_ETIMEOUT
+//    and every block leaves its loop.
+//  * deterministic block / grid reductions of doubles (fixed shuffle tree,
+//    then every block sums the per-block partials in the same order).
+//  * MRG32k3a in exact 32-bit modular integer arithmetic (the generator of
+//    L'Ecuyer 1999 used by the reference's RngStream, src/RngStream.cpp), with
+//    jump-ahead by precomputed transition-matrix powers.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+#include <cuda/atomic>
+
+namespace ffea {
+
+struct DevStatus {
+    int inversions;   // elements with det sign change this step
+    int cg_fail;      // CG hit max_iterations_cg
+    int nonfinite;    // non-finite solver output
+    int timeout;      // a bounded wait gave up
+    int abort;        // any of the above: later kernels of the step return at once
+    int last_iters;   // CG iterations of the last completed solve
+    long long total_iters;
+    int steps_done;   // completed steps since the counter was reset
+    int pad;
+};
+
+struct GridBarrier {
+    unsigned int count;
+    unsigned int gen;
+};
+
+__device__ __forceinline__ unsigned long long globaltimer_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Bounded grid barrier. All blocks of the grid must be co-resident
+// (cudaLaunchCooperativeKernel). Returns false if this block gave up waiting
+// or another block recorded a timeout; the caller then leaves its loop.
+__device__ __forceinline__ bool grid_sync(GridBarrier *gb, DevStatus *st, unsigned long long limit_ns) {
+    __shared__ int s_ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int ok = 1;
+        cuda::atomic_ref<unsigned int, cuda::thread_scope_device> gen(gb->gen);
+        cuda::atomic_ref<unsigned int, cuda::thread_scope_device> cnt(gb->count);
+        const unsigned int g = gen.load(cuda::memory_order_acquire);
+        __threadfence();
+        const unsigned int arrived = cnt.fetch_add(1u, cuda::memory_order_acq_rel);
+        if (arrived == gridDim.x - 1) {
+            cnt.store(0u, cuda::memory_order_relaxed);
+            gen.fetch_add(1u, cuda::memory_order_release);
+        } else {
+            const unsigned long long t0 = globaltimer_ns();
+            unsigned int polls = 0;
+            while (gen.load(cuda::memory_order_acquire) == g) {
+                if ((++polls & 255u) == 0u) {
+                    if (globaltimer_ns() - t0 > limit_ns) {
+                        atomicExch(&st->timeout, 1);
+                        atomicExch(&st->abort, 1);
+                        ok = 0;
+                        break;
+                    }
+                    if (*((volatile int *)&st->timeout)) { ok = 0; break; }
+                }
+            }
+        }
+        __threadfence();
+        s_ok = ok;
+    }
+    __syncthreads();
+    return s_ok != 0;
+}
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Sum of `v` over the block in a fixed order; the result is valid in every thread.
+template <int NV>
+__device__ __forceinline__ void block_sum(double (&v)[NV], double *smem /* NV*32 */) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+#pragma unroll
+    for (int i = 0; i < NV; ++i) v[i] = warp_sum(v[i]);
+    __syncthreads();
+    if (lane == 0)
+#pragma unroll
+        for (int i = 0; i < NV; ++i) smem[i * 32 + wid] = v[i];
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < NV; ++i) {
+        double t = (lane < nw) ? smem[i * 32 + lane] : 0.0;
+        v[i] = warp_sum(t);
+    }
+    __syncthreads();
+}
+
+// Every block sums partials[i*stride + b] over b < nb in the same order.
+template <int NV>
+__device__ __forceinline__ void grid_partials_sum(const double *partials, int stride, int nb, double (&out)[NV],
+                                                  double *smem) {
+    __shared__ double s_out[NV];
+    if (threadIdx.x < 32) {
+        const int lane = threadIdx.x;
+#pragma unroll
+        for (int i = 0; i < NV; ++i) {
+            double t = 0.0;
+            for (int b = lane; b < nb; b += 32) t += __ldcg(partials + i * stride + b);
+            t = warp_sum(t);
+            if (lane == 0) s_out[i] = t;
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < NV; ++i) out[i] = s_out[i];
+    __syncthreads();
+    (void)smem;
+}
+
+// ---------------------------------------------------------------------------
+// MRG32k3a
+// ---------------------------------------------------------------------------
+constexpr uint32_t MRG_M1 = 4294967087u;  // 2^32 - 209
+constexpr uint32_t MRG_M2 = 4294944443u;  // 2^32 - 22853
+
+__host__ __device__ __forceinline__ uint32_t mod_m1(uint64_t x) {
+    x = (x >> 32) * 209ull + (x & 0xffffffffull);
+    x = (x >> 32) * 209ull + (x & 0xffffffffull);
+    return (uint32_t)(x >= MRG_M1 ? x - MRG_M1 : x);
+}
+__host__ __device__ __forceinline__ uint32_t mod_m2(uint64_t x) {
+    x = (x >> 32) * 22853ull + (x & 0xffffffffull);
+    x = (x >> 32) * 22853ull + (x & 0xffffffffull);
+    return (uint32_t)(x >= MRG_M2 ? x - MRG_M2 : x);
+}
+
+// one jump: a pair of 3x3 transition-matrix powers (component 1 mod m1, component 2 mod m2)
+struct MrgJump {
+    uint32_t a[9];
+    uint32_t b[9];
+};
+
+__host__ __device__ __forceinline__ void mrg_apply(const MrgJump &J, const uint32_t s[6], uint32_t o[6]) {
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        uint32_t t = mod_m1((uint64_t)J.a[3 * i] * s[0]);
+        uint32_t u = mod_m1((uint64_t)J.a[3 * i + 1] * s[1]);
+        uint32_t w = mod_m1((uint64_t)J.a[3 * i + 2] * s[2]);
+        uint64_t acc = (uint64_t)t + u;
+        acc = acc >= MRG_M1 ? acc - MRG_M1 : acc;
+        acc += w;
+        o[i] = (uint32_t)(acc >= MRG_M1 ? acc - MRG_M1 : acc);
+    }
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        uint32_t t = mod_m2((uint64_t)J.b[3 * i] * s[3]);
+        uint32_t u = mod_m2((uint64_t)J.b[3 * i + 1] * s[4]);
+        uint32_t w = mod_m2((uint64_t)J.b[3 * i + 2] * s[5]);
+        uint64_t acc = (uint64_t)t + u;
+        acc = acc >= MRG_M2 ? acc - MRG_M2 : acc;
+        acc += w;
+        o[3 + i] = (uint32_t)(acc >= MRG_M2 ? acc - MRG_M2 : acc);
+    }
+}
+
+// One MRG32k3a draw in (0,1), formed as RngStream::U01 forms it (src/RngStream.cpp:266-289).
+__host__ __device__ __forceinline__ double mrg_u01(uint32_t s[6]) {
+    // component 1: x_n = 1403580 x_{n-2} - 810728 x_{n-3}  (mod m1)
+    uint32_t t1 = mod_m1(1403580ull * s[1]);
+    uint32_t t2 = mod_m1((uint64_t)(MRG_M1 - 810728u) * s[0]);
+    uint64_t p1 = (uint64_t)t1 + t2;
+    p1 = p1 >= MRG_M1 ? p1 - MRG_M1 : p1;
+    s[0] = s[1];
+    s[1] = s[2];
+    s[2] = (uint32_t)p1;
+    // component 2: x_n = 527612 x_{n-1} - 1370589 x_{n-3}  (mod m2)
+    uint32_t t3 = mod_m2(527612ull * s[5]);
+    uint32_t t4 = mod_m2((uint64_t)(MRG_M2 - 1370589u) * s[3]);
+    uint64_t p2 = (uint64_t)t3 + t4;
+    p2 = p2 >= MRG_M2 ? p2 - MRG_M2 : p2;
+    s[3] = s[4];
+    s[4] = s[5];
+    s[5] = (uint32_t)p2;
+    const double norm = 1.0 / (4294967087.0 + 1.0);
+    const double d1 = (double)(uint32_t)p1, d2 = (double)(uint32_t)p2;
+    return (p1 > p2) ? (d1 - d2) * norm : (d1 - d2 + 4294967087.0) * norm;
+}
+
+// RAND(-.5,.5) of include/tetra_element_linear.h:119
+__host__ __device__ __forceinline__ double mrg_rand_half(uint32_t s[6]) {
+    return (-.5) + ((.5) - (-.5)) * mrg_u01(s);
+}
+
+}  // namespace ffea

@@ -1,0 +1,32 @@
+// engine.h -- host-visible launchers of the blob-step kernels.
+//
+// The kernels are instantiated in two translation units: engine_fp64.cu
+// (R = double, compiled with -fmad=false so that each FP64 expression keeps
+// the reference's rounding) and engine_mixed.cu (R = float, FMA allowed).
+// Host code calls them only through Launch<R>.
+#pragma once
+
+#include "kernels.cuh"
+
+namespace ffea {
+
+template <class R>
+struct Launch {
+    static cudaError_t element(const ElemArgs<R> &a, cudaStream_t s);
+    static cudaError_t assemble(const AsmArgs<R> &a, cudaStream_t s);
+    static cudaError_t gather(const GatherArgs<R> &a, int blocks, cudaStream_t s);
+    static int gather_threads();
+    // persistent cooperative CG; returns the grid actually used in *grid
+    static cudaError_t cg(const CgArgs<R> &a, int grid, cudaStream_t s);
+    static int cg_max_grid(int device);
+    static int cg_threads();
+    static cudaError_t euler(const EulerArgs<R> &a, cudaStream_t s);
+};
+
+extern template struct Launch<double>;
+extern template struct Launch<float>;
+
+cudaError_t launch_finish_step(uint32_t *rng_state, const MrgJump *step_jump, DevStatus *st, cudaStream_t s);
+void count_launch(int n = 1);
+
+}  // namespace ffea

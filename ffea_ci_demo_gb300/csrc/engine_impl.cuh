@@ -1,0 +1,68 @@
+// engine_impl.cuh -- Launch<R> definitions; included by exactly one
+// translation unit per arithmetic type (engine_fp64.cu, engine_mixed.cu).
+#pragma once
+
+#include "engine.h"
+
+namespace ffea {
+
+constexpr int ELEM_THREADS = 128;
+constexpr int ASM_THREADS = 128;
+constexpr int GATHER_THREADS = 256;
+constexpr int CG_THREADS = 512;
+constexpr int EULER_THREADS = 256;
+
+template <class R>
+cudaError_t Launch<R>::element(const ElemArgs<R> &a, cudaStream_t s) {
+    if (a.T <= 0) return cudaSuccess;
+    element_kernel<R><<<(a.T + ELEM_THREADS - 1) / ELEM_THREADS, ELEM_THREADS, 0, s>>>(a);
+    count_launch();
+    return cudaGetLastError();
+}
+
+template <class R>
+cudaError_t Launch<R>::assemble(const AsmArgs<R> &a, cudaStream_t s) {
+    if (a.N <= 0) return cudaSuccess;
+    assemble_kernel<R><<<(a.N + ASM_THREADS - 1) / ASM_THREADS, ASM_THREADS, 0, s>>>(a);
+    count_launch();
+    return cudaGetLastError();
+}
+
+template <class R>
+int Launch<R>::gather_threads() { return GATHER_THREADS; }
+
+template <class R>
+cudaError_t Launch<R>::gather(const GatherArgs<R> &a, int blocks, cudaStream_t s) {
+    gather_kernel<R><<<blocks, GATHER_THREADS, 0, s>>>(a);
+    count_launch();
+    return cudaGetLastError();
+}
+
+template <class R>
+int Launch<R>::cg_threads() { return CG_THREADS; }
+
+template <class R>
+int Launch<R>::cg_max_grid(int device) {
+    int nsm = 0, per_sm = 0;
+    if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) return 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, cg_kernel<R>, CG_THREADS, 0) != cudaSuccess) return 0;
+    return nsm * per_sm;
+}
+
+template <class R>
+cudaError_t Launch<R>::cg(const CgArgs<R> &a, int grid, cudaStream_t s) {
+    CgArgs<R> args = a;
+    void *params[] = {&args};
+    cudaError_t e = cudaLaunchCooperativeKernel((const void *)cg_kernel<R>, dim3(grid), dim3(CG_THREADS), params, 0, s);
+    count_launch();
+    return e;
+}
+
+template <class R>
+cudaError_t Launch<R>::euler(const EulerArgs<R> &a, cudaStream_t s) {
+    euler_kernel<R><<<(a.N + EULER_THREADS - 1) / EULER_THREADS, EULER_THREADS, 0, s>>>(a);
+    count_launch();
+    return cudaGetLastError();
+}
+
+}  // namespace ffea

@@ -1,0 +1,517 @@
+// kernels.cuh -- the blob-step kernels, templated on the arithmetic type R.
+//
+// R = double is the plain FP64 path. Its translation unit is compiled with
+// -fmad=false, and every expression below is written in the reference's
+// evaluation order, so the element forces, viscosity matrices, assembled
+// matrix values, right-hand sides and SpMV rows are bit-identical to the
+// reference's (src/tetra_element_linear.cpp, src/Blob.cpp,
+// src/SparseMatrixFixedPattern.cpp); only the CG's cross-node reductions are
+// summed in a different (fixed) order.
+//
+// R = float is the mixed path: Jacobian, determinant, inversion check and
+// volume stay FP64; stress, noise scaling, matrix values, SpMV and CG vectors
+// are FP32; dot products and norms are accumulated across nodes in FP64;
+// positions are FP64 accumulators.
+//
+// Layouts (N vertex nodes, T elements):
+//   positions/velocities   SoA double px,py,pz / vx,vy,vz
+//   element data           SoA by field (coalesced per element)
+//   element outputs        ef[12*e + 3*a + c] (node a of element e, component c), geom[16*e + k]
+//   CG vectors             padded AoS, 4 per node: v[4*a + c]
+//   matrix                 3x3 blocks in SELL-32: slice s = 32 consecutive rows, slot(k,lane) =
+//                          slice_ptr[s] + 32*k + lane; block values val[9*slice_ptr[s] + 32*(9*k + c) + lane]
+#pragma once
+
+#include "common.cuh"
+
+namespace ffea {
+
+// ---------------------------------------------------------------------------
+// element kernel
+// ---------------------------------------------------------------------------
+template <class R>
+struct ElemArgs {
+    int T, nomass, calc_noise;
+    R kT, dt;
+    const int4 *tet;
+    const double *px, *py, *pz;
+    const double *vx, *vy, *vz;
+    const R *jinv;                 // 9*T, SoA jinv[k*T + e]
+    const R *G, *E, *A, *B, *vol0; // per element
+    double *last_det;
+    R *ef;    // 12*T
+    R *geom;  // 16*T: dpsi[12], vol
+    const uint32_t *rng_state;     // 6: stream state at the start of the step
+    const MrgJump *chunk_jump;     // ceil(T/32): A^(7*32*c)
+    const MrgJump *lane_jump;      // 32: A^(7*l)
+    DevStatus *st;
+};
+
+// V[r][c] of tetra_element_linear::create_viscosity_matrix (src/tetra_element_linear.cpp:298-327)
+// for r = a + 4i, c = b + 4j, evaluated exactly as the reference builds the entry it mirrors.
+template <class R>
+__device__ __forceinline__ R visc_entry(const R *dpsi, R A, R B, R vol, int r, int c) {
+    if (r > c) { int t = r; r = c; c = t; }
+    const int i = r >> 2, a = r & 3, j = c >> 2, b = c & 3;
+    if (i == j) {
+        const R t = dpsi[4 * i + a] * dpsi[4 * i + b] * (A + B);
+        const R d2 = (dpsi[a] * dpsi[b] + dpsi[4 + a] * dpsi[4 + b] + dpsi[8 + a] * dpsi[8 + b]);
+        return (t + d2 * A) * vol;
+    }
+    if (a == b) return ((B + A) * (dpsi[4 * i + a] * dpsi[4 * j + a])) * vol;
+    return (B * (dpsi[4 * i + a] * dpsi[4 * j + b]) + A * (dpsi[4 * i + b] * dpsi[4 * j + a])) * vol;
+}
+
+template <class R>
+__global__ void __launch_bounds__(128) element_kernel(ElemArgs<R> g) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= g.T || g.st->abort) return;
+    const int4 t = g.tet[e];
+    // calculate_jacobian :191-203 (FP64 in both paths)
+    const double x0 = g.px[t.x], y0 = g.py[t.x], z0 = g.pz[t.x];
+    double J[3][3];
+    J[0][0] = g.px[t.y] - x0; J[0][1] = g.py[t.y] - y0; J[0][2] = g.pz[t.y] - z0;
+    J[1][0] = g.px[t.z] - x0; J[1][1] = g.py[t.z] - y0; J[1][2] = g.pz[t.z] - z0;
+    J[2][0] = g.px[t.w] - x0; J[2][1] = g.py[t.w] - y0; J[2][2] = g.pz[t.w] - z0;
+    // calc_shape_function_derivatives_and_volume :222-292 (FP64 in both paths)
+    double d[12];
+    d[1] = J[2][2] * J[1][1] - J[2][1] * J[1][2];
+    d[2] = J[2][1] * J[0][2] - J[2][2] * J[0][1];
+    d[3] = J[1][2] * J[0][1] - J[1][1] * J[0][2];
+    d[5] = J[2][0] * J[1][2] - J[2][2] * J[1][0];
+    d[6] = J[2][2] * J[0][0] - J[2][0] * J[0][2];
+    d[7] = J[1][0] * J[0][2] - J[1][2] * J[0][0];
+    d[9] = J[2][1] * J[1][0] - J[2][0] * J[1][1];
+    d[10] = J[2][0] * J[0][1] - J[2][1] * J[0][0];
+    d[11] = J[1][1] * J[0][0] - J[1][0] * J[0][1];
+    double det = J[0][0] * d[1] + J[1][0] * d[2] + J[2][0] * d[3];
+    const double last = g.last_det[e];
+    double vold;
+    if (last * det < 0) {
+        // inverted: the reference returns before updating vol and dividing dpsi; the step is void
+        atomicAdd(&g.st->inversions, 1);
+        atomicExch(&g.st->abort, 1);
+        return;
+    }
+    g.last_det[e] = det;
+    vold = (1.0 / 6.0) * fabs(det);
+    det = 1.0 / det;
+    d[1] *= det; d[2] *= det; d[3] *= det;
+    d[5] *= det; d[6] *= det; d[7] *= det;
+    d[9] *= det; d[10] *= det; d[11] *= det;
+    d[0] = -(d[1] + d[2] + d[3]);
+    d[4] = -(d[5] + d[6] + d[7]);
+    d[8] = -(d[9] + d[10] + d[11]);
+    R dpsi[12];
+#pragma unroll
+    for (int k = 0; k < 12; ++k) dpsi[k] = (R)d[k];
+    const R vol = (R)vold;
+    R Jr[3][3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) Jr[i][j] = (R)J[i][j];
+    const R G = g.G[e], E = g.E[e], A = g.A[e], B = g.B[e], vol0 = g.vol0[e];
+    // add_shear_elastic_stress :375-392
+    R Ji[9];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) Ji[k] = g.jinv[(size_t)k * g.T + e];
+    R F[3][3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+            R s = 0;
+#pragma unroll
+            for (int k = 0; k < 3; ++k) s += Jr[k][i] * Ji[3 * j + k];
+            F[i][j] = s;
+        }
+    R S[3][3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+            R s = 0;
+#pragma unroll
+            for (int k = 0; k < 3; ++k) s += F[i][k] * F[j][k];
+            S[i][j] = s;
+        }
+    const R sc = (G * vol0 / vol);
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) S[i][j] *= sc;
+    S[0][0] -= G;
+    S[1][1] -= G;
+    S[2][2] -= G;
+    // add_bulk_elastic_stress :397-403
+    {
+        const R c_2 = E - G * (R)2.0 / (R)3.0;
+        const R c = G * ((R)1.0 - (vol0 / vol)) + (R)0.5 * c_2 * ((vol / vol0) - (vol0 / vol));
+        S[0][0] += c;
+        S[1][1] += c;
+        S[2][2] += c;
+    }
+    // add_fluctuating_stress :412-431, draws in the single-thread reference order
+    if (g.calc_noise == 1) {
+        uint32_t base[6], s6[6];
+#pragma unroll
+        for (int k = 0; k < 6; ++k) s6[k] = g.rng_state[k];
+        mrg_apply(g.chunk_jump[e >> 5], s6, base);
+        mrg_apply(g.lane_jump[e & 31], base, s6);
+        const R c = sqrt(((R)24 * g.kT) / (vol * g.dt));
+        const R bf = sqrt(B) * (R)mrg_rand_half(s6);
+        S[0][0] += c * (sqrt((R)2 * A) * (R)mrg_rand_half(s6) + bf);
+        S[1][1] += c * (sqrt((R)2 * A) * (R)mrg_rand_half(s6) + bf);
+        S[2][2] += c * (sqrt((R)2 * A) * (R)mrg_rand_half(s6) + bf);
+        S[0][1] += c * sqrt(A) * (R)mrg_rand_half(s6);
+        S[0][2] += c * sqrt(A) * (R)mrg_rand_half(s6);
+        S[1][2] += c * sqrt(A) * (R)mrg_rand_half(s6);
+        S[1][0] = S[0][1];
+        S[2][0] = S[0][2];
+        S[2][1] = S[1][2];
+    }
+    R du[12];
+    if (!g.nomass) {
+        // get_element_velocity_vector :448-463 + mat12_apply (src/mat_vec_fns.cpp:28-36)
+        const int nd[4] = {t.x, t.y, t.z, t.w};
+        R v[12];
+#pragma unroll
+        for (int a = 0; a < 4; ++a) {
+            v[a] = (R)g.vx[nd[a]];
+            v[4 + a] = (R)g.vy[nd[a]];
+            v[8 + a] = (R)g.vz[nd[a]];
+        }
+#pragma unroll 1
+        for (int i = 0; i < 12; ++i) {
+            R s = 0;
+#pragma unroll
+            for (int j = 0; j < 12; ++j) s += visc_entry<R>(dpsi, A, B, vol, i, j) * v[j];
+            du[i] = s;
+        }
+    } else {
+#pragma unroll
+        for (int i = 0; i < 12; ++i) du[i] = 0;
+    }
+    // apply_stress_tensor :436-443
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        du[4 * i] += vol * (dpsi[0] * S[i][0] + dpsi[4] * S[i][1] + dpsi[8] * S[i][2]);
+        du[4 * i + 1] += vol * (dpsi[1] * S[i][0] + dpsi[5] * S[i][1] + dpsi[9] * S[i][2]);
+        du[4 * i + 2] += vol * (dpsi[2] * S[i][0] + dpsi[6] * S[i][1] + dpsi[10] * S[i][2]);
+        du[4 * i + 3] += vol * (dpsi[3] * S[i][0] + dpsi[7] * S[i][1] + dpsi[11] * S[i][2]);
+    }
+    // add_element_force_vector :468-483 (node_force starts at zero every step)
+    R *ef = g.ef + 12 * (size_t)e;
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) ef[3 * a + c] = (R)0 - du[4 * c + a];
+    R *gm = g.geom + 16 * (size_t)e;
+#pragma unroll
+    for (int k = 0; k < 12; ++k) gm[k] = dpsi[k];
+    gm[12] = vol;
+}
+
+// ---------------------------------------------------------------------------
+// matrix assembly: CSR values = sum of element sources in element order
+// (SparseMatrixFixedPattern::build + sparse_entry_sources::sum_all_sources)
+// ---------------------------------------------------------------------------
+template <class R>
+struct AsmArgs {
+    int N;
+    const int *slice_ptr, *rowlen, *bcol, *diagk;
+    const int *src_ptr;
+    const unsigned *src;    // (element << 4) | (slot_a << 2) | slot_b ; 0xffffffff = identity
+    const R *geom, *A, *B;  // per element
+    const double *drag;     // per node or null
+    R *val;
+    R *dinv;                // 4*N
+    DevStatus *st;
+};
+
+constexpr unsigned SRC_IDENTITY = 0xffffffffu;
+
+template <class R>
+__global__ void __launch_bounds__(128) assemble_kernel(AsmArgs<R> g) {
+    const int a = blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= g.N || g.st->abort) return;
+    const int s = a >> 5, lane = a & 31;
+    const int base = g.slice_ptr[s];
+    const int len = g.rowlen[a];
+    const int dk = g.diagk[a];
+    R *vbase = g.val + 9 * (size_t)base + lane;
+    for (int k = 0; k < len; ++k) {
+        const int slot = base + 32 * k + lane;
+        R v[9];
+#pragma unroll
+        for (int c = 0; c < 9; ++c) v[c] = (R)0.0;
+        for (int q = g.src_ptr[slot]; q < g.src_ptr[slot + 1]; ++q) {
+            const unsigned code = g.src[q];
+            if (code == SRC_IDENTITY) {
+                v[0] += (R)1; v[4] += (R)1; v[8] += (R)1;
+                continue;
+            }
+            const int e = (int)(code >> 4), pa = (code >> 2) & 3, pb = code & 3;
+            const R *gm = g.geom + 16 * (size_t)e;
+            R dpsi[12];
+#pragma unroll
+            for (int m = 0; m < 12; ++m) dpsi[m] = gm[m];
+            const R vol = gm[12], A = g.A[e], B = g.B[e];
+#pragma unroll
+            for (int i = 0; i < 3; ++i)
+#pragma unroll
+                for (int j = 0; j < 3; ++j) v[3 * i + j] += visc_entry<R>(dpsi, A, B, vol, pa + 4 * i, pb + 4 * j);
+        }
+        if (k == dk) {
+            if (g.drag) {
+                const R dr = (R)g.drag[a];
+                v[0] += dr; v[4] += dr; v[8] += dr;
+            }
+            // calc_inverse_diagonal (src/SparseMatrixFixedPattern.cpp:305-312)
+            g.dinv[4 * a] = (R)1.0 / v[0];
+            g.dinv[4 * a + 1] = (R)1.0 / v[4];
+            g.dinv[4 * a + 2] = (R)1.0 / v[8];
+        }
+        R *vp = vbase + (size_t)32 * 9 * k;
+#pragma unroll
+        for (int c = 0; c < 9; ++c) vp[32 * c] = v[c];
+    }
+}
+
+// ---------------------------------------------------------------------------
+// force gather (Blob::aggregate_forces_and_solve :3152-3158) + solver set-up
+// ---------------------------------------------------------------------------
+template <class R>
+struct GatherArgs {
+    int N;
+    int mode;             // 0: CG (NoMass or consistent mass), 1: mass-lumped scaling
+    const int *inc_ptr, *inc;  // element*4 + slot, element order
+    const R *ef;
+    const int *pinned;
+    const double *drag;   // inertial Stokes drag (force -= v * drag) or null
+    const double *vx, *vy, *vz;
+    const R *dinv;        // Jacobi preconditioner (CG) or inverse lumped mass (mode 1)
+    double *f;            // 4*N assembled force (solver input)
+    R *x, *r, *p;
+    double *partials;     // [0]: f.f, [stride]: r.z per block
+    int stride;
+    DevStatus *st;
+};
+
+template <class R>
+__global__ void __launch_bounds__(256) gather_kernel(GatherArgs<R> g) {
+    __shared__ double smem[64];
+    const int a = blockIdx.x * blockDim.x + threadIdx.x;
+    double acc[2] = {0.0, 0.0};
+    const bool live = a < g.N && !g.st->abort;
+    if (live) {
+        R F0 = 0, F1 = 0, F2 = 0;
+        for (int m = g.inc_ptr[a]; m < g.inc_ptr[a + 1]; ++m) {
+            const int es = g.inc[m];
+            const R *c = g.ef + 12 * (size_t)(es >> 2) + 3 * (es & 3);
+            F0 += c[0];
+            F1 += c[1];
+            F2 += c[2];
+        }
+        if (g.drag) {  // inertial Stokes drag (src/Blob.cpp:3186-3188)
+            const double dr = g.drag[a];
+            F0 -= (R)(g.vx[a] * dr);
+            F1 -= (R)(g.vy[a] * dr);
+            F2 -= (R)(g.vz[a] * dr);
+        }
+        if (g.pinned[a]) { F0 = 0; F1 = 0; F2 = 0; }
+        g.f[4 * a] = (double)F0;
+        g.f[4 * a + 1] = (double)F1;
+        g.f[4 * a + 2] = (double)F2;
+        if (g.mode == 1) {  // MassLumpedSolver::solve, src/MassLumpedSolver.cpp:65-72
+            g.x[4 * a] = F0 * g.dinv[4 * a];
+            g.x[4 * a + 1] = F1 * g.dinv[4 * a + 1];
+            g.x[4 * a + 2] = F2 * g.dinv[4 * a + 2];
+        } else {  // conjugate_gradient_residual_assume_x_zero (src/NoMassCGSolver.cpp:196-220)
+            const R z0 = g.dinv[4 * a] * F0, z1 = g.dinv[4 * a + 1] * F1, z2 = g.dinv[4 * a + 2] * F2;
+            g.r[4 * a] = F0; g.r[4 * a + 1] = F1; g.r[4 * a + 2] = F2;
+            g.x[4 * a] = 0; g.x[4 * a + 1] = 0; g.x[4 * a + 2] = 0;
+            g.p[4 * a] = z0; g.p[4 * a + 1] = z1; g.p[4 * a + 2] = z2;
+            acc[0] = (double)(F0 * F0 + F1 * F1 + F2 * F2);
+            acc[1] = (double)(F0 * z0 + F1 * z1 + F2 * z2);
+        }
+    }
+    if (g.mode == 1) return;
+    block_sum<2>(acc, smem);
+    if (threadIdx.x == 0) {
+        g.partials[blockIdx.x] = acc[0];
+        g.partials[g.stride + blockIdx.x] = acc[1];
+    }
+}
+
+// ---------------------------------------------------------------------------
+// persistent Jacobi-PCG (NoMassCGSolver::solve :156-188 / ConjugateGradientSolver::solve :193-217)
+// ---------------------------------------------------------------------------
+template <class R>
+struct CgArgs {
+    int N;
+    int block3;           // 1: 3x3-block viscosity matrix, 0: scalar mass matrix applied per component
+    int check_last;       // 1: also test convergence after the last allowed iteration (NoMass order)
+    int nomass_zero_rhs_nan;  // NoMass: zero right-hand side gives 0/0 as in the reference
+    const int *slice_ptr, *rowlen, *bcol;
+    const R *val;
+    const R *dinv;
+    R *x, *r, *p, *q;
+    const double *init_partials;  // from gather_kernel: f.f and r.z per block
+    int n_init, init_stride;
+    double *partials;     // 3 * max_blocks
+    int stride;
+    GridBarrier *gb;
+    DevStatus *st;
+    int imax;
+    double eps2;
+    unsigned long long limit_ns;
+};
+
+template <class R>
+__device__ __forceinline__ void spmv_row(const CgArgs<R> &g, int a, R &q0, R &q1, R &q2) {
+    const int s = a >> 5, lane = a & 31;
+    const int base = g.slice_ptr[s];
+    const int len = g.rowlen[a];
+    q0 = 0.0; q1 = 0.0; q2 = 0.0;
+    if (g.block3) {
+        const R *v = g.val + 9 * (size_t)base + lane;
+        for (int k = 0; k < len; ++k) {
+            const int b = g.bcol[base + 32 * k + lane];
+            const R p0 = g.p[4 * b], p1 = g.p[4 * b + 1], p2 = g.p[4 * b + 2];
+            const R *vk = v + (size_t)32 * 9 * k;
+            q0 += vk[0] * p0; q0 += vk[32] * p1; q0 += vk[64] * p2;
+            q1 += vk[96] * p0; q1 += vk[128] * p1; q1 += vk[160] * p2;
+            q2 += vk[192] * p0; q2 += vk[224] * p1; q2 += vk[256] * p2;
+        }
+    } else {
+        const R *v = g.val + base + lane;
+        for (int k = 0; k < len; ++k) {
+            const int b = g.bcol[base + 32 * k + lane];
+            const R m = v[32 * k];
+            q0 += m * g.p[4 * b];
+            q1 += m * g.p[4 * b + 1];
+            q2 += m * g.p[4 * b + 2];
+        }
+    }
+}
+
+template <class R>
+__global__ void __launch_bounds__(512) cg_kernel(CgArgs<R> g) {
+    __shared__ double smem[96];
+    DevStatus *st = g.st;
+    if (st->abort) return;
+    const int nthr = gridDim.x * blockDim.x;
+    const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+    double init[2];
+    grid_partials_sum<2>(g.init_partials, g.init_stride, g.n_init, init, smem);
+    const double f2 = init[0];
+    double delta = init[1];
+    int it = 0;
+    bool converged = false, ok = true;
+    for (; it < g.imax; ++it) {
+        // q = V p ; pTq   (get_alpha_denominator :253-266)
+        double acc1[1] = {0.0};
+        for (int a = tid; a < g.N; a += nthr) {
+            R q0, q1, q2;
+            spmv_row(g, a, q0, q1, q2);
+            g.q[4 * a] = q0; g.q[4 * a + 1] = q1; g.q[4 * a + 2] = q2;
+            acc1[0] += (double)(g.p[4 * a] * q0 + g.p[4 * a + 1] * q1 + g.p[4 * a + 2] * q2);
+        }
+        block_sum<1>(acc1, smem);
+        if (threadIdx.x == 0) g.partials[blockIdx.x] = acc1[0];
+        if (!(ok = grid_sync(g.gb, st, g.limit_ns))) break;
+        double pTq[1];
+        grid_partials_sum<1>(g.partials, 0, gridDim.x, pTq, smem);
+        const double alpha = delta / pTq[0];
+        const R ar = (R)alpha, mar = (R)(-alpha);
+        // x += alpha p ; r += (-alpha) q ; |r|^2 ; r.z   (vec3_add_to_scaled, residual2, apply_preconditioner)
+        double acc2[2] = {0.0, 0.0};
+        for (int a = tid; a < g.N; a += nthr) {
+#pragma unroll
+            for (int c = 0; c < 3; ++c) g.x[4 * a + c] += ar * g.p[4 * a + c];
+            R r[3], z[3];
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                r[c] = g.r[4 * a + c] + mar * g.q[4 * a + c];
+                g.r[4 * a + c] = r[c];
+                z[c] = g.dinv[4 * a + c] * r[c];
+            }
+            acc2[0] += (double)(r[0] * r[0] + r[1] * r[1] + r[2] * r[2]);
+            acc2[1] += (double)(r[0] * z[0] + r[1] * z[1] + r[2] * z[2]);
+        }
+        block_sum<2>(acc2, smem);
+        if (threadIdx.x == 0) {
+            g.partials[g.stride + blockIdx.x] = acc2[0];
+            g.partials[2 * g.stride + blockIdx.x] = acc2[1];
+        }
+        if (!(ok = grid_sync(g.gb, st, g.limit_ns))) break;
+        double rz[2];
+        grid_partials_sum<2>(g.partials + g.stride, g.stride, gridDim.x, rz, smem);
+        const double res2 = (f2 == 0.0) ? 0.0 : rz[0] / f2;
+        if ((g.check_last || it + 1 < g.imax) && res2 < g.eps2) {
+            converged = true;
+            ++it;
+            break;
+        }
+        const double delta_old = delta;
+        delta = rz[1];
+        const R beta = (R)(delta / delta_old);
+        // p = beta p + z   (vec3_scale_and_add :202-212)
+        for (int a = tid; a < g.N; a += nthr) {
+#pragma unroll
+            for (int c = 0; c < 3; ++c) g.p[4 * a + c] = beta * g.p[4 * a + c] + g.dinv[4 * a + c] * g.r[4 * a + c];
+        }
+        if (!(ok = grid_sync(g.gb, st, g.limit_ns))) break;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        if (!ok) {
+            st->abort = 1;
+        } else if (!converged) {
+            st->cg_fail = 1;
+            st->abort = 1;
+            st->last_iters = g.imax;
+            st->total_iters += g.imax;
+        } else {
+            st->last_iters = it;
+            st->total_iters += it;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Euler update (Blob::euler_integrate :3249-3279), non-finite check, RNG advance
+// ---------------------------------------------------------------------------
+template <class R>
+struct EulerArgs {
+    int N, nomass;
+    double dt;
+    const R *x;
+    double *px, *py, *pz, *vx, *vy, *vz;
+    uint32_t *rng_state;     // advanced by step_jump once per step
+    const MrgJump *step_jump;
+    DevStatus *st;
+};
+
+template <class R>
+__global__ void __launch_bounds__(256) euler_kernel(EulerArgs<R> g) {
+    const int a = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g.st->abort) return;
+    if (a < g.N) {
+        const double x0 = (double)g.x[4 * a], x1 = (double)g.x[4 * a + 1], x2 = (double)g.x[4 * a + 2];
+        if (!(isfinite(x0) && isfinite(x1) && isfinite(x2))) atomicExch(&g.st->nonfinite, 1);
+        if (g.nomass) {
+            g.vx[a] = x0; g.vy[a] = x1; g.vz[a] = x2;
+            g.px[a] += x0 * g.dt; g.py[a] += x1 * g.dt; g.pz[a] += x2 * g.dt;
+        } else {
+            g.vx[a] += x0 * g.dt; g.vy[a] += x1 * g.dt; g.vz[a] += x2 * g.dt;
+            g.px[a] += g.vx[a] * g.dt; g.py[a] += g.vy[a] * g.dt; g.pz[a] += g.vz[a] * g.dt;
+        }
+    }
+}
+
+// closes a step: RNG advance and step counter (one thread), after euler_kernel
+__global__ void finish_step_kernel(uint32_t *rng_state, const MrgJump *step_jump, DevStatus *st);
+
+}  // namespace ffea

@@ -1,0 +1,303 @@
+"""ctypes binding of the C ABI (include/ffea_gpu.h) and a Python ``Blob``.
+
+``Blob`` mirrors the reference's ``Blob`` step surface for the hot path
+(include/Blob.h:94-718): construct from a mesh or from the reference's
+structure files, then ``update(nsteps)`` runs the per-blob slice of
+``World::run`` (zero forces, ``update_internal_forces``, ``update_positions``).
+Errors surface as exceptions, as the reference's ``FFEAException`` does.
+
+The CUDA library must be built (``ffea_ci_demo_gb300.build.build()``); there
+is no CPU fallback: loading fails loudly when it is missing.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import re
+
+import numpy as np
+
+from .mesh import Mesh
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+LIB_PATH = os.path.join(HERE, "_build", "libffea_gpu.so")
+HEADER = os.path.join(ROOT, "include", "ffea_gpu.h")
+
+OK, EINVERTED, ECGMAXIT, EINPUT, ENOMEM, ECUDA, ENAN, ETIMEOUT, EFILE = range(9)
+SOLVERS = {"CG_nomass": 0, "CG": 1, "masslumped": 2}
+PRECISIONS = {"fp64": 0, "mixed": 1}
+MESO_LENGTH = 1.7e-10
+
+
+class FFEAError(RuntimeError):
+    """A non-zero status from the C ABI."""
+
+    def __init__(self, code: int, where: str, detail: str = ""):
+        self.code = code
+        names = {1: "element inverted", 2: "CG did not converge", 3: "invalid input", 4: "out of memory",
+                 5: "CUDA error", 6: "non-finite solver output", 7: "device wait timed out", 8: "file error"}
+        super().__init__(f"{where}: {names.get(code, code)}" + (f" ({detail})" if detail else ""))
+
+
+class Params(C.Structure):
+    """ffea_gpu_params: the hot-path fields of SimulationParams (meso units)."""
+
+    _fields_ = [("dt", C.c_double), ("kT", C.c_double), ("epsilon2", C.c_double), ("stokes_visc", C.c_double),
+                ("max_iterations_cg", C.c_int), ("calc_noise", C.c_int), ("calc_stokes", C.c_int),
+                ("solver", C.c_int), ("precision", C.c_int), ("reserved", C.c_int)]
+
+
+class MeshStruct(C.Structure):
+    _fields_ = [("num_nodes", C.c_int), ("num_elements", C.c_int), ("num_pinned", C.c_int),
+                ("pos", C.c_void_p), ("tets", C.c_void_p), ("rho", C.c_void_p), ("A", C.c_void_p),
+                ("B", C.c_void_p), ("G", C.c_void_p), ("E", C.c_void_p), ("stokes_radius", C.c_void_p),
+                ("pinned", C.c_void_p)]
+
+
+_lib = None
+
+
+def header_functions() -> list[str]:
+    """Names of every function the C header declares."""
+    src = open(HEADER).read()
+    return sorted(set(re.findall(r"^\s*(?:[\w]+\s+)+\*?\s*(ffea_gpu_\w+)\s*\(", src, re.M)))
+
+
+def load():
+    """Load the CUDA library (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError(f"{LIB_PATH} is missing: build it with ffea_ci_demo_gb300.build.build()")
+    lib = C.CDLL(LIB_PATH)
+    vp, ip, dp = C.c_void_p, C.POINTER(C.c_int), C.c_void_p
+    sig = {
+        "ffea_gpu_params_default": (C.c_int, [C.POINTER(Params)]),
+        "ffea_gpu_params_assign": (C.c_int, [C.POINTER(Params), C.c_char_p, C.c_char_p]),
+        "ffea_gpu_material_from_si": (C.c_int, [C.c_int, dp, dp, dp, dp, dp, dp]),
+        "ffea_gpu_blob_create": (C.c_int, [C.POINTER(MeshStruct), C.POINTER(Params), C.POINTER(vp)]),
+        "ffea_gpu_blob_load": (C.c_int, [C.c_char_p] * 5 + [C.c_double, C.POINTER(Params), C.POINTER(vp)]),
+        "ffea_gpu_blob_destroy": (None, [vp]),
+        "ffea_gpu_blob_set_rng_state": (C.c_int, [vp, dp]),
+        "ffea_gpu_blob_get_rng_state": (C.c_int, [vp, dp]),
+        "ffea_gpu_blob_step": (C.c_int, [vp, C.c_int, ip]),
+        "ffea_gpu_blob_step_timed": (C.c_int, [vp, C.c_int, C.c_longlong, ip, C.POINTER(C.c_double), dp]),
+        "ffea_gpu_blob_get_state": (C.c_int, [vp, dp, dp, dp]),
+        "ffea_gpu_blob_set_state": (C.c_int, [vp, dp, dp]),
+        "ffea_gpu_blob_measure": (C.c_int, [vp, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
+        "ffea_gpu_blob_cg_iterations": (C.c_int, [vp, ip, C.POINTER(C.c_longlong)]),
+        "ffea_gpu_blob_sizes": (C.c_int, [vp, ip, ip, C.POINTER(C.c_longlong)]),
+        "ffea_gpu_blob_get_pattern": (C.c_int, [vp, dp, dp, dp, dp, C.POINTER(C.c_longlong)]),
+        "ffea_gpu_blob_get_connectivity": (C.c_int, [vp, dp, dp, C.POINTER(C.c_longlong)]),
+        "ffea_gpu_blob_get_elements": (C.c_int, [vp, dp, dp, dp]),
+        "ffea_gpu_blob_get_rhs": (C.c_int, [vp, dp]),
+        "ffea_gpu_last_error": (C.c_char_p, []),
+        "ffea_gpu_launch_count": (C.c_longlong, []),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = lib
+    return lib
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def last_error() -> str:
+    return load().ffea_gpu_last_error().decode()
+
+
+def _check(rc: int, where: str) -> None:
+    if rc != OK:
+        raise FFEAError(rc, where, last_error())
+
+
+def make_params(*, solver: str = "CG_nomass", precision: str = "fp64", **si) -> Params:
+    """SimulationParams defaults, then ``assign`` for each SI key (dt, kT, epsilon, ...)."""
+    lib = load()
+    p = Params()
+    _check(lib.ffea_gpu_params_default(C.byref(p)), "params_default")
+    for k, v in si.items():
+        _check(lib.ffea_gpu_params_assign(C.byref(p), k.encode(), repr(v).encode() if isinstance(v, float)
+                                          else str(v).encode()), f"params_assign({k})")
+    _check(lib.ffea_gpu_params_assign(C.byref(p), b"solver", solver.encode()), "params_assign(solver)")
+    _check(lib.ffea_gpu_params_assign(C.byref(p), b"precision", precision.encode()), "params_assign(precision)")
+    return p
+
+
+def material_from_si(mat6: np.ndarray) -> dict:
+    lib = load()
+    mat6 = np.ascontiguousarray(mat6, np.float64)
+    n = mat6.shape[0]
+    out = {k: np.empty(n) for k in ("rho", "A", "B", "G", "E")}
+    _check(lib.ffea_gpu_material_from_si(n, _p(mat6), *(_p(out[k]) for k in ("rho", "A", "B", "G", "E"))),
+           "material_from_si")
+    return out
+
+
+class Blob:
+    """One FFEA blob on the GPU (vertex nodes resident in HBM)."""
+
+    def __init__(self, mesh: Mesh | None = None, *, solver: str = "CG_nomass", precision: str = "fp64",
+                 dt: float = 1e-12, kT: float = 4.11e-21, epsilon: float = 1e-10, max_iterations_cg: int = 10000,
+                 calc_noise: int = 1, calc_stokes: int = 0, stokes_visc: float = 1e-3,
+                 rng_state=(12345,) * 6, _handle=None, _n=None):
+        self._lib = load()
+        self._h = C.c_void_p()
+        if _handle is not None:
+            self._h = _handle
+            self.n_nodes, self.n_elem = _n
+        else:
+            params = make_params(solver=solver, precision=precision, dt=dt, kT=kT, epsilon=epsilon,
+                                 max_iterations_cg=max_iterations_cg, calc_noise=calc_noise,
+                                 calc_stokes=calc_stokes, stokes_visc=stokes_visc)
+            s = mesh.scale / MESO_LENGTH
+            self._keep = [np.ascontiguousarray(mesh.pos * s, np.float64),
+                          np.ascontiguousarray(mesh.tets, np.int32),
+                          np.ascontiguousarray(mesh.stokes_radius * s, np.float64),
+                          np.ascontiguousarray(mesh.pinned, np.int32) if len(mesh.pinned) else None]
+            mat = material_from_si(mesh.material)
+            self._keep += [mat[k] for k in ("rho", "A", "B", "G", "E")]
+            m = MeshStruct(mesh.n_nodes, mesh.n_elem, len(mesh.pinned), _p(self._keep[0]), _p(self._keep[1]),
+                           *(_p(mat[k]) for k in ("rho", "A", "B", "G", "E")), _p(self._keep[2]),
+                           _p(self._keep[3]))
+            _check(self._lib.ffea_gpu_blob_create(C.byref(m), C.byref(params), C.byref(self._h)), "blob_create")
+            self._keep = None
+            self.n_nodes, self.n_elem = mesh.n_nodes, mesh.n_elem
+        self.set_rng_state(rng_state)
+
+    @classmethod
+    def from_files(cls, node, top, mat, stokes, pin, scale, *, solver="CG_nomass", precision="fp64",
+                   rng_state=(12345,) * 6, **si):
+        """Blob::config + Blob::init from the reference's structure files."""
+        lib = load()
+        params = make_params(solver=solver, precision=precision, **si)
+        h = C.c_void_p()
+        enc = lambda s: None if s is None else str(s).encode()  # noqa: E731
+        _check(lib.ffea_gpu_blob_load(enc(node), enc(top), enc(mat), enc(stokes), enc(pin), float(scale),
+                                      C.byref(params), C.byref(h)), "blob_load")
+        with open(node) as f:
+            f.readline()
+            n = int(f.readline().split()[1])
+        with open(top) as f:
+            f.readline()
+            t = int(f.readline().split()[1])
+        return cls(_handle=h, _n=(n, t), rng_state=rng_state)
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) and self._h.value:
+            self._lib.ffea_gpu_blob_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        self.close()
+
+    # -- the step -------------------------------------------------------------
+    def update(self, nsteps: int = 1) -> int:
+        """Run nsteps; raises FFEAError at the first failing step. Returns steps done."""
+        done = C.c_int(0)
+        rc = self._lib.ffea_gpu_blob_step(self._h, int(nsteps), C.byref(done))
+        self.steps_done = done.value
+        _check(rc, f"step (after {done.value} completed steps)")
+        return done.value
+
+    def update_timed(self, nsteps: int, flush_bytes: int = 0) -> dict:
+        """update() with per-step CUDA-event timing on the blob's stream (flush outside the timed window)."""
+        done, ms = C.c_int(0), C.c_double(0)
+        ph = np.zeros(5)
+        rc = self._lib.ffea_gpu_blob_step_timed(self._h, int(nsteps), int(flush_bytes), C.byref(done), C.byref(ms),
+                                                _p(ph))
+        _check(rc, f"step_timed (after {done.value} completed steps)")
+        return {"steps": done.value, "ms": ms.value,
+                "phase_ms": dict(zip(("element", "assemble", "gather", "cg", "euler"), ph.tolist()))}
+
+    def try_update(self, nsteps: int = 1) -> tuple[int, int]:
+        """Like update() but returns (status, steps_done) instead of raising."""
+        done = C.c_int(0)
+        rc = self._lib.ffea_gpu_blob_step(self._h, int(nsteps), C.byref(done))
+        return rc, done.value
+
+    # -- state ------------------------------------------------------------------
+    def state(self):
+        pos = np.empty((self.n_nodes, 3))
+        vel = np.empty((self.n_nodes, 3))
+        force = np.empty((self.n_nodes, 3))
+        _check(self._lib.ffea_gpu_blob_get_state(self._h, _p(pos), _p(vel), _p(force)), "get_state")
+        return pos, vel, force
+
+    def pos(self) -> np.ndarray:
+        o = np.empty((self.n_nodes, 3))
+        _check(self._lib.ffea_gpu_blob_get_state(self._h, _p(o), None, None), "get_state")
+        return o
+
+    def vel(self) -> np.ndarray:
+        o = np.empty((self.n_nodes, 3))
+        _check(self._lib.ffea_gpu_blob_get_state(self._h, None, _p(o), None), "get_state")
+        return o
+
+    def set_state(self, pos=None, vel=None) -> None:
+        pa = None if pos is None else np.ascontiguousarray(pos, np.float64)
+        va = None if vel is None else np.ascontiguousarray(vel, np.float64)
+        _check(self._lib.ffea_gpu_blob_set_state(self._h, _p(pa), _p(va)), "set_state")
+
+    def set_rng_state(self, s) -> None:
+        a = np.ascontiguousarray(s, np.uint32)
+        _check(self._lib.ffea_gpu_blob_set_rng_state(self._h, _p(a)), "set_rng_state")
+
+    def rng_state(self) -> np.ndarray:
+        a = np.empty(6, np.uint32)
+        _check(self._lib.ffea_gpu_blob_get_rng_state(self._h, _p(a)), "get_rng_state")
+        return a
+
+    def measure(self) -> tuple[float, float]:
+        se, ke = C.c_double(), C.c_double()
+        _check(self._lib.ffea_gpu_blob_measure(self._h, C.byref(se), C.byref(ke)), "measure")
+        return se.value, ke.value
+
+    def cg_iterations(self) -> tuple[int, int]:
+        last, total = C.c_int(), C.c_longlong()
+        _check(self._lib.ffea_gpu_blob_cg_iterations(self._h, C.byref(last), C.byref(total)), "cg_iterations")
+        return last.value, total.value
+
+    def sizes(self) -> tuple[int, int, int]:
+        nl, ne, nb = C.c_int(), C.c_int(), C.c_longlong()
+        _check(self._lib.ffea_gpu_blob_sizes(self._h, C.byref(nl), C.byref(ne), C.byref(nb)), "sizes")
+        return nl.value, ne.value, nb.value
+
+    def pattern(self, values: bool = True) -> dict:
+        nnz = C.c_longlong()
+        _check(self._lib.ffea_gpu_blob_get_pattern(self._h, None, None, None, None, C.byref(nnz)), "get_pattern")
+        d = {"key": np.empty(3 * self.n_nodes + 1, np.int32), "col": np.empty(nnz.value, np.int32),
+             "nsrc": np.empty(nnz.value, np.int32), "val": np.empty(nnz.value) if values else None}
+        _check(self._lib.ffea_gpu_blob_get_pattern(self._h, _p(d["key"]), _p(d["col"]), _p(d["val"]), _p(d["nsrc"]),
+                                                   C.byref(nnz)), "get_pattern")
+        return d
+
+    def connectivity(self) -> dict:
+        cnt = C.c_longlong()
+        _check(self._lib.ffea_gpu_blob_get_connectivity(self._h, None, None, C.byref(cnt)), "get_connectivity")
+        d = {"ptr": np.empty(self.n_nodes + 1, np.int32), "elem_slot": np.empty(cnt.value, np.int32)}
+        _check(self._lib.ffea_gpu_blob_get_connectivity(self._h, _p(d["ptr"]), _p(d["elem_slot"]), C.byref(cnt)),
+               "get_connectivity")
+        return d
+
+    def elements(self, visc: bool = False) -> dict:
+        T = self.n_elem
+        d = {"node_force": np.empty((T, 4, 3)), "vol": np.empty(T), "visc": np.empty((T, 12, 12)) if visc else None}
+        _check(self._lib.ffea_gpu_blob_get_elements(self._h, _p(d["node_force"]), _p(d["vol"]), _p(d["visc"])),
+               "get_elements")
+        return d
+
+    def rhs(self) -> np.ndarray:
+        o = np.empty((self.n_nodes, 3))
+        _check(self._lib.ffea_gpu_blob_get_rhs(self._h, _p(o)), "get_rhs")
+        return o
+
+
+def launch_count() -> int:
+    return int(load().ffea_gpu_launch_count())

@@ -1,0 +1,178 @@
+/*
+ * ffea_gpu.h -- C ABI of the GB300 (sm_103a) FFEA blob-step engine.
+ *
+ * Drop-in for FFEA's per-timestep blob update (RSE-Sheffield/ffea_ci_demo,
+ * FFEA 2.7.2). The reference has no C ABI: its path sits behind the C++
+ * classes Blob (include/Blob.h:94-718) and Solver (include/Solver.h:31-52).
+ * Each entry point below names the reference member it replaces.
+ *
+ * Conventions
+ *  - Every call returns an int status (FFEA_GPU_OK or an FFEA_GPU_E* code);
+ *    nothing throws across the ABI and device code never traps.
+ *  - Host arrays are caller-owned and copied; device memory is owned by the
+ *    handle. Calls on one handle are not thread-safe.
+ *  - Units are FFEA's meso units (include/dimensions.h:30-41) unless a
+ *    function says SI; helpers convert exactly as the reference loaders do.
+ *  - Node arrays cover every node of the 10-node ("quadratic") topology in
+ *    the reference's node order; the device carries vertex nodes only and
+ *    rebuilds edge-midpoint nodes when state is read back, as the reference
+ *    does every step (tetra_element_linear::linearise_element).
+ */
+#ifndef FFEA_GPU_H
+#define FFEA_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define FFEA_GPU_OK 0
+#define FFEA_GPU_EINVERTED 1 /* an element inverted (Blob::update_internal_forces, src/Blob.cpp:484-490) */
+#define FFEA_GPU_ECGMAXIT 2  /* CG hit max_iterations_cg (NoMassCGSolver::solve, src/NoMassCGSolver.cpp:187) */
+#define FFEA_GPU_EINPUT 3    /* invalid argument, mesh or parameter */
+#define FFEA_GPU_ENOMEM 4    /* device or host allocation failed */
+#define FFEA_GPU_ECUDA 5     /* CUDA runtime error or extension built for another GPU */
+#define FFEA_GPU_ENAN 6      /* non-finite solver output (e.g. zero right-hand side, see the reference's alpha = 0/0) */
+#define FFEA_GPU_ETIMEOUT 7  /* a bounded device-side wait gave up */
+#define FFEA_GPU_EFILE 8     /* structure file missing or malformed (FFEAFileException) */
+
+/* solvers: the `solver` keyword of a .ffea <blob> block (src/World.cpp:2601-2627) */
+#define FFEA_GPU_NOMASS_CG 0  /* "CG_nomass"  -> NoMassCGSolver */
+#define FFEA_GPU_CG 1         /* "CG"         -> ConjugateGradientSolver (consistent mass) */
+#define FFEA_GPU_MASSLUMPED 2 /* "masslumped" -> MassLumpedSolver */
+
+/* arithmetic of the step */
+#define FFEA_GPU_FP64 0  /* every operation in FP64, in the reference's evaluation order */
+#define FFEA_GPU_MIXED 1 /* FP32 element stress, noise scaling, matrix and SpMV; FP64 dot products,
+                            residual norms, near-degenerate Jacobians and the position accumulator */
+
+/* the hot-path fields of SimulationParams (include/SimulationParams.h:75-211), meso units */
+typedef struct ffea_gpu_params {
+    double dt;          /* time step */
+    double kT;          /* thermal energy */
+    double epsilon2;    /* CG stop: |r|^2/|f|^2 < epsilon2 (the script's epsilon, squared) */
+    double stokes_visc; /* medium viscosity for Stokes drag */
+    int max_iterations_cg;
+    int calc_noise;   /* 1: thermal fluctuating stress (and Stokes noise) */
+    int calc_stokes;  /* 1: Stokes drag 6 pi eta r on every node */
+    int solver;       /* FFEA_GPU_NOMASS_CG / FFEA_GPU_CG / FFEA_GPU_MASSLUMPED */
+    int precision;    /* FFEA_GPU_FP64 / FFEA_GPU_MIXED */
+    int reserved;
+} ffea_gpu_params;
+
+/* SimulationParams::SimulationParams() defaults for the hot-path fields
+ * (src/SimulationParams.cpp:26-60); solver CG_nomass, precision FP64. */
+int ffea_gpu_params_default(ffea_gpu_params *p);
+
+/* SimulationParams::assign for one `<key = value>` of a .ffea <param> block
+ * (src/SimulationParams.cpp:245-560): SI -> meso conversion for dt, kT,
+ * stokes_visc; epsilon is squared; calc_stokes also accepts do_stokes.
+ * Keys outside the hot path return FFEA_GPU_EINPUT. */
+int ffea_gpu_params_assign(ffea_gpu_params *p, const char *key, const char *value);
+
+/* Blob::load_material_params per-element conversion (src/Blob.cpp:2275-2283):
+ * mat6 = n x {density, shear_visc, bulk_visc, shear_mod, bulk_mod, dielectric} (SI)
+ * -> rho, A, B, G, E in meso units, including the reference's second-viscosity
+ * expression B = bulk_visc/(P t) - (2/3) shear_visc. */
+int ffea_gpu_material_from_si(int n, const double *mat6, double *rho, double *A, double *B, double *G, double *E);
+
+/* a blob's structure in the units the reference holds after Blob::init loads it */
+typedef struct ffea_gpu_mesh {
+    int num_nodes;              /* all nodes, vertices and edge midpoints */
+    int num_elements;
+    int num_pinned;
+    const double *pos;          /* 3 * num_nodes, meso */
+    const int *tets;            /* 10 * num_elements, node indices (4 vertices then 6 midpoints) */
+    const double *rho, *A, *B, *G, *E; /* num_elements each, meso */
+    const double *stokes_radius;       /* num_nodes, meso (may be NULL when calc_stokes == 0) */
+    const int *pinned;          /* num_pinned node indices */
+} ffea_gpu_mesh;
+
+typedef struct ffea_gpu_blob ffea_gpu_blob;
+
+/* Blob::config + Blob::init (src/Blob.cpp:108-365) + Solver::init: rest state
+ * (calc_rest_state_info :3080-3143), node-element connectivity (:3284-3314),
+ * fixed sparsity pattern (NoMassCGSolver::init, src/NoMassCGSolver.cpp:56-153;
+ * ConjugateGradientSolver::init; MassLumpedSolver::init) and device upload. */
+int ffea_gpu_blob_create(const ffea_gpu_mesh *mesh, const ffea_gpu_params *params, ffea_gpu_blob **out);
+
+/* Same from the reference's structure files (.node/.top/.mat/.stokes/.pin; pin may be NULL),
+ * with `scale` the .ffea scale in metres per file unit (src/World.cpp:2632). */
+int ffea_gpu_blob_load(const char *node_file, const char *top_file, const char *mat_file, const char *stokes_file,
+                       const char *pin_file, double scale, const ffea_gpu_params *params, ffea_gpu_blob **out);
+
+void ffea_gpu_blob_destroy(ffea_gpu_blob *blob);
+
+/* The state of the blob's RngStream (RngStream::SetSeed/GetState semantics:
+ * 6 integers, the first three < 4294967087, the last three < 4294944443).
+ * Draws are consumed in the reference's single-thread order: 7 per element in
+ * element order (tetra_element_linear::add_fluctuating_stress), then 3 per
+ * node in node order when Stokes noise is on (src/Blob.cpp:3172-3224). A
+ * reference run with OMP_NUM_THREADS=1 seeded with the package seed s uses
+ * exactly the stream whose state is s. */
+int ffea_gpu_blob_set_rng_state(ffea_gpu_blob *blob, const uint32_t state[6]);
+int ffea_gpu_blob_get_rng_state(ffea_gpu_blob *blob, uint32_t state[6]);
+
+/* nsteps x { Blob::zero_force; set_forces_to_zero; update_internal_forces;
+ * update_positions } (the per-blob slice of World::run, src/World.cpp:1788-2059).
+ * Stops at the first failing step; *steps_done (may be NULL) gets the number
+ * of completed steps. */
+int ffea_gpu_blob_step(ffea_gpu_blob *blob, int nsteps, int *steps_done);
+
+/* Phases of one step, in launch order (for ffea_gpu_blob_step_timed). */
+#define FFEA_GPU_NUM_PHASES 5 /* 0 element stress/forces, 1 matrix assembly, 2 force gather, 3 CG solve, 4 Euler */
+
+/* ffea_gpu_blob_step, with every step timed by CUDA events on the blob's stream.
+ * Before each step, flush_bytes of scratch device memory are written (outside the
+ * timed window) so that each step starts with a cold L2; 0 disables the flush.
+ * *step_ms gets the summed device time of the steps; phase_ms (may be NULL) gets
+ * FFEA_GPU_NUM_PHASES per-phase sums (events between the kernels of each step). */
+int ffea_gpu_blob_step_timed(ffea_gpu_blob *blob, int nsteps, long long flush_bytes, int *steps_done,
+                             double *step_ms, double *phase_ms);
+
+/* Host state in the reference's node order, all nodes (midpoints rebuilt). Any pointer may be NULL. */
+int ffea_gpu_blob_get_state(ffea_gpu_blob *blob, double *pos, double *vel, double *force);
+/* Overwrite positions (3 * num_nodes, meso; midpoint entries are ignored) and/or velocities. */
+int ffea_gpu_blob_set_state(ffea_gpu_blob *blob, const double *pos, const double *vel);
+
+/* Blob::make_measurements energies (src/Blob.cpp:1066-1125), meso units. */
+int ffea_gpu_blob_measure(ffea_gpu_blob *blob, double *strain_energy, double *kinetic_energy);
+
+/* CG iterations of the last step and in total (0 for masslumped). */
+int ffea_gpu_blob_cg_iterations(ffea_gpu_blob *blob, int *last, long long *total);
+
+/* Problem sizes: vertex nodes, elements, matrix 3x3 blocks. */
+int ffea_gpu_blob_sizes(ffea_gpu_blob *blob, int *num_linear_nodes, int *num_elements, long long *num_blocks);
+
+/* NoMass viscosity matrix in the reference's scalar CSR over all 3*num_nodes
+ * rows (SparsityPattern::create_sparse_matrix, src/SparsityPattern.cpp:69-110):
+ * key has 3*num_nodes+1 entries; col and val have *nnz entries. Call once
+ * with col == NULL to get *nnz. val holds the values of the last assembly;
+ * nsrc (may be NULL) the number of summed sources per entry. */
+int ffea_gpu_blob_get_pattern(ffea_gpu_blob *blob, int *key, int *col, double *val, int *nsrc, long long *nnz);
+
+/* Node -> (element*10 + slot) force-contribution lists in the reference's
+ * order (Blob::calculate_node_element_connectivity, src/Blob.cpp:3284-3314);
+ * ptr has num_nodes+1 entries. Call with elem_slot == NULL to get *count. */
+int ffea_gpu_blob_get_connectivity(ffea_gpu_blob *blob, int *ptr, int *elem_slot, long long *count);
+
+/* Per-element outputs of the last update_internal_forces: node forces of the
+ * four vertices (12 per element: node-major xyz, as tetra_element_linear::node_force[0..3]),
+ * volume, and the 12x12 viscosity matrix (144 per element, may be NULL). */
+int ffea_gpu_blob_get_elements(ffea_gpu_blob *blob, double *node_force12, double *vol, double *visc144);
+
+/* The assembled force vector of the last step (solver input, 3 * num_nodes, midpoints zero). */
+int ffea_gpu_blob_get_rhs(ffea_gpu_blob *blob, double *rhs);
+
+/* Last CUDA error text for FFEA_GPU_ECUDA (static storage). */
+const char *ffea_gpu_last_error(void);
+
+/* Kernel launches issued by this library since load (for benchmarking claims). */
+long long ffea_gpu_launch_count(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

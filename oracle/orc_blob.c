@@ -1046,7 +1046,9 @@ long long orc_blob_total_cg_iters(const orc_blob *b) { return b->total_iters; }
 void orc_blob_get_rng_state(const orc_blob *b, int t, uint32_t o[6]) { orc_rng_get_state(&b->rng[t], o); }
 void orc_blob_set_rng_state(orc_blob *b, int t, const uint32_t s[6]) { orc_rng_set_state(&b->rng[t], s); }
 
-/* Blob::make_measurements energies, src/Blob.cpp:1066-1125 (F_ij and vol from the last element pass) */
+/* Blob::make_measurements energies, src/Blob.cpp:1066-1125, of the current state: F_ij and the volume
+ * are recomputed from the current positions, which is what the reference measures when it next calls
+ * make_measurements (after the next update_internal_forces) */
 void orc_blob_measure(const orc_blob *b, double *strain, double *kinetic) {
     double ke = 0.0, se = 0.0;
     for (int e = 0; e < b->T; ++e) {
@@ -1064,9 +1066,18 @@ void orc_blob_measure(const orc_blob *b, double *strain, double *kinetic) {
             for (int i = 0; i < 12; ++i) s += v[i] * tmp[i];
             ke += s;
         }
+        double J[3][3], F[9] = {0};
+        elem_jacobian(b, e, J);
+        const double c1 = J[2][2] * J[1][1] - J[2][1] * J[1][2];
+        const double c2 = J[2][1] * J[0][2] - J[2][2] * J[0][1];
+        const double c3 = J[1][2] * J[0][1] - J[1][1] * J[0][2];
+        const double vol = (1.0 / 6.0) * fabs(J[0][0] * c1 + J[1][0] * c2 + J[2][0] * c3);
+        const double *Ji = b->jinv0 + 9 * (size_t)e;
+        for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j)
+                for (int k = 0; k < 3; ++k) F[3 * i + j] += J[k][i] * Ji[3 * j + k];
         const double C = b->E[e] - (2.0 / 3.0) * b->G[e];
-        const double t1 = b->vol[e] / b->vol0[e];
-        const double *F = b->F + 9 * (size_t)e;
+        const double t1 = vol / b->vol0[e];
         /* mat3_double_contraction, src/mat_vec_fns.cpp:116-120 (its term order) */
         const double ff = F[0] * F[0] + F[4] * F[4] + F[8] * F[8] + F[1] * F[1] + F[3] * F[3] + F[2] * F[2] +
                           F[6] * F[6] + F[5] * F[5] + F[7] * F[7];

@@ -395,6 +395,12 @@ void ref_blob_measure(void *h, double *strain, double *kinetic) {
                        el.n[2]->vel[1] * vec[6] + el.n[3]->vel[1] * vec[7] + el.n[0]->vel[2] * vec[8] +
                        el.n[1]->vel[2] * vec[9] + el.n[2]->vel[2] * vec[10] + el.n[3]->vel[2] * vec[11];
         }
+        // energies of the current state: F_ij and vol from the current positions (the values the
+        // reference's make_measurements sees after its next update_internal_forces)
+        matrix3 J;
+        el.calculate_jacobian(J);
+        el.calc_deformation(J);
+        el.calc_volume();
         const scalar C = el.E - (2.0 / 3.0) * el.G;
         const scalar temp1 = el.vol / el.vol_0;
         senergy += el.vol_0 * (el.G * (mat3_double_contraction(el.F_ij) - 3) + 0.5 * C * (temp1 * temp1 - 1) -

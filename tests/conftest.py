@@ -20,3 +20,12 @@ def oracle_built():
 
     pyoracle.build()
     return True
+
+
+@pytest.fixture(scope="session")
+def gpu():
+    """Build (if stale) and load the CUDA library; GPU tests need a GB300."""
+    from ffea_ci_demo_gb300 import build, lib
+
+    build.build()
+    return lib.load()

@@ -1,0 +1,205 @@
+"""GPU parity: the CUDA path through the C ABI against the reference.
+
+Reference results come from tests/golden/*.npz (produced by the reference's
+own compiled classes) and from the oracle (oracle/orc_*.c, pinned bit-exact
+to those goldens by tests/test_oracle.py), run on the same seeded inputs.
+
+Tolerances:
+* integer structure (pattern, connectivity, RNG states): bit-exact.
+* FP64 path, per-element forces / volumes / assembled matrix values /
+  right-hand side: bit-exact (same expression order, no FMA).
+* FP64 path, trajectories through the CG: the CG's cross-node dot products
+  are reduced in a different order than the reference's sequential loop, so
+  positions agree to rounding: max |x_gpu - x_ref| <= 1e-8 * max |x_ref - x_0|.
+* mass-lumped FP64 trajectories (no reductions at all): bit-exact.
+* mixed path, kT = 0: max |x_mixed - x_ref| <= 1e-5 * max |x_ref - x_0| after 1000 steps.
+"""
+import os
+import tempfile
+
+import numpy as np
+import pytest
+
+import pyoracle as po
+from ffea_ci_demo_gb300 import lib
+from ffea_ci_demo_gb300.mesh import write_structure
+from gen_golden import case_mesh, sheared
+
+pytestmark = pytest.mark.gpu
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def load(name):
+    return np.load(os.path.join(GOLD, name + ".npz"))
+
+
+def gpu_blob(m, strain, **kw):
+    b = lib.Blob(m, **kw)
+    b.set_state(pos=sheared(m, strain))
+    return b
+
+
+def disp_err(x, ref, x0):
+    return float(np.abs(x - ref).max() / np.abs(ref - x0).max())
+
+
+def test_pattern_and_connectivity_bit_exact(gpu):
+    g = load("cube2_nomass_kT0")
+    b = gpu_blob(case_mesh(2, 11), 0.02, solver="CG_nomass", kT=0.0, calc_noise=0)
+    pat = b.pattern(values=False)
+    for k in ("key", "col", "nsrc"):
+        assert np.array_equal(pat[k], g["csr_" + k]), k
+    c = b.connectivity()
+    assert np.array_equal(c["ptr"], g["contrib_ptr"]) and np.array_equal(c["elem_slot"], g["contrib_es"])
+    # pinned vertex + pinned midpoint + Stokes drag sources on the diagonal
+    g3 = load("cube3_nomass_pin_stokes")
+    b3 = gpu_blob(case_mesh(3, 7, [0, 1, 5, 66]), 0.02, solver="CG_nomass", kT=0.0, calc_noise=0, calc_stokes=1)
+    pat3 = b3.pattern(values=False)
+    for k in ("key", "col", "nsrc"):
+        assert np.array_equal(pat3[k], g3["csr_" + k]), k
+
+
+@pytest.mark.parametrize("name,kw", [
+    ("cube2_nomass_kT0", dict(kT=0.0, calc_noise=0)),
+    ("cube2_nomass_noise", dict(kT=4.11e-21, calc_noise=1)),
+])
+def test_fp64_step_bit_exact(gpu, name, kw):
+    g = load(name)
+    m = case_mesh(2, 11)
+    b = gpu_blob(m, 0.02, solver="CG_nomass", dt=1e-12, **kw)
+    b.update(1)
+    e = b.elements(visc=True)
+    assert np.array_equal(e["node_force"], g["step1_node_force"])
+    assert np.array_equal(e["vol"], g["step1_vol"])
+    assert np.array_equal(e["visc"], g["step1_visc"])
+    assert np.array_equal(b.rhs(), g["step1_rhs"])
+    assert np.array_equal(b.pattern()["val"], g["step1_csr_val"])
+    x0 = sheared(m, 0.02)
+    assert disp_err(b.pos(), g["step1_pos"], x0) < 1e-10
+    steps = int(g["steps"])
+    b.update(steps - 1)
+    assert disp_err(b.pos(), g["final_pos"], x0) < 1e-8
+    assert np.array_equal(b.rng_state(), g["final_rng"])
+
+
+@pytest.mark.parametrize("name,strain,kw", [
+    ("cube6_masslumped_kT0_1000", 0.02, dict(solver="masslumped", dt=1e-14, kT=0.0, calc_noise=0)),
+    ("cube6_masslumped_noise_1000", 0.0, dict(solver="masslumped", dt=1e-14, kT=4.11e-21, calc_noise=1)),
+])
+def test_masslumped_1000_steps_bit_exact(gpu, name, strain, kw):
+    g = load(name)
+    m = case_mesh(6, 12345)
+    b = gpu_blob(m, strain, **kw)
+    b.update(1)
+    assert np.array_equal(b.rhs(), g["step1_rhs"])
+    b.update(int(g["steps"]) - 1)
+    assert np.array_equal(b.pos(), g["final_pos"])
+    assert np.array_equal(b.vel(), g["final_vel"])
+    assert np.array_equal(b.rng_state(), g["final_rng"])
+    np.testing.assert_allclose(b.measure(), g["final_energy"], rtol=1e-12)
+
+
+@pytest.mark.parametrize("name,strain,kw,tol", [
+    ("cube6_nomass_kT0_1000", 0.02, dict(solver="CG_nomass", dt=1e-12, kT=0.0, calc_noise=0), 1e-8),
+    ("cube6_nomass_noise_100", 0.0, dict(solver="CG_nomass", dt=1e-12, kT=4.11e-21, calc_noise=1), 1e-8),
+    ("cube6_CG_kT0_1000", 0.02, dict(solver="CG", dt=1e-14, kT=0.0, calc_noise=0), 1e-8),
+    ("cube6_CG_noise_1000", 0.0, dict(solver="CG", dt=1e-14, kT=4.11e-21, calc_noise=1), 1e-8),
+])
+def test_fp64_trajectories_match_reference(gpu, name, strain, kw, tol):
+    g = load(name)
+    m = case_mesh(6, 12345)
+    b = gpu_blob(m, strain, **kw)
+    b.update(1)
+    assert np.array_equal(b.rhs(), g["step1_rhs"])
+    b.update(int(g["steps"]) - 1)
+    x0 = sheared(m, strain)
+    assert disp_err(b.pos(), g["final_pos"], x0) < tol
+    assert np.array_equal(b.rng_state(), g["final_rng"])
+    np.testing.assert_allclose(b.measure(), g["final_energy"], rtol=1e-6)
+
+
+def test_mixed_precision_kT0_error_bound(gpu):
+    """Mixed path after 1000 kT=0 steps within 1e-5 of the reference displacement."""
+    g = load("cube6_nomass_kT0_1000")
+    m = case_mesh(6, 12345)
+    b = gpu_blob(m, 0.02, solver="CG_nomass", precision="mixed", dt=1e-12, kT=0.0, calc_noise=0)
+    b.update(1000)
+    err = disp_err(b.pos(), g["final_pos"], sheared(m, 0.02))
+    print("mixed kT=0 1000-step displacement error", err)
+    assert err < 1e-5
+
+
+def test_pinned_nodes_and_stokes_drag_match_oracle(gpu, oracle_built):
+    m = case_mesh(3, 7, [0, 1, 5, 66])
+    kw = dict(solver="CG_nomass", dt=1e-12, kT=0.0, calc_noise=0, calc_stokes=1)
+    o = po.OracleBlob(m, threads=1, **kw)
+    o.set_pos(sheared(m, 0.02))
+    b = gpu_blob(m, 0.02, **kw)
+    assert o.step(1) == 0
+    b.update(1)
+    assert np.array_equal(b.rhs(), o.rhs())
+    assert np.array_equal(b.pattern()["val"], o.csr()["val"])
+    assert o.step(9) == 0
+    b.update(9)
+    assert disp_err(b.pos(), o.pos(), sheared(m, 0.02)) < 1e-8
+    p = b.pos()
+    assert np.array_equal(p[[0, 1, 5]], sheared(m, 0.02)[[0, 1, 5]])  # pinned vertices never move
+
+
+def test_structure_files_load_like_arrays(gpu):
+    m = case_mesh(2, 11)
+    with tempfile.TemporaryDirectory() as d:
+        paths = write_structure(m, d, "cube2")
+        bf = lib.Blob.from_files(paths["node"], paths["top"], paths["mat"], paths["stokes"], paths["pin"], m.scale,
+                                 solver="CG_nomass", dt=1e-12, kT=4.11e-21, epsilon=1e-10, calc_noise=1,
+                                 calc_stokes=0, max_iterations_cg=10000)
+    ba = lib.Blob(m, solver="CG_nomass", dt=1e-12, kT=4.11e-21, calc_noise=1)
+    bf.update(5)
+    ba.update(5)
+    assert np.array_equal(bf.pos(), ba.pos())
+
+
+def test_deterministic_rerun(gpu):
+    m = case_mesh(4, 5)
+    out = []
+    for _ in range(2):
+        b = gpu_blob(m, 0.01, solver="CG_nomass", kT=4.11e-21, calc_noise=1)
+        b.update(10)
+        out.append(b.pos())
+    assert np.array_equal(out[0], out[1])
+
+
+def test_inversion_is_reported(gpu):
+    m = case_mesh(2, 11)
+    p = sheared(m, 0.0)
+    t = m.tets[0]
+    p[t[3]] = p[t[0]] - (p[t[3]] - p[t[0]])
+    b = lib.Blob(m, solver="CG_nomass", kT=0.0, calc_noise=0)
+    b.set_state(pos=p)
+    rc, done = b.try_update(3)
+    assert rc == lib.EINVERTED and done == 0
+
+
+def test_cg_max_iterations_is_reported(gpu):
+    m = case_mesh(2, 11)
+    b = gpu_blob(m, 0.02, solver="CG_nomass", kT=0.0, calc_noise=0, max_iterations_cg=2)
+    rc, done = b.try_update(1)
+    assert rc == lib.ECGMAXIT and done == 0
+    with pytest.raises(lib.FFEAError):
+        b.update(1)
+
+
+def test_larger_cube_fp64_matches_oracle(gpu, oracle_built):
+    """A 10^3-cell cube (6000 tets): one step bit-exact forces, 5 steps to CG rounding."""
+    m = case_mesh(10, 99)
+    kw = dict(solver="CG_nomass", dt=1e-12, kT=4.11e-21, calc_noise=1)
+    o = po.OracleBlob(m, threads=1, **kw)
+    o.set_pos(sheared(m, 0.01))
+    b = gpu_blob(m, 0.01, **kw)
+    assert o.step(1) == 0
+    b.update(1)
+    assert np.array_equal(b.rhs(), o.rhs())
+    assert o.step(4) == 0
+    b.update(4)
+    assert disp_err(b.pos(), o.pos(), sheared(m, 0.01)) < 1e-8
+    assert np.array_equal(b.rng_state(), o.rng_state())
