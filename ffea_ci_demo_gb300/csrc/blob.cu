@@ -22,7 +22,10 @@
 #include <vector>
 
 #include "../../include/ffea_gpu.h"
+#include <type_traits>
+
 #include "engine.h"
+#include "kernels_mixed.cuh"
 
 namespace ffea {
 long long launch_count();
@@ -403,6 +406,70 @@ std::vector<R> cast_vec(const std::vector<double> &v) {
     return std::vector<R>(v.begin(), v.end());
 }
 
+// Rigid motions v_a = t + omega x (x_a - x_c) that leave every pinned vertex at rest: the null
+// space of the viscosity matrix when there is no Stokes drag (mixed-path CG deflation). Returns the
+// mode coefficients (t, omega) row-wise in modes[6*k..6*k+5].
+int rigid_modes(const HostModel &h, const ffea_gpu_params &p, double xc[3], double modes[36]) {
+    xc[0] = xc[1] = xc[2] = 0.0;
+    for (int a = 0; a < h.N; ++a)
+        for (int c = 0; c < 3; ++c) xc[c] += h.pos[3 * (size_t)a + c];
+    for (int c = 0; c < 3; ++c) xc[c] /= std::max(h.N, 1);
+    if (p.calc_stokes == 1) return 0;
+    // M = sum over pinned vertices of C^T C, C = [I | -[d]x]
+    double M[6][6] = {};
+    int npin = 0;
+    for (int a = 0; a < h.N; ++a) {
+        if (!h.pinned[a]) continue;
+        ++npin;
+        const double d[3] = {h.pos[3 * (size_t)a] - xc[0], h.pos[3 * (size_t)a + 1] - xc[1],
+                             h.pos[3 * (size_t)a + 2] - xc[2]};
+        double C[3][6] = {{1, 0, 0, 0, d[2], -d[1]}, {0, 1, 0, -d[2], 0, d[0]}, {0, 0, 1, d[1], -d[0], 0}};
+        for (int i = 0; i < 6; ++i)
+            for (int j = 0; j < 6; ++j)
+                for (int k = 0; k < 3; ++k) M[i][j] += C[k][i] * C[k][j];
+    }
+    double V[6][6] = {};
+    for (int i = 0; i < 6; ++i) V[i][i] = 1.0;
+    if (npin > 0) {  // cyclic Jacobi eigen-decomposition of the 6x6 symmetric M
+        for (int sweep = 0; sweep < 100; ++sweep) {
+            double off = 0.0;
+            for (int i = 0; i < 6; ++i)
+                for (int j = i + 1; j < 6; ++j) off += M[i][j] * M[i][j];
+            if (off < 1e-30) break;
+            for (int i = 0; i < 6; ++i)
+                for (int j = i + 1; j < 6; ++j) {
+                    if (fabs(M[i][j]) < 1e-300) continue;
+                    const double th = 0.5 * atan2(2 * M[i][j], M[j][j] - M[i][i]);
+                    const double c = cos(th), sn = sin(th);
+                    for (int k = 0; k < 6; ++k) {
+                        const double a = M[k][i], b = M[k][j];
+                        M[k][i] = c * a - sn * b;
+                        M[k][j] = sn * a + c * b;
+                    }
+                    for (int k = 0; k < 6; ++k) {
+                        const double a = M[i][k], b = M[j][k];
+                        M[i][k] = c * a - sn * b;
+                        M[j][k] = sn * a + c * b;
+                    }
+                    for (int k = 0; k < 6; ++k) {
+                        const double a = V[k][i], b = V[k][j];
+                        V[k][i] = c * a - sn * b;
+                        V[k][j] = sn * a + c * b;
+                    }
+                }
+        }
+    }
+    double emax = 0.0;
+    for (int i = 0; i < 6; ++i) emax = std::max(emax, fabs(M[i][i]));
+    int k = 0;
+    for (int i = 0; i < 6; ++i) {
+        if (npin > 0 && fabs(M[i][i]) > 1e-9 * std::max(emax, 1.0)) continue;
+        for (int j = 0; j < 6; ++j) modes[6 * k + j] = V[j][i];
+        ++k;
+    }
+    return k;
+}
+
 // V[r][c] of the element viscosity matrix, same evaluation as the device's visc_entry
 double host_visc_entry(const double *dpsi, double A, double B, double vol, int r, int c) {
     if (r > c) std::swap(r, c);
@@ -465,6 +532,10 @@ struct BlobImpl final : ffea_gpu_blob {
     DevStatus *st;
     GridBarrier *gb;
     int cg_grid = 0, gather_blocks = 0, partial_stride = 0;
+    double *r64 = nullptr;   // mixed path: FP64 CG residual
+    float4 *dpos = nullptr;  // mixed path: node offsets from the rest centroid
+    int nmodes = 0;
+    double modes[36] = {}, xc[3] = {};
     cudaEvent_t ev[FFEA_GPU_NUM_PHASES + 1] = {};
     bool record_phases = false;
     double *staging = nullptr;  // pinned host buffer, 3*N doubles, for state copies
@@ -558,7 +629,13 @@ struct BlobImpl final : ffea_gpu_blob {
         CK(mem.alloc(&q, 4 * (size_t)N));
         const int gthreads = Launch<R>::gather_threads();
         gather_blocks = (N + gthreads - 1) / gthreads;
-        CK(mem.alloc(&init_partials, 2 * (size_t)gather_blocks));
+        constexpr bool mixed = std::is_same<R, float>::value;
+        CK(mem.alloc(&init_partials, (mixed ? MIXED_GATHER_NP : 2) * (size_t)gather_blocks));
+        if (mixed) {
+            CK(mem.alloc(&r64, 4 * (size_t)N));
+            CK(mem.alloc(&dpos, (size_t)N));
+            nmodes = rigid_modes(h, p, xc, modes);
+        }
         const int maxg = Launch<R>::cg_max_grid(device);
         if (maxg <= 0) {
             g_last_error = "cg kernel cannot be made resident";
@@ -566,7 +643,7 @@ struct BlobImpl final : ffea_gpu_blob {
         }
         cg_grid = std::max(1, std::min(maxg, (N + Launch<R>::cg_threads() - 1) / Launch<R>::cg_threads()));
         partial_stride = cg_grid;
-        CK(mem.alloc(&partials, 3 * (size_t)partial_stride));
+        CK(mem.alloc(&partials, (mixed ? MIXED_A_NP + 2 : 3) * (size_t)partial_stride));
         CK(mem.alloc(&st, 1));
         CK(mem.alloc(&gb, 1));
         // RNG jump tables: draws of element e start 7e after the step's state; a step consumes 7T
@@ -583,7 +660,8 @@ struct BlobImpl final : ffea_gpu_blob {
         for (int l = 0; l < 32; ++l) lj[l] = jump_pow(7ull * l);
         CK(mem.upload(&chunk_jump, cj));
         CK(mem.upload(&lane_jump, lj));
-        std::vector<MrgJump> sj(1, jump_pow(7ull * (uint64_t)T));
+        // a step consumes 7 draws per element when noise is on, none otherwise
+        std::vector<MrgJump> sj(1, jump_pow(p.calc_noise == 1 ? 7ull * (uint64_t)T : 0ull));
         CK(mem.upload(&step_jump, sj));
         std::vector<uint32_t> rs(rng_host, rng_host + 6);
         CK(mem.upload(&rng_state, rs));
@@ -634,6 +712,8 @@ struct BlobImpl final : ffea_gpu_blob {
         ga.vx = vx; ga.vy = vy; ga.vz = vz;
         ga.dinv = dinv; ga.f = f; ga.x = x; ga.r = r; ga.p = pv;
         ga.partials = init_partials; ga.stride = gather_blocks; ga.st = st;
+        ga.r64 = r64; ga.dpos = dpos; ga.px = px; ga.py = py; ga.pz = pz;
+        ga.xc[0] = xc[0]; ga.xc[1] = xc[1]; ga.xc[2] = xc[2];
         CK(Launch<R>::gather(ga, gather_blocks, stream));
         if ((rc = mark(3))) return rc;
         if (p.solver != FFEA_GPU_MASSLUMPED) {
@@ -650,6 +730,8 @@ struct BlobImpl final : ffea_gpu_blob {
             ca.imax = p.max_iterations_cg;
             ca.eps2 = p.epsilon2;
             ca.limit_ns = 2000000000ull;
+            ca.r64 = r64; ca.dpos = dpos; ca.nmodes = nomass ? nmodes : 0;
+            for (int i = 0; i < 36; ++i) ca.modes[i] = modes[i];
             CK(Launch<R>::cg(ca, cg_grid, stream));
         }
         if ((rc = mark(4))) return rc;

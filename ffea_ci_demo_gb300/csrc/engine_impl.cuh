@@ -2,7 +2,10 @@
 // translation unit per arithmetic type (engine_fp64.cu, engine_mixed.cu).
 #pragma once
 
+#include <type_traits>
+
 #include "engine.h"
+#include "kernels_mixed.cuh"
 
 namespace ffea {
 
@@ -33,7 +36,8 @@ int Launch<R>::gather_threads() { return GATHER_THREADS; }
 
 template <class R>
 cudaError_t Launch<R>::gather(const GatherArgs<R> &a, int blocks, cudaStream_t s) {
-    gather_kernel<R><<<blocks, GATHER_THREADS, 0, s>>>(a);
+    if constexpr (std::is_same<R, float>::value) gather_mixed_kernel<R><<<blocks, GATHER_THREADS, 0, s>>>(a);
+    else gather_kernel<R><<<blocks, GATHER_THREADS, 0, s>>>(a);
     count_launch();
     return cudaGetLastError();
 }
@@ -45,7 +49,12 @@ template <class R>
 int Launch<R>::cg_max_grid(int device) {
     int nsm = 0, per_sm = 0;
     if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) return 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, cg_kernel<R>, CG_THREADS, 0) != cudaSuccess) return 0;
+    cudaError_t e;
+    if constexpr (std::is_same<R, float>::value)
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, cg_mixed_kernel<R>, CG_THREADS, 0);
+    else
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, cg_kernel<R>, CG_THREADS, 0);
+    if (e != cudaSuccess) return 0;
     return nsm * per_sm;
 }
 
@@ -53,7 +62,10 @@ template <class R>
 cudaError_t Launch<R>::cg(const CgArgs<R> &a, int grid, cudaStream_t s) {
     CgArgs<R> args = a;
     void *params[] = {&args};
-    cudaError_t e = cudaLaunchCooperativeKernel((const void *)cg_kernel<R>, dim3(grid), dim3(CG_THREADS), params, 0, s);
+    const void *fn;
+    if constexpr (std::is_same<R, float>::value) fn = (const void *)cg_mixed_kernel<R>;
+    else fn = (const void *)cg_kernel<R>;
+    cudaError_t e = cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(CG_THREADS), params, 0, s);
     count_launch();
     return e;
 }

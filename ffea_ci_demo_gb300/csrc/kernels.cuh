@@ -294,9 +294,14 @@ struct GatherArgs {
     const R *dinv;        // Jacobi preconditioner (CG) or inverse lumped mass (mode 1)
     double *f;            // 4*N assembled force (solver input)
     R *x, *r, *p;
-    double *partials;     // [0]: f.f, [stride]: r.z per block
+    double *partials;     // [0]: f.f, [stride]: r.z per block (mixed path: 16 moments per block)
     int stride;
     DevStatus *st;
+    // mixed path only: FP64 residual, node offsets from the rest centroid, positions
+    double *r64;
+    float4 *dpos;
+    const double *px, *py, *pz;
+    double xc[3];
 };
 
 template <class R>
@@ -367,6 +372,11 @@ struct CgArgs {
     int imax;
     double eps2;
     unsigned long long limit_ns;
+    // mixed path only: FP64 residual, node offsets, rigid-mode coefficients (t, omega) per mode
+    double *r64;
+    const float4 *dpos;
+    int nmodes;
+    double modes[36];
 };
 
 template <class R>

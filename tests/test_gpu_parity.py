@@ -129,6 +129,37 @@ def test_mixed_precision_kT0_error_bound(gpu):
     assert err < 1e-5
 
 
+@pytest.mark.parametrize("kw", [
+    dict(kT=4.11e-21, calc_noise=1),
+    dict(kT=0.0, calc_noise=0, calc_stokes=1),
+])
+def test_mixed_precision_iterations_and_error(gpu, kw):
+    """Mixed CG (FP32 matrix, deflated rigid modes) needs the FP64 path's iteration count."""
+    m = case_mesh(8, 21)
+    out = {}
+    for prec in ("fp64", "mixed"):
+        b = gpu_blob(m, 0.02, solver="CG_nomass", precision=prec, dt=1e-12, **kw)
+        its = []
+        for _ in range(5):
+            b.update(1)
+            its.append(b.cg_iterations()[0])
+        out[prec] = (its, b.pos())
+    assert all(abs(a - b) <= 2 for a, b in zip(out["fp64"][0], out["mixed"][0])), out
+    assert disp_err(out["mixed"][1], out["fp64"][1], sheared(m, 0.02)) < 1e-5
+
+
+def test_mixed_precision_pinned_nodes(gpu):
+    """With pinned vertices the deflated modes are the rigid motions that keep them at rest."""
+    for pins in ([0], [0, 1], [0, 1, 5]):
+        m = case_mesh(4, 3, pins)
+        res = {}
+        for prec in ("fp64", "mixed"):
+            b = gpu_blob(m, 0.02, solver="CG_nomass", precision=prec, kT=0.0, calc_noise=0)
+            b.update(20)
+            res[prec] = b.pos()
+        assert disp_err(res["mixed"], res["fp64"], sheared(m, 0.02)) < 1e-5, pins
+
+
 def test_pinned_nodes_and_stokes_drag_match_oracle(gpu, oracle_built):
     m = case_mesh(3, 7, [0, 1, 5, 66])
     kw = dict(solver="CG_nomass", dt=1e-12, kT=0.0, calc_noise=0, calc_stokes=1)
