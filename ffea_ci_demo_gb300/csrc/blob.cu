@@ -15,6 +15,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <memory>
 #include <new>
@@ -504,6 +505,7 @@ struct ffea_gpu_blob {
     virtual int cg_iters(int *last, long long *total) = 0;
     virtual int get_elements(double *nf, double *vol, double *visc) = 0;
     virtual int get_rhs(double *rhs) = 0;
+    virtual int cg_history(double *res2, int max_entries, int *count) = 0;
     virtual int get_matrix_values(std::vector<double> &val_sell) = 0;
 };
 
@@ -536,6 +538,8 @@ struct BlobImpl final : ffea_gpu_blob {
     float4 *dpos = nullptr;  // mixed path: node offsets from the rest centroid
     int nmodes = 0;
     double modes[36] = {}, xc[3] = {};
+    double *history = nullptr;
+    int hist_cap = 0, debug = 0;
     cudaEvent_t ev[FFEA_GPU_NUM_PHASES + 1] = {};
     bool record_phases = false;
     double *staging = nullptr;  // pinned host buffer, 3*N doubles, for state copies
@@ -643,8 +647,11 @@ struct BlobImpl final : ffea_gpu_blob {
         }
         cg_grid = std::max(1, std::min(maxg, (N + Launch<R>::cg_threads() - 1) / Launch<R>::cg_threads()));
         partial_stride = cg_grid;
-        CK(mem.alloc(&partials, (mixed ? MIXED_A_NP + 2 : 3) * (size_t)partial_stride));
+        CK(mem.alloc(&partials, (mixed ? MIXED_PARTIAL_ROWS : 3) * (size_t)partial_stride));
+        if (const char *dbg = getenv("FFEA_GPU_DEBUG")) debug = atoi(dbg);
         CK(mem.alloc(&st, 1));
+        hist_cap = std::min(std::max(p.max_iterations_cg, 1), 1 << 20);
+        CK(mem.alloc(&history, (size_t)hist_cap));
         CK(mem.alloc(&gb, 1));
         // RNG jump tables: draws of element e start 7e after the step's state; a step consumes 7T
         const int nchunks = (T + 31) / 32;
@@ -730,6 +737,7 @@ struct BlobImpl final : ffea_gpu_blob {
             ca.imax = p.max_iterations_cg;
             ca.eps2 = p.epsilon2;
             ca.limit_ns = 2000000000ull;
+            ca.history = history; ca.hist_cap = hist_cap; ca.debug = debug;
             ca.r64 = r64; ca.dpos = dpos; ca.nmodes = nomass ? nmodes : 0;
             for (int i = 0; i < 36; ++i) ca.modes[i] = modes[i];
             CK(Launch<R>::cg(ca, cg_grid, stream));
@@ -917,6 +925,19 @@ struct BlobImpl final : ffea_gpu_blob {
                         visc[144 * (size_t)e + 12 * rr + cc] =
                             host_visc_entry(d, (double)(R)h.A[e], (double)(R)h.B[e], v, rr, cc);
             }
+        return FFEA_GPU_OK;
+    }
+
+    int cg_history(double *res2, int max_entries, int *count) override {
+        DevStatus s{};
+        int rc = read_status(s);
+        if (rc) return rc;
+        const int n = std::max(0, std::min({s.last_iters, hist_cap, max_entries}));
+        if (n > 0 && res2) {
+            CK(cudaMemcpyAsync(res2, history, n * sizeof(double), cudaMemcpyDeviceToHost, stream));
+            CK(cudaStreamSynchronize(stream));
+        }
+        if (count) *count = n;
         return FFEA_GPU_OK;
     }
 
@@ -1113,6 +1134,11 @@ int ffea_gpu_blob_measure(ffea_gpu_blob *b, double *se, double *ke) {
 int ffea_gpu_blob_cg_iterations(ffea_gpu_blob *b, int *last, long long *total) {
     if (!b) return FFEA_GPU_EINPUT;
     return b->cg_iters(last, total);
+}
+
+int ffea_gpu_blob_cg_history(ffea_gpu_blob *b, double *res2, int max_entries, int *count) {
+    if (!b || max_entries < 0) return FFEA_GPU_EINPUT;
+    return b->cg_history(res2, max_entries, count);
 }
 
 int ffea_gpu_blob_sizes(ffea_gpu_blob *b, int *nl, int *ne, long long *nb) {

@@ -372,6 +372,9 @@ struct CgArgs {
     int imax;
     double eps2;
     unsigned long long limit_ns;
+    double *history;      // res2 per iteration (block 0 writes), capacity hist_cap
+    int hist_cap;
+    int debug;            // diagnostics (mixed path): bit 1 records the rigid-mode content of r instead of |r|^2
     // mixed path only: FP64 residual, node offsets, rigid-mode coefficients (t, omega) per mode
     double *r64;
     const float4 *dpos;
@@ -460,6 +463,7 @@ __global__ void __launch_bounds__(512) cg_kernel(CgArgs<R> g) {
         double rz[2];
         grid_partials_sum<2>(g.partials + g.stride, g.stride, gridDim.x, rz, smem);
         const double res2 = (f2 == 0.0) ? 0.0 : rz[0] / f2;
+        if (blockIdx.x == 0 && threadIdx.x == 0 && it < g.hist_cap) g.history[it] = res2;
         if ((g.check_last || it + 1 < g.imax) && res2 < g.eps2) {
             converged = true;
             ++it;

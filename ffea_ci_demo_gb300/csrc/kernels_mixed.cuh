@@ -23,6 +23,11 @@ namespace ffea {
 
 constexpr int MIXED_GATHER_NP = 16;  // f.f, S1_f(3), S2_f(3), sum d(3), inertia(6)
 constexpr int MIXED_A_NP = 13;       // p.q, S1_q(3), S2_q(3), S1_p(3), S2_p(3)
+constexpr int MIXED_B_NP = 8;        // r.r, r.z, and (diagnostics) S1_r(3), S2_r(3)
+// partials rows: [0, A) phase A, [A, A+B) phase B, A+B the initial r.z. Each row is written in one phase
+// and read right after the next grid barrier; no row is written again before every block has passed
+// the barrier that follows its read.
+constexpr int MIXED_PARTIAL_ROWS = MIXED_A_NP + MIXED_B_NP + 1;
 
 // mixed-path gather: f (FP64) and r = f; per-node offsets d; projection moments
 template <class R>
@@ -170,12 +175,13 @@ __global__ void __launch_bounds__(512) cg_mixed_kernel(CgArgs<R> g) {
         acc0[0] += r0 * z0 + r1 * z1 + r2 * z2;
     }
     block_sum<1>(acc0, smem);
-    if (threadIdx.x == 0) g.partials[blockIdx.x] = acc0[0];
+    const int row0 = MIXED_A_NP + MIXED_B_NP;
+    if (threadIdx.x == 0) g.partials[row0 * g.stride + blockIdx.x] = acc0[0];
     bool ok = grid_sync(g.gb, st, g.limit_ns);
     double delta = 0.0;
     if (ok) {
         double d0[1];
-        grid_partials_sum<1>(g.partials, 0, gridDim.x, d0, smem);
+        grid_partials_sum<1>(g.partials + row0 * g.stride, 0, gridDim.x, d0, smem);
         delta = d0[0];
     }
     int it = 0;
@@ -229,7 +235,7 @@ __global__ void __launch_bounds__(512) cg_mixed_kernel(CgArgs<R> g) {
         const float af = (float)alpha;
         const double t0 = s_tau[0], t1 = s_tau[1], t2 = s_tau[2], O0 = s_Om[0], O1 = s_Om[1], O2 = s_Om[2];
         // phase B: x += alpha p ; r -= alpha (q - tau - Omega x d) ; r.r ; r.z
-        double acc2[2] = {0.0, 0.0};
+        double acc2[MIXED_B_NP] = {0, 0, 0, 0, 0, 0, 0, 0};
         for (int a = tid; a < g.N; a += nthr) {
 #pragma unroll
             for (int c = 0; c < 3; ++c) g.x[4 * a + c] += af * g.p[4 * a + c];
@@ -248,16 +254,32 @@ __global__ void __launch_bounds__(512) cg_mixed_kernel(CgArgs<R> g) {
                          z2 = (double)g.dinv[4 * a + 2] * r2;
             acc2[0] += r0 * r0 + r1 * r1 + r2 * r2;
             acc2[1] += r0 * z0 + r1 * z1 + r2 * z2;
+            if (g.debug & 2) {
+                const float4 d = g.dpos[a];
+                const double e0 = d.x, e1 = d.y, e2 = d.z;
+                acc2[2] += r0; acc2[3] += r1; acc2[4] += r2;
+                acc2[5] += e1 * r2 - e2 * r1; acc2[6] += e2 * r0 - e0 * r2; acc2[7] += e0 * r1 - e1 * r0;
+            }
         }
-        block_sum<2>(acc2, smem);
-        if (threadIdx.x == 0) {
-            g.partials[MIXED_A_NP * g.stride + blockIdx.x] = acc2[0];
-            g.partials[(MIXED_A_NP + 1) * g.stride + blockIdx.x] = acc2[1];
-        }
+        block_sum<MIXED_B_NP>(acc2, smem);
+        if (threadIdx.x == 0)
+            for (int i = 0; i < MIXED_B_NP; ++i) g.partials[(MIXED_A_NP + i) * g.stride + blockIdx.x] = acc2[i];
         if (!(ok = grid_sync(g.gb, st, g.limit_ns))) break;
-        double rz[2];
-        grid_partials_sum<2>(g.partials + MIXED_A_NP * g.stride, g.stride, gridDim.x, rz, smem);
+        double rz[MIXED_B_NP];
+        grid_partials_sum<MIXED_B_NP>(g.partials + MIXED_A_NP * g.stride, g.stride, gridDim.x, rz, smem);
         const double res2 = (f2 == 0.0) ? 0.0 : rz[0] / f2;
+        if ((g.debug & 2) && blockIdx.x == 0 && threadIdx.x == 0 && it < g.hist_cap && defl) {
+            double c[6], tau[3], Om[3];
+            const double S1r[3] = {rz[2], rz[3], rz[4]}, S2r[3] = {rz[5], rz[6], rz[7]};
+            mode_coeffs(g, s_Ginv, S1r, S2r, c, tau, Om);
+            double v = 0.0;  // (Z^T r)^T G^-1 (Z^T r) / f2
+            for (int k = 0; k < g.nmodes; ++k) {
+                const double *m = g.modes + 6 * k;
+                v += c[k] * (m[0] * S1r[0] + m[1] * S1r[1] + m[2] * S1r[2] + m[3] * S2r[0] + m[4] * S2r[1] + m[5] * S2r[2]);
+            }
+            g.history[it] = v / f2;  // replaces res2 in the history when debugging
+        }
+        if (blockIdx.x == 0 && threadIdx.x == 0 && it < g.hist_cap && !(g.debug & 2)) g.history[it] = res2;
         if ((g.check_last || it + 1 < g.imax) && res2 < g.eps2) {
             converged = true;
             ++it;

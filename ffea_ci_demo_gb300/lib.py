@@ -89,6 +89,7 @@ def load():
         "ffea_gpu_blob_measure": (C.c_int, [vp, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
         "ffea_gpu_blob_cg_iterations": (C.c_int, [vp, ip, C.POINTER(C.c_longlong)]),
         "ffea_gpu_blob_sizes": (C.c_int, [vp, ip, ip, C.POINTER(C.c_longlong)]),
+        "ffea_gpu_blob_cg_history": (C.c_int, [vp, dp, C.c_int, ip]),
         "ffea_gpu_blob_get_pattern": (C.c_int, [vp, dp, dp, dp, dp, C.POINTER(C.c_longlong)]),
         "ffea_gpu_blob_get_connectivity": (C.c_int, [vp, dp, dp, C.POINTER(C.c_longlong)]),
         "ffea_gpu_blob_get_elements": (C.c_int, [vp, dp, dp, dp]),
@@ -263,6 +264,13 @@ class Blob:
         last, total = C.c_int(), C.c_longlong()
         _check(self._lib.ffea_gpu_blob_cg_iterations(self._h, C.byref(last), C.byref(total)), "cg_iterations")
         return last.value, total.value
+
+    def cg_history(self, max_entries: int = 100000) -> np.ndarray:
+        """|r|^2/|f|^2 after each CG iteration of the last solve."""
+        buf = np.empty(max_entries)
+        n = C.c_int()
+        _check(self._lib.ffea_gpu_blob_cg_history(self._h, _p(buf), max_entries, C.byref(n)), "cg_history")
+        return buf[:n.value].copy()
 
     def sizes(self) -> tuple[int, int, int]:
         nl, ne, nb = C.c_int(), C.c_int(), C.c_longlong()

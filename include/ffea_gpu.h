@@ -143,6 +143,10 @@ int ffea_gpu_blob_measure(ffea_gpu_blob *blob, double *strain_energy, double *ki
 /* CG iterations of the last step and in total (0 for masslumped). */
 int ffea_gpu_blob_cg_iterations(ffea_gpu_blob *blob, int *last, long long *total);
 
+/* Relative squared residual |r|^2/|f|^2 after each CG iteration of the last solve (the quantity
+ * NoMassCGSolver::solve tests against epsilon2); *count gets the number written (<= max_entries). */
+int ffea_gpu_blob_cg_history(ffea_gpu_blob *blob, double *res2, int max_entries, int *count);
+
 /* Problem sizes: vertex nodes, elements, matrix 3x3 blocks. */
 int ffea_gpu_blob_sizes(ffea_gpu_blob *blob, int *num_linear_nodes, int *num_elements, long long *num_blocks);
 
