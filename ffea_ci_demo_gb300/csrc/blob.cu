@@ -718,7 +718,7 @@ struct BlobImpl final : ffea_gpu_blob {
         ga.drag = (!nomass && p.calc_stokes == 1) ? drag : nullptr;
         ga.vx = vx; ga.vy = vy; ga.vz = vz;
         ga.dinv = dinv; ga.f = f; ga.x = x; ga.r = r; ga.p = pv;
-        ga.partials = init_partials; ga.stride = gather_blocks; ga.st = st;
+        ga.partials = init_partials; ga.stride = gather_blocks; ga.st = st; ga.gb = gb;
         ga.r64 = r64; ga.dpos = dpos; ga.px = px; ga.py = py; ga.pz = pz;
         ga.xc[0] = xc[0]; ga.xc[1] = xc[1]; ga.xc[2] = xc[2];
         CK(Launch<R>::gather(ga, gather_blocks, stream));
@@ -881,6 +881,12 @@ struct BlobImpl final : ffea_gpu_blob {
         int rc;
         if (pos && (rc = put(pos, px, py, pz))) return rc;
         if (vel && (rc = put(vel, vx, vy, vz))) return rc;
+        if (pos && std::is_same<R, float>::value) {
+            // the rigid modes must vanish at the pinned nodes' current positions
+            for (int k = 0; k < N; ++k)
+                for (int c = 0; c < 3; ++c) h.pos[3 * (size_t)k + c] = pos[3 * (size_t)h.node_of[k] + c];
+            nmodes = rigid_modes(h, p, xc, modes);
+        }
         return FFEA_GPU_OK;
     }
 

@@ -31,7 +31,7 @@ struct DevStatus {
 };
 
 struct GridBarrier {
-    unsigned int count;
+    unsigned int count;  // arrivals since the last reset; barrier k completes at count == (k+1) * gridDim.x
     unsigned int gen;
 };
 
@@ -42,25 +42,25 @@ __device__ __forceinline__ unsigned long long globaltimer_ns() {
 }
 
 // Bounded grid barrier. All blocks of the grid must be co-resident
-// (cudaLaunchCooperativeKernel). Returns false if this block gave up waiting
-// or another block recorded a timeout; the caller then leaves its loop.
+// (cudaLaunchCooperativeKernel), and gb->count must be zero when the kernel
+// starts (the launch before it on the stream resets it). Arrivals only ever
+// increase the counter, so a block that arrives as number `old` waits for the
+// counter to reach the next multiple of gridDim.x: one atomic and one polled
+// load per barrier. Returns false if this block gave up waiting or another
+// block recorded a timeout; the caller then leaves its loop.
 __device__ __forceinline__ bool grid_sync(GridBarrier *gb, DevStatus *st, unsigned long long limit_ns) {
     __shared__ int s_ok;
     __syncthreads();
     if (threadIdx.x == 0) {
         int ok = 1;
-        cuda::atomic_ref<unsigned int, cuda::thread_scope_device> gen(gb->gen);
         cuda::atomic_ref<unsigned int, cuda::thread_scope_device> cnt(gb->count);
-        const unsigned int g = gen.load(cuda::memory_order_acquire);
         __threadfence();
-        const unsigned int arrived = cnt.fetch_add(1u, cuda::memory_order_acq_rel);
-        if (arrived == gridDim.x - 1) {
-            cnt.store(0u, cuda::memory_order_relaxed);
-            gen.fetch_add(1u, cuda::memory_order_release);
-        } else {
+        const unsigned int old = cnt.fetch_add(1u, cuda::memory_order_acq_rel);
+        const unsigned int target = (old / gridDim.x + 1u) * gridDim.x;
+        if ((int)(cnt.load(cuda::memory_order_acquire) - target) < 0) {
             const unsigned long long t0 = globaltimer_ns();
             unsigned int polls = 0;
-            while (gen.load(cuda::memory_order_acquire) == g) {
+            while ((int)(cnt.load(cuda::memory_order_acquire) - target) < 0) {
                 if ((++polls & 255u) == 0u) {
                     if (globaltimer_ns() - t0 > limit_ns) {
                         atomicExch(&st->timeout, 1);
@@ -104,20 +104,18 @@ __device__ __forceinline__ void block_sum(double (&v)[NV], double *smem /* NV*32
     __syncthreads();
 }
 
-// Every block sums partials[i*stride + b] over b < nb in the same order.
+// Every block sums partials[i*stride + b] over b < nb in the same fixed order;
+// warp w of the block handles values w, w + nwarps, ... in parallel.
 template <int NV>
 __device__ __forceinline__ void grid_partials_sum(const double *partials, int stride, int nb, double (&out)[NV],
                                                   double *smem) {
     __shared__ double s_out[NV];
-    if (threadIdx.x < 32) {
-        const int lane = threadIdx.x;
-#pragma unroll
-        for (int i = 0; i < NV; ++i) {
-            double t = 0.0;
-            for (int b = lane; b < nb; b += 32) t += __ldcg(partials + i * stride + b);
-            t = warp_sum(t);
-            if (lane == 0) s_out[i] = t;
-        }
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int i = wid; i < NV; i += nw) {
+        double t = 0.0;
+        for (int b = lane; b < nb; b += 32) t += __ldcg(partials + i * stride + b);
+        t = warp_sum(t);
+        if (lane == 0) s_out[i] = t;
     }
     __syncthreads();
 #pragma unroll

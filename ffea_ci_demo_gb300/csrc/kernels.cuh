@@ -297,6 +297,7 @@ struct GatherArgs {
     double *partials;     // [0]: f.f, [stride]: r.z per block (mixed path: 16 moments per block)
     int stride;
     DevStatus *st;
+    GridBarrier *gb;      // reset here for the CG launch that follows on the stream
     // mixed path only: FP64 residual, node offsets from the rest centroid, positions
     double *r64;
     float4 *dpos;
@@ -308,6 +309,7 @@ template <class R>
 __global__ void __launch_bounds__(256) gather_kernel(GatherArgs<R> g) {
     __shared__ double smem[64];
     const int a = blockIdx.x * blockDim.x + threadIdx.x;
+    if (a == 0 && g.gb) g.gb->count = 0u;
     double acc[2] = {0.0, 0.0};
     const bool live = a < g.N && !g.st->abort;
     if (live) {
@@ -382,36 +384,62 @@ struct CgArgs {
     double modes[36];
 };
 
+constexpr int SPMV_TPN = 4;  // threads per matrix row (node) in the SpMV
+
+// Row a of q = V p, summed by the SPMV_TPN lanes of a node group over blocks k = sub, sub + TPN, ...
+// and combined with shuffles; every lane of the group returns the row. All 32 lanes of the warp call
+// it together (rows past the end pass len = 0).
 template <class R>
-__device__ __forceinline__ void spmv_row(const CgArgs<R> &g, int a, R &q0, R &q1, R &q2) {
-    const int s = a >> 5, lane = a & 31;
-    const int base = g.slice_ptr[s];
-    const int len = g.rowlen[a];
+__device__ __forceinline__ void spmv_row(const CgArgs<R> &g, int a, int sub, bool valid, R &q0, R &q1, R &q2) {
     q0 = 0.0; q1 = 0.0; q2 = 0.0;
-    if (g.block3) {
-        const R *v = g.val + 9 * (size_t)base + lane;
-        for (int k = 0; k < len; ++k) {
-            const int b = g.bcol[base + 32 * k + lane];
-            const R p0 = g.p[4 * b], p1 = g.p[4 * b + 1], p2 = g.p[4 * b + 2];
-            const R *vk = v + (size_t)32 * 9 * k;
-            q0 += vk[0] * p0; q0 += vk[32] * p1; q0 += vk[64] * p2;
-            q1 += vk[96] * p0; q1 += vk[128] * p1; q1 += vk[160] * p2;
-            q2 += vk[192] * p0; q2 += vk[224] * p1; q2 += vk[256] * p2;
+    if (valid) {
+        const int s = a >> 5, lane = a & 31;
+        const int base = g.slice_ptr[s];
+        const int len = g.rowlen[a];
+        if (g.block3) {
+            const R *v = g.val + 9 * (size_t)base + lane;
+#pragma unroll 2
+            for (int k = sub; k < len; k += SPMV_TPN) {
+                const int b = g.bcol[base + 32 * k + lane];
+                const R *vk = v + (size_t)32 * 9 * k;
+                const R v0 = vk[0], v1 = vk[32], v2 = vk[64], v3 = vk[96], v4 = vk[128], v5 = vk[160], v6 = vk[192],
+                        v7 = vk[224], v8 = vk[256];
+                const R p0 = g.p[4 * b], p1 = g.p[4 * b + 1], p2 = g.p[4 * b + 2];
+                q0 += v0 * p0; q0 += v1 * p1; q0 += v2 * p2;
+                q1 += v3 * p0; q1 += v4 * p1; q1 += v5 * p2;
+                q2 += v6 * p0; q2 += v7 * p1; q2 += v8 * p2;
+            }
+        } else {
+            const R *v = g.val + base + lane;
+            for (int k = sub; k < len; k += SPMV_TPN) {
+                const int b = g.bcol[base + 32 * k + lane];
+                const R m = v[32 * k];
+                q0 += m * g.p[4 * b];
+                q1 += m * g.p[4 * b + 1];
+                q2 += m * g.p[4 * b + 2];
+            }
         }
-    } else {
-        const R *v = g.val + base + lane;
-        for (int k = 0; k < len; ++k) {
-            const int b = g.bcol[base + 32 * k + lane];
-            const R m = v[32 * k];
-            q0 += m * g.p[4 * b];
-            q1 += m * g.p[4 * b + 1];
-            q2 += m * g.p[4 * b + 2];
-        }
+    }
+#pragma unroll
+    for (int o = 1; o < SPMV_TPN; o <<= 1) {
+        q0 += __shfl_xor_sync(0xffffffffu, q0, o);
+        q1 += __shfl_xor_sync(0xffffffffu, q1, o);
+        q2 += __shfl_xor_sync(0xffffffffu, q2, o);
     }
 }
 
+// node loop of the SpMV phase: warp w covers nodes [w*NPW, (w+1)*NPW), NPW = 32 / SPMV_TPN, grid-strided
+#define FFEA_SPMV_LOOP(g, a, sub, valid)                                                        \
+    const int sub = threadIdx.x % SPMV_TPN;                                                     \
+    const int npw_ = 32 / SPMV_TPN;                                                              \
+    const int wglob_ = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;                            \
+    const int wstride_ = (gridDim.x * blockDim.x) >> 5;                                          \
+    for (int a0_ = wglob_ * npw_, a = a0_ + (threadIdx.x & 31) / SPMV_TPN; a0_ < (g).N;         \
+         a0_ += wstride_ * npw_, a = a0_ + (threadIdx.x & 31) / SPMV_TPN)                      \
+        for (bool valid = a < (g).N, once_ = true; once_; once_ = false)
+
 template <class R>
-__global__ void __launch_bounds__(512) cg_kernel(CgArgs<R> g) {
+__global__ void __launch_bounds__(1024, 1) cg_kernel(CgArgs<R> g) {
     __shared__ double smem[96];
     DevStatus *st = g.st;
     if (st->abort) return;
@@ -426,11 +454,13 @@ __global__ void __launch_bounds__(512) cg_kernel(CgArgs<R> g) {
     for (; it < g.imax; ++it) {
         // q = V p ; pTq   (get_alpha_denominator :253-266)
         double acc1[1] = {0.0};
-        for (int a = tid; a < g.N; a += nthr) {
+        FFEA_SPMV_LOOP(g, a, sub, valid) {
             R q0, q1, q2;
-            spmv_row(g, a, q0, q1, q2);
-            g.q[4 * a] = q0; g.q[4 * a + 1] = q1; g.q[4 * a + 2] = q2;
-            acc1[0] += (double)(g.p[4 * a] * q0 + g.p[4 * a + 1] * q1 + g.p[4 * a + 2] * q2);
+            spmv_row(g, a, sub, valid, q0, q1, q2);
+            if (valid && sub == 0) {
+                g.q[4 * a] = q0; g.q[4 * a + 1] = q1; g.q[4 * a + 2] = q2;
+                acc1[0] += (double)(g.p[4 * a] * q0 + g.p[4 * a + 1] * q1 + g.p[4 * a + 2] * q2);
+            }
         }
         block_sum<1>(acc1, smem);
         if (threadIdx.x == 0) g.partials[blockIdx.x] = acc1[0];

@@ -34,6 +34,7 @@ template <class R>
 __global__ void __launch_bounds__(256) gather_mixed_kernel(GatherArgs<R> g) {
     __shared__ double smem[MIXED_GATHER_NP * 32];
     const int a = blockIdx.x * blockDim.x + threadIdx.x;
+    if (a == 0 && g.gb) g.gb->count = 0u;
     double acc[MIXED_GATHER_NP];
 #pragma unroll
     for (int i = 0; i < MIXED_GATHER_NP; ++i) acc[i] = 0.0;
@@ -103,7 +104,7 @@ __device__ __forceinline__ void mode_coeffs(const CgArgs<R> &g, const double *Gi
 }
 
 template <class R>
-__global__ void __launch_bounds__(512) cg_mixed_kernel(CgArgs<R> g) {
+__global__ void __launch_bounds__(1024, 1) cg_mixed_kernel(CgArgs<R> g) {
     __shared__ double smem[MIXED_A_NP * 32];
     __shared__ double s_Ginv[36];
     __shared__ double s_tau[3], s_Om[3], s_pq;
@@ -191,9 +192,10 @@ __global__ void __launch_bounds__(512) cg_mixed_kernel(CgArgs<R> g) {
         double acc[MIXED_A_NP];
 #pragma unroll
         for (int i = 0; i < MIXED_A_NP; ++i) acc[i] = 0.0;
-        for (int a = tid; a < g.N; a += nthr) {
+        FFEA_SPMV_LOOP(g, a, sub, valid) {
             float q0, q1, q2;
-            spmv_row(g, a, q0, q1, q2);
+            spmv_row(g, a, sub, valid, q0, q1, q2);
+            if (!valid || sub != 0) continue;
             g.q[4 * a] = q0; g.q[4 * a + 1] = q1; g.q[4 * a + 2] = q2;
             const float p0 = g.p[4 * a], p1 = g.p[4 * a + 1], p2 = g.p[4 * a + 2];
             acc[0] += (double)(p0 * q0 + p1 * q1 + p2 * q2);
