@@ -527,19 +527,19 @@ struct BlobImpl final : ffea_gpu_blob {
     double *drag = nullptr;
     R *val, *dinv;
     double *f;
-    R *x, *r, *pv, *q;
+    R *x, *r, *q, *pbuf0, *pbuf1;
+    R *diag = nullptr;       // mixed path: diagonal of V
     double *partials, *init_partials;
     uint32_t *rng_state;
     MrgJump *chunk_jump, *lane_jump, *step_jump;
     DevStatus *st;
     GridBarrier *gb;
     int cg_grid = 0, gather_blocks = 0, partial_stride = 0;
-    double *r64 = nullptr;   // mixed path: FP64 CG residual
-    float4 *dpos = nullptr;  // mixed path: node offsets from the rest centroid
+    float4 *dpos = nullptr;  // mixed path: node offsets from the reference point
     int nmodes = 0;
     double modes[36] = {}, xc[3] = {};
     double *history = nullptr;
-    int hist_cap = 0, debug = 0;
+    int hist_cap = 0;
     cudaEvent_t ev[FFEA_GPU_NUM_PHASES + 1] = {};
     bool record_phases = false;
     double *staging = nullptr;  // pinned host buffer, 3*N doubles, for state copies
@@ -629,14 +629,15 @@ struct BlobImpl final : ffea_gpu_blob {
         CK(mem.alloc(&f, 4 * (size_t)N));
         CK(mem.alloc(&x, 4 * (size_t)N));
         CK(mem.alloc(&r, 4 * (size_t)N));
-        CK(mem.alloc(&pv, 4 * (size_t)N));
+        CK(mem.alloc(&pbuf0, 4 * (size_t)N));
+        CK(mem.alloc(&pbuf1, 4 * (size_t)N));
         CK(mem.alloc(&q, 4 * (size_t)N));
         const int gthreads = Launch<R>::gather_threads();
         gather_blocks = (N + gthreads - 1) / gthreads;
         constexpr bool mixed = std::is_same<R, float>::value;
         CK(mem.alloc(&init_partials, (mixed ? MIXED_GATHER_NP : 2) * (size_t)gather_blocks));
         if (mixed) {
-            CK(mem.alloc(&r64, 4 * (size_t)N));
+            CK(mem.alloc(&diag, 4 * (size_t)N));
             CK(mem.alloc(&dpos, (size_t)N));
             nmodes = rigid_modes(h, p, xc, modes);
         }
@@ -645,10 +646,11 @@ struct BlobImpl final : ffea_gpu_blob {
             g_last_error = "cg kernel cannot be made resident";
             return FFEA_GPU_ECUDA;
         }
-        cg_grid = std::max(1, std::min(maxg, (N + Launch<R>::cg_threads() - 1) / Launch<R>::cg_threads()));
+        // enough blocks for one SpMV row group per SPMV_TPN threads, at most one block per SM
+        const int rows_per_block = Launch<R>::cg_threads() / SPMV_TPN;
+        cg_grid = std::max(1, std::min(maxg, (N + rows_per_block - 1) / rows_per_block));
         partial_stride = cg_grid;
         CK(mem.alloc(&partials, (mixed ? MIXED_PARTIAL_ROWS : 3) * (size_t)partial_stride));
-        if (const char *dbg = getenv("FFEA_GPU_DEBUG")) debug = atoi(dbg);
         CK(mem.alloc(&st, 1));
         hist_cap = std::min(std::max(p.max_iterations_cg, 1), 1 << 20);
         CK(mem.alloc(&history, (size_t)hist_cap));
@@ -707,7 +709,7 @@ struct BlobImpl final : ffea_gpu_blob {
             aa.src_ptr = src_ptr; aa.src = src;
             aa.geom = geom; aa.A = A; aa.B = B;
             aa.drag = (p.calc_stokes == 1) ? drag : nullptr;
-            aa.val = val; aa.dinv = dinv; aa.st = st;
+            aa.val = val; aa.dinv = dinv; aa.diag = diag; aa.st = st;
             CK(Launch<R>::assemble(aa, stream));
         }
         if ((rc = mark(2))) return rc;
@@ -717,9 +719,9 @@ struct BlobImpl final : ffea_gpu_blob {
         ga.inc_ptr = inc_ptr; ga.inc = inc; ga.ef = ef; ga.pinned = pinned;
         ga.drag = (!nomass && p.calc_stokes == 1) ? drag : nullptr;
         ga.vx = vx; ga.vy = vy; ga.vz = vz;
-        ga.dinv = dinv; ga.f = f; ga.x = x; ga.r = r; ga.p = pv;
+        ga.dinv = dinv; ga.f = f; ga.x = x; ga.r = r;
         ga.partials = init_partials; ga.stride = gather_blocks; ga.st = st; ga.gb = gb;
-        ga.r64 = r64; ga.dpos = dpos; ga.px = px; ga.py = py; ga.pz = pz;
+        ga.dpos = dpos; ga.px = px; ga.py = py; ga.pz = pz; ga.diag = diag;
         ga.xc[0] = xc[0]; ga.xc[1] = xc[1]; ga.xc[2] = xc[2];
         CK(Launch<R>::gather(ga, gather_blocks, stream));
         if ((rc = mark(3))) return rc;
@@ -730,15 +732,15 @@ struct BlobImpl final : ffea_gpu_blob {
             ca.check_last = nomass;
             ca.slice_ptr = slice_ptr; ca.rowlen = rowlen; ca.bcol = bcol;
             ca.val = val; ca.dinv = dinv;
-            ca.x = x; ca.r = r; ca.p = pv; ca.q = q;
+            ca.x = x; ca.r = r; ca.q = q; ca.pbuf0 = pbuf0; ca.pbuf1 = pbuf1; ca.diag = diag;
             ca.init_partials = init_partials; ca.n_init = gather_blocks; ca.init_stride = gather_blocks;
             ca.partials = partials; ca.stride = partial_stride;
             ca.gb = gb; ca.st = st;
             ca.imax = p.max_iterations_cg;
             ca.eps2 = p.epsilon2;
             ca.limit_ns = 2000000000ull;
-            ca.history = history; ca.hist_cap = hist_cap; ca.debug = debug;
-            ca.r64 = r64; ca.dpos = dpos; ca.nmodes = nomass ? nmodes : 0;
+            ca.history = history; ca.hist_cap = hist_cap;
+            ca.dpos = dpos; ca.nmodes = nomass ? nmodes : 0;
             for (int i = 0; i < 36; ++i) ca.modes[i] = modes[i];
             CK(Launch<R>::cg(ca, cg_grid, stream));
         }

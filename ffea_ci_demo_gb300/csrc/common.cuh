@@ -31,8 +31,10 @@ struct DevStatus {
 };
 
 struct GridBarrier {
-    unsigned int count;  // arrivals since the last reset; barrier k completes at count == (k+1) * gridDim.x
-    unsigned int gen;
+    unsigned int count;     // arrivals since the last reset
+    unsigned int pad0[31];  // keep the polled word on its own 128-byte line
+    unsigned int passed;    // number of completed barriers since the last reset (written by the last arriver)
+    unsigned int pad1[31];
 };
 
 __device__ __forceinline__ unsigned long long globaltimer_ns() {
@@ -42,25 +44,29 @@ __device__ __forceinline__ unsigned long long globaltimer_ns() {
 }
 
 // Bounded grid barrier. All blocks of the grid must be co-resident
-// (cudaLaunchCooperativeKernel), and gb->count must be zero when the kernel
-// starts (the launch before it on the stream resets it). Arrivals only ever
-// increase the counter, so a block that arrives as number `old` waits for the
-// counter to reach the next multiple of gridDim.x: one atomic and one polled
-// load per barrier. Returns false if this block gave up waiting or another
-// block recorded a timeout; the caller then leaves its loop.
+// (cudaLaunchCooperativeKernel), and gb->count and gb->passed must be zero
+// when the kernel starts (the launch before it on the stream resets them).
+// Arrival is one relaxed atomic on gb->count after a release fence; the block
+// that completes barrier k (arrival number (k+1)*gridDim.x - 1) publishes k+1
+// in gb->passed, which lives on its own cache line and is the only word the
+// others poll (volatile loads), followed by one acquire fence. Returns false
+// if this block gave up waiting or another block recorded a timeout; the
+// caller then leaves its loop.
 __device__ __forceinline__ bool grid_sync(GridBarrier *gb, DevStatus *st, unsigned long long limit_ns) {
     __shared__ int s_ok;
     __syncthreads();
     if (threadIdx.x == 0) {
         int ok = 1;
-        cuda::atomic_ref<unsigned int, cuda::thread_scope_device> cnt(gb->count);
         __threadfence();
-        const unsigned int old = cnt.fetch_add(1u, cuda::memory_order_acq_rel);
-        const unsigned int target = (old / gridDim.x + 1u) * gridDim.x;
-        if ((int)(cnt.load(cuda::memory_order_acquire) - target) < 0) {
+        const unsigned int old = atomicAdd(&gb->count, 1u);
+        const unsigned int k1 = old / gridDim.x + 1u;  // this barrier completes when passed == k1
+        if (old == k1 * gridDim.x - 1u) {
+            atomicExch(&gb->passed, k1);
+        } else {
+            volatile unsigned int *passed = &gb->passed;
             const unsigned long long t0 = globaltimer_ns();
             unsigned int polls = 0;
-            while ((int)(cnt.load(cuda::memory_order_acquire) - target) < 0) {
+            while ((int)(*passed - k1) < 0) {
                 if ((++polls & 255u) == 0u) {
                     if (globaltimer_ns() - t0 > limit_ns) {
                         atomicExch(&st->timeout, 1);
@@ -122,6 +128,114 @@ __device__ __forceinline__ void grid_partials_sum(const double *partials, int st
     for (int i = 0; i < NV; ++i) out[i] = s_out[i];
     __syncthreads();
     (void)smem;
+}
+
+// ---------------------------------------------------------------------------
+// double-float (pairs of FP32, ~48-bit significand) accumulation. GB300 runs
+// FP64 at 1/64 of the FP32 rate, so reductions over nodes keep their extra
+// precision in FP32 pairs: two_sum is Knuth's error-free sum, df_add the
+// usual accurate pair addition.
+// ---------------------------------------------------------------------------
+struct df32 {
+    float hi, lo;
+};
+
+__device__ __forceinline__ df32 df_add(df32 a, df32 b) {
+    const float s = a.hi + b.hi;
+    const float v = s - a.hi;
+    float e = (a.hi - (s - v)) + (b.hi - v);
+    e += a.lo + b.lo;
+    const float hi = s + e;
+    return {hi, e - (hi - s)};
+}
+
+__device__ __forceinline__ df32 df_add_f(df32 a, float b) { return df_add(a, df32{b, 0.f}); }
+
+__device__ __forceinline__ df32 warp_sum_df(df32 v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        df32 w;
+        w.hi = __shfl_xor_sync(0xffffffffu, v.hi, o);
+        w.lo = __shfl_xor_sync(0xffffffffu, v.lo, o);
+        v = df_add(v, w);
+    }
+    return v;
+}
+
+// Block reduction of NV double-float values; thread 0 gets the sums in out[] (other threads: undefined).
+// smem needs NV * 32 float2.
+template <int NV>
+__device__ __forceinline__ void block_sum_df(const df32 (&v)[NV], float2 *smem, df32 (&out)[NV]) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+    for (int i = 0; i < NV; ++i) {
+        const df32 w = warp_sum_df(v[i]);
+        if (lane == 0) smem[i * 32 + wid] = make_float2(w.hi, w.lo);
+    }
+    __syncthreads();
+    for (int i = wid; i < NV; i += nw) {
+        df32 t = {0.f, 0.f};
+        if (lane < nw) t = df32{smem[i * 32 + lane].x, smem[i * 32 + lane].y};
+        t = warp_sum_df(t);
+        if (lane == 0) smem[i * 32] = make_float2(t.hi, t.lo);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0)
+#pragma unroll
+        for (int i = 0; i < NV; ++i) out[i] = df32{smem[i * 32].x, smem[i * 32].y};
+    __syncthreads();
+}
+
+// Every block sums the per-block pairs partials[i*stride + b], b < nb, in the same order; results
+// (as doubles, hi + lo) land in s_out[0..NV) in shared memory for the whole block.
+template <int NV>
+__device__ __forceinline__ void grid_sum_df(const float2 *partials, int stride, int nb, double *s_out) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int i = wid; i < NV; i += nw) {
+        df32 t = {0.f, 0.f};
+        for (int b = lane; b < nb; b += 32) {
+            const float2 q = __ldcg(partials + i * stride + b);
+            t = df_add(t, df32{q.x, q.y});
+        }
+        t = warp_sum_df(t);
+        if (lane == 0) s_out[i] = (double)t.hi + (double)t.lo;
+    }
+    __syncthreads();
+}
+
+// FP64 block reduction through shared memory: one warp per value sums the block's threads, so the
+// FP64 pipe sees ~blockDim adds per value instead of a shuffle tree in every warp.
+// smem needs NV * blockDim doubles; thread 0 gets out[].
+template <int NV>
+__device__ __forceinline__ void block_sum_smem(const double (&v)[NV], double *smem, double (&out)[NV]) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5, nt = blockDim.x;
+#pragma unroll
+    for (int i = 0; i < NV; ++i) smem[i * nt + threadIdx.x] = v[i];
+    __syncthreads();
+    for (int i = wid; i < NV; i += nw) {
+        double t = 0.0;
+        for (int k = lane; k < nt; k += 32) t += smem[i * nt + k];
+        t = warp_sum(t);
+        if (lane == 0) smem[i * nt] = t;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0)
+#pragma unroll
+        for (int i = 0; i < NV; ++i) out[i] = smem[i * nt];
+    __syncthreads();
+}
+
+// FP64 cross-block sums (one warp per value), results in s_out[] for the whole block.
+template <int NV>
+__device__ __forceinline__ void grid_sum_d(const double *partials, int stride, int nb, double *s_out) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int i = wid; i < NV; i += nw) {
+        double t = 0.0;
+        for (int b = lane; b < nb; b += 32) t += __ldcg(partials + i * stride + b);
+        t = warp_sum(t);
+        if (lane == 0) s_out[i] = t;
+    }
+    __syncthreads();
 }
 
 // ---------------------------------------------------------------------------

@@ -12,7 +12,7 @@ namespace ffea {
 constexpr int ELEM_THREADS = 128;
 constexpr int ASM_THREADS = 128;
 constexpr int GATHER_THREADS = 256;
-constexpr int CG_THREADS = 1024;
+constexpr int CG_THREADS = CG_MAX_THREADS;
 constexpr int EULER_THREADS = 256;
 
 template <class R>

@@ -227,6 +227,7 @@ struct AsmArgs {
     const double *drag;     // per node or null
     R *val;
     R *dinv;                // 4*N
+    R *diag;                // 4*N diagonal of V (mixed path) or null
     DevStatus *st;
 };
 
@@ -272,6 +273,7 @@ __global__ void __launch_bounds__(128) assemble_kernel(AsmArgs<R> g) {
             g.dinv[4 * a] = (R)1.0 / v[0];
             g.dinv[4 * a + 1] = (R)1.0 / v[4];
             g.dinv[4 * a + 2] = (R)1.0 / v[8];
+            if (g.diag) { g.diag[4 * a] = v[0]; g.diag[4 * a + 1] = v[4]; g.diag[4 * a + 2] = v[8]; }
         }
         R *vp = vbase + (size_t)32 * 9 * k;
 #pragma unroll
@@ -293,23 +295,23 @@ struct GatherArgs {
     const double *vx, *vy, *vz;
     const R *dinv;        // Jacobi preconditioner (CG) or inverse lumped mass (mode 1)
     double *f;            // 4*N assembled force (solver input)
-    R *x, *r, *p;
-    double *partials;     // [0]: f.f, [stride]: r.z per block (mixed path: 16 moments per block)
+    R *x, *r;
+    double *partials;     // [0]: f.f, [stride]: r.z per block (mixed path: moments, float2 pairs)
     int stride;
     DevStatus *st;
     GridBarrier *gb;      // reset here for the CG launch that follows on the stream
-    // mixed path only: FP64 residual, node offsets from the rest centroid, positions
-    double *r64;
+    // mixed path only: node offsets from the reference point, positions, diagonal of V
     float4 *dpos;
     const double *px, *py, *pz;
     double xc[3];
+    const R *diag;
 };
 
 template <class R>
 __global__ void __launch_bounds__(256) gather_kernel(GatherArgs<R> g) {
     __shared__ double smem[64];
     const int a = blockIdx.x * blockDim.x + threadIdx.x;
-    if (a == 0 && g.gb) g.gb->count = 0u;
+    if (a == 0 && g.gb) { g.gb->count = 0u; g.gb->passed = 0u; }
     double acc[2] = {0.0, 0.0};
     const bool live = a < g.N && !g.st->abort;
     if (live) {
@@ -339,7 +341,6 @@ __global__ void __launch_bounds__(256) gather_kernel(GatherArgs<R> g) {
             const R z0 = g.dinv[4 * a] * F0, z1 = g.dinv[4 * a + 1] * F1, z2 = g.dinv[4 * a + 2] * F2;
             g.r[4 * a] = F0; g.r[4 * a + 1] = F1; g.r[4 * a + 2] = F2;
             g.x[4 * a] = 0; g.x[4 * a + 1] = 0; g.x[4 * a + 2] = 0;
-            g.p[4 * a] = z0; g.p[4 * a + 1] = z1; g.p[4 * a + 2] = z2;
             acc[0] = (double)(F0 * F0 + F1 * F1 + F2 * F2);
             acc[1] = (double)(F0 * z0 + F1 * z1 + F2 * z2);
         }
@@ -354,31 +355,36 @@ __global__ void __launch_bounds__(256) gather_kernel(GatherArgs<R> g) {
 
 // ---------------------------------------------------------------------------
 // persistent Jacobi-PCG (NoMassCGSolver::solve :156-188 / ConjugateGradientSolver::solve :193-217)
+//
+// One cooperative launch runs the whole solve with two grid barriers per
+// iteration: the search direction p = beta p + z of the previous iteration is
+// not stored in a separate phase but recomputed on the fly, element by
+// element, wherever the SpMV reads it (p lives in two buffers, old and new,
+// which swap every iteration).
 // ---------------------------------------------------------------------------
 template <class R>
 struct CgArgs {
     int N;
     int block3;           // 1: 3x3-block viscosity matrix, 0: scalar mass matrix applied per component
     int check_last;       // 1: also test convergence after the last allowed iteration (NoMass order)
-    int nomass_zero_rhs_nan;  // NoMass: zero right-hand side gives 0/0 as in the reference
     const int *slice_ptr, *rowlen, *bcol;
     const R *val;
-    const R *dinv;
-    R *x, *r, *p, *q;
-    const double *init_partials;  // from gather_kernel: f.f and r.z per block
+    const R *dinv;        // Jacobi preconditioner, 4 per node
+    const R *diag;        // mixed path: diagonal of V, 4 per node
+    R *x, *r, *q;
+    R *pbuf0, *pbuf1;     // search direction, double-buffered
+    const double *init_partials;  // from the gather kernel
     int n_init, init_stride;
-    double *partials;     // 3 * max_blocks
+    double *partials;     // per-block partial sums (float2 pairs on the mixed path)
     int stride;
     GridBarrier *gb;
     DevStatus *st;
     int imax;
     double eps2;
     unsigned long long limit_ns;
-    double *history;      // res2 per iteration (block 0 writes), capacity hist_cap
+    double *history;      // |r|^2/|f|^2 per iteration (block 0 writes), capacity hist_cap
     int hist_cap;
-    int debug;            // diagnostics (mixed path): bit 1 records the rigid-mode content of r instead of |r|^2
-    // mixed path only: FP64 residual, node offsets, rigid-mode coefficients (t, omega) per mode
-    double *r64;
+    // mixed path: node offsets from the reference point and the rigid-mode coefficients (t, omega)
     const float4 *dpos;
     int nmodes;
     double modes[36];
@@ -386,11 +392,28 @@ struct CgArgs {
 
 constexpr int SPMV_TPN = 4;  // threads per matrix row (node) in the SpMV
 
-// Row a of q = V p, summed by the SPMV_TPN lanes of a node group over blocks k = sub, sub + TPN, ...
-// and combined with shuffles; every lane of the group returns the row. All 32 lanes of the warp call
-// it together (rows past the end pass len = 0).
+// p at node b for this iteration: p_new = beta p_old + D^{-1} r (vec3_scale_and_add with the
+// preconditioned residual, src/NoMassCGSolver.cpp:181-183), or z itself on the first iteration.
 template <class R>
-__device__ __forceinline__ void spmv_row(const CgArgs<R> &g, int a, int sub, bool valid, R &q0, R &q1, R &q2) {
+__device__ __forceinline__ void p_on_the_fly(const CgArgs<R> &g, const R *pold, R beta, bool first, int b, R &p0,
+                                              R &p1, R &p2) {
+    const R z0 = g.dinv[4 * b] * g.r[4 * b], z1 = g.dinv[4 * b + 1] * g.r[4 * b + 1],
+            z2 = g.dinv[4 * b + 2] * g.r[4 * b + 2];
+    if (first) {
+        p0 = z0; p1 = z1; p2 = z2;
+    } else {
+        p0 = beta * pold[4 * b] + z0;
+        p1 = beta * pold[4 * b + 1] + z1;
+        p2 = beta * pold[4 * b + 2] + z2;
+    }
+}
+
+// Row a of q = V p, summed by the SPMV_TPN lanes of a node group over blocks k = sub, sub + TPN, ...
+// (p recomputed on the fly) and combined with shuffles; every lane of the group returns the row.
+// All 32 lanes of the warp call it together (rows past the end pass valid = false).
+template <class R>
+__device__ __forceinline__ void spmv_row(const CgArgs<R> &g, const R *pold, R beta, bool first, int a, int sub,
+                                         bool valid, R &q0, R &q1, R &q2) {
     q0 = 0.0; q1 = 0.0; q2 = 0.0;
     if (valid) {
         const int s = a >> 5, lane = a & 31;
@@ -404,7 +427,8 @@ __device__ __forceinline__ void spmv_row(const CgArgs<R> &g, int a, int sub, boo
                 const R *vk = v + (size_t)32 * 9 * k;
                 const R v0 = vk[0], v1 = vk[32], v2 = vk[64], v3 = vk[96], v4 = vk[128], v5 = vk[160], v6 = vk[192],
                         v7 = vk[224], v8 = vk[256];
-                const R p0 = g.p[4 * b], p1 = g.p[4 * b + 1], p2 = g.p[4 * b + 2];
+                R p0, p1, p2;
+                p_on_the_fly(g, pold, beta, first, b, p0, p1, p2);
                 q0 += v0 * p0; q0 += v1 * p1; q0 += v2 * p2;
                 q1 += v3 * p0; q1 += v4 * p1; q1 += v5 * p2;
                 q2 += v6 * p0; q2 += v7 * p1; q2 += v8 * p2;
@@ -414,9 +438,11 @@ __device__ __forceinline__ void spmv_row(const CgArgs<R> &g, int a, int sub, boo
             for (int k = sub; k < len; k += SPMV_TPN) {
                 const int b = g.bcol[base + 32 * k + lane];
                 const R m = v[32 * k];
-                q0 += m * g.p[4 * b];
-                q1 += m * g.p[4 * b + 1];
-                q2 += m * g.p[4 * b + 2];
+                R p0, p1, p2;
+                p_on_the_fly(g, pold, beta, first, b, p0, p1, p2);
+                q0 += m * p0;
+                q1 += m * p1;
+                q2 += m * p2;
             }
         }
     }
@@ -438,81 +464,94 @@ __device__ __forceinline__ void spmv_row(const CgArgs<R> &g, int a, int sub, boo
          a0_ += wstride_ * npw_, a = a0_ + (threadIdx.x & 31) / SPMV_TPN)                      \
         for (bool valid = a < (g).N, once_ = true; once_; once_ = false)
 
+constexpr int CG_MAX_THREADS = 1024;
+
 template <class R>
 __global__ void __launch_bounds__(1024, 1) cg_kernel(CgArgs<R> g) {
-    __shared__ double smem[96];
+    __shared__ double smem[2 * CG_MAX_THREADS];
+    __shared__ double s_sc[4];
+    __shared__ R s_alpha, s_beta;
+    __shared__ double s_delta;
+    __shared__ int s_conv;
     DevStatus *st = g.st;
     if (st->abort) return;
     const int nthr = gridDim.x * blockDim.x;
     const int tid = blockIdx.x * blockDim.x + threadIdx.x;
-    double init[2];
-    grid_partials_sum<2>(g.init_partials, g.init_stride, g.n_init, init, smem);
-    const double f2 = init[0];
-    double delta = init[1];
+    grid_sum_d<2>(g.init_partials, g.init_stride, g.n_init, s_sc);
+    const double f2 = s_sc[0];
+    if (threadIdx.x == 0) { s_delta = s_sc[1]; s_beta = 0; s_conv = 0; }
+    __syncthreads();
+    R *pold = g.pbuf0, *pnew = g.pbuf1;
     int it = 0;
-    bool converged = false, ok = true;
+    bool ok = true;
     for (; it < g.imax; ++it) {
-        // q = V p ; pTq   (get_alpha_denominator :253-266)
+        const bool first = it == 0;
+        const R beta = s_beta;
+        // q = V p ; pTq   (get_alpha_denominator :253-266), p formed on the fly
         double acc1[1] = {0.0};
-        FFEA_SPMV_LOOP(g, a, sub, valid) {
-            R q0, q1, q2;
-            spmv_row(g, a, sub, valid, q0, q1, q2);
-            if (valid && sub == 0) {
-                g.q[4 * a] = q0; g.q[4 * a + 1] = q1; g.q[4 * a + 2] = q2;
-                acc1[0] += (double)(g.p[4 * a] * q0 + g.p[4 * a + 1] * q1 + g.p[4 * a + 2] * q2);
+        {
+            FFEA_SPMV_LOOP(g, a, sub, valid) {
+                R q0, q1, q2;
+                spmv_row(g, pold, beta, first, a, sub, valid, q0, q1, q2);
+                if (valid && sub == 0) {
+                    R p0, p1, p2;
+                    p_on_the_fly(g, pold, beta, first, a, p0, p1, p2);
+                    pnew[4 * a] = p0; pnew[4 * a + 1] = p1; pnew[4 * a + 2] = p2;
+                    g.q[4 * a] = q0; g.q[4 * a + 1] = q1; g.q[4 * a + 2] = q2;
+                    acc1[0] += (double)(p0 * q0 + p1 * q1 + p2 * q2);
+                }
             }
         }
-        block_sum<1>(acc1, smem);
-        if (threadIdx.x == 0) g.partials[blockIdx.x] = acc1[0];
+        double out1[1];
+        block_sum_smem<1>(acc1, smem, out1);
+        if (threadIdx.x == 0) g.partials[blockIdx.x] = out1[0];
         if (!(ok = grid_sync(g.gb, st, g.limit_ns))) break;
-        double pTq[1];
-        grid_partials_sum<1>(g.partials, 0, gridDim.x, pTq, smem);
-        const double alpha = delta / pTq[0];
-        const R ar = (R)alpha, mar = (R)(-alpha);
+        grid_sum_d<1>(g.partials, 0, gridDim.x, s_sc);
+        if (threadIdx.x == 0) s_alpha = (R)(s_delta / s_sc[0]);
+        __syncthreads();
+        const R alpha = s_alpha, malpha = -s_alpha;
         // x += alpha p ; r += (-alpha) q ; |r|^2 ; r.z   (vec3_add_to_scaled, residual2, apply_preconditioner)
         double acc2[2] = {0.0, 0.0};
         for (int a = tid; a < g.N; a += nthr) {
 #pragma unroll
-            for (int c = 0; c < 3; ++c) g.x[4 * a + c] += ar * g.p[4 * a + c];
+            for (int c = 0; c < 3; ++c) g.x[4 * a + c] += alpha * pnew[4 * a + c];
             R r[3], z[3];
 #pragma unroll
             for (int c = 0; c < 3; ++c) {
-                r[c] = g.r[4 * a + c] + mar * g.q[4 * a + c];
+                r[c] = g.r[4 * a + c] + malpha * g.q[4 * a + c];
                 g.r[4 * a + c] = r[c];
                 z[c] = g.dinv[4 * a + c] * r[c];
             }
             acc2[0] += (double)(r[0] * r[0] + r[1] * r[1] + r[2] * r[2]);
             acc2[1] += (double)(r[0] * z[0] + r[1] * z[1] + r[2] * z[2]);
         }
-        block_sum<2>(acc2, smem);
+        double out2[2];
+        block_sum_smem<2>(acc2, smem, out2);
         if (threadIdx.x == 0) {
-            g.partials[g.stride + blockIdx.x] = acc2[0];
-            g.partials[2 * g.stride + blockIdx.x] = acc2[1];
+            g.partials[g.stride + blockIdx.x] = out2[0];
+            g.partials[2 * g.stride + blockIdx.x] = out2[1];
         }
         if (!(ok = grid_sync(g.gb, st, g.limit_ns))) break;
-        double rz[2];
-        grid_partials_sum<2>(g.partials + g.stride, g.stride, gridDim.x, rz, smem);
-        const double res2 = (f2 == 0.0) ? 0.0 : rz[0] / f2;
-        if (blockIdx.x == 0 && threadIdx.x == 0 && it < g.hist_cap) g.history[it] = res2;
-        if ((g.check_last || it + 1 < g.imax) && res2 < g.eps2) {
-            converged = true;
+        grid_sum_d<2>(g.partials + g.stride, g.stride, gridDim.x, s_sc);
+        if (threadIdx.x == 0) {
+            const double res2 = (f2 == 0.0) ? 0.0 : s_sc[0] / f2;
+            if (blockIdx.x == 0 && it < g.hist_cap) g.history[it] = res2;
+            s_conv = (g.check_last || it + 1 < g.imax) && res2 < g.eps2;
+            const double delta_old = s_delta;
+            s_delta = s_sc[1];
+            s_beta = (R)(s_delta / delta_old);
+        }
+        __syncthreads();
+        if (s_conv) {
             ++it;
             break;
         }
-        const double delta_old = delta;
-        delta = rz[1];
-        const R beta = (R)(delta / delta_old);
-        // p = beta p + z   (vec3_scale_and_add :202-212)
-        for (int a = tid; a < g.N; a += nthr) {
-#pragma unroll
-            for (int c = 0; c < 3; ++c) g.p[4 * a + c] = beta * g.p[4 * a + c] + g.dinv[4 * a + c] * g.r[4 * a + c];
-        }
-        if (!(ok = grid_sync(g.gb, st, g.limit_ns))) break;
+        R *t = pold; pold = pnew; pnew = t;
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         if (!ok) {
             st->abort = 1;
-        } else if (!converged) {
+        } else if (!s_conv) {
             st->cg_fail = 1;
             st->abort = 1;
             st->last_iters = g.imax;

@@ -1,43 +1,59 @@
 // kernels_mixed.cuh -- the mixed-precision force gather and CG solve.
 //
-// The viscosity matrix of a blob with no Stokes drag is singular: rigid
-// translations and rotations (restricted to motions that leave every pinned
-// node at rest) produce no viscous stress, so K z = 0 for them. The reference's
-// FP64 CG never excites these directions far enough to matter before it
-// converges; with an FP32 matrix and SpMV, rounding puts ~1e-7 of every
-// product into them and the 1e-10 relative residual becomes unreachable.
-// This solver therefore keeps the residual orthogonal to the rigid modes:
-// every SpMV output q is replaced by q - Z G^{-1} Z^T q, which is what exact
-// arithmetic would give, with Z^T q formed from the moments
-// S1 = sum_a q_a and S2 = sum_a d_a x q_a (d_a = node position minus the rest
-// centroid) accumulated with exact FP64 products.
+// The viscosity matrix V of a blob without Stokes drag is singular: rigid
+// translations and rotations that leave every pinned node at rest produce no
+// viscous stress, so V z = 0 for them (the columns of Z). The reference's FP64
+// CG converges before rounding excites these directions; with V in FP32 the
+// rounding of every product (~1e-7) feeds them and the 1e-10 relative
+// residual becomes unreachable. This solver runs CG on
+//     V~ = V + D Z G^{-1} Z^T D,     G = Z^T D Z,  D = diag(V),
+// with the right-hand side projected to f^ = f - D Z G^{-1} Z^T f. V~ is
+// symmetric positive definite, D^{-1} V~ maps each rigid mode to itself, and
+// its solution x satisfies Z^T D x = 0 and V x = f^: exactly the solution the
+// reference's Jacobi-PCG builds from x = 0 (its iterates stay in D^{-1} times
+// the range of V, i.e. D-orthogonal to Z). With V~ nonsingular the whole CG
+// can run in FP32: matrix, SpMV, x, r, p, q.
 //
-// Precision: matrix values, SpMV, p, q, x in FP32; the residual r, its
-// updates, the preconditioned residual z = D^{-1} r, every dot product and
-// the projection moments in FP64. Iteration counts match the FP64 solver.
+// Reductions: each node's contribution is formed in FP32, summed over the
+// block and the grid as double-float pairs (two FP32 values, ~48-bit
+// significand) and finished in FP64; GB300 runs FP64 at 1/64 of the FP32
+// rate, so no per-node work touches the FP64 pipe. The scalars alpha, beta
+// and the mode coefficients are computed once per block in FP64.
+//
+// Z is expressed through per-node offsets d_a from a reference point: the
+// k-th mode is t_k + w_k x d_a. Z^T v needs only S1 = sum v_a and
+// S2 = sum d_a x v_a; D Z c at node a is D_a (tau + Omega x d_a).
 #pragma once
 
 #include "kernels.cuh"
 
 namespace ffea {
 
-constexpr int MIXED_GATHER_NP = 16;  // f.f, S1_f(3), S2_f(3), sum d(3), inertia(6)
-constexpr int MIXED_A_NP = 13;       // p.q, S1_q(3), S2_q(3), S1_p(3), S2_p(3)
-constexpr int MIXED_B_NP = 8;        // r.r, r.z, and (diagnostics) S1_r(3), S2_r(3)
-// partials rows: [0, A) phase A, [A, A+B) phase B, A+B the initial r.z. Each row is written in one phase
-// and read right after the next grid barrier; no row is written again before every block has passed
-// the barrier that follows its read.
+constexpr int MIXED_GATHER_NP = 28;  // f.f, S1_f(3), S2_f(3), M = sum Phi^T D Phi (21)
+constexpr int MIXED_A_NP = 7;        // p.q, S1(Dp)(3), S2(Dp)(3)
+constexpr int MIXED_B_NP = 2;        // r.r, r.z
+// partial rows: [0, A) phase A, [A, A+B) phase B, A+B the initial r.z
 constexpr int MIXED_PARTIAL_ROWS = MIXED_A_NP + MIXED_B_NP + 1;
 
-// mixed-path gather: f (FP64) and r = f; per-node offsets d; projection moments
+// the six basis columns phi_j of Phi_a = [I | (.) x d]: e_x, e_y, e_z, e_x x d, e_y x d, e_z x d
+__device__ __forceinline__ void phi_cols(float dx, float dy, float dz, float (&phi)[6][3]) {
+    phi[0][0] = 1; phi[0][1] = 0; phi[0][2] = 0;
+    phi[1][0] = 0; phi[1][1] = 1; phi[1][2] = 0;
+    phi[2][0] = 0; phi[2][1] = 0; phi[2][2] = 1;
+    phi[3][0] = 0; phi[3][1] = -dz; phi[3][2] = dy;
+    phi[4][0] = dz; phi[4][1] = 0; phi[4][2] = -dx;
+    phi[5][0] = -dy; phi[5][1] = dx; phi[5][2] = 0;
+}
+
+// mixed-path gather: f (FP64 copy) and r = f (FP32); node offsets; moments for the rigid-mode set-up
 template <class R>
 __global__ void __launch_bounds__(256) gather_mixed_kernel(GatherArgs<R> g) {
-    __shared__ double smem[MIXED_GATHER_NP * 32];
+    __shared__ float2 smem[MIXED_GATHER_NP * 32];
     const int a = blockIdx.x * blockDim.x + threadIdx.x;
-    if (a == 0 && g.gb) g.gb->count = 0u;
-    double acc[MIXED_GATHER_NP];
+    if (a == 0 && g.gb) { g.gb->count = 0u; g.gb->passed = 0u; }
+    df32 acc[MIXED_GATHER_NP];
 #pragma unroll
-    for (int i = 0; i < MIXED_GATHER_NP; ++i) acc[i] = 0.0;
+    for (int i = 0; i < MIXED_GATHER_NP; ++i) acc[i] = df32{0.f, 0.f};
     if (a < g.N && !g.st->abort) {
         float F0 = 0, F1 = 0, F2 = 0;
         for (int m = g.inc_ptr[a]; m < g.inc_ptr[a + 1]; ++m) {
@@ -54,93 +70,61 @@ __global__ void __launch_bounds__(256) gather_mixed_kernel(GatherArgs<R> g) {
             F2 -= (float)(g.vz[a] * dr);
         }
         if (g.pinned[a]) { F0 = 0; F1 = 0; F2 = 0; }
-        const double f0 = F0, f1 = F1, f2 = F2;
-        g.f[4 * a] = f0; g.f[4 * a + 1] = f1; g.f[4 * a + 2] = f2;
+        g.f[4 * a] = F0; g.f[4 * a + 1] = F1; g.f[4 * a + 2] = F2;
         if (g.mode == 1) {
             g.x[4 * a] = F0 * g.dinv[4 * a];
             g.x[4 * a + 1] = F1 * g.dinv[4 * a + 1];
             g.x[4 * a + 2] = F2 * g.dinv[4 * a + 2];
             return;
         }
-        g.r64[4 * a] = f0; g.r64[4 * a + 1] = f1; g.r64[4 * a + 2] = f2;
-        const float d0 = (float)(g.px[a] - g.xc[0]), d1 = (float)(g.py[a] - g.xc[1]), d2 = (float)(g.pz[a] - g.xc[2]);
-        g.dpos[a] = make_float4(d0, d1, d2, 0.f);
-        const double e0 = d0, e1 = d1, e2 = d2;
-        acc[0] = f0 * f0 + f1 * f1 + f2 * f2;
-        acc[1] = f0; acc[2] = f1; acc[3] = f2;
-        acc[4] = e1 * f2 - e2 * f1; acc[5] = e2 * f0 - e0 * f2; acc[6] = e0 * f1 - e1 * f0;
-        acc[7] = e0; acc[8] = e1; acc[9] = e2;
-        // sum_a (|d|^2 I - d d^T): xx, yy, zz, xy, xz, yz
-        const double dd = e0 * e0 + e1 * e1 + e2 * e2;
-        acc[10] = dd - e0 * e0; acc[11] = dd - e1 * e1; acc[12] = dd - e2 * e2;
-        acc[13] = -e0 * e1; acc[14] = -e0 * e2; acc[15] = -e1 * e2;
+        g.r[4 * a] = F0; g.r[4 * a + 1] = F1; g.r[4 * a + 2] = F2;
+        const float dx = (float)(g.px[a] - g.xc[0]), dy = (float)(g.py[a] - g.xc[1]), dz = (float)(g.pz[a] - g.xc[2]);
+        g.dpos[a] = make_float4(dx, dy, dz, 0.f);
+        acc[0] = df32{F0 * F0 + F1 * F1 + F2 * F2, 0.f};
+        acc[1].hi = F0; acc[2].hi = F1; acc[3].hi = F2;
+        acc[4].hi = dy * F2 - dz * F1; acc[5].hi = dz * F0 - dx * F2; acc[6].hi = dx * F1 - dy * F0;
+        if (g.diag) {
+            float phi[6][3];
+            phi_cols(dx, dy, dz, phi);
+            const float D[3] = {(float)g.diag[4 * a], (float)g.diag[4 * a + 1], (float)g.diag[4 * a + 2]};
+            int k = 7;
+#pragma unroll
+            for (int i = 0; i < 6; ++i)
+#pragma unroll
+                for (int j = i; j < 6; ++j, ++k)
+                    acc[k].hi = phi[i][0] * D[0] * phi[j][0] + phi[i][1] * D[1] * phi[j][1] + phi[i][2] * D[2] * phi[j][2];
+        }
     }
     if (g.mode == 1) return;
-    block_sum<MIXED_GATHER_NP>(acc, smem);
-    if (threadIdx.x == 0)
-#pragma unroll
-        for (int i = 0; i < MIXED_GATHER_NP; ++i) g.partials[i * g.stride + blockIdx.x] = acc[i];
-}
-
-// c = Ginv (T S1 + W S2); tau = T^T c; Omega = W^T c  (one thread)
-template <class R>
-__device__ __forceinline__ void mode_coeffs(const CgArgs<R> &g, const double *Ginv, const double S1[3],
-                                            const double S2[3], double c[6], double tau[3], double Om[3]) {
-    double v[6];
-    for (int k = 0; k < g.nmodes; ++k) {
-        const double *m = g.modes + 6 * k;
-        v[k] = m[0] * S1[0] + m[1] * S1[1] + m[2] * S1[2] + m[3] * S2[0] + m[4] * S2[1] + m[5] * S2[2];
-    }
-    for (int j = 0; j < g.nmodes; ++j) {
-        double s = 0.0;
-        for (int k = 0; k < g.nmodes; ++k) s += Ginv[6 * j + k] * v[k];
-        c[j] = s;
-    }
-    for (int i = 0; i < 3; ++i) { tau[i] = 0.0; Om[i] = 0.0; }
-    for (int k = 0; k < g.nmodes; ++k) {
-        const double *m = g.modes + 6 * k;
-        for (int i = 0; i < 3; ++i) { tau[i] += c[k] * m[i]; Om[i] += c[k] * m[3 + i]; }
-    }
-}
-
-template <class R>
-__global__ void __launch_bounds__(1024, 1) cg_mixed_kernel(CgArgs<R> g) {
-    __shared__ double smem[MIXED_A_NP * 32];
-    __shared__ double s_Ginv[36];
-    __shared__ double s_tau[3], s_Om[3], s_pq;
-    DevStatus *st = g.st;
-    if (st->abort) return;
-    const int nthr = gridDim.x * blockDim.x;
-    const int tid = blockIdx.x * blockDim.x + threadIdx.x;
-    const bool defl = g.nmodes > 0;
-    // set-up: moments of f, Gram matrix of the modes, projected initial residual
-    double gp[MIXED_GATHER_NP];
-    grid_partials_sum<MIXED_GATHER_NP>(g.init_partials, g.init_stride, g.n_init, gp, smem);
-    const double f2 = gp[0];
+    df32 out[MIXED_GATHER_NP];
+    block_sum_df<MIXED_GATHER_NP>(acc, smem, out);
     if (threadIdx.x == 0) {
-        double G[36], Ginv[36];
+        float2 *pp = reinterpret_cast<float2 *>(g.partials);
+#pragma unroll
+        for (int i = 0; i < MIXED_GATHER_NP; ++i) pp[i * g.stride + blockIdx.x] = make_float2(out[i].hi, out[i].lo);
+    }
+}
+
+// thread 0 of every block: G = Z^T D Z from the moments, its inverse, and the coefficients of the
+// projection of the right-hand side (kept out of line: it runs once per solve)
+template <class R>
+__device__ __noinline__ void mixed_setup(const CgArgs<R> &g, const double *s_sc, double *s_Ginv, float *s_tau,
+                                         float *s_Om, float *s_beta, int *s_conv) {
         const int k = g.nmodes;
-        const double Nn = (double)g.N;
+        double M[6][6];
+        int idx = 7;
+        for (int i = 0; i < 6; ++i)
+            for (int j = i; j < 6; ++j, ++idx) M[i][j] = M[j][i] = s_sc[idx];
+        double G[36], Ginv[36];
         for (int i = 0; i < k; ++i)
             for (int j = 0; j < k; ++j) {
-                const double *ti = g.modes + 6 * i, *tj = g.modes + 6 * j;
-                // t_i.t_j N + t_i.(w_j x sd) + t_j.(w_i x sd) + w_i^T I w_j
-                const double sd[3] = {gp[7], gp[8], gp[9]};
-                auto cross_dot = [&](const double *t, const double *w) {
-                    return t[0] * (w[1] * sd[2] - w[2] * sd[1]) + t[1] * (w[2] * sd[0] - w[0] * sd[2]) +
-                           t[2] * (w[0] * sd[1] - w[1] * sd[0]);
-                };
-                const double I[9] = {gp[10], gp[13], gp[14], gp[13], gp[11], gp[15], gp[14], gp[15], gp[12]};
-                double wIw = 0.0;
-                for (int p = 0; p < 3; ++p)
-                    for (int q = 0; q < 3; ++q) wIw += ti[3 + p] * I[3 * p + q] * tj[3 + q];
-                G[6 * i + j] = Nn * (ti[0] * tj[0] + ti[1] * tj[1] + ti[2] * tj[2]) + cross_dot(ti, tj + 3) +
-                               cross_dot(tj, ti + 3) + wIw;
+                double sum = 0.0;
+                for (int p = 0; p < 6; ++p)
+                    for (int q = 0; q < 6; ++q) sum += g.modes[6 * i + p] * M[p][q] * g.modes[6 * j + q];
+                G[6 * i + j] = sum;
+                Ginv[6 * i + j] = (i == j) ? 1.0 : 0.0;
             }
-        // Gauss-Jordan inverse of the small SPD Gram matrix
-        for (int i = 0; i < k; ++i)
-            for (int j = 0; j < k; ++j) Ginv[6 * i + j] = (i == j) ? 1.0 : 0.0;
-        for (int col = 0; col < k; ++col) {
+        for (int col = 0; col < k; ++col) {  // Gauss-Jordan on the SPD Gram matrix
             const double piv = G[6 * col + col];
             for (int j = 0; j < k; ++j) { G[6 * col + j] /= piv; Ginv[6 * col + j] /= piv; }
             for (int i = 0; i < k; ++i) {
@@ -150,158 +134,173 @@ __global__ void __launch_bounds__(1024, 1) cg_mixed_kernel(CgArgs<R> g) {
             }
         }
         for (int i = 0; i < 36; ++i) s_Ginv[i] = Ginv[i];
-        double c[6], tau[3] = {0, 0, 0}, Om[3] = {0, 0, 0};
-        if (defl) {
-            const double S1[3] = {gp[1], gp[2], gp[3]}, S2[3] = {gp[4], gp[5], gp[6]};
-            mode_coeffs(g, Ginv, S1, S2, c, tau, Om);
+        // c0 = G^{-1} Z^T f; tau, Omega of D Z c0
+        double v[6], tau[3] = {0, 0, 0}, Om[3] = {0, 0, 0};
+        for (int i = 0; i < k; ++i) {
+            const double *m = g.modes + 6 * i;
+            v[i] = m[0] * s_sc[1] + m[1] * s_sc[2] + m[2] * s_sc[3] + m[3] * s_sc[4] + m[4] * s_sc[5] + m[5] * s_sc[6];
         }
-        for (int i = 0; i < 3; ++i) { s_tau[i] = tau[i]; s_Om[i] = Om[i]; }
+        for (int i = 0; i < k; ++i) {
+            double c = 0.0;
+            for (int j = 0; j < k; ++j) c += Ginv[6 * i + j] * v[j];
+            for (int t = 0; t < 3; ++t) { tau[t] += c * g.modes[6 * i + t]; Om[t] += c * g.modes[6 * i + 3 + t]; }
+        }
+        for (int t = 0; t < 3; ++t) { s_tau[t] = (float)tau[t]; s_Om[t] = (float)Om[t]; }
+        *s_beta = 0.f;
+        *s_conv = 0;
     }
+
+template <class R>
+__global__ void __launch_bounds__(1024, 1) cg_mixed_kernel(CgArgs<R> g) {
+    __shared__ float2 smem[MIXED_GATHER_NP * 32];
+    __shared__ double s_sc[MIXED_GATHER_NP];
+    __shared__ double s_Ginv[36];
+    __shared__ float s_alpha, s_beta, s_tau[3], s_Om[3];
+    __shared__ double s_delta;
+    __shared__ int s_conv;
+    DevStatus *st = g.st;
+    if (st->abort) return;
+    const int nthr = gridDim.x * blockDim.x;
+    const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool defl = g.nmodes > 0;
+    float2 *partials = reinterpret_cast<float2 *>(g.partials);
+    // set-up: G = Z^T D Z from the moments M, projected right-hand side
+    grid_sum_df<MIXED_GATHER_NP>(reinterpret_cast<const float2 *>(g.init_partials), g.init_stride, g.n_init, s_sc);
+    const double f2 = s_sc[0];
+    if (threadIdx.x == 0) mixed_setup(g, s_sc, s_Ginv, s_tau, s_Om, &s_beta, &s_conv);
     __syncthreads();
-    double acc0[1] = {0.0};
+    df32 acc0[1] = {{0.f, 0.f}};
     for (int a = tid; a < g.N; a += nthr) {
-        const float4 d = g.dpos[a];
-        const double e0 = d.x, e1 = d.y, e2 = d.z;
-        double r0 = g.r64[4 * a], r1 = g.r64[4 * a + 1], r2 = g.r64[4 * a + 2];
+        float r0 = g.r[4 * a], r1 = g.r[4 * a + 1], r2 = g.r[4 * a + 2];
         if (defl) {
-            r0 -= s_tau[0] + (s_Om[1] * e2 - s_Om[2] * e1);
-            r1 -= s_tau[1] + (s_Om[2] * e0 - s_Om[0] * e2);
-            r2 -= s_tau[2] + (s_Om[0] * e1 - s_Om[1] * e0);
-            g.r64[4 * a] = r0; g.r64[4 * a + 1] = r1; g.r64[4 * a + 2] = r2;
+            const float4 d = g.dpos[a];
+            r0 -= g.diag[4 * a] * (s_tau[0] + (s_Om[1] * d.z - s_Om[2] * d.y));
+            r1 -= g.diag[4 * a + 1] * (s_tau[1] + (s_Om[2] * d.x - s_Om[0] * d.z));
+            r2 -= g.diag[4 * a + 2] * (s_tau[2] + (s_Om[0] * d.y - s_Om[1] * d.x));
+            g.r[4 * a] = r0; g.r[4 * a + 1] = r1; g.r[4 * a + 2] = r2;
         }
-        const double z0 = (double)g.dinv[4 * a] * r0, z1 = (double)g.dinv[4 * a + 1] * r1,
-                     z2 = (double)g.dinv[4 * a + 2] * r2;
-        g.p[4 * a] = (float)z0; g.p[4 * a + 1] = (float)z1; g.p[4 * a + 2] = (float)z2;
         g.x[4 * a] = 0.f; g.x[4 * a + 1] = 0.f; g.x[4 * a + 2] = 0.f;
-        acc0[0] += r0 * z0 + r1 * z1 + r2 * z2;
+        acc0[0] = df_add_f(acc0[0], r0 * (g.dinv[4 * a] * r0) + r1 * (g.dinv[4 * a + 1] * r1) + r2 * (g.dinv[4 * a + 2] * r2));
     }
-    block_sum<1>(acc0, smem);
     const int row0 = MIXED_A_NP + MIXED_B_NP;
-    if (threadIdx.x == 0) g.partials[row0 * g.stride + blockIdx.x] = acc0[0];
-    bool ok = grid_sync(g.gb, st, g.limit_ns);
-    double delta = 0.0;
-    if (ok) {
-        double d0[1];
-        grid_partials_sum<1>(g.partials + row0 * g.stride, 0, gridDim.x, d0, smem);
-        delta = d0[0];
+    {
+        df32 o[1];
+        block_sum_df<1>(acc0, smem, o);
+        if (threadIdx.x == 0) partials[row0 * g.stride + blockIdx.x] = make_float2(o[0].hi, o[0].lo);
     }
+    bool ok = grid_sync(g.gb, st, g.limit_ns);
+    if (ok) {
+        grid_sum_df<1>(partials + row0 * g.stride, 0, gridDim.x, s_sc);
+        if (threadIdx.x == 0) s_delta = s_sc[0];
+        __syncthreads();
+    }
+    float *pold = g.pbuf0, *pnew = g.pbuf1;
     int it = 0;
-    bool converged = false;
     for (; ok && it < g.imax; ++it) {
-        // phase A: q = V p, p.q and the projection moments of q and p
-        double acc[MIXED_A_NP];
+        const bool first = it == 0;
+        const float beta = s_beta;
+        // phase A: q = V p with p formed on the fly; p.q; moments of D p for Z^T D p
+        df32 acc[MIXED_A_NP];
 #pragma unroll
-        for (int i = 0; i < MIXED_A_NP; ++i) acc[i] = 0.0;
-        FFEA_SPMV_LOOP(g, a, sub, valid) {
-            float q0, q1, q2;
-            spmv_row(g, a, sub, valid, q0, q1, q2);
-            if (!valid || sub != 0) continue;
-            g.q[4 * a] = q0; g.q[4 * a + 1] = q1; g.q[4 * a + 2] = q2;
-            const float p0 = g.p[4 * a], p1 = g.p[4 * a + 1], p2 = g.p[4 * a + 2];
-            acc[0] += (double)(p0 * q0 + p1 * q1 + p2 * q2);
-            if (defl) {
-                const float4 d = g.dpos[a];
-                const double e0 = d.x, e1 = d.y, e2 = d.z, Q0 = q0, Q1 = q1, Q2 = q2;
-                acc[1] += Q0; acc[2] += Q1; acc[3] += Q2;
-                acc[4] += e1 * Q2 - e2 * Q1; acc[5] += e2 * Q0 - e0 * Q2; acc[6] += e0 * Q1 - e1 * Q0;
-                acc[7] += (double)p0; acc[8] += (double)p1; acc[9] += (double)p2;
-                acc[10] += (double)(d.y * p2 - d.z * p1);
-                acc[11] += (double)(d.z * p0 - d.x * p2);
-                acc[12] += (double)(d.x * p1 - d.y * p0);
-            }
-        }
-        block_sum<MIXED_A_NP>(acc, smem);
-        if (threadIdx.x == 0)
-#pragma unroll
-            for (int i = 0; i < MIXED_A_NP; ++i) g.partials[i * g.stride + blockIdx.x] = acc[i];
-        if (!(ok = grid_sync(g.gb, st, g.limit_ns))) break;
-        double sa[MIXED_A_NP];
-        grid_partials_sum<MIXED_A_NP>(g.partials, g.stride, gridDim.x, sa, smem);
-        if (threadIdx.x == 0) {
-            double c[6], tau[3] = {0, 0, 0}, Om[3] = {0, 0, 0}, pq = sa[0];
-            if (defl) {
-                const double S1q[3] = {sa[1], sa[2], sa[3]}, S2q[3] = {sa[4], sa[5], sa[6]};
-                mode_coeffs(g, s_Ginv, S1q, S2q, c, tau, Om);
-                for (int k = 0; k < g.nmodes; ++k) {
-                    const double *m = g.modes + 6 * k;
-                    const double zp = m[0] * sa[7] + m[1] * sa[8] + m[2] * sa[9] + m[3] * sa[10] + m[4] * sa[11] +
-                                      m[5] * sa[12];
-                    pq -= zp * c[k];
+        for (int i = 0; i < MIXED_A_NP; ++i) acc[i] = df32{0.f, 0.f};
+        {
+            FFEA_SPMV_LOOP(g, a, sub, valid) {
+                float q0, q1, q2;
+                spmv_row(g, pold, beta, first, a, sub, valid, q0, q1, q2);
+                if (!valid || sub != 0) continue;
+                float p0, p1, p2;
+                p_on_the_fly(g, pold, beta, first, a, p0, p1, p2);
+                pnew[4 * a] = p0; pnew[4 * a + 1] = p1; pnew[4 * a + 2] = p2;
+                g.q[4 * a] = q0; g.q[4 * a + 1] = q1; g.q[4 * a + 2] = q2;
+                acc[0] = df_add_f(acc[0], p0 * q0 + p1 * q1 + p2 * q2);
+                if (defl) {
+                    const float4 d = g.dpos[a];
+                    const float e0 = g.diag[4 * a] * p0, e1 = g.diag[4 * a + 1] * p1, e2 = g.diag[4 * a + 2] * p2;
+                    acc[1] = df_add_f(acc[1], e0); acc[2] = df_add_f(acc[2], e1); acc[3] = df_add_f(acc[3], e2);
+                    acc[4] = df_add_f(acc[4], d.y * e2 - d.z * e1);
+                    acc[5] = df_add_f(acc[5], d.z * e0 - d.x * e2);
+                    acc[6] = df_add_f(acc[6], d.x * e1 - d.y * e0);
                 }
             }
-            for (int i = 0; i < 3; ++i) { s_tau[i] = tau[i]; s_Om[i] = Om[i]; }
-            s_pq = pq;
+        }
+        {
+            df32 o[MIXED_A_NP];
+            block_sum_df<MIXED_A_NP>(acc, smem, o);
+            if (threadIdx.x == 0)
+#pragma unroll
+                for (int i = 0; i < MIXED_A_NP; ++i) partials[i * g.stride + blockIdx.x] = make_float2(o[i].hi, o[i].lo);
+        }
+        if (!(ok = grid_sync(g.gb, st, g.limit_ns))) break;
+        grid_sum_df<MIXED_A_NP>(partials, g.stride, gridDim.x, s_sc);
+        if (threadIdx.x == 0) {
+            // v = Z^T D p, c = G^{-1} v, p.V~p = p.q + v.c, alpha = delta / p.V~p
+            double pq = s_sc[0], tau[3] = {0, 0, 0}, Om[3] = {0, 0, 0};
+            if (defl) {
+                double v[6];
+                for (int i = 0; i < g.nmodes; ++i) {
+                    const double *m = g.modes + 6 * i;
+                    v[i] = m[0] * s_sc[1] + m[1] * s_sc[2] + m[2] * s_sc[3] + m[3] * s_sc[4] + m[4] * s_sc[5] +
+                           m[5] * s_sc[6];
+                }
+                for (int i = 0; i < g.nmodes; ++i) {
+                    double c = 0.0;
+                    for (int j = 0; j < g.nmodes; ++j) c += s_Ginv[6 * i + j] * v[j];
+                    pq += v[i] * c;
+                    for (int t = 0; t < 3; ++t) { tau[t] += c * g.modes[6 * i + t]; Om[t] += c * g.modes[6 * i + 3 + t]; }
+                }
+            }
+            for (int t = 0; t < 3; ++t) { s_tau[t] = (float)tau[t]; s_Om[t] = (float)Om[t]; }
+            s_alpha = (float)(s_delta / pq);
         }
         __syncthreads();
-        const double alpha = delta / s_pq;
-        const float af = (float)alpha;
-        const double t0 = s_tau[0], t1 = s_tau[1], t2 = s_tau[2], O0 = s_Om[0], O1 = s_Om[1], O2 = s_Om[2];
-        // phase B: x += alpha p ; r -= alpha (q - tau - Omega x d) ; r.r ; r.z
-        double acc2[MIXED_B_NP] = {0, 0, 0, 0, 0, 0, 0, 0};
+        const float alpha = s_alpha;
+        const float t0 = s_tau[0], t1 = s_tau[1], t2 = s_tau[2], O0 = s_Om[0], O1 = s_Om[1], O2 = s_Om[2];
+        // phase B: x += alpha p ; r -= alpha (q + D (tau + Omega x d)) ; r.r ; r.z
+        df32 acc2[MIXED_B_NP] = {{0.f, 0.f}, {0.f, 0.f}};
         for (int a = tid; a < g.N; a += nthr) {
 #pragma unroll
-            for (int c = 0; c < 3; ++c) g.x[4 * a + c] += af * g.p[4 * a + c];
-            double qh0 = g.q[4 * a], qh1 = g.q[4 * a + 1], qh2 = g.q[4 * a + 2];
+            for (int c = 0; c < 3; ++c) g.x[4 * a + c] += alpha * pnew[4 * a + c];
+            float q0 = g.q[4 * a], q1 = g.q[4 * a + 1], q2 = g.q[4 * a + 2];
             if (defl) {
                 const float4 d = g.dpos[a];
-                const double e0 = d.x, e1 = d.y, e2 = d.z;
-                qh0 -= t0 + (O1 * e2 - O2 * e1);
-                qh1 -= t1 + (O2 * e0 - O0 * e2);
-                qh2 -= t2 + (O0 * e1 - O1 * e0);
+                q0 += g.diag[4 * a] * (t0 + (O1 * d.z - O2 * d.y));
+                q1 += g.diag[4 * a + 1] * (t1 + (O2 * d.x - O0 * d.z));
+                q2 += g.diag[4 * a + 2] * (t2 + (O0 * d.y - O1 * d.x));
             }
-            const double r0 = g.r64[4 * a] - alpha * qh0, r1 = g.r64[4 * a + 1] - alpha * qh1,
-                         r2 = g.r64[4 * a + 2] - alpha * qh2;
-            g.r64[4 * a] = r0; g.r64[4 * a + 1] = r1; g.r64[4 * a + 2] = r2;
-            const double z0 = (double)g.dinv[4 * a] * r0, z1 = (double)g.dinv[4 * a + 1] * r1,
-                         z2 = (double)g.dinv[4 * a + 2] * r2;
-            acc2[0] += r0 * r0 + r1 * r1 + r2 * r2;
-            acc2[1] += r0 * z0 + r1 * z1 + r2 * z2;
-            if (g.debug & 2) {
-                const float4 d = g.dpos[a];
-                const double e0 = d.x, e1 = d.y, e2 = d.z;
-                acc2[2] += r0; acc2[3] += r1; acc2[4] += r2;
-                acc2[5] += e1 * r2 - e2 * r1; acc2[6] += e2 * r0 - e0 * r2; acc2[7] += e0 * r1 - e1 * r0;
-            }
+            const float r0 = g.r[4 * a] - alpha * q0, r1 = g.r[4 * a + 1] - alpha * q1, r2 = g.r[4 * a + 2] - alpha * q2;
+            g.r[4 * a] = r0; g.r[4 * a + 1] = r1; g.r[4 * a + 2] = r2;
+            acc2[0] = df_add_f(acc2[0], r0 * r0 + r1 * r1 + r2 * r2);
+            acc2[1] = df_add_f(acc2[1], r0 * (g.dinv[4 * a] * r0) + r1 * (g.dinv[4 * a + 1] * r1) +
+                                            r2 * (g.dinv[4 * a + 2] * r2));
         }
-        block_sum<MIXED_B_NP>(acc2, smem);
-        if (threadIdx.x == 0)
-            for (int i = 0; i < MIXED_B_NP; ++i) g.partials[(MIXED_A_NP + i) * g.stride + blockIdx.x] = acc2[i];
+        {
+            df32 o[MIXED_B_NP];
+            block_sum_df<MIXED_B_NP>(acc2, smem, o);
+            if (threadIdx.x == 0)
+                for (int i = 0; i < MIXED_B_NP; ++i)
+                    partials[(MIXED_A_NP + i) * g.stride + blockIdx.x] = make_float2(o[i].hi, o[i].lo);
+        }
         if (!(ok = grid_sync(g.gb, st, g.limit_ns))) break;
-        double rz[MIXED_B_NP];
-        grid_partials_sum<MIXED_B_NP>(g.partials + MIXED_A_NP * g.stride, g.stride, gridDim.x, rz, smem);
-        const double res2 = (f2 == 0.0) ? 0.0 : rz[0] / f2;
-        if ((g.debug & 2) && blockIdx.x == 0 && threadIdx.x == 0 && it < g.hist_cap && defl) {
-            double c[6], tau[3], Om[3];
-            const double S1r[3] = {rz[2], rz[3], rz[4]}, S2r[3] = {rz[5], rz[6], rz[7]};
-            mode_coeffs(g, s_Ginv, S1r, S2r, c, tau, Om);
-            double v = 0.0;  // (Z^T r)^T G^-1 (Z^T r) / f2
-            for (int k = 0; k < g.nmodes; ++k) {
-                const double *m = g.modes + 6 * k;
-                v += c[k] * (m[0] * S1r[0] + m[1] * S1r[1] + m[2] * S1r[2] + m[3] * S2r[0] + m[4] * S2r[1] + m[5] * S2r[2]);
-            }
-            g.history[it] = v / f2;  // replaces res2 in the history when debugging
+        grid_sum_df<MIXED_B_NP>(partials + MIXED_A_NP * g.stride, g.stride, gridDim.x, s_sc);
+        if (threadIdx.x == 0) {
+            const double res2 = (f2 == 0.0) ? 0.0 : s_sc[0] / f2;
+            if (blockIdx.x == 0 && it < g.hist_cap) g.history[it] = res2;
+            s_conv = (g.check_last || it + 1 < g.imax) && res2 < g.eps2;
+            const double delta_old = s_delta;
+            s_delta = s_sc[1];
+            s_beta = (float)(s_delta / delta_old);
         }
-        if (blockIdx.x == 0 && threadIdx.x == 0 && it < g.hist_cap && !(g.debug & 2)) g.history[it] = res2;
-        if ((g.check_last || it + 1 < g.imax) && res2 < g.eps2) {
-            converged = true;
+        __syncthreads();
+        if (s_conv) {
             ++it;
             break;
         }
-        const double delta_old = delta;
-        delta = rz[1];
-        const float beta = (float)(delta / delta_old);
-        // phase C: p = beta p + z
-        for (int a = tid; a < g.N; a += nthr) {
-#pragma unroll
-            for (int c = 0; c < 3; ++c)
-                g.p[4 * a + c] = beta * g.p[4 * a + c] + (float)((double)g.dinv[4 * a + c] * g.r64[4 * a + c]);
-        }
-        if (!(ok = grid_sync(g.gb, st, g.limit_ns))) break;
+        float *t = pold; pold = pnew; pnew = t;
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         if (!ok) {
             st->abort = 1;
-        } else if (!converged) {
+        } else if (!s_conv) {
             st->cg_fail = 1;
             st->abort = 1;
             st->last_iters = g.imax;
