@@ -534,7 +534,7 @@ struct BlobImpl final : ffea_gpu_blob {
     MrgJump *chunk_jump, *lane_jump, *step_jump;
     DevStatus *st;
     GridBarrier *gb;
-    int cg_grid = 0, gather_blocks = 0, partial_stride = 0;
+    int cg_grid = 0, gather_blocks = 0, partial_stride = 0, tpn = 4;
     float4 *dpos = nullptr;  // mixed path: node offsets from the reference point
     int nmodes = 0;
     double modes[36] = {}, xc[3] = {};
@@ -646,9 +646,12 @@ struct BlobImpl final : ffea_gpu_blob {
             g_last_error = "cg kernel cannot be made resident";
             return FFEA_GPU_ECUDA;
         }
-        // enough blocks for one SpMV row group per SPMV_TPN threads, at most one block per SM
-        const int rows_per_block = Launch<R>::cg_threads() / SPMV_TPN;
-        cg_grid = std::max(1, std::min(maxg, (N + rows_per_block - 1) / rows_per_block));
+        // one block per SM (fewer for small meshes); threads per SpMV row chosen so that every warp
+        // handles its rows in one pass: tpn = the largest power of two <= 8 with N <= warps * 32 / tpn
+        cg_grid = std::max(1, std::min(maxg, (N + 255) / 256));
+        const long long lanes = (long long)cg_grid * Launch<R>::cg_threads();
+        tpn = 8;
+        while (tpn > 1 && (long long)N * tpn > lanes) tpn >>= 1;
         partial_stride = cg_grid;
         CK(mem.alloc(&partials, (mixed ? MIXED_PARTIAL_ROWS : 3) * (size_t)partial_stride));
         CK(mem.alloc(&st, 1));
@@ -739,7 +742,7 @@ struct BlobImpl final : ffea_gpu_blob {
             ca.imax = p.max_iterations_cg;
             ca.eps2 = p.epsilon2;
             ca.limit_ns = 2000000000ull;
-            ca.history = history; ca.hist_cap = hist_cap;
+            ca.history = history; ca.hist_cap = hist_cap; ca.tpn = tpn;
             ca.dpos = dpos; ca.nmodes = nomass ? nmodes : 0;
             for (int i = 0; i < 36; ++i) ca.modes[i] = modes[i];
             CK(Launch<R>::cg(ca, cg_grid, stream));

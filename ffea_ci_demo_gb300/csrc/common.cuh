@@ -186,6 +186,34 @@ __device__ __forceinline__ void block_sum_df(const df32 (&v)[NV], float2 *smem, 
     __syncthreads();
 }
 
+__device__ __forceinline__ float warp_sum_f(float v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Block reduction of NV per-thread FP32 values: FP32 within each warp (32 values), double-float
+// across the warps (warp 0). Thread 0 gets the block totals. smem needs NV * 32 floats; the caller
+// must pass a __syncthreads() before smem is written again.
+template <int NV>
+__device__ __forceinline__ void block_reduce_f(const float (&v)[NV], float *smem, df32 (&out)[NV]) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+    for (int i = 0; i < NV; ++i) {
+        const float w = warp_sum_f(v[i]);
+        if (lane == 0) smem[i * 32 + wid] = w;
+    }
+    __syncthreads();
+    if (wid == 0) {
+#pragma unroll
+        for (int i = 0; i < NV; ++i) {
+            df32 t = {lane < nw ? smem[i * 32 + lane] : 0.f, 0.f};
+            t = warp_sum_df(t);
+            if (lane == 0) out[i] = t;
+        }
+    }
+}
+
 // Every block sums the per-block pairs partials[i*stride + b], b < nb, in the same order; results
 // (as doubles, hi + lo) land in s_out[0..NV) in shared memory for the whole block.
 template <int NV>

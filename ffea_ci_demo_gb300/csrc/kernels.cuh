@@ -372,7 +372,8 @@ struct CgArgs {
     const R *dinv;        // Jacobi preconditioner, 4 per node
     const R *diag;        // mixed path: diagonal of V, 4 per node
     R *x, *r, *q;
-    R *pbuf0, *pbuf1;     // search direction, double-buffered
+    R *pbuf0, *pbuf1;     // search direction (mixed path: double-buffered; FP64 path: pbuf0 only)
+    int tpn;              // threads per matrix row in the SpMV (1, 2, 4 or 8)
     const double *init_partials;  // from the gather kernel
     int n_init, init_stride;
     double *partials;     // per-block partial sums (float2 pairs on the mixed path)
@@ -390,8 +391,6 @@ struct CgArgs {
     double modes[36];
 };
 
-constexpr int SPMV_TPN = 4;  // threads per matrix row (node) in the SpMV
-
 // p at node b for this iteration: p_new = beta p_old + D^{-1} r (vec3_scale_and_add with the
 // preconditioned residual, src/NoMassCGSolver.cpp:181-183), or z itself on the first iteration.
 template <class R>
@@ -402,70 +401,82 @@ __device__ __forceinline__ void p_on_the_fly(const CgArgs<R> &g, const R *pold, 
     if (first) {
         p0 = z0; p1 = z1; p2 = z2;
     } else {
-        p0 = beta * pold[4 * b] + z0;
-        p1 = beta * pold[4 * b + 1] + z1;
-        p2 = beta * pold[4 * b + 2] + z2;
+        p0 = fma(beta, pold[4 * b], z0);
+        p1 = fma(beta, pold[4 * b + 1], z1);
+        p2 = fma(beta, pold[4 * b + 2], z2);
     }
 }
 
-// Row a of q = V p, summed by the SPMV_TPN lanes of a node group over blocks k = sub, sub + TPN, ...
-// (p recomputed on the fly) and combined with shuffles; every lane of the group returns the row.
-// All 32 lanes of the warp call it together (rows past the end pass valid = false).
-template <class R>
+// Row a of q = V p, summed by the tpn lanes of a node group over blocks k = sub, sub + tpn, ... and
+// combined with shuffles; every lane of the group returns the row. All 32 lanes of the warp call it
+// together (rows past the end pass valid = false). ONTHEFLY: p is formed from p_old, r and D^{-1}
+// (mixed path); otherwise it is read from pold (FP64 path).
+template <bool ONTHEFLY, class R>
 __device__ __forceinline__ void spmv_row(const CgArgs<R> &g, const R *pold, R beta, bool first, int a, int sub,
                                          bool valid, R &q0, R &q1, R &q2) {
     q0 = 0.0; q1 = 0.0; q2 = 0.0;
+    const int tpn = g.tpn;
     if (valid) {
         const int s = a >> 5, lane = a & 31;
         const int base = g.slice_ptr[s];
         const int len = g.rowlen[a];
         if (g.block3) {
             const R *v = g.val + 9 * (size_t)base + lane;
-#pragma unroll 2
-            for (int k = sub; k < len; k += SPMV_TPN) {
+#pragma unroll 1
+            for (int k = sub; k < len; k += tpn) {
                 const int b = g.bcol[base + 32 * k + lane];
                 const R *vk = v + (size_t)32 * 9 * k;
                 const R v0 = vk[0], v1 = vk[32], v2 = vk[64], v3 = vk[96], v4 = vk[128], v5 = vk[160], v6 = vk[192],
                         v7 = vk[224], v8 = vk[256];
                 R p0, p1, p2;
-                p_on_the_fly(g, pold, beta, first, b, p0, p1, p2);
-                q0 += v0 * p0; q0 += v1 * p1; q0 += v2 * p2;
-                q1 += v3 * p0; q1 += v4 * p1; q1 += v5 * p2;
-                q2 += v6 * p0; q2 += v7 * p1; q2 += v8 * p2;
+                if (ONTHEFLY) {
+                    p_on_the_fly(g, pold, beta, first, b, p0, p1, p2);
+                } else {
+                    p0 = pold[4 * b]; p1 = pold[4 * b + 1]; p2 = pold[4 * b + 2];
+                }
+                q0 = fma(v0, p0, q0); q0 = fma(v1, p1, q0); q0 = fma(v2, p2, q0);
+                q1 = fma(v3, p0, q1); q1 = fma(v4, p1, q1); q1 = fma(v5, p2, q1);
+                q2 = fma(v6, p0, q2); q2 = fma(v7, p1, q2); q2 = fma(v8, p2, q2);
             }
         } else {
             const R *v = g.val + base + lane;
-            for (int k = sub; k < len; k += SPMV_TPN) {
+            for (int k = sub; k < len; k += tpn) {
                 const int b = g.bcol[base + 32 * k + lane];
                 const R m = v[32 * k];
                 R p0, p1, p2;
-                p_on_the_fly(g, pold, beta, first, b, p0, p1, p2);
-                q0 += m * p0;
-                q1 += m * p1;
-                q2 += m * p2;
+                if (ONTHEFLY) {
+                    p_on_the_fly(g, pold, beta, first, b, p0, p1, p2);
+                } else {
+                    p0 = pold[4 * b]; p1 = pold[4 * b + 1]; p2 = pold[4 * b + 2];
+                }
+                q0 = fma(m, p0, q0);
+                q1 = fma(m, p1, q1);
+                q2 = fma(m, p2, q2);
             }
         }
     }
-#pragma unroll
-    for (int o = 1; o < SPMV_TPN; o <<= 1) {
+    for (int o = 1; o < tpn; o <<= 1) {
         q0 += __shfl_xor_sync(0xffffffffu, q0, o);
         q1 += __shfl_xor_sync(0xffffffffu, q1, o);
         q2 += __shfl_xor_sync(0xffffffffu, q2, o);
     }
 }
 
-// node loop of the SpMV phase: warp w covers nodes [w*NPW, (w+1)*NPW), NPW = 32 / SPMV_TPN, grid-strided
+// node loop of the SpMV phase: warp w covers nodes [w*NPW, (w+1)*NPW), NPW = 32 / tpn, grid-strided
 #define FFEA_SPMV_LOOP(g, a, sub, valid)                                                        \
-    const int sub = threadIdx.x % SPMV_TPN;                                                     \
-    const int npw_ = 32 / SPMV_TPN;                                                              \
+    const int sub = threadIdx.x % (g).tpn;                                                      \
+    const int npw_ = 32 / (g).tpn;                                                               \
     const int wglob_ = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;                            \
     const int wstride_ = (gridDim.x * blockDim.x) >> 5;                                          \
-    for (int a0_ = wglob_ * npw_, a = a0_ + (threadIdx.x & 31) / SPMV_TPN; a0_ < (g).N;         \
-         a0_ += wstride_ * npw_, a = a0_ + (threadIdx.x & 31) / SPMV_TPN)                      \
+    for (int a0_ = wglob_ * npw_, a = a0_ + (threadIdx.x & 31) / (g).tpn; a0_ < (g).N;          \
+         a0_ += wstride_ * npw_, a = a0_ + (threadIdx.x & 31) / (g).tpn)                       \
         for (bool valid = a < (g).N, once_ = true; once_; once_ = false)
 
 constexpr int CG_MAX_THREADS = 1024;
 
+// FP64 CG: three phases (SpMV, residual update, direction update) with a grid barrier after each;
+// every multiply-add is fused (the cross-node sums are reordered anyway, so the CG agrees with the
+// reference to rounding, not bitwise).
 template <class R>
 __global__ void __launch_bounds__(1024, 1) cg_kernel(CgArgs<R> g) {
     __shared__ double smem[2 * CG_MAX_THREADS];
@@ -477,28 +488,26 @@ __global__ void __launch_bounds__(1024, 1) cg_kernel(CgArgs<R> g) {
     if (st->abort) return;
     const int nthr = gridDim.x * blockDim.x;
     const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+    R *p = g.pbuf0;
+    // p = z = D^{-1} r  (conjugate_gradient_residual_assume_x_zero, src/NoMassCGSolver.cpp:196-220)
+    for (int a = tid; a < g.N; a += nthr)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) p[4 * a + c] = g.dinv[4 * a + c] * g.r[4 * a + c];
     grid_sum_d<2>(g.init_partials, g.init_stride, g.n_init, s_sc);
     const double f2 = s_sc[0];
-    if (threadIdx.x == 0) { s_delta = s_sc[1]; s_beta = 0; s_conv = 0; }
-    __syncthreads();
-    R *pold = g.pbuf0, *pnew = g.pbuf1;
+    if (threadIdx.x == 0) { s_delta = s_sc[1]; s_conv = 0; }
+    bool ok = grid_sync(g.gb, st, g.limit_ns);
     int it = 0;
-    bool ok = true;
-    for (; it < g.imax; ++it) {
-        const bool first = it == 0;
-        const R beta = s_beta;
-        // q = V p ; pTq   (get_alpha_denominator :253-266), p formed on the fly
+    for (; ok && it < g.imax; ++it) {
+        // q = V p ; pTq   (get_alpha_denominator :253-266)
         double acc1[1] = {0.0};
         {
             FFEA_SPMV_LOOP(g, a, sub, valid) {
                 R q0, q1, q2;
-                spmv_row(g, pold, beta, first, a, sub, valid, q0, q1, q2);
+                spmv_row<false>(g, p, (R)0, false, a, sub, valid, q0, q1, q2);
                 if (valid && sub == 0) {
-                    R p0, p1, p2;
-                    p_on_the_fly(g, pold, beta, first, a, p0, p1, p2);
-                    pnew[4 * a] = p0; pnew[4 * a + 1] = p1; pnew[4 * a + 2] = p2;
                     g.q[4 * a] = q0; g.q[4 * a + 1] = q1; g.q[4 * a + 2] = q2;
-                    acc1[0] += (double)(p0 * q0 + p1 * q1 + p2 * q2);
+                    acc1[0] += (double)fma(p[4 * a + 2], q2, fma(p[4 * a + 1], q1, p[4 * a] * q0));
                 }
             }
         }
@@ -514,16 +523,16 @@ __global__ void __launch_bounds__(1024, 1) cg_kernel(CgArgs<R> g) {
         double acc2[2] = {0.0, 0.0};
         for (int a = tid; a < g.N; a += nthr) {
 #pragma unroll
-            for (int c = 0; c < 3; ++c) g.x[4 * a + c] += alpha * pnew[4 * a + c];
+            for (int c = 0; c < 3; ++c) g.x[4 * a + c] = fma(alpha, p[4 * a + c], g.x[4 * a + c]);
             R r[3], z[3];
 #pragma unroll
             for (int c = 0; c < 3; ++c) {
-                r[c] = g.r[4 * a + c] + malpha * g.q[4 * a + c];
+                r[c] = fma(malpha, g.q[4 * a + c], g.r[4 * a + c]);
                 g.r[4 * a + c] = r[c];
                 z[c] = g.dinv[4 * a + c] * r[c];
             }
-            acc2[0] += (double)(r[0] * r[0] + r[1] * r[1] + r[2] * r[2]);
-            acc2[1] += (double)(r[0] * z[0] + r[1] * z[1] + r[2] * z[2]);
+            acc2[0] += (double)fma(r[2], r[2], fma(r[1], r[1], r[0] * r[0]));
+            acc2[1] += (double)fma(r[2], z[2], fma(r[1], z[1], r[0] * z[0]));
         }
         double out2[2];
         block_sum_smem<2>(acc2, smem, out2);
@@ -546,7 +555,12 @@ __global__ void __launch_bounds__(1024, 1) cg_kernel(CgArgs<R> g) {
             ++it;
             break;
         }
-        R *t = pold; pold = pnew; pnew = t;
+        // p = beta p + z   (vec3_scale_and_add :202-212)
+        const R beta = s_beta;
+        for (int a = tid; a < g.N; a += nthr)
+#pragma unroll
+            for (int c = 0; c < 3; ++c) p[4 * a + c] = fma(beta, p[4 * a + c], g.dinv[4 * a + c] * g.r[4 * a + c]);
+        if (!(ok = grid_sync(g.gb, st, g.limit_ns))) break;
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         if (!ok) {

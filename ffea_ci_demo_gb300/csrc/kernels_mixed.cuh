@@ -153,6 +153,7 @@ __device__ __noinline__ void mixed_setup(const CgArgs<R> &g, const double *s_sc,
 template <class R>
 __global__ void __launch_bounds__(1024, 1) cg_mixed_kernel(CgArgs<R> g) {
     __shared__ float2 smem[MIXED_GATHER_NP * 32];
+    __shared__ float smemf[MIXED_A_NP * 32];
     __shared__ double s_sc[MIXED_GATHER_NP];
     __shared__ double s_Ginv[36];
     __shared__ float s_alpha, s_beta, s_tau[3], s_Om[3];
@@ -200,32 +201,32 @@ __global__ void __launch_bounds__(1024, 1) cg_mixed_kernel(CgArgs<R> g) {
         const bool first = it == 0;
         const float beta = s_beta;
         // phase A: q = V p with p formed on the fly; p.q; moments of D p for Z^T D p
-        df32 acc[MIXED_A_NP];
+        float acc[MIXED_A_NP];
 #pragma unroll
-        for (int i = 0; i < MIXED_A_NP; ++i) acc[i] = df32{0.f, 0.f};
+        for (int i = 0; i < MIXED_A_NP; ++i) acc[i] = 0.f;
         {
             FFEA_SPMV_LOOP(g, a, sub, valid) {
                 float q0, q1, q2;
-                spmv_row(g, pold, beta, first, a, sub, valid, q0, q1, q2);
+                spmv_row<true>(g, pold, beta, first, a, sub, valid, q0, q1, q2);
                 if (!valid || sub != 0) continue;
                 float p0, p1, p2;
                 p_on_the_fly(g, pold, beta, first, a, p0, p1, p2);
                 pnew[4 * a] = p0; pnew[4 * a + 1] = p1; pnew[4 * a + 2] = p2;
                 g.q[4 * a] = q0; g.q[4 * a + 1] = q1; g.q[4 * a + 2] = q2;
-                acc[0] = df_add_f(acc[0], p0 * q0 + p1 * q1 + p2 * q2);
+                acc[0] += p0 * q0 + p1 * q1 + p2 * q2;
                 if (defl) {
                     const float4 d = g.dpos[a];
                     const float e0 = g.diag[4 * a] * p0, e1 = g.diag[4 * a + 1] * p1, e2 = g.diag[4 * a + 2] * p2;
-                    acc[1] = df_add_f(acc[1], e0); acc[2] = df_add_f(acc[2], e1); acc[3] = df_add_f(acc[3], e2);
-                    acc[4] = df_add_f(acc[4], d.y * e2 - d.z * e1);
-                    acc[5] = df_add_f(acc[5], d.z * e0 - d.x * e2);
-                    acc[6] = df_add_f(acc[6], d.x * e1 - d.y * e0);
+                    acc[1] += e0; acc[2] += e1; acc[3] += e2;
+                    acc[4] += d.y * e2 - d.z * e1;
+                    acc[5] += d.z * e0 - d.x * e2;
+                    acc[6] += d.x * e1 - d.y * e0;
                 }
             }
         }
         {
             df32 o[MIXED_A_NP];
-            block_sum_df<MIXED_A_NP>(acc, smem, o);
+            block_reduce_f<MIXED_A_NP>(acc, smemf, o);
             if (threadIdx.x == 0)
 #pragma unroll
                 for (int i = 0; i < MIXED_A_NP; ++i) partials[i * g.stride + blockIdx.x] = make_float2(o[i].hi, o[i].lo);
@@ -256,7 +257,7 @@ __global__ void __launch_bounds__(1024, 1) cg_mixed_kernel(CgArgs<R> g) {
         const float alpha = s_alpha;
         const float t0 = s_tau[0], t1 = s_tau[1], t2 = s_tau[2], O0 = s_Om[0], O1 = s_Om[1], O2 = s_Om[2];
         // phase B: x += alpha p ; r -= alpha (q + D (tau + Omega x d)) ; r.r ; r.z
-        df32 acc2[MIXED_B_NP] = {{0.f, 0.f}, {0.f, 0.f}};
+        float acc2[MIXED_B_NP] = {0.f, 0.f};
         for (int a = tid; a < g.N; a += nthr) {
 #pragma unroll
             for (int c = 0; c < 3; ++c) g.x[4 * a + c] += alpha * pnew[4 * a + c];
@@ -269,13 +270,12 @@ __global__ void __launch_bounds__(1024, 1) cg_mixed_kernel(CgArgs<R> g) {
             }
             const float r0 = g.r[4 * a] - alpha * q0, r1 = g.r[4 * a + 1] - alpha * q1, r2 = g.r[4 * a + 2] - alpha * q2;
             g.r[4 * a] = r0; g.r[4 * a + 1] = r1; g.r[4 * a + 2] = r2;
-            acc2[0] = df_add_f(acc2[0], r0 * r0 + r1 * r1 + r2 * r2);
-            acc2[1] = df_add_f(acc2[1], r0 * (g.dinv[4 * a] * r0) + r1 * (g.dinv[4 * a + 1] * r1) +
-                                            r2 * (g.dinv[4 * a + 2] * r2));
+            acc2[0] += r0 * r0 + r1 * r1 + r2 * r2;
+            acc2[1] += r0 * (g.dinv[4 * a] * r0) + r1 * (g.dinv[4 * a + 1] * r1) + r2 * (g.dinv[4 * a + 2] * r2);
         }
         {
             df32 o[MIXED_B_NP];
-            block_sum_df<MIXED_B_NP>(acc2, smem, o);
+            block_reduce_f<MIXED_B_NP>(acc2, smemf, o);
             if (threadIdx.x == 0)
                 for (int i = 0; i < MIXED_B_NP; ++i)
                     partials[(MIXED_A_NP + i) * g.stride + blockIdx.x] = make_float2(o[i].hi, o[i].lo);
