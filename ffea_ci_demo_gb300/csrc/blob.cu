@@ -506,6 +506,7 @@ struct ffea_gpu_blob {
     virtual int get_elements(double *nf, double *vol, double *visc) = 0;
     virtual int get_rhs(double *rhs) = 0;
     virtual int cg_history(double *res2, int max_entries, int *count) = 0;
+    virtual int cg_profile(double *ns, int n) = 0;
     virtual int get_matrix_values(std::vector<double> &val_sell) = 0;
 };
 
@@ -539,6 +540,7 @@ struct BlobImpl final : ffea_gpu_blob {
     int nmodes = 0;
     double modes[36] = {}, xc[3] = {};
     double *history = nullptr;
+    unsigned long long *phase_ns = nullptr;
     int hist_cap = 0;
     cudaEvent_t ev[FFEA_GPU_NUM_PHASES + 1] = {};
     bool record_phases = false;
@@ -657,6 +659,7 @@ struct BlobImpl final : ffea_gpu_blob {
         CK(mem.alloc(&st, 1));
         hist_cap = std::min(std::max(p.max_iterations_cg, 1), 1 << 20);
         CK(mem.alloc(&history, (size_t)hist_cap));
+        CK(mem.alloc(&phase_ns, (size_t)FFEA_GPU_CG_PHASES));
         CK(mem.alloc(&gb, 1));
         // RNG jump tables: draws of element e start 7e after the step's state; a step consumes 7T
         const int nchunks = (T + 31) / 32;
@@ -742,7 +745,8 @@ struct BlobImpl final : ffea_gpu_blob {
             ca.imax = p.max_iterations_cg;
             ca.eps2 = p.epsilon2;
             ca.limit_ns = 2000000000ull;
-            ca.history = history; ca.hist_cap = hist_cap; ca.tpn = tpn;
+            ca.history = history; ca.hist_cap = hist_cap; ca.tpn = tpn; ca.phase_ns = phase_ns;
+            CK(cudaMemsetAsync(phase_ns, 0, FFEA_GPU_CG_PHASES * sizeof(unsigned long long), stream));
             ca.dpos = dpos; ca.nmodes = nomass ? nmodes : 0;
             for (int i = 0; i < 36; ++i) ca.modes[i] = modes[i];
             CK(Launch<R>::cg(ca, cg_grid, stream));
@@ -952,6 +956,14 @@ struct BlobImpl final : ffea_gpu_blob {
         return FFEA_GPU_OK;
     }
 
+    int cg_profile(double *ns, int n) override {
+        unsigned long long t[FFEA_GPU_CG_PHASES];
+        CK(cudaMemcpyAsync(t, phase_ns, sizeof t, cudaMemcpyDeviceToHost, stream));
+        CK(cudaStreamSynchronize(stream));
+        for (int k = 0; k < n && k < FFEA_GPU_CG_PHASES; ++k) ns[k] = (double)t[k];
+        return FFEA_GPU_OK;
+    }
+
     int get_rhs(double *rhs) override {
         const int N = h.N;
         std::vector<double> hf(4 * (size_t)N);
@@ -1150,6 +1162,15 @@ int ffea_gpu_blob_cg_iterations(ffea_gpu_blob *b, int *last, long long *total) {
 int ffea_gpu_blob_cg_history(ffea_gpu_blob *b, double *res2, int max_entries, int *count) {
     if (!b || max_entries < 0) return FFEA_GPU_EINPUT;
     return b->cg_history(res2, max_entries, count);
+}
+
+int ffea_gpu_blob_cg_profile(ffea_gpu_blob *b, double *ns, int n) {
+    if (!b || !ns || n < 0) return FFEA_GPU_EINPUT;
+    if (b->p.solver == FFEA_GPU_MASSLUMPED) {
+        for (int k = 0; k < n; ++k) ns[k] = 0.0;
+        return FFEA_GPU_OK;
+    }
+    return b->cg_profile(ns, n);
 }
 
 int ffea_gpu_blob_sizes(ffea_gpu_blob *b, int *nl, int *ne, long long *nb) {

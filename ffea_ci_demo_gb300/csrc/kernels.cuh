@@ -385,6 +385,7 @@ struct CgArgs {
     unsigned long long limit_ns;
     double *history;      // |r|^2/|f|^2 per iteration (block 0 writes), capacity hist_cap
     int hist_cap;
+    unsigned long long *phase_ns;  // FFEA_GPU_CG_PHASES timers of block 0 (thread 0), summed over iterations
     // mixed path: node offsets from the reference point and the rigid-mode coefficients (t, omega)
     const float4 *dpos;
     int nmodes;
@@ -420,7 +421,28 @@ __device__ __forceinline__ void spmv_row(const CgArgs<R> &g, const R *pold, R be
         const int s = a >> 5, lane = a & 31;
         const int base = g.slice_ptr[s];
         const int len = g.rowlen[a];
-        if (g.block3) {
+        if (g.block3 && ONTHEFLY) {
+            // two blocks per trip: both column indices and all their loads are in flight together
+            const R *v = g.val + 9 * (size_t)base + lane;
+            for (int k = sub; k < len; k += 2 * tpn) {
+                const int k2 = k + tpn;
+                const bool two = k2 < len;
+                const int b1 = g.bcol[base + 32 * k + lane];
+                const int b2 = two ? g.bcol[base + 32 * k2 + lane] : b1;
+                const R *vk = v + (size_t)32 * 9 * k;
+                const R *vk2 = v + (size_t)32 * 9 * (two ? k2 : k);
+                R p0, p1, p2, u0, u1, u2;
+                p_on_the_fly(g, pold, beta, first, b1, p0, p1, p2);
+                p_on_the_fly(g, pold, beta, first, b2, u0, u1, u2);
+                if (!two) { u0 = 0; u1 = 0; u2 = 0; }
+                q0 = fma(vk[0], p0, q0); q0 = fma(vk[32], p1, q0); q0 = fma(vk[64], p2, q0);
+                q1 = fma(vk[96], p0, q1); q1 = fma(vk[128], p1, q1); q1 = fma(vk[160], p2, q1);
+                q2 = fma(vk[192], p0, q2); q2 = fma(vk[224], p1, q2); q2 = fma(vk[256], p2, q2);
+                q0 = fma(vk2[0], u0, q0); q0 = fma(vk2[32], u1, q0); q0 = fma(vk2[64], u2, q0);
+                q1 = fma(vk2[96], u0, q1); q1 = fma(vk2[128], u1, q1); q1 = fma(vk2[160], u2, q1);
+                q2 = fma(vk2[192], u0, q2); q2 = fma(vk2[224], u1, q2); q2 = fma(vk2[256], u2, q2);
+            }
+        } else if (g.block3) {
             const R *v = g.val + 9 * (size_t)base + lane;
 #pragma unroll 1
             for (int k = sub; k < len; k += tpn) {
@@ -474,6 +496,16 @@ __device__ __forceinline__ void spmv_row(const CgArgs<R> &g, const R *pold, R be
 
 constexpr int CG_MAX_THREADS = 1024;
 
+// phase timer of block 0, thread 0: adds the time since the previous mark to phase_ns[k]
+#define FFEA_MARK(g, t_prev, k)                                                   \
+    do {                                                                          \
+        if (blockIdx.x == 0 && threadIdx.x == 0) {                                \
+            const unsigned long long t_now_ = globaltimer_ns();                   \
+            (g).phase_ns[k] += t_now_ - (t_prev);                                 \
+            (t_prev) = t_now_;                                                    \
+        }                                                                         \
+    } while (0)
+
 // FP64 CG: three phases (SpMV, residual update, direction update) with a grid barrier after each;
 // every multiply-add is fused (the cross-node sums are reordered anyway, so the CG agrees with the
 // reference to rounding, not bitwise).
@@ -488,6 +520,7 @@ __global__ void __launch_bounds__(1024, 1) cg_kernel(CgArgs<R> g) {
     if (st->abort) return;
     const int nthr = gridDim.x * blockDim.x;
     const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+    unsigned long long tm = (blockIdx.x == 0 && threadIdx.x == 0) ? globaltimer_ns() : 0ull;
     R *p = g.pbuf0;
     // p = z = D^{-1} r  (conjugate_gradient_residual_assume_x_zero, src/NoMassCGSolver.cpp:196-220)
     for (int a = tid; a < g.N; a += nthr)
@@ -497,6 +530,7 @@ __global__ void __launch_bounds__(1024, 1) cg_kernel(CgArgs<R> g) {
     const double f2 = s_sc[0];
     if (threadIdx.x == 0) { s_delta = s_sc[1]; s_conv = 0; }
     bool ok = grid_sync(g.gb, st, g.limit_ns);
+    FFEA_MARK(g, tm, 0);
     int it = 0;
     for (; ok && it < g.imax; ++it) {
         // q = V p ; pTq   (get_alpha_denominator :253-266)
@@ -511,13 +545,17 @@ __global__ void __launch_bounds__(1024, 1) cg_kernel(CgArgs<R> g) {
                 }
             }
         }
+        FFEA_MARK(g, tm, 1);
         double out1[1];
         block_sum_smem<1>(acc1, smem, out1);
         if (threadIdx.x == 0) g.partials[blockIdx.x] = out1[0];
+        FFEA_MARK(g, tm, 2);
         if (!(ok = grid_sync(g.gb, st, g.limit_ns))) break;
+        FFEA_MARK(g, tm, 3);
         grid_sum_d<1>(g.partials, 0, gridDim.x, s_sc);
         if (threadIdx.x == 0) s_alpha = (R)(s_delta / s_sc[0]);
         __syncthreads();
+        FFEA_MARK(g, tm, 4);
         const R alpha = s_alpha, malpha = -s_alpha;
         // x += alpha p ; r += (-alpha) q ; |r|^2 ; r.z   (vec3_add_to_scaled, residual2, apply_preconditioner)
         double acc2[2] = {0.0, 0.0};
@@ -534,13 +572,16 @@ __global__ void __launch_bounds__(1024, 1) cg_kernel(CgArgs<R> g) {
             acc2[0] += (double)fma(r[2], r[2], fma(r[1], r[1], r[0] * r[0]));
             acc2[1] += (double)fma(r[2], z[2], fma(r[1], z[1], r[0] * z[0]));
         }
+        FFEA_MARK(g, tm, 5);
         double out2[2];
         block_sum_smem<2>(acc2, smem, out2);
         if (threadIdx.x == 0) {
             g.partials[g.stride + blockIdx.x] = out2[0];
             g.partials[2 * g.stride + blockIdx.x] = out2[1];
         }
+        FFEA_MARK(g, tm, 6);
         if (!(ok = grid_sync(g.gb, st, g.limit_ns))) break;
+        FFEA_MARK(g, tm, 7);
         grid_sum_d<2>(g.partials + g.stride, g.stride, gridDim.x, s_sc);
         if (threadIdx.x == 0) {
             const double res2 = (f2 == 0.0) ? 0.0 : s_sc[0] / f2;
@@ -551,6 +592,7 @@ __global__ void __launch_bounds__(1024, 1) cg_kernel(CgArgs<R> g) {
             s_beta = (R)(s_delta / delta_old);
         }
         __syncthreads();
+        FFEA_MARK(g, tm, 8);
         if (s_conv) {
             ++it;
             break;
@@ -561,6 +603,7 @@ __global__ void __launch_bounds__(1024, 1) cg_kernel(CgArgs<R> g) {
 #pragma unroll
             for (int c = 0; c < 3; ++c) p[4 * a + c] = fma(beta, p[4 * a + c], g.dinv[4 * a + c] * g.r[4 * a + c]);
         if (!(ok = grid_sync(g.gb, st, g.limit_ns))) break;
+        FFEA_MARK(g, tm, 9);
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         if (!ok) {

@@ -108,7 +108,7 @@ __global__ void __launch_bounds__(256) gather_mixed_kernel(GatherArgs<R> g) {
 // thread 0 of every block: G = Z^T D Z from the moments, its inverse, and the coefficients of the
 // projection of the right-hand side (kept out of line: it runs once per solve)
 template <class R>
-__device__ __noinline__ void mixed_setup(const CgArgs<R> &g, const double *s_sc, double *s_Ginv, float *s_tau,
+__device__ __noinline__ void mixed_setup(const CgArgs<R> &g, const double *s_sc, double *s_A6, float *s_tau,
                                          float *s_Om, float *s_beta, int *s_conv) {
         const int k = g.nmodes;
         double M[6][6];
@@ -133,7 +133,15 @@ __device__ __noinline__ void mixed_setup(const CgArgs<R> &g, const double *s_sc,
                 for (int j = 0; j < k; ++j) { G[6 * i + j] -= fct * G[6 * col + j]; Ginv[6 * i + j] -= fct * Ginv[6 * col + j]; }
             }
         }
-        for (int i = 0; i < 36; ++i) s_Ginv[i] = Ginv[i];
+        // A6 = modes^T G^{-1} modes: maps the moments (S1, S2) of a vector v to the (tau, Omega) of
+        // D Z G^{-1} Z^T D v, and S . A6 S = v^T D Z G^{-1} Z^T D v
+        for (int p = 0; p < 6; ++p)
+            for (int q = 0; q < 6; ++q) {
+                double sum = 0.0;
+                for (int i = 0; i < k; ++i)
+                    for (int j = 0; j < k; ++j) sum += g.modes[6 * i + p] * Ginv[6 * i + j] * g.modes[6 * j + q];
+                s_A6[6 * p + q] = sum;
+            }
         // c0 = G^{-1} Z^T f; tau, Omega of D Z c0
         double v[6], tau[3] = {0, 0, 0}, Om[3] = {0, 0, 0};
         for (int i = 0; i < k; ++i) {
@@ -155,7 +163,8 @@ __global__ void __launch_bounds__(1024, 1) cg_mixed_kernel(CgArgs<R> g) {
     __shared__ float2 smem[MIXED_GATHER_NP * 32];
     __shared__ float smemf[MIXED_A_NP * 32];
     __shared__ double s_sc[MIXED_GATHER_NP];
-    __shared__ double s_Ginv[36];
+    __shared__ double s_A6[36];
+    __shared__ double s_tO[6];
     __shared__ float s_alpha, s_beta, s_tau[3], s_Om[3];
     __shared__ double s_delta;
     __shared__ int s_conv;
@@ -164,11 +173,12 @@ __global__ void __launch_bounds__(1024, 1) cg_mixed_kernel(CgArgs<R> g) {
     const int nthr = gridDim.x * blockDim.x;
     const int tid = blockIdx.x * blockDim.x + threadIdx.x;
     const bool defl = g.nmodes > 0;
+    unsigned long long tm = (blockIdx.x == 0 && threadIdx.x == 0) ? globaltimer_ns() : 0ull;
     float2 *partials = reinterpret_cast<float2 *>(g.partials);
     // set-up: G = Z^T D Z from the moments M, projected right-hand side
     grid_sum_df<MIXED_GATHER_NP>(reinterpret_cast<const float2 *>(g.init_partials), g.init_stride, g.n_init, s_sc);
     const double f2 = s_sc[0];
-    if (threadIdx.x == 0) mixed_setup(g, s_sc, s_Ginv, s_tau, s_Om, &s_beta, &s_conv);
+    if (threadIdx.x == 0) mixed_setup(g, s_sc, s_A6, s_tau, s_Om, &s_beta, &s_conv);
     __syncthreads();
     df32 acc0[1] = {{0.f, 0.f}};
     for (int a = tid; a < g.N; a += nthr) {
@@ -196,6 +206,7 @@ __global__ void __launch_bounds__(1024, 1) cg_mixed_kernel(CgArgs<R> g) {
         __syncthreads();
     }
     float *pold = g.pbuf0, *pnew = g.pbuf1;
+    FFEA_MARK(g, tm, 0);
     int it = 0;
     for (; ok && it < g.imax; ++it) {
         const bool first = it == 0;
@@ -224,6 +235,7 @@ __global__ void __launch_bounds__(1024, 1) cg_mixed_kernel(CgArgs<R> g) {
                 }
             }
         }
+        FFEA_MARK(g, tm, 1);
         {
             df32 o[MIXED_A_NP];
             block_reduce_f<MIXED_A_NP>(acc, smemf, o);
@@ -231,29 +243,28 @@ __global__ void __launch_bounds__(1024, 1) cg_mixed_kernel(CgArgs<R> g) {
 #pragma unroll
                 for (int i = 0; i < MIXED_A_NP; ++i) partials[i * g.stride + blockIdx.x] = make_float2(o[i].hi, o[i].lo);
         }
+        FFEA_MARK(g, tm, 2);
         if (!(ok = grid_sync(g.gb, st, g.limit_ns))) break;
+        FFEA_MARK(g, tm, 3);
         grid_sum_df<MIXED_A_NP>(partials, g.stride, gridDim.x, s_sc);
-        if (threadIdx.x == 0) {
-            // v = Z^T D p, c = G^{-1} v, p.V~p = p.q + v.c, alpha = delta / p.V~p
-            double pq = s_sc[0], tau[3] = {0, 0, 0}, Om[3] = {0, 0, 0};
-            if (defl) {
-                double v[6];
-                for (int i = 0; i < g.nmodes; ++i) {
-                    const double *m = g.modes + 6 * i;
-                    v[i] = m[0] * s_sc[1] + m[1] * s_sc[2] + m[2] * s_sc[3] + m[3] * s_sc[4] + m[4] * s_sc[5] +
-                           m[5] * s_sc[6];
-                }
-                for (int i = 0; i < g.nmodes; ++i) {
-                    double c = 0.0;
-                    for (int j = 0; j < g.nmodes; ++j) c += s_Ginv[6 * i + j] * v[j];
-                    pq += v[i] * c;
-                    for (int t = 0; t < 3; ++t) { tau[t] += c * g.modes[6 * i + t]; Om[t] += c * g.modes[6 * i + 3 + t]; }
-                }
+        // (tau, Omega) = A6 S over six lanes of warp 0; p.V~p = p.q + S . (tau, Omega); alpha = delta / p.V~p
+        if (threadIdx.x < 32) {
+            const int l = threadIdx.x;
+            double tO = 0.0;
+            if (defl && l < 6) {
+#pragma unroll
+                for (int q = 0; q < 6; ++q) tO += s_A6[6 * l + q] * s_sc[1 + q];
             }
-            for (int t = 0; t < 3; ++t) { s_tau[t] = (float)tau[t]; s_Om[t] = (float)Om[t]; }
-            s_alpha = (float)(s_delta / pq);
+            double prod = (l < 6) ? tO * s_sc[1 + l] : 0.0;
+#pragma unroll
+            for (int o = 4; o > 0; o >>= 1) prod += __shfl_xor_sync(0xffffffffu, prod, o);
+            if (l < 6) {
+                if (l < 3) s_tau[l] = (float)tO; else s_Om[l - 3] = (float)tO;
+            }
+            if (l == 0) s_alpha = (float)s_delta / (float)(s_sc[0] + prod);
         }
         __syncthreads();
+        FFEA_MARK(g, tm, 4);
         const float alpha = s_alpha;
         const float t0 = s_tau[0], t1 = s_tau[1], t2 = s_tau[2], O0 = s_Om[0], O1 = s_Om[1], O2 = s_Om[2];
         // phase B: x += alpha p ; r -= alpha (q + D (tau + Omega x d)) ; r.r ; r.z
@@ -273,6 +284,7 @@ __global__ void __launch_bounds__(1024, 1) cg_mixed_kernel(CgArgs<R> g) {
             acc2[0] += r0 * r0 + r1 * r1 + r2 * r2;
             acc2[1] += r0 * (g.dinv[4 * a] * r0) + r1 * (g.dinv[4 * a + 1] * r1) + r2 * (g.dinv[4 * a + 2] * r2);
         }
+        FFEA_MARK(g, tm, 5);
         {
             df32 o[MIXED_B_NP];
             block_reduce_f<MIXED_B_NP>(acc2, smemf, o);
@@ -280,17 +292,20 @@ __global__ void __launch_bounds__(1024, 1) cg_mixed_kernel(CgArgs<R> g) {
                 for (int i = 0; i < MIXED_B_NP; ++i)
                     partials[(MIXED_A_NP + i) * g.stride + blockIdx.x] = make_float2(o[i].hi, o[i].lo);
         }
+        FFEA_MARK(g, tm, 6);
         if (!(ok = grid_sync(g.gb, st, g.limit_ns))) break;
+        FFEA_MARK(g, tm, 7);
         grid_sum_df<MIXED_B_NP>(partials + MIXED_A_NP * g.stride, g.stride, gridDim.x, s_sc);
         if (threadIdx.x == 0) {
-            const double res2 = (f2 == 0.0) ? 0.0 : s_sc[0] / f2;
-            if (blockIdx.x == 0 && it < g.hist_cap) g.history[it] = res2;
-            s_conv = (g.check_last || it + 1 < g.imax) && res2 < g.eps2;
+            // |r|^2/|f|^2 < epsilon2 tested as |r|^2 < epsilon2 |f|^2 (f2 == 0 counts as converged)
+            s_conv = (g.check_last || it + 1 < g.imax) && (f2 == 0.0 || s_sc[0] < g.eps2 * f2);
+            if (blockIdx.x == 0 && it < g.hist_cap) g.history[it] = (f2 == 0.0) ? 0.0 : s_sc[0] / f2;
             const double delta_old = s_delta;
             s_delta = s_sc[1];
-            s_beta = (float)(s_delta / delta_old);
+            s_beta = (float)s_delta / (float)delta_old;
         }
         __syncthreads();
+        FFEA_MARK(g, tm, 8);
         if (s_conv) {
             ++it;
             break;

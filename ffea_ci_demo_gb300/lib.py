@@ -90,6 +90,7 @@ def load():
         "ffea_gpu_blob_cg_iterations": (C.c_int, [vp, ip, C.POINTER(C.c_longlong)]),
         "ffea_gpu_blob_sizes": (C.c_int, [vp, ip, ip, C.POINTER(C.c_longlong)]),
         "ffea_gpu_blob_cg_history": (C.c_int, [vp, dp, C.c_int, ip]),
+        "ffea_gpu_blob_cg_profile": (C.c_int, [vp, dp, C.c_int]),
         "ffea_gpu_blob_get_pattern": (C.c_int, [vp, dp, dp, dp, dp, C.POINTER(C.c_longlong)]),
         "ffea_gpu_blob_get_connectivity": (C.c_int, [vp, dp, dp, C.POINTER(C.c_longlong)]),
         "ffea_gpu_blob_get_elements": (C.c_int, [vp, dp, dp, dp]),
@@ -271,6 +272,15 @@ class Blob:
         n = C.c_int()
         _check(self._lib.ffea_gpu_blob_cg_history(self._h, _p(buf), max_entries, C.byref(n)), "cg_history")
         return buf[:n.value].copy()
+
+    CG_PHASES = ("setup", "spmv", "reduce_a", "barrier_a", "sum_a", "update", "reduce_b", "barrier_b", "sum_b",
+                 "direction")
+
+    def cg_profile(self) -> dict:
+        """Device time (ns) of the last CG solve per phase, as seen by one thread block."""
+        buf = np.zeros(len(self.CG_PHASES))
+        _check(self._lib.ffea_gpu_blob_cg_profile(self._h, _p(buf), buf.size), "cg_profile")
+        return dict(zip(self.CG_PHASES, buf.tolist()))
 
     def sizes(self) -> tuple[int, int, int]:
         nl, ne, nb = C.c_int(), C.c_int(), C.c_longlong()

@@ -147,6 +147,14 @@ int ffea_gpu_blob_cg_iterations(ffea_gpu_blob *blob, int *last, long long *total
  * NoMassCGSolver::solve tests against epsilon2); *count gets the number written (<= max_entries). */
 int ffea_gpu_blob_cg_history(ffea_gpu_blob *blob, double *res2, int max_entries, int *count);
 
+/* Where the last CG solve spent its time, as seen by one thread block (device timer, ns, summed
+ * over iterations): [0] set-up, [1] SpMV, [2] block reduction after the SpMV, [3] grid barrier
+ * after the SpMV, [4] cross-block sums and step length, [5] solution/residual update, [6] its block
+ * reduction, [7] its grid barrier, [8] its cross-block sums, [9] direction update and its barrier
+ * (FP64 path only). n_phases is 10. */
+#define FFEA_GPU_CG_PHASES 10
+int ffea_gpu_blob_cg_profile(ffea_gpu_blob *blob, double *phase_ns, int n_phases);
+
 /* Problem sizes: vertex nodes, elements, matrix 3x3 blocks. */
 int ffea_gpu_blob_sizes(ffea_gpu_blob *blob, int *num_linear_nodes, int *num_elements, long long *num_blocks);
 
