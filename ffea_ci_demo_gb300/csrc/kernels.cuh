@@ -422,25 +422,23 @@ __device__ __forceinline__ void spmv_row(const CgArgs<R> &g, const R *pold, R be
         const int base = g.slice_ptr[s];
         const int len = g.rowlen[a];
         if (g.block3 && ONTHEFLY) {
-            // two blocks per trip: both column indices and all their loads are in flight together
+            // one block per trip, the next block's column index prefetched so that its dependent
+            // loads can issue as soon as the current trip's loads are out
             const R *v = g.val + 9 * (size_t)base + lane;
-            for (int k = sub; k < len; k += 2 * tpn) {
-                const int k2 = k + tpn;
-                const bool two = k2 < len;
-                const int b1 = g.bcol[base + 32 * k + lane];
-                const int b2 = two ? g.bcol[base + 32 * k2 + lane] : b1;
+            int k = sub;
+            int bn = (k < len) ? g.bcol[base + 32 * k + lane] : 0;
+#pragma unroll 1
+            for (; k < len; k += tpn) {
+                const int b = bn;
+                if (k + tpn < len) bn = g.bcol[base + 32 * (k + tpn) + lane];
                 const R *vk = v + (size_t)32 * 9 * k;
-                const R *vk2 = v + (size_t)32 * 9 * (two ? k2 : k);
-                R p0, p1, p2, u0, u1, u2;
-                p_on_the_fly(g, pold, beta, first, b1, p0, p1, p2);
-                p_on_the_fly(g, pold, beta, first, b2, u0, u1, u2);
-                if (!two) { u0 = 0; u1 = 0; u2 = 0; }
-                q0 = fma(vk[0], p0, q0); q0 = fma(vk[32], p1, q0); q0 = fma(vk[64], p2, q0);
-                q1 = fma(vk[96], p0, q1); q1 = fma(vk[128], p1, q1); q1 = fma(vk[160], p2, q1);
-                q2 = fma(vk[192], p0, q2); q2 = fma(vk[224], p1, q2); q2 = fma(vk[256], p2, q2);
-                q0 = fma(vk2[0], u0, q0); q0 = fma(vk2[32], u1, q0); q0 = fma(vk2[64], u2, q0);
-                q1 = fma(vk2[96], u0, q1); q1 = fma(vk2[128], u1, q1); q1 = fma(vk2[160], u2, q1);
-                q2 = fma(vk2[192], u0, q2); q2 = fma(vk2[224], u1, q2); q2 = fma(vk2[256], u2, q2);
+                const R v0 = vk[0], v1 = vk[32], v2 = vk[64], v3 = vk[96], v4 = vk[128], v5 = vk[160], v6 = vk[192],
+                        v7 = vk[224], v8 = vk[256];
+                R p0, p1, p2;
+                p_on_the_fly(g, pold, beta, first, b, p0, p1, p2);
+                q0 = fma(v0, p0, q0); q0 = fma(v1, p1, q0); q0 = fma(v2, p2, q0);
+                q1 = fma(v3, p0, q1); q1 = fma(v4, p1, q1); q1 = fma(v5, p2, q1);
+                q2 = fma(v6, p0, q2); q2 = fma(v7, p1, q2); q2 = fma(v8, p2, q2);
             }
         } else if (g.block3) {
             const R *v = g.val + 9 * (size_t)base + lane;
@@ -484,15 +482,29 @@ __device__ __forceinline__ void spmv_row(const CgArgs<R> &g, const R *pold, R be
     }
 }
 
-// node loop of the SpMV phase: warp w covers nodes [w*NPW, (w+1)*NPW), NPW = 32 / tpn, grid-strided
-#define FFEA_SPMV_LOOP(g, a, sub, valid)                                                        \
-    const int sub = threadIdx.x % (g).tpn;                                                      \
-    const int npw_ = 32 / (g).tpn;                                                               \
+// Row (node) loop shared by every phase of the CG kernels. The W warps of the grid take consecutive
+// runs of rppw = min(32 / tpn, ceil(N / W)) rows per pass, so that all SMs get the same number of rows;
+// the tpn lanes of a row group work on the SpMV row together and its first lane (sub == 0) owns the
+// node in the vector phases. All 32 lanes of a warp run every pass (rows past the end: valid = false).
+#define FFEA_ROW_LOOP(g, a, sub, valid)                                                         \
+    const int sub = (threadIdx.x & 31) % (g).tpn;                                               \
+    const int wtot_ = (gridDim.x * blockDim.x) >> 5;                                            \
+    const int rppw_ = min(32 / (g).tpn, ((g).N + wtot_ - 1) / wtot_);                           \
     const int wglob_ = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;                            \
-    const int wstride_ = (gridDim.x * blockDim.x) >> 5;                                          \
-    for (int a0_ = wglob_ * npw_, a = a0_ + (threadIdx.x & 31) / (g).tpn; a0_ < (g).N;          \
-         a0_ += wstride_ * npw_, a = a0_ + (threadIdx.x & 31) / (g).tpn)                       \
-        for (bool valid = a < (g).N, once_ = true; once_; once_ = false)
+    const int lrow_ = (threadIdx.x & 31) / (g).tpn;                                             \
+    for (int a0_ = wglob_ * rppw_, a = a0_ + lrow_; a0_ < (g).N;                               \
+         a0_ += wtot_ * rppw_, a = a0_ + lrow_)                                                 \
+        for (bool valid = lrow_ < rppw_ && a < (g).N, once_ = true; once_; once_ = false)
+
+#define FFEA_SPMV_LOOP FFEA_ROW_LOOP
+
+// Node loop of the vector phases: the N nodes are split into gridDim.x equal runs, one per block,
+// one node per thread (every block gets the same share; a phase's writes are read by other
+// threads only after the grid barrier that ends the phase).
+#define FFEA_NODE_LOOP(g, a)                                                                    \
+    for (int npb_ = ((g).N + gridDim.x - 1) / gridDim.x, a = blockIdx.x * npb_ + threadIdx.x,    \
+             aend_ = min((g).N, (blockIdx.x + 1) * npb_);                                       \
+         a < aend_; a += blockDim.x)
 
 constexpr int CG_MAX_THREADS = 1024;
 
@@ -510,7 +522,7 @@ constexpr int CG_MAX_THREADS = 1024;
 // every multiply-add is fused (the cross-node sums are reordered anyway, so the CG agrees with the
 // reference to rounding, not bitwise).
 template <class R>
-__global__ void __launch_bounds__(1024, 1) cg_kernel(CgArgs<R> g) {
+__global__ void __launch_bounds__(1024, 1) cg_kernel(const __grid_constant__ CgArgs<R> g) {
     __shared__ double smem[2 * CG_MAX_THREADS];
     __shared__ double s_sc[4];
     __shared__ R s_alpha, s_beta;
@@ -518,14 +530,13 @@ __global__ void __launch_bounds__(1024, 1) cg_kernel(CgArgs<R> g) {
     __shared__ int s_conv;
     DevStatus *st = g.st;
     if (st->abort) return;
-    const int nthr = gridDim.x * blockDim.x;
-    const int tid = blockIdx.x * blockDim.x + threadIdx.x;
     unsigned long long tm = (blockIdx.x == 0 && threadIdx.x == 0) ? globaltimer_ns() : 0ull;
     R *p = g.pbuf0;
     // p = z = D^{-1} r  (conjugate_gradient_residual_assume_x_zero, src/NoMassCGSolver.cpp:196-220)
-    for (int a = tid; a < g.N; a += nthr)
+    FFEA_NODE_LOOP(g, a) {
 #pragma unroll
         for (int c = 0; c < 3; ++c) p[4 * a + c] = g.dinv[4 * a + c] * g.r[4 * a + c];
+    }
     grid_sum_d<2>(g.init_partials, g.init_stride, g.n_init, s_sc);
     const double f2 = s_sc[0];
     if (threadIdx.x == 0) { s_delta = s_sc[1]; s_conv = 0; }
@@ -559,7 +570,7 @@ __global__ void __launch_bounds__(1024, 1) cg_kernel(CgArgs<R> g) {
         const R alpha = s_alpha, malpha = -s_alpha;
         // x += alpha p ; r += (-alpha) q ; |r|^2 ; r.z   (vec3_add_to_scaled, residual2, apply_preconditioner)
         double acc2[2] = {0.0, 0.0};
-        for (int a = tid; a < g.N; a += nthr) {
+        FFEA_NODE_LOOP(g, a) {
 #pragma unroll
             for (int c = 0; c < 3; ++c) g.x[4 * a + c] = fma(alpha, p[4 * a + c], g.x[4 * a + c]);
             R r[3], z[3];
@@ -599,9 +610,10 @@ __global__ void __launch_bounds__(1024, 1) cg_kernel(CgArgs<R> g) {
         }
         // p = beta p + z   (vec3_scale_and_add :202-212)
         const R beta = s_beta;
-        for (int a = tid; a < g.N; a += nthr)
+        FFEA_NODE_LOOP(g, a) {
 #pragma unroll
             for (int c = 0; c < 3; ++c) p[4 * a + c] = fma(beta, p[4 * a + c], g.dinv[4 * a + c] * g.r[4 * a + c]);
+        }
         if (!(ok = grid_sync(g.gb, st, g.limit_ns))) break;
         FFEA_MARK(g, tm, 9);
     }

@@ -159,19 +159,15 @@ __device__ __noinline__ void mixed_setup(const CgArgs<R> &g, const double *s_sc,
     }
 
 template <class R>
-__global__ void __launch_bounds__(1024, 1) cg_mixed_kernel(CgArgs<R> g) {
-    __shared__ float2 smem[MIXED_GATHER_NP * 32];
+__global__ void __launch_bounds__(1024, 1) cg_mixed_kernel(const __grid_constant__ CgArgs<R> g) {
     __shared__ float smemf[MIXED_A_NP * 32];
     __shared__ double s_sc[MIXED_GATHER_NP];
     __shared__ double s_A6[36];
-    __shared__ double s_tO[6];
     __shared__ float s_alpha, s_beta, s_tau[3], s_Om[3];
     __shared__ double s_delta;
     __shared__ int s_conv;
     DevStatus *st = g.st;
     if (st->abort) return;
-    const int nthr = gridDim.x * blockDim.x;
-    const int tid = blockIdx.x * blockDim.x + threadIdx.x;
     const bool defl = g.nmodes > 0;
     unsigned long long tm = (blockIdx.x == 0 && threadIdx.x == 0) ? globaltimer_ns() : 0ull;
     float2 *partials = reinterpret_cast<float2 *>(g.partials);
@@ -180,8 +176,8 @@ __global__ void __launch_bounds__(1024, 1) cg_mixed_kernel(CgArgs<R> g) {
     const double f2 = s_sc[0];
     if (threadIdx.x == 0) mixed_setup(g, s_sc, s_A6, s_tau, s_Om, &s_beta, &s_conv);
     __syncthreads();
-    df32 acc0[1] = {{0.f, 0.f}};
-    for (int a = tid; a < g.N; a += nthr) {
+    float acc0[1] = {0.f};
+    FFEA_NODE_LOOP(g, a) {
         float r0 = g.r[4 * a], r1 = g.r[4 * a + 1], r2 = g.r[4 * a + 2];
         if (defl) {
             const float4 d = g.dpos[a];
@@ -191,12 +187,12 @@ __global__ void __launch_bounds__(1024, 1) cg_mixed_kernel(CgArgs<R> g) {
             g.r[4 * a] = r0; g.r[4 * a + 1] = r1; g.r[4 * a + 2] = r2;
         }
         g.x[4 * a] = 0.f; g.x[4 * a + 1] = 0.f; g.x[4 * a + 2] = 0.f;
-        acc0[0] = df_add_f(acc0[0], r0 * (g.dinv[4 * a] * r0) + r1 * (g.dinv[4 * a + 1] * r1) + r2 * (g.dinv[4 * a + 2] * r2));
+        acc0[0] += r0 * (g.dinv[4 * a] * r0) + r1 * (g.dinv[4 * a + 1] * r1) + r2 * (g.dinv[4 * a + 2] * r2);
     }
     const int row0 = MIXED_A_NP + MIXED_B_NP;
     {
         df32 o[1];
-        block_sum_df<1>(acc0, smem, o);
+        block_reduce_f<1>(acc0, smemf, o);
         if (threadIdx.x == 0) partials[row0 * g.stride + blockIdx.x] = make_float2(o[0].hi, o[0].lo);
     }
     bool ok = grid_sync(g.gb, st, g.limit_ns);
@@ -269,7 +265,7 @@ __global__ void __launch_bounds__(1024, 1) cg_mixed_kernel(CgArgs<R> g) {
         const float t0 = s_tau[0], t1 = s_tau[1], t2 = s_tau[2], O0 = s_Om[0], O1 = s_Om[1], O2 = s_Om[2];
         // phase B: x += alpha p ; r -= alpha (q + D (tau + Omega x d)) ; r.r ; r.z
         float acc2[MIXED_B_NP] = {0.f, 0.f};
-        for (int a = tid; a < g.N; a += nthr) {
+        FFEA_NODE_LOOP(g, a) {
 #pragma unroll
             for (int c = 0; c < 3; ++c) g.x[4 * a + c] += alpha * pnew[4 * a + c];
             float q0 = g.q[4 * a], q1 = g.q[4 * a + 1], q2 = g.q[4 * a + 2];
