@@ -18,6 +18,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <memory>
+#include <mutex>
 #include <new>
 #include <string>
 #include <vector>
@@ -484,6 +485,105 @@ double host_visc_entry(const double *dpsi, double A, double B, double vol, int r
     return (B * (dpsi[4 * i + a] * dpsi[4 * j + b]) + A * (dpsi[4 * i + b] * dpsi[4 * j + a])) * vol;
 }
 
+// ---------------------------------------------------------------------------
+// Scratch of the allocation-free solve (ffea_gpu_blob_solve_static).
+//
+// Some callers cannot allocate device memory at the moment they want a solve:
+// a host program whose own memory pool already holds (nearly) all of the GPU's
+// memory, so that a cudaMalloc would fail, or an outer integrator that calls
+// the solve inside its fixed-memory time-step loop, where a cudaMalloc/cudaFree
+// pair would also synchronise the whole device every call. For them the CG
+// work vectors, block partial sums, grid barrier, status word and phase timers
+// come from this one file-scope device array, sized for
+// FFEA_GPU_SOLVE_STATIC_MAX_NODES vertex nodes (4.99 MB), instead of from the
+// blob's own buffers. Each region starts on a 256-byte boundary. The array
+// keeps its contents between calls: every call rewrites x, r and the partial
+// sums and zeroes the status word, the barrier counters and the timers before
+// the CG reads them.
+// ---------------------------------------------------------------------------
+constexpr int SOLVE_STATIC_MAX_NODES = FFEA_GPU_SOLVE_STATIC_MAX_NODES;
+constexpr int SOLVE_PREP_THREADS = 256;
+constexpr int SOLVE_MAX_BLOCKS = (SOLVE_STATIC_MAX_NODES + SOLVE_PREP_THREADS - 1) / SOLVE_PREP_THREADS;
+constexpr size_t ss_round(size_t n) { return (n + 31) / 32 * 32; }  // doubles, to 256 bytes
+constexpr size_t SS_VEC = 4 * (size_t)SOLVE_STATIC_MAX_NODES;        // one node vector, 4 doubles per node
+constexpr size_t SS_RHS = 0;                                          // input, 3 doubles per node
+constexpr size_t SS_X = SS_RHS + ss_round(3 * (size_t)SOLVE_STATIC_MAX_NODES);
+constexpr size_t SS_R = SS_X + SS_VEC;
+constexpr size_t SS_Q = SS_R + SS_VEC;
+constexpr size_t SS_P = SS_Q + SS_VEC;
+constexpr size_t SS_INIT = SS_P + SS_VEC;                             // 2 rows of SOLVE_MAX_BLOCKS
+constexpr size_t SS_PART = SS_INIT + ss_round(2 * (size_t)SOLVE_MAX_BLOCKS);  // 3 rows of SOLVE_MAX_BLOCKS
+constexpr size_t SS_PHASE = SS_PART + ss_round(3 * (size_t)SOLVE_MAX_BLOCKS);
+constexpr size_t SS_STATUS = SS_PHASE + 32;
+constexpr size_t SS_BARRIER = SS_STATUS + 32;
+constexpr size_t SS_TOTAL = SS_BARRIER + 32;
+static_assert(FFEA_GPU_CG_PHASES <= 32 && sizeof(DevStatus) <= 256 && sizeof(GridBarrier) <= 256,
+              "scratch regions too small");
+
+static __device__ __align__(256) double g_solve_scratch[SS_TOTAL];
+
+constexpr int SOLVE_STATIC_MAX_DEVICES = 64;
+std::mutex g_solve_mutex;  // held for a whole call: the array is shared by every call on a device
+double *g_solve_ptr[SOLVE_STATIC_MAX_DEVICES] = {};
+
+// Device address of g_solve_scratch on `device`: looked up once per device, with that device
+// current, and cached. The first lookup also loads this library's module on the device.
+int solve_scratch(int device, double **out) {
+    if (device < 0 || device >= SOLVE_STATIC_MAX_DEVICES) {
+        g_last_error = "ffea_gpu_blob_solve_static: device ordinal beyond the scratch table";
+        return FFEA_GPU_EINPUT;
+    }
+    if (!g_solve_ptr[device]) {
+        int cur = -1;
+        CK(cudaGetDevice(&cur));
+        if (cur != device) CK(cudaSetDevice(device));
+        void *ptr = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&ptr, g_solve_scratch);
+        if (cur != device) {
+            const cudaError_t e2 = cudaSetDevice(cur);
+            if (e == cudaSuccess) e = e2;
+        }
+        if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(g_solve_scratch)");
+        g_solve_ptr[device] = static_cast<double *>(ptr);
+    }
+    *out = g_solve_ptr[device];
+    return FFEA_GPU_OK;
+}
+
+// r = rhs, x = 0 and the block sums of |r|^2 and r.D^{-1}r that open the CG, as the gather kernel
+// leaves them for a step (same per-block order, products and sums rounded separately); thread 0
+// also clears the status word, the barrier counters and the phase timers.
+__global__ void __launch_bounds__(SOLVE_PREP_THREADS)
+    solve_static_prep_kernel(int N, const double *rhs3, const double *dinv, double *x, double *r,
+                             double *init_partials, int stride, GridBarrier *gb, DevStatus *st,
+                             unsigned long long *phase_ns) {
+    __shared__ double smem[64];
+    const int a = blockIdx.x * blockDim.x + threadIdx.x;
+    if (a == 0) {
+        *st = DevStatus{};
+        gb->count = 0u;
+        gb->passed = 0u;
+        for (int k = 0; k < FFEA_GPU_CG_PHASES; ++k) phase_ns[k] = 0ull;
+    }
+    double acc[2] = {0.0, 0.0};
+    if (a < N) {
+        double F[3], z[3];
+        for (int c = 0; c < 3; ++c) {
+            F[c] = rhs3[3 * (size_t)a + c];
+            z[c] = __dmul_rn(dinv[4 * (size_t)a + c], F[c]);
+            r[4 * (size_t)a + c] = F[c];
+            x[4 * (size_t)a + c] = 0.0;
+        }
+        acc[0] = __dadd_rn(__dadd_rn(__dmul_rn(F[0], F[0]), __dmul_rn(F[1], F[1])), __dmul_rn(F[2], F[2]));
+        acc[1] = __dadd_rn(__dadd_rn(__dmul_rn(F[0], z[0]), __dmul_rn(F[1], z[1])), __dmul_rn(F[2], z[2]));
+    }
+    block_sum<2>(acc, smem);
+    if (threadIdx.x == 0) {
+        init_partials[blockIdx.x] = acc[0];
+        init_partials[stride + blockIdx.x] = acc[1];
+    }
+}
+
 }  // namespace
 
 // ---------------------------------------------------------------------------
@@ -508,6 +608,7 @@ struct ffea_gpu_blob {
     virtual int cg_history(double *res2, int max_entries, int *count) = 0;
     virtual int cg_profile(double *ns, int n) = 0;
     virtual int get_matrix_values(std::vector<double> &val_sell) = 0;
+    virtual int solve_static(const double *rhs, double *x, int *iterations) = 0;
 };
 
 namespace {
@@ -984,6 +1085,74 @@ struct BlobImpl final : ffea_gpu_blob {
         return FFEA_GPU_OK;
     }
 
+    // Jacobi-PCG solve of the blob's current matrix with every work array in g_solve_scratch:
+    // the same persistent cg_kernel as a step, opened by solve_static_prep_kernel instead of the
+    // gather. Host copies go through the blob's pinned staging buffer; nothing is allocated.
+    int solve_static(const double *rhs, double *xout, int *iterations) override {
+        if constexpr (std::is_same<R, float>::value) {
+            g_last_error = "ffea_gpu_blob_solve_static: FP64 blobs only";
+            return FFEA_GPU_EINPUT;
+        } else {
+            if (p.solver == FFEA_GPU_MASSLUMPED) {
+                g_last_error = "ffea_gpu_blob_solve_static: the mass-lumped solver has no CG solve";
+                return FFEA_GPU_EINPUT;
+            }
+            const int N = h.N;
+            if (N > SOLVE_STATIC_MAX_NODES || cg_grid > SOLVE_MAX_BLOCKS) {
+                g_last_error = "ffea_gpu_blob_solve_static: " + std::to_string(N) +
+                               " vertex nodes exceed the static scratch limit of " +
+                               std::to_string(SOLVE_STATIC_MAX_NODES);
+                return FFEA_GPU_EINPUT;
+            }
+            std::lock_guard<std::mutex> lock(g_solve_mutex);
+            double *s = nullptr;
+            int rc = solve_scratch(device, &s);
+            if (rc) return rc;
+            CK(cudaStreamSynchronize(stream));  // staging may still feed an earlier copy
+            for (int k = 0; k < N; ++k)
+                for (int c = 0; c < 3; ++c) staging[3 * (size_t)k + c] = rhs[3 * (size_t)h.node_of[k] + c];
+            CK(cudaMemcpyAsync(s + SS_RHS, staging, 3 * (size_t)N * sizeof(double), cudaMemcpyHostToDevice, stream));
+            const int blocks = (N + SOLVE_PREP_THREADS - 1) / SOLVE_PREP_THREADS;
+            GridBarrier *sgb = reinterpret_cast<GridBarrier *>(s + SS_BARRIER);
+            DevStatus *sst = reinterpret_cast<DevStatus *>(s + SS_STATUS);
+            unsigned long long *sphase = reinterpret_cast<unsigned long long *>(s + SS_PHASE);
+            solve_static_prep_kernel<<<blocks, SOLVE_PREP_THREADS, 0, stream>>>(
+                N, s + SS_RHS, dinv, s + SS_X, s + SS_R, s + SS_INIT, SOLVE_MAX_BLOCKS, sgb, sst, sphase);
+            count_launch();
+            CK(cudaGetLastError());
+            const bool nomass = p.solver == FFEA_GPU_NOMASS_CG;
+            CgArgs<R> ca{};
+            ca.N = N;
+            ca.block3 = nomass;
+            ca.check_last = nomass;
+            ca.slice_ptr = slice_ptr; ca.rowlen = rowlen; ca.bcol = bcol;
+            ca.val = val; ca.dinv = dinv;
+            ca.x = s + SS_X; ca.r = s + SS_R; ca.q = s + SS_Q; ca.pbuf0 = s + SS_P; ca.pbuf1 = nullptr;
+            ca.init_partials = s + SS_INIT; ca.n_init = blocks; ca.init_stride = SOLVE_MAX_BLOCKS;
+            ca.partials = s + SS_PART; ca.stride = SOLVE_MAX_BLOCKS;
+            ca.gb = sgb; ca.st = sst;
+            ca.imax = p.max_iterations_cg;
+            ca.eps2 = p.epsilon2;
+            ca.limit_ns = 2000000000ull;
+            ca.history = nullptr; ca.hist_cap = 0; ca.tpn = tpn; ca.phase_ns = sphase;
+            CK(Launch<R>::cg(ca, cg_grid, stream));
+            DevStatus ds{};
+            CK(cudaMemcpy2DAsync(staging, 3 * sizeof(double), s + SS_X, 4 * sizeof(double), 3 * sizeof(double), N,
+                                 cudaMemcpyDeviceToHost, stream));
+            CK(cudaMemcpyAsync(&ds, sst, sizeof(DevStatus), cudaMemcpyDeviceToHost, stream));
+            CK(cudaStreamSynchronize(stream));
+            if (iterations) *iterations = ds.last_iters;
+            if ((rc = status_code(ds))) return rc;
+            // midpoint rows are identity rows of the reference's system; rhs and xout may be one array
+            for (int i = 0; i < h.n_all; ++i)
+                if (h.lin_of[i] < 0)
+                    for (int c = 0; c < 3; ++c) xout[3 * (size_t)i + c] = rhs[3 * (size_t)i + c];
+            for (int k = 0; k < N; ++k)
+                for (int c = 0; c < 3; ++c) xout[3 * (size_t)h.node_of[k] + c] = staging[3 * (size_t)k + c];
+            return FFEA_GPU_OK;
+        }
+    }
+
     // Blob::make_measurements energies (src/Blob.cpp:1066-1125), evaluated on the host from device state
     int measure(double *se, double *ke) override {
         const int N = h.N, T = h.T;
@@ -1263,6 +1432,11 @@ int ffea_gpu_blob_get_elements(ffea_gpu_blob *b, double *nf, double *vol, double
 int ffea_gpu_blob_get_rhs(ffea_gpu_blob *b, double *rhs) {
     if (!b || !rhs) return FFEA_GPU_EINPUT;
     return b->get_rhs(rhs);
+}
+
+int ffea_gpu_blob_solve_static(ffea_gpu_blob *b, const double *rhs, double *x, int *iterations) {
+    if (!b || !rhs || !x) return FFEA_GPU_EINPUT;
+    return b->solve_static(rhs, x, iterations);
 }
 
 const char *ffea_gpu_last_error(void) { return g_last_error.c_str(); }

@@ -95,6 +95,7 @@ def load():
         "ffea_gpu_blob_get_connectivity": (C.c_int, [vp, dp, dp, C.POINTER(C.c_longlong)]),
         "ffea_gpu_blob_get_elements": (C.c_int, [vp, dp, dp, dp]),
         "ffea_gpu_blob_get_rhs": (C.c_int, [vp, dp]),
+        "ffea_gpu_blob_solve_static": (C.c_int, [vp, dp, dp, ip]),
         "ffea_gpu_last_error": (C.c_char_p, []),
         "ffea_gpu_launch_count": (C.c_longlong, []),
     }

@@ -178,6 +178,33 @@ int ffea_gpu_blob_get_elements(ffea_gpu_blob *blob, double *node_force12, double
 /* The assembled force vector of the last step (solver input, 3 * num_nodes, midpoints zero). */
 int ffea_gpu_blob_get_rhs(ffea_gpu_blob *blob, double *rhs);
 
+/* Allocation-free solve. No counterpart in the reference (the nearest is
+ * Solver::solve, include/Solver.h:31-52, as NoMassCGSolver::solve,
+ * src/NoMassCGSolver.cpp:156-188, and ConjugateGradientSolver::solve,
+ * src/ConjugateGradientSolver.cpp:193-217).
+ *
+ * Solves M x = rhs with the blob's current matrix (CG_nomass: the viscosity
+ * matrix assembled by the last ffea_gpu_blob_step; CG: the constant mass
+ * matrix) by the persistent Jacobi-PCG kernel of a step, from x = 0, with the
+ * blob's epsilon and max_iterations_cg. rhs and x hold 3 * num_nodes doubles
+ * in the layout of ffea_gpu_blob_get_rhs and may be the same array; midpoint
+ * rows are identity rows (x = rhs there). *iterations (may be NULL) gets the
+ * CG iterations used. Returns FFEA_GPU_ECGMAXIT / FFEA_GPU_ETIMEOUT like a step.
+ *
+ * It allocates no memory, on the device or through any library: every work
+ * array comes from one static device array of this library, sized for
+ * FFEA_GPU_SOLVE_STATIC_MAX_NODES vertex nodes (4.99 MB). Blobs with more
+ * vertex nodes, mixed-precision blobs and mass-lumped blobs are rejected with
+ * FFEA_GPU_EINPUT and a message in ffea_gpu_last_error. The first call on a
+ * device looks the array up (cudaGetSymbolAddress, which also loads the
+ * library's module there); make that first call before any stream capture on
+ * the device. The array is shared by all calls on a device, so two calls whose
+ * kernels overlapped would corrupt each other: each call holds a process-wide
+ * lock and waits for its result, so calls from several host threads run one
+ * after another. */
+#define FFEA_GPU_SOLVE_STATIC_MAX_NODES 32768
+int ffea_gpu_blob_solve_static(ffea_gpu_blob *blob, const double *rhs, double *x, int *iterations);
+
 /* Last CUDA error text for FFEA_GPU_ECUDA (static storage). */
 const char *ffea_gpu_last_error(void);
 
