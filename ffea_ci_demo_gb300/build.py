@@ -25,6 +25,7 @@ UNITS = {
     "engine_fp64.cu": ["-fmad=false"],
     "engine_mixed.cu": [],
     "blob.cu": [],
+    "batch.cu": [],
     "io.cu": [],
 }
 

@@ -6,7 +6,7 @@
 // Host code calls them only through Launch<R>.
 #pragma once
 
-#include "kernels.cuh"
+#include "batch_types.cuh"
 
 namespace ffea {
 
@@ -27,6 +27,18 @@ extern template struct Launch<double>;
 extern template struct Launch<float>;
 
 cudaError_t launch_finish_step(uint32_t *rng_state, const MrgJump *step_jump, DevStatus *st, cudaStream_t s);
+
+// launchers of the batch kernels (mixed precision; instantiated in engine_mixed.cu)
+struct BatchLaunch {
+    static cudaError_t schedule(BlobCgDesc *desc, const int *blob_iters, int nblobs, int ncta, int *cta_blob,
+                                const DevStatus *st, cudaStream_t s);
+    // cooperative launch of cg_batch_kernel (capturable in a CUDA graph)
+    static cudaError_t cg(const BatchCgArgs &a, int grid, int threads, cudaStream_t s);
+    // CTAs of `threads` threads that can be resident at once on `device`
+    static int cg_max_grid(int device, int threads);
+    static cudaError_t finish(uint32_t *rng_states, const MrgJump *step_jumps, int nblobs, DevStatus *st,
+                              cudaStream_t s);
+};
 void count_launch(int n = 1);
 
 }  // namespace ffea

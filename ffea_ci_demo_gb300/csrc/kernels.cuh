@@ -41,7 +41,9 @@ struct ElemArgs {
     double *last_det;
     R *ef;    // 12*T
     R *geom;  // 16*T: dpsi[12], vol
-    const uint32_t *rng_state;     // 6: stream state at the start of the step
+    const uint32_t *rng_state;     // 6 per stream: stream state at the start of the step
+    const int *elem_blob;          // batch: blob of each element (null for one blob)
+    const int *elem_off;           // batch: first element of each blob
     const MrgJump *chunk_jump;     // ceil(T/32): A^(7*32*c)
     const MrgJump *lane_jump;      // 32: A^(7*l)
     DevStatus *st;
@@ -154,11 +156,19 @@ __global__ void __launch_bounds__(128) element_kernel(ElemArgs<R> g) {
     }
     // add_fluctuating_stress :412-431, draws in the single-thread reference order
     if (g.calc_noise == 1) {
+        // element e of a blob starts 7e draws after the blob's stream state
         uint32_t base[6], s6[6];
+        int le = e;
+        const uint32_t *rs = g.rng_state;
+        if (g.elem_blob) {
+            const int b = g.elem_blob[e];
+            le = e - g.elem_off[b];
+            rs += 6 * (size_t)b;
+        }
 #pragma unroll
-        for (int k = 0; k < 6; ++k) s6[k] = g.rng_state[k];
-        mrg_apply(g.chunk_jump[e >> 5], s6, base);
-        mrg_apply(g.lane_jump[e & 31], base, s6);
+        for (int k = 0; k < 6; ++k) s6[k] = rs[k];
+        mrg_apply(g.chunk_jump[le >> 5], s6, base);
+        mrg_apply(g.lane_jump[le & 31], base, s6);
         const R c = sqrt(((R)24 * g.kT) / (vol * g.dt));
         const R bf = sqrt(B) * (R)mrg_rand_half(s6);
         S[0][0] += c * (sqrt((R)2 * A) * (R)mrg_rand_half(s6) + bf);
@@ -287,7 +297,7 @@ __global__ void __launch_bounds__(128) assemble_kernel(AsmArgs<R> g) {
 template <class R>
 struct GatherArgs {
     int N;
-    int mode;             // 0: CG (NoMass or consistent mass), 1: mass-lumped scaling
+    int mode;             // 0: CG (NoMass or consistent mass), 1: mass-lumped scaling, 2: batch CG (f, r only)
     const int *inc_ptr, *inc;  // element*4 + slot, element order
     const R *ef;
     const int *pinned;
@@ -394,9 +404,9 @@ struct CgArgs {
 
 // p at node b for this iteration: p_new = beta p_old + D^{-1} r (vec3_scale_and_add with the
 // preconditioned residual, src/NoMassCGSolver.cpp:181-183), or z itself on the first iteration.
-template <class R>
-__device__ __forceinline__ void p_on_the_fly(const CgArgs<R> &g, const R *pold, R beta, bool first, int b, R &p0,
-                                              R &p1, R &p2) {
+template <class A, class R>
+__device__ __forceinline__ void p_on_the_fly(const A &g, const R *pold, R beta, bool first, int b, R &p0, R &p1,
+                                              R &p2) {
     const R z0 = g.dinv[4 * b] * g.r[4 * b], z1 = g.dinv[4 * b + 1] * g.r[4 * b + 1],
             z2 = g.dinv[4 * b + 2] * g.r[4 * b + 2];
     if (first) {
@@ -412,9 +422,9 @@ __device__ __forceinline__ void p_on_the_fly(const CgArgs<R> &g, const R *pold, 
 // combined with shuffles; every lane of the group returns the row. All 32 lanes of the warp call it
 // together (rows past the end pass valid = false). ONTHEFLY: p is formed from p_old, r and D^{-1}
 // (mixed path); otherwise it is read from pold (FP64 path).
-template <bool ONTHEFLY, class R>
-__device__ __forceinline__ void spmv_row(const CgArgs<R> &g, const R *pold, R beta, bool first, int a, int sub,
-                                         bool valid, R &q0, R &q1, R &q2) {
+template <bool ONTHEFLY, class A, class R>
+__device__ __forceinline__ void spmv_row(const A &g, const R *pold, R beta, bool first, int a, int sub, bool valid,
+                                         R &q0, R &q1, R &q2) {
     q0 = 0.0; q1 = 0.0; q2 = 0.0;
     const int tpn = g.tpn;
     if (valid) {
@@ -649,7 +659,7 @@ struct EulerArgs {
 template <class R>
 __global__ void __launch_bounds__(256) euler_kernel(EulerArgs<R> g) {
     const int a = blockIdx.x * blockDim.x + threadIdx.x;
-    if (g.st->abort) return;
+    if (g.st->abort || g.st->cg_fail) return;
     if (a < g.N) {
         const double x0 = (double)g.x[4 * a], x1 = (double)g.x[4 * a + 1], x2 = (double)g.x[4 * a + 2];
         if (!(isfinite(x0) && isfinite(x1) && isfinite(x2))) atomicExch(&g.st->nonfinite, 1);

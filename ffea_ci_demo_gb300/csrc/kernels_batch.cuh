@@ -1,0 +1,361 @@
+// kernels_batch.cuh -- many replica blobs advanced by one set of launches.
+// (Included by engine_mixed.cu only: its kernels are not templates.)
+//
+// A batch packs B independent blobs of uneven size CSR-style: the vertex
+// nodes of blob b are rows [row0_b, row0_b + nrows_b) of one global
+// numbering, its elements a contiguous range, and the element, assembly,
+// gather and Euler kernels of the single-blob step run unchanged over the
+// concatenation (they never look across a blob's edge because no element or
+// matrix block does). What is per blob is the thermal noise (one MRG32k3a
+// substream per blob) and the CG: every blob has its own right-hand side,
+// rigid modes, step lengths and stopping test.
+//
+// cg_batch_kernel is one persistent cooperative launch for the whole batch.
+// The scheduler (schedule_kernel, run at the head of every step) splits the
+// grid's CTAs into one group per blob, sized in proportion to the blob's
+// rows x CG iterations of the previous step, so that all groups finish
+// together. Each group runs the mixed-precision deflated Jacobi-PCG of
+// cg_mixed_kernel on its rows with its own bounded barrier (a one-CTA group
+// synchronises with __syncthreads alone) and its own partial sums, and leaves
+// its loop when its own blob has converged: the per-blob convergence mask is
+// the group's exit.
+#pragma once
+
+#include "batch_types.cuh"
+
+namespace ffea {
+
+// Barrier of the nblk CTAs of one group: grid_sync with the group's own counter. A one-CTA group
+// needs only __syncthreads (global writes of a block are visible to the block after it).
+__device__ __forceinline__ bool group_sync(GridBarrier *gb, unsigned nblk, DevStatus *st,
+                                           unsigned long long limit_ns) {
+    if (nblk == 1u) {
+        __syncthreads();
+        return true;
+    }
+    __shared__ int s_ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int ok = 1;
+        __threadfence();
+        const unsigned int old = atomicAdd(&gb->count, 1u);
+        const unsigned int k1 = old / nblk + 1u;
+        if (old == k1 * nblk - 1u) {
+            atomicExch(&gb->passed, k1);
+        } else {
+            volatile unsigned int *passed = &gb->passed;
+            const unsigned long long t0 = globaltimer_ns();
+            unsigned int polls = 0;
+            while ((int)(*passed - k1) < 0) {
+                if ((++polls & 255u) == 0u) {
+                    if (globaltimer_ns() - t0 > limit_ns) {
+                        atomicExch(&st->timeout, 1);
+                        atomicExch(&st->abort, 1);
+                        ok = 0;
+                        break;
+                    }
+                    if (*((volatile int *)&st->timeout)) { ok = 0; break; }
+                }
+            }
+        }
+        __threadfence();
+        s_ok = ok;
+    }
+    __syncthreads();
+    return s_ok != 0;
+}
+
+// Rows of one blob split over the warps of its group: the group's W warps take consecutive runs of
+// rppw = min(32 / tpn, ceil(nrows / W)) rows per pass, tpn lanes per row (see FFEA_ROW_LOOP).
+#define BATCH_ROW_LOOP(tpn, row0, nrows, rank, gsz, a, sub, valid)                                   \
+    const int sub = (threadIdx.x & 31) % (tpn);                                                      \
+    const int wtot_ = (gsz) * (int)(blockDim.x >> 5);                                                \
+    const int rppw_ = min(32 / (tpn), ((nrows) + wtot_ - 1) / wtot_);                                \
+    const int wglob_ = (rank) * (int)(blockDim.x >> 5) + (int)(threadIdx.x >> 5);                    \
+    const int lrow_ = (threadIdx.x & 31) / (tpn);                                                    \
+    for (int a0_ = wglob_ * rppw_, la_ = a0_ + lrow_, a = (row0) + la_; a0_ < (nrows);                 \
+         a0_ += wtot_ * rppw_, la_ = a0_ + lrow_, a = (row0) + la_)                                    \
+        for (bool valid = lrow_ < rppw_ && la_ < (nrows), once_ = true; once_; once_ = false)
+
+// Nodes of one blob split into equal runs, one per CTA of its group, one node per thread.
+#define BATCH_NODE_LOOP(row0, nrows, rank, gsz, a)                                                    \
+    for (int npb_ = ((nrows) + (gsz) - 1) / (gsz), la_ = (rank) * npb_ + (int)threadIdx.x,             \
+             laend_ = min((nrows), ((rank) + 1) * npb_), a = (row0) + la_;                               \
+         la_ < laend_; la_ += blockDim.x, a += blockDim.x)
+
+__global__ void __launch_bounds__(BATCH_MAX_THREADS) cg_batch_kernel(const __grid_constant__ BatchCgArgs g) {
+    __shared__ BlobCgDesc s_desc;
+    __shared__ float smemf[MIXED_GATHER_NP * 32];
+    __shared__ double s_sc[MIXED_GATHER_NP];
+    __shared__ double s_A6[36];
+    __shared__ float s_alpha, s_beta, s_tau[3], s_Om[3];
+    __shared__ double s_delta;
+    __shared__ int s_conv;
+    DevStatus *st = g.st;
+    if (st->abort) return;
+    const int b = g.cta_blob[blockIdx.x];
+    if (b < 0) return;
+    if (threadIdx.x == 0) s_desc = g.desc[b];
+    __syncthreads();
+    const int row0 = s_desc.row0, nrows = s_desc.nrows, gsz = s_desc.grp_size;
+    const int rank = (int)blockIdx.x - s_desc.grp_first;
+    GridBarrier *gb = g.gbs + b;
+    float2 *spart = g.partials + (size_t)BATCH_ROWS * s_desc.grp_first;  // set-up rows [0, 28)
+    float2 *ipart = spart + (size_t)MIXED_GATHER_NP * gsz;                 // iteration rows [0, 10)
+    const bool defl = s_desc.nmodes > 0;
+    // set-up: node offsets d = x - x_c, moments f.f, S1_f, S2_f and M = sum Phi^T D Phi (cf. gather_mixed_kernel)
+    {
+        float acc[MIXED_GATHER_NP];
+#pragma unroll
+        for (int i = 0; i < MIXED_GATHER_NP; ++i) acc[i] = 0.f;
+        BATCH_NODE_LOOP(row0, nrows, rank, gsz, a) {
+            const float F0 = g.r[4 * a], F1 = g.r[4 * a + 1], F2 = g.r[4 * a + 2];
+            const float dx = (float)(g.px[a] - s_desc.xc[0]), dy = (float)(g.py[a] - s_desc.xc[1]),
+                        dz = (float)(g.pz[a] - s_desc.xc[2]);
+            g.dpos[a] = make_float4(dx, dy, dz, 0.f);
+            g.x[4 * a] = 0.f; g.x[4 * a + 1] = 0.f; g.x[4 * a + 2] = 0.f;
+            acc[0] += F0 * F0 + F1 * F1 + F2 * F2;
+            acc[1] += F0; acc[2] += F1; acc[3] += F2;
+            acc[4] += dy * F2 - dz * F1; acc[5] += dz * F0 - dx * F2; acc[6] += dx * F1 - dy * F0;
+            float phi[6][3];
+            phi_cols(dx, dy, dz, phi);
+            const float D[3] = {g.diag[4 * a], g.diag[4 * a + 1], g.diag[4 * a + 2]};
+            int k = 7;
+#pragma unroll
+            for (int i = 0; i < 6; ++i)
+#pragma unroll
+                for (int j = i; j < 6; ++j, ++k)
+                    acc[k] += phi[i][0] * D[0] * phi[j][0] + phi[i][1] * D[1] * phi[j][1] + phi[i][2] * D[2] * phi[j][2];
+        }
+        df32 o[MIXED_GATHER_NP];
+        block_reduce_f<MIXED_GATHER_NP>(acc, smemf, o);
+        if (threadIdx.x == 0)
+#pragma unroll
+            for (int i = 0; i < MIXED_GATHER_NP; ++i) spart[i * gsz + rank] = make_float2(o[i].hi, o[i].lo);
+    }
+    bool ok = group_sync(gb, gsz, st, g.limit_ns);
+    if (!ok) return;
+    grid_sum_df<MIXED_GATHER_NP>(spart, gsz, gsz, s_sc);
+    const double f2 = s_sc[0];
+    if (threadIdx.x == 0) mixed_setup(s_desc, s_sc, s_A6, s_tau, s_Om, &s_beta, &s_conv);
+    __syncthreads();
+    // r = f^ (projected), initial r.z
+    float acc0[1] = {0.f};
+    BATCH_NODE_LOOP(row0, nrows, rank, gsz, a) {
+        float r0 = g.r[4 * a], r1 = g.r[4 * a + 1], r2 = g.r[4 * a + 2];
+        if (defl) {
+            const float4 d = g.dpos[a];
+            r0 -= g.diag[4 * a] * (s_tau[0] + (s_Om[1] * d.z - s_Om[2] * d.y));
+            r1 -= g.diag[4 * a + 1] * (s_tau[1] + (s_Om[2] * d.x - s_Om[0] * d.z));
+            r2 -= g.diag[4 * a + 2] * (s_tau[2] + (s_Om[0] * d.y - s_Om[1] * d.x));
+            g.r[4 * a] = r0; g.r[4 * a + 1] = r1; g.r[4 * a + 2] = r2;
+        }
+        acc0[0] += r0 * (g.dinv[4 * a] * r0) + r1 * (g.dinv[4 * a + 1] * r1) + r2 * (g.dinv[4 * a + 2] * r2);
+    }
+    const int rowz = MIXED_A_NP + MIXED_B_NP;
+    {
+        __syncthreads();  // smemf is reused
+        df32 o[1];
+        block_reduce_f<1>(acc0, smemf, o);
+        if (threadIdx.x == 0) ipart[rowz * gsz + rank] = make_float2(o[0].hi, o[0].lo);
+    }
+    ok = group_sync(gb, gsz, st, g.limit_ns);
+    if (ok) {
+        grid_sum_df<1>(ipart + rowz * gsz, 0, gsz, s_sc);
+        if (threadIdx.x == 0) s_delta = s_sc[0];
+        __syncthreads();
+    }
+    float *pold = g.pbuf0, *pnew = g.pbuf1;
+    int it = 0;
+    for (; ok && it < g.imax; ++it) {
+        const bool first = it == 0;
+        const float beta = s_beta;
+        // phase A: q = V p with p formed on the fly; p.q; moments of D p
+        float acc[MIXED_A_NP];
+#pragma unroll
+        for (int i = 0; i < MIXED_A_NP; ++i) acc[i] = 0.f;
+        {
+            BATCH_ROW_LOOP(g.tpn, row0, nrows, rank, gsz, a, sub, valid) {
+                float q0, q1, q2;
+                spmv_row<true>(g, pold, beta, first, a, sub, valid, q0, q1, q2);
+                if (!valid || sub != 0) continue;
+                float p0, p1, p2;
+                p_on_the_fly(g, pold, beta, first, a, p0, p1, p2);
+                pnew[4 * a] = p0; pnew[4 * a + 1] = p1; pnew[4 * a + 2] = p2;
+                g.q[4 * a] = q0; g.q[4 * a + 1] = q1; g.q[4 * a + 2] = q2;
+                acc[0] += p0 * q0 + p1 * q1 + p2 * q2;
+                if (defl) {
+                    const float4 d = g.dpos[a];
+                    const float e0 = g.diag[4 * a] * p0, e1 = g.diag[4 * a + 1] * p1, e2 = g.diag[4 * a + 2] * p2;
+                    acc[1] += e0; acc[2] += e1; acc[3] += e2;
+                    acc[4] += d.y * e2 - d.z * e1;
+                    acc[5] += d.z * e0 - d.x * e2;
+                    acc[6] += d.x * e1 - d.y * e0;
+                }
+            }
+        }
+        {
+            df32 o[MIXED_A_NP];
+            block_reduce_f<MIXED_A_NP>(acc, smemf, o);
+            if (threadIdx.x == 0)
+#pragma unroll
+                for (int i = 0; i < MIXED_A_NP; ++i) ipart[i * gsz + rank] = make_float2(o[i].hi, o[i].lo);
+        }
+        if (!(ok = group_sync(gb, gsz, st, g.limit_ns))) break;
+        grid_sum_df<MIXED_A_NP>(ipart, gsz, gsz, s_sc);
+        if (threadIdx.x < 32) {
+            const int l = threadIdx.x;
+            double tO = 0.0;
+            if (defl && l < 6) {
+#pragma unroll
+                for (int q = 0; q < 6; ++q) tO += s_A6[6 * l + q] * s_sc[1 + q];
+            }
+            double prod = (l < 6) ? tO * s_sc[1 + l] : 0.0;
+#pragma unroll
+            for (int o = 4; o > 0; o >>= 1) prod += __shfl_xor_sync(0xffffffffu, prod, o);
+            if (l < 6) {
+                if (l < 3) s_tau[l] = (float)tO; else s_Om[l - 3] = (float)tO;
+            }
+            if (l == 0) s_alpha = (float)s_delta / (float)(s_sc[0] + prod);
+        }
+        __syncthreads();
+        const float alpha = s_alpha;
+        const float t0 = s_tau[0], t1 = s_tau[1], t2 = s_tau[2], O0 = s_Om[0], O1 = s_Om[1], O2 = s_Om[2];
+        // phase B: x += alpha p ; r -= alpha (q + D (tau + Omega x d)) ; r.r ; r.z
+        float acc2[MIXED_B_NP] = {0.f, 0.f};
+        BATCH_NODE_LOOP(row0, nrows, rank, gsz, a) {
+#pragma unroll
+            for (int c = 0; c < 3; ++c) g.x[4 * a + c] += alpha * pnew[4 * a + c];
+            float q0 = g.q[4 * a], q1 = g.q[4 * a + 1], q2 = g.q[4 * a + 2];
+            if (defl) {
+                const float4 d = g.dpos[a];
+                q0 += g.diag[4 * a] * (t0 + (O1 * d.z - O2 * d.y));
+                q1 += g.diag[4 * a + 1] * (t1 + (O2 * d.x - O0 * d.z));
+                q2 += g.diag[4 * a + 2] * (t2 + (O0 * d.y - O1 * d.x));
+            }
+            const float r0 = g.r[4 * a] - alpha * q0, r1 = g.r[4 * a + 1] - alpha * q1, r2 = g.r[4 * a + 2] - alpha * q2;
+            g.r[4 * a] = r0; g.r[4 * a + 1] = r1; g.r[4 * a + 2] = r2;
+            acc2[0] += r0 * r0 + r1 * r1 + r2 * r2;
+            acc2[1] += r0 * (g.dinv[4 * a] * r0) + r1 * (g.dinv[4 * a + 1] * r1) + r2 * (g.dinv[4 * a + 2] * r2);
+        }
+        {
+            df32 o[MIXED_B_NP];
+            block_reduce_f<MIXED_B_NP>(acc2, smemf, o);
+            if (threadIdx.x == 0)
+                for (int i = 0; i < MIXED_B_NP; ++i) ipart[(MIXED_A_NP + i) * gsz + rank] = make_float2(o[i].hi, o[i].lo);
+        }
+        if (!(ok = group_sync(gb, gsz, st, g.limit_ns))) break;
+        grid_sum_df<MIXED_B_NP>(ipart + MIXED_A_NP * gsz, gsz, gsz, s_sc);
+        if (threadIdx.x == 0) {
+            s_conv = (f2 == 0.0 || s_sc[0] < g.eps2 * f2);
+            const double delta_old = s_delta;
+            s_delta = s_sc[1];
+            s_beta = (float)s_delta / (float)delta_old;
+        }
+        __syncthreads();
+        if (s_conv) {
+            ++it;
+            break;
+        }
+        float *t = pold; pold = pnew; pnew = t;
+    }
+    if (rank == 0 && threadIdx.x == 0) {
+        if (!ok) {
+            atomicExch(&st->abort, 1);
+        } else if (!s_conv) {
+            // cg_fail alone: `abort` raised now could stop a CTA of another group that has not yet
+            // passed its start-up check, and its group would wait for it; batch_finish_kernel raises it
+            atomicExch(&st->cg_fail, 1);
+            g.blob_iters[b] = g.imax;
+        } else {
+            g.blob_iters[b] = it;
+            atomicMax(&st->last_iters, it);
+            atomicAdd(reinterpret_cast<unsigned long long *>(&st->total_iters), (unsigned long long)it);
+        }
+    }
+}
+
+// CTA groups for the next solve, from the rows and last iteration counts of every blob: each blob
+// gets one CTA plus a share of the other C - B CTAs in proportion to rows x iterations (largest
+// remainders first), so that the groups' solves take about equally long. One block.
+__global__ void __launch_bounds__(1024) schedule_kernel(BlobCgDesc *desc, const int *blob_iters, int nblobs,
+                                                        int ncta, int *cta_blob, const DevStatus *st) {
+    __shared__ double s_wsum;
+    __shared__ int s_given;
+    if (st->abort) return;
+    extern __shared__ double s_w[];  // nblobs weights, then nblobs remainders
+    double *s_rem = s_w + nblobs;
+    int *s_g = reinterpret_cast<int *>(s_rem + nblobs);
+    if (threadIdx.x == 0) { s_wsum = 0.0; s_given = 0; }
+    __syncthreads();
+    for (int b = threadIdx.x; b < nblobs; b += blockDim.x) {
+        const double w = (double)desc[b].nrows * (double)max(blob_iters[b], 1);
+        s_w[b] = w;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double s = 0.0;
+        for (int b = 0; b < nblobs; ++b) s += s_w[b];  // fixed order
+        s_wsum = s;
+    }
+    __syncthreads();
+    const int spare = ncta - nblobs;
+    for (int b = threadIdx.x; b < nblobs; b += blockDim.x) {
+        const double share = s_wsum > 0.0 ? (double)spare * s_w[b] / s_wsum : 0.0;
+        const int whole = (int)floor(share);
+        s_g[b] = 1 + whole;
+        s_rem[b] = share - whole;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int t = 0;
+        for (int b = 0; b < nblobs; ++b) t += s_g[b];
+        s_given = t;
+    }
+    __syncthreads();
+    const int left = ncta - s_given;  // < nblobs: one more CTA for the `left` largest remainders
+    for (int b = threadIdx.x; b < nblobs; b += blockDim.x) {
+        int rankr = 0;
+        const double rb = s_rem[b];
+        for (int c = 0; c < nblobs; ++c) {
+            const double rc = s_rem[c];
+            rankr += (rc > rb || (rc == rb && c < b)) ? 1 : 0;
+        }
+        if (rankr < left) s_g[b] += 1;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int first = 0;
+        for (int b = 0; b < nblobs; ++b) {
+            desc[b].grp_first = first;
+            desc[b].grp_size = s_g[b];
+            first += s_g[b];
+        }
+        s_given = first;
+    }
+    __syncthreads();
+    for (int b = threadIdx.x; b < nblobs; b += blockDim.x) {
+        const int f = desc[b].grp_first, n = desc[b].grp_size;
+        for (int c = f; c < f + n; ++c) cta_blob[c] = b;
+    }
+    for (int c = s_given + threadIdx.x; c < ncta; c += blockDim.x) cta_blob[c] = -1;
+}
+
+// closes a batch step: every blob's stream advances by its own A^(7 T_b) (when noise is on)
+__global__ void batch_finish_kernel(uint32_t *rng_states, const MrgJump *step_jumps, int nblobs, DevStatus *st) {
+    if (st->abort) return;
+    if (st->cg_fail) {  // a blob's CG hit its cap: the step is void, later steps of the call do nothing
+        if (blockIdx.x == 0 && threadIdx.x == 0) st->abort = 1;
+        return;
+    }
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b < nblobs) {
+        uint32_t s[6], o[6];
+        for (int k = 0; k < 6; ++k) s[k] = rng_states[6 * (size_t)b + k];
+        mrg_apply(step_jumps[b], s, o);
+        for (int k = 0; k < 6; ++k) rng_states[6 * (size_t)b + k] = o[k];
+    }
+    if (b == 0) st->steps_done += 1;
+}
+
+}  // namespace ffea

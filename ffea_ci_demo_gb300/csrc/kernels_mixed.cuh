@@ -78,6 +78,7 @@ __global__ void __launch_bounds__(256) gather_mixed_kernel(GatherArgs<R> g) {
             return;
         }
         g.r[4 * a] = F0; g.r[4 * a + 1] = F1; g.r[4 * a + 2] = F2;
+        if (g.mode == 2) return;  // batch: the per-blob CG set-up forms the moments
         const float dx = (float)(g.px[a] - g.xc[0]), dy = (float)(g.py[a] - g.xc[1]), dz = (float)(g.pz[a] - g.xc[2]);
         g.dpos[a] = make_float4(dx, dy, dz, 0.f);
         acc[0] = df32{F0 * F0 + F1 * F1 + F2 * F2, 0.f};
@@ -95,7 +96,7 @@ __global__ void __launch_bounds__(256) gather_mixed_kernel(GatherArgs<R> g) {
                     acc[k].hi = phi[i][0] * D[0] * phi[j][0] + phi[i][1] * D[1] * phi[j][1] + phi[i][2] * D[2] * phi[j][2];
         }
     }
-    if (g.mode == 1) return;
+    if (g.mode != 0) return;
     df32 out[MIXED_GATHER_NP];
     block_sum_df<MIXED_GATHER_NP>(acc, smem, out);
     if (threadIdx.x == 0) {
@@ -107,8 +108,8 @@ __global__ void __launch_bounds__(256) gather_mixed_kernel(GatherArgs<R> g) {
 
 // thread 0 of every block: G = Z^T D Z from the moments, its inverse, and the coefficients of the
 // projection of the right-hand side (kept out of line: it runs once per solve)
-template <class R>
-__device__ __noinline__ void mixed_setup(const CgArgs<R> &g, const double *s_sc, double *s_A6, float *s_tau,
+template <class A>
+__device__ __noinline__ void mixed_setup(const A &g, const double *s_sc, double *s_A6, float *s_tau,
                                          float *s_Om, float *s_beta, int *s_conv) {
         const int k = g.nmodes;
         double M[6][6];

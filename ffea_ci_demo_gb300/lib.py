@@ -96,6 +96,20 @@ def load():
         "ffea_gpu_blob_get_elements": (C.c_int, [vp, dp, dp, dp]),
         "ffea_gpu_blob_get_rhs": (C.c_int, [vp, dp]),
         "ffea_gpu_blob_solve_static": (C.c_int, [vp, dp, dp, ip]),
+        "ffea_gpu_batch_create": (C.c_int, [vp, C.c_int, C.POINTER(Params), C.POINTER(vp)]),
+        "ffea_gpu_batch_destroy": (None, [vp]),
+        "ffea_gpu_batch_sizes": (C.c_int, [vp, ip, ip, ip, C.POINTER(C.c_longlong)]),
+        "ffea_gpu_batch_blob_sizes": (C.c_int, [vp, C.c_int, ip, ip, ip]),
+        "ffea_gpu_batch_step": (C.c_int, [vp, C.c_int, ip]),
+        "ffea_gpu_batch_step_timed": (C.c_int, [vp, C.c_int, C.c_longlong, ip, C.POINTER(C.c_double)]),
+        "ffea_gpu_batch_get_state": (C.c_int, [vp, C.c_int, dp, dp]),
+        "ffea_gpu_batch_set_state": (C.c_int, [vp, C.c_int, dp, dp]),
+        "ffea_gpu_batch_set_rng_state": (C.c_int, [vp, C.c_int, dp]),
+        "ffea_gpu_batch_get_rng_state": (C.c_int, [vp, C.c_int, dp]),
+        "ffea_gpu_batch_cg_iterations": (C.c_int, [vp, dp, C.POINTER(C.c_longlong)]),
+        "ffea_gpu_batch_config": (C.c_int, [vp, ip, ip, ip]),
+        "ffea_gpu_batch_set_config": (C.c_int, [vp, C.c_int, C.c_int]),
+        "ffea_gpu_batch_tune": (C.c_int, [vp, C.c_int, C.POINTER(C.c_double)]),
         "ffea_gpu_last_error": (C.c_char_p, []),
         "ffea_gpu_launch_count": (C.c_longlong, []),
     }
@@ -316,6 +330,119 @@ class Blob:
         o = np.empty((self.n_nodes, 3))
         _check(self._lib.ffea_gpu_blob_get_rhs(self._h, _p(o)), "get_rhs")
         return o
+
+
+def _mesh_struct(mesh: Mesh, keep: list) -> MeshStruct:
+    """ffea_gpu_mesh of a Mesh in meso units; the arrays it points to are appended to `keep`."""
+    s = mesh.scale / MESO_LENGTH
+    arrs = [np.ascontiguousarray(mesh.pos * s, np.float64), np.ascontiguousarray(mesh.tets, np.int32),
+            np.ascontiguousarray(mesh.stokes_radius * s, np.float64),
+            np.ascontiguousarray(mesh.pinned, np.int32) if len(mesh.pinned) else None]
+    mat = material_from_si(mesh.material)
+    arrs += [mat[k] for k in ("rho", "A", "B", "G", "E")]
+    keep += arrs
+    return MeshStruct(mesh.n_nodes, mesh.n_elem, len(mesh.pinned), _p(arrs[0]), _p(arrs[1]),
+                      *(_p(mat[k]) for k in ("rho", "A", "B", "G", "E")), _p(arrs[2]), _p(arrs[3]))
+
+
+class Batch:
+    """Many independent blobs of uneven size advanced together (mixed precision, CG_nomass).
+
+    Every blob runs the per-blob step of the reference's World::run; blob b's noise is substream b of
+    the package seed's stream. One step of the whole batch is one CUDA graph replay."""
+
+    def __init__(self, meshes: list[Mesh], *, dt: float = 1e-12, kT: float = 4.11e-21, epsilon: float = 1e-10,
+                 max_iterations_cg: int = 10000, calc_noise: int = 1, calc_stokes: int = 0,
+                 stokes_visc: float = 1e-3):
+        self._lib = load()
+        self._h = C.c_void_p()
+        params = make_params(solver="CG_nomass", precision="mixed", dt=dt, kT=kT, epsilon=epsilon,
+                             max_iterations_cg=max_iterations_cg, calc_noise=calc_noise, calc_stokes=calc_stokes,
+                             stokes_visc=stokes_visc)
+        keep: list = []
+        arr = (MeshStruct * len(meshes))(*[_mesh_struct(m, keep) for m in meshes])
+        _check(self._lib.ffea_gpu_batch_create(C.cast(arr, C.c_void_p), len(meshes), C.byref(params),
+                                               C.byref(self._h)), "batch_create")
+        self.n_blobs = len(meshes)
+        self.n_nodes = [m.n_nodes for m in meshes]
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) and self._h.value:
+            self._lib.ffea_gpu_batch_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        self.close()
+
+    def update(self, nsteps: int = 1) -> int:
+        done = C.c_int(0)
+        rc = self._lib.ffea_gpu_batch_step(self._h, int(nsteps), C.byref(done))
+        _check(rc, f"batch_step (after {done.value} completed steps)")
+        return done.value
+
+    def update_timed(self, nsteps: int, flush_bytes: int = 0) -> dict:
+        done, ms = C.c_int(0), C.c_double(0)
+        rc = self._lib.ffea_gpu_batch_step_timed(self._h, int(nsteps), int(flush_bytes), C.byref(done), C.byref(ms))
+        _check(rc, f"batch_step_timed (after {done.value} completed steps)")
+        return {"steps": done.value, "ms": ms.value}
+
+    def state(self, blob: int):
+        pos = np.empty((self.n_nodes[blob], 3))
+        vel = np.empty((self.n_nodes[blob], 3))
+        _check(self._lib.ffea_gpu_batch_get_state(self._h, blob, _p(pos), _p(vel)), "batch_get_state")
+        return pos, vel
+
+    def pos(self, blob: int) -> np.ndarray:
+        o = np.empty((self.n_nodes[blob], 3))
+        _check(self._lib.ffea_gpu_batch_get_state(self._h, blob, _p(o), None), "batch_get_state")
+        return o
+
+    def set_state(self, blob: int, pos=None, vel=None) -> None:
+        pa = None if pos is None else np.ascontiguousarray(pos, np.float64)
+        va = None if vel is None else np.ascontiguousarray(vel, np.float64)
+        _check(self._lib.ffea_gpu_batch_set_state(self._h, blob, _p(pa), _p(va)), "batch_set_state")
+
+    def rng_state(self, blob: int) -> np.ndarray:
+        a = np.empty(6, np.uint32)
+        _check(self._lib.ffea_gpu_batch_get_rng_state(self._h, blob, _p(a)), "batch_get_rng_state")
+        return a
+
+    def set_rng_state(self, blob: int, s) -> None:
+        a = np.ascontiguousarray(s, np.uint32)
+        _check(self._lib.ffea_gpu_batch_set_rng_state(self._h, blob, _p(a)), "batch_set_rng_state")
+
+    def cg_iterations(self) -> tuple[np.ndarray, int]:
+        last = np.zeros(self.n_blobs, np.int32)
+        total = C.c_longlong()
+        _check(self._lib.ffea_gpu_batch_cg_iterations(self._h, _p(last), C.byref(total)), "batch_cg_iterations")
+        return last, total.value
+
+    def sizes(self) -> dict:
+        nb, nl, ne, blocks = C.c_int(), C.c_int(), C.c_int(), C.c_longlong()
+        _check(self._lib.ffea_gpu_batch_sizes(self._h, C.byref(nb), C.byref(nl), C.byref(ne), C.byref(blocks)),
+               "batch_sizes")
+        return {"blobs": nb.value, "nodes": nl.value, "elements": ne.value, "blocks": blocks.value}
+
+    def blob_sizes(self, blob: int) -> tuple[int, int, int]:
+        n, nv, ne = C.c_int(), C.c_int(), C.c_int()
+        _check(self._lib.ffea_gpu_batch_blob_sizes(self._h, blob, C.byref(n), C.byref(nv), C.byref(ne)),
+               "batch_blob_sizes")
+        return n.value, nv.value, ne.value
+
+    def config(self) -> dict:
+        t, p, c = C.c_int(), C.c_int(), C.c_int()
+        _check(self._lib.ffea_gpu_batch_config(self._h, C.byref(t), C.byref(p), C.byref(c)), "batch_config")
+        return {"cg_threads": t.value, "threads_per_row": p.value, "ctas": c.value}
+
+    def set_config(self, cg_threads: int, threads_per_row: int) -> None:
+        _check(self._lib.ffea_gpu_batch_set_config(self._h, int(cg_threads), int(threads_per_row)),
+               "batch_set_config")
+
+    def tune(self, solves: int = 2) -> float:
+        """Autotune the CG launch (CTA size, threads per row) on the current forces; returns the best ms."""
+        best = C.c_double()
+        _check(self._lib.ffea_gpu_batch_tune(self._h, int(solves), C.byref(best)), "batch_tune")
+        return best.value
 
 
 def launch_count() -> int:

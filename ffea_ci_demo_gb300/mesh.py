@@ -240,3 +240,25 @@ def counts(n: int) -> dict:
     E = 3 * n * (n + 1) ** 2 + 3 * n * n * (n + 1) + n ** 3
     return {"T": 6 * n ** 3, "N": N, "E_lin": E, "N_all": (2 * n + 1) ** 3,
             "nnz_linear": 9 * (N + 2 * E), "nnz_blocks": N + 2 * E}
+
+
+def ensemble_cells(nblobs: int = 256, *, seed: int = 2024, nmin: int = 8, nmax: int = 32) -> np.ndarray:
+    """Cells per side of each replica: log-uniform in [nmin, nmax], rounded, seeded."""
+    rng = np.random.default_rng(seed)
+    return np.rint(np.exp(rng.uniform(np.log(nmin), np.log(nmax), size=nblobs))).astype(int)
+
+
+def ensemble(nblobs: int = 256, *, seed: int = 2024, nmin: int = 8, nmax: int = 32, cell: float = 5.0,
+             g_min: float = 1e8, g_max: float = 1e9, bulk_ratio: float = 3.9) -> list[Mesh]:
+    """Replica ensemble of uneven Kuhn cubes: cells per side log-uniform in [nmin, nmax] (so
+    6 nmin^3 .. 6 nmax^3 tets per blob), cell size ``cell`` file units, per-blob shear modulus
+    uniform in [g_min, g_max] Pa and bulk modulus ``bulk_ratio`` x shear; other material as
+    :func:`kuhn_cube`. Every draw comes from ``seed``."""
+    cells = ensemble_cells(nblobs, seed=seed, nmin=nmin, nmax=nmax)
+    rng = np.random.default_rng(seed + 1)
+    gs = rng.uniform(g_min, g_max, size=nblobs)
+    out = []
+    for b, (n, gmod) in enumerate(zip(cells, gs)):
+        out.append(kuhn_cube(int(n), side=cell * int(n), seed=seed + 100 + b, shear_mod=float(gmod),
+                             bulk_mod=bulk_ratio * float(gmod)))
+    return out

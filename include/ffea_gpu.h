@@ -205,6 +205,56 @@ int ffea_gpu_blob_get_rhs(ffea_gpu_blob *blob, double *rhs);
 #define FFEA_GPU_SOLVE_STATIC_MAX_NODES 32768
 int ffea_gpu_blob_solve_static(ffea_gpu_blob *blob, const double *rhs, double *x, int *iterations);
 
+/* ---------------------------------------------------------------------------
+ * Replica batch: many independent blobs of uneven size advanced together.
+ *
+ * The reference advances the blobs of a World one after another with the same
+ * per-blob slice of World::run (src/World.cpp:1788-2059); a batch runs that
+ * slice for every blob at once: one CUDA graph per step, one persistent
+ * cooperative CG launch in which each blob's CTA group iterates until its own
+ * blob has converged. Mixed precision and the CG_nomass solver only. Blob b's
+ * noise comes from substream b of the stream whose state is the package seed
+ * 12345 x 6 (RngStream::ResetNextSubstream applied b times), drawn in the
+ * reference's single-thread order within the blob.
+ * ------------------------------------------------------------------------- */
+typedef struct ffea_gpu_batch ffea_gpu_batch;
+#define FFEA_GPU_BATCH_MAX_BLOBS 2048
+
+/* meshes[b] as for ffea_gpu_blob_create; params shared by every blob. */
+int ffea_gpu_batch_create(const ffea_gpu_mesh *meshes, int num_blobs, const ffea_gpu_params *params,
+                          ffea_gpu_batch **out);
+void ffea_gpu_batch_destroy(ffea_gpu_batch *batch);
+
+/* Totals over the batch: blobs, vertex nodes, elements, nonzero 3x3 matrix blocks. */
+int ffea_gpu_batch_sizes(ffea_gpu_batch *batch, int *num_blobs, int *vertex_nodes, int *elements, long long *blocks);
+/* One blob: all nodes (the length of its state arrays / 3), vertex nodes, elements. */
+int ffea_gpu_batch_blob_sizes(ffea_gpu_batch *batch, int blob, int *num_nodes, int *vertex_nodes, int *elements);
+
+/* nsteps steps of every blob; stops at the first failing step (*steps_done gets the completed steps). */
+int ffea_gpu_batch_step(ffea_gpu_batch *batch, int nsteps, int *steps_done);
+/* Same, each step timed by CUDA events around its graph launch, with flush_bytes of scratch written
+ * before every step outside the timed window; *step_ms = summed device time. */
+int ffea_gpu_batch_step_timed(ffea_gpu_batch *batch, int nsteps, long long flush_bytes, int *steps_done,
+                              double *step_ms);
+
+/* State of one blob in its own node order (as ffea_gpu_blob_get_state / set_state). */
+int ffea_gpu_batch_get_state(ffea_gpu_batch *batch, int blob, double *pos, double *vel);
+int ffea_gpu_batch_set_state(ffea_gpu_batch *batch, int blob, const double *pos, const double *vel);
+int ffea_gpu_batch_set_rng_state(ffea_gpu_batch *batch, int blob, const uint32_t state[6]);
+int ffea_gpu_batch_get_rng_state(ffea_gpu_batch *batch, int blob, uint32_t state[6]);
+
+/* CG iterations of each blob's last solve (num_blobs entries, may be NULL) and the total since creation. */
+int ffea_gpu_batch_cg_iterations(ffea_gpu_batch *batch, int *last_per_blob, long long *total);
+
+/* Launch configuration of the batch CG: CTA size, threads per matrix row, CTAs in the grid. */
+int ffea_gpu_batch_config(ffea_gpu_batch *batch, int *cg_threads, int *threads_per_row, int *ctas);
+int ffea_gpu_batch_set_config(ffea_gpu_batch *batch, int cg_threads, int threads_per_row);
+
+/* Autotuner: times `solves` CG solves of the current forces for every CTA size (128..1024) and
+ * threads per row (1, 2, 4, 8) and keeps the fastest; positions, velocities and RNG states are not
+ * changed. *best_ms (may be NULL) gets the best mean solve time. */
+int ffea_gpu_batch_tune(ffea_gpu_batch *batch, int solves, double *best_ms);
+
 /* Last CUDA error text for FFEA_GPU_ECUDA (static storage). */
 const char *ffea_gpu_last_error(void);
 

@@ -1,0 +1,150 @@
+"""Replica batch (ffea_gpu_batch_*): many blobs of uneven size in one graph-captured step.
+
+Each blob of a batch must follow the trajectory the single-blob mixed path gives
+for it (same element math, same noise draws; only the CG's cross-node sums are
+split over a different set of CTAs, so positions agree to the CG's rounding),
+and its noise must come from substream b of the package seed, bit-exact
+against the oracle's RngStream restatement (itself pinned to the reference's
+known answer).
+
+Tolerances: batch vs single-blob mixed path <= 1e-5 of the largest displacement
+after 10 steps at kT > 0 (FP32 CG rounding, the mixed path's own bound against
+FP64); batch at kT = 0 vs the FP64 path <= 1e-5 after 200 steps; CG iteration
+counts within 2 of the single blob's; RNG states bit-exact.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+import pyoracle as po
+from ffea_ci_demo_gb300 import build, lib
+from ffea_ci_demo_gb300.lib import MESO_LENGTH
+from gen_golden import case_mesh, sheared
+
+
+def substream_states(n):
+    po.OracleRng.set_package_seed([12345] * 6)
+    g = po.OracleRng()
+    out = []
+    for _ in range(n):
+        out.append(g.get_state())
+        g.reset_next_substream()
+    return out
+
+
+def test_batch_rejects_unsupported_params_without_gpu_work():
+    build.build()
+    L = lib.load()
+    h = C.c_void_p()
+    arr = (lib.MeshStruct * 1)()
+    for prec, solver in (("fp64", "CG_nomass"), ("mixed", "masslumped")):
+        p = lib.make_params(solver=solver, precision=prec)
+        assert L.ffea_gpu_batch_create(C.cast(arr, C.c_void_p), 1, C.byref(p), C.byref(h)) == lib.EINPUT
+    p = lib.make_params(solver="CG_nomass", precision="mixed")
+    assert L.ffea_gpu_batch_create(C.cast(arr, C.c_void_p), 0, C.byref(p), C.byref(h)) == lib.EINPUT
+    assert L.ffea_gpu_batch_step(None, 1, None) == lib.EINPUT
+
+
+MESHES = [(3, 5), (5, 8), (2, 13), (4, 21), (6, 2)]
+
+
+@pytest.mark.gpu
+def test_batch_rng_substreams(gpu, oracle_built):
+    meshes = [case_mesh(n, s) for n, s in MESHES]
+    bt = lib.Batch(meshes, calc_noise=1)
+    want = substream_states(len(meshes))
+    for b in range(len(meshes)):
+        assert np.array_equal(bt.rng_state(b), want[b]), b
+    # after one step each stream has advanced by 7 draws per element of its blob
+    bt.update(1)
+    for b, m in enumerate(meshes):
+        o = po.OracleRng()
+        o.set_state(want[b])
+        for _ in range(7 * m.n_elem):
+            o.rand_u01()
+        assert np.array_equal(bt.rng_state(b), o.get_state()), b
+
+
+@pytest.mark.gpu
+def test_batch_matches_single_blobs(gpu, oracle_built):
+    meshes = [case_mesh(n, s) for n, s in MESHES]
+    kw = dict(dt=1e-12, kT=4.11e-21, calc_noise=1)
+    bt = lib.Batch(meshes, **kw)
+    x0 = [sheared(m, 0.02, seed=7 + b) for b, m in enumerate(meshes)]
+    for b in range(len(meshes)):
+        bt.set_state(b, pos=x0[b])
+    bt.update(10)
+    its, _ = bt.cg_iterations()
+    for b, m in enumerate(meshes):
+        s = lib.Blob(m, solver="CG_nomass", precision="mixed", rng_state=substream_states(b + 1)[b], **kw)
+        s.set_state(pos=x0[b])
+        s.update(10)
+        err = np.abs(bt.pos(b) - s.pos()).max() / np.abs(s.pos() - x0[b]).max()
+        print(f"blob {b}: {m.n_elem} tets, batch vs single error {err:.2e}, iterations {its[b]} / "
+              f"{s.cg_iterations()[0]}")
+        assert err < 1e-5, b
+        assert abs(int(its[b]) - s.cg_iterations()[0]) <= 2, b
+        assert np.array_equal(bt.rng_state(b), s.rng_state()), b
+
+
+@pytest.mark.gpu
+def test_batch_kT0_error_vs_fp64():
+    meshes = [case_mesh(n, s) for n, s in ((4, 1), (6, 12345), (3, 9))]
+    kw = dict(dt=1e-12, kT=0.0, calc_noise=0)
+    bt = lib.Batch(meshes, **kw)
+    x0 = [sheared(m, 0.02) for m in meshes]
+    for b in range(len(meshes)):
+        bt.set_state(b, pos=x0[b])
+    bt.update(200)
+    for b, m in enumerate(meshes):
+        f = lib.Blob(m, solver="CG_nomass", precision="fp64", **kw)
+        f.set_state(pos=x0[b])
+        f.update(200)
+        err = np.abs(bt.pos(b) - f.pos()).max() / np.abs(f.pos() - x0[b]).max()
+        print(f"blob {b}: kT=0 200-step error vs FP64 {err:.2e}")
+        assert err < 1e-5, b
+
+
+@pytest.mark.gpu
+def test_batch_pinned_blob():
+    meshes = [case_mesh(4, 3, [0, 1, 5]), case_mesh(3, 4)]
+    kw = dict(kT=0.0, calc_noise=0)
+    bt = lib.Batch(meshes, **kw)
+    x0 = [sheared(m, 0.02) for m in meshes]
+    for b in range(2):
+        bt.set_state(b, pos=x0[b])
+    bt.update(20)
+    for b, m in enumerate(meshes):
+        f = lib.Blob(m, solver="CG_nomass", precision="fp64", **kw)
+        f.set_state(pos=x0[b])
+        f.update(20)
+        assert np.abs(bt.pos(b) - f.pos()).max() / np.abs(f.pos() - x0[b]).max() < 1e-5, b
+    p = bt.pos(0)
+    assert np.array_equal(p[[0, 1, 5]], x0[0][[0, 1, 5]])
+
+
+@pytest.mark.gpu
+def test_batch_tuner_keeps_state():
+    meshes = [case_mesh(n, s) for n, s in MESHES]
+    bt = lib.Batch(meshes, calc_noise=1)
+    bt.update(2)
+    before = [bt.state(b) for b in range(len(meshes))]
+    rng = [bt.rng_state(b) for b in range(len(meshes))]
+    total = bt.cg_iterations()[1]
+    best = bt.tune(solves=1)
+    cfg = bt.config()
+    assert best > 0 and cfg["cg_threads"] in (128, 256, 512, 1024) and cfg["threads_per_row"] in (1, 2, 4, 8)
+    for b in range(len(meshes)):
+        p, v = bt.state(b)
+        assert np.array_equal(p, before[b][0]) and np.array_equal(v, before[b][1])
+        assert np.array_equal(bt.rng_state(b), rng[b])
+    assert bt.cg_iterations()[1] == total
+    bt.update(2)  # the tuned configuration steps
+    # every configuration gives the same trajectory to rounding
+    ref = lib.Batch(meshes, calc_noise=1)
+    ref.update(4)
+    for b, m in enumerate(meshes):
+        p0 = m.pos * (m.scale / MESO_LENGTH)
+        d = np.abs(bt.pos(b) - ref.pos(b)).max()
+        assert d <= 1e-5 * np.abs(ref.pos(b) - p0).max(), b
