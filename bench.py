@@ -8,6 +8,10 @@ viscosity 1e-3 Pa s; NoMassCGSolver with CG tolerance 1e-10, dt = 1e-12 s,
 kT = 4.11e-21 J (thermal noise on, MRG32k3a stream 12345 x 6). Inputs are
 seeded synthetic meshes; there is no dataset.
 
+A second workload (`--workload batch`, and the "batched" object of the default line) is the
+replica ensemble: 256 Kuhn cubes with cells per side log-uniform in [8, 32] (seeded), per-blob
+G ~ U[1e8, 1e9] Pa and K = 3.9 G, all advanced by one graph-captured step (mixed precision).
+
 Metric: node-steps/s = vertex nodes x steps / time (whole job, all GPUs).
 Default arm: the mixed-precision GPU path (headline), with the plain FP64
 GPU path timed beside it. `--impl reference` times the reference algorithm on
@@ -139,6 +143,18 @@ def profiled_traffic(precision: str):
     return None
 
 
+def profiled_batch_traffic_ratio():
+    """DRAM bytes per model byte of cg_batch_kernel, from the committed ncu summary, if one exists."""
+    path = os.path.join(ROOT, "profiles", "cg_batch_kernel_ensemble64.txt")
+    try:
+        for ln in open(path):
+            if ln.startswith("dram_bytes_per_model_byte"):
+                return float(ln.split("=")[1].split()[0])
+    except (OSError, ValueError, IndexError):
+        pass
+    return None
+
+
 def cg_bytes_per_iteration(n: int, p: int) -> float:
     """Compulsory bytes of one CG iteration by the per-unit model: nnz (p + 4) + (R + 1) 4 + 8 R p."""
     from ffea_ci_demo_gb300.mesh import counts
@@ -236,6 +252,100 @@ def run_gpu_arm(args, ws, rank, local) -> dict | None:
     return out if rank == 0 else None
 
 
+def batch_bytes_per_iteration(cells: int, p: int) -> tuple[float, float]:
+    """Per-unit model bytes and SELL-format bytes of one CG iteration of one n^3-cell blob."""
+    from ffea_ci_demo_gb300.mesh import counts
+
+    c = counts(cells)
+    R = 3 * c["N"]
+    model = c["nnz_linear"] * (p + 4) + (R + 1) * 4 + 8 * R * p
+    fmt = c["nnz_blocks"] * (9 * p + 4) + c["N"] * 8 + 8 * c["N"] * 4 * p
+    return float(model), float(fmt)
+
+
+def run_batch(args, ws) -> dict:
+    """Configuration 2: the replica ensemble, all blobs advanced by one graph-captured step."""
+    from ffea_ci_demo_gb300 import build, lib
+    from ffea_ci_demo_gb300.mesh import ensemble, ensemble_cells
+
+    build.build()
+    cells = [int(n) for n in ensemble_cells(args.blobs)]
+    meshes = ensemble(args.blobs)
+    bt = lib.Batch(meshes, **{k: v for k, v in PHYS.items() if k != "solver"})
+    sz = bt.sizes()
+    bt.update(args.warmup)
+    tuned_ms = None
+    if args.no_tune:
+        bt.set_config(args.cg_threads, args.tpn)
+    else:
+        tuned_ms = bt.tune(1)
+    cfg = bt.config()
+    tot0 = bt.cg_iterations()[1]
+    l0 = lib.launch_count()
+    k = args.steps
+    with Clocks(os.environ.get("CUDA_VISIBLE_DEVICES", "0")) as clk:
+        t = bt.update_timed(k, FLUSH_BYTES)
+    launches = lib.launch_count() - l0
+    last, tot1 = bt.cg_iterations()
+    iters_per_step = (tot1 - tot0) / k
+    # per-blob iterations of the timed steps, estimated from the last step's split of the total
+    scale = iters_per_step / max(1, int(last.sum()))
+    model = fmt = 0.0
+    for n, it in zip(cells, last.tolist()):
+        mb, fb = batch_bytes_per_iteration(n, 4)
+        model += it * scale * mb
+        fmt += it * scale * fb
+    ms = t["ms"] / k
+    peak, peak_kind = measured_peak()
+    out = {"workload": f"ensemble of {args.blobs} Kuhn cubes, cells per side log-uniform in [8,32] (seeded), "
+                       f"G ~ U[1e8,1e9] Pa, K = 3.9 G; NoMassCG eps=1e-10, dt=1e-12 s, kT=4.11e-21 J, mixed",
+           "blobs": sz["blobs"], "nodes": sz["nodes"], "tets": sz["elements"], "matrix_blocks": sz["blocks"],
+           "value": ws * sz["nodes"] * k / (t["ms"] / 1e3), "unit": "node-steps/s", "ms_per_step": ms, "steps": k,
+           "warmup": args.warmup, "cg_iters_per_step_all_blobs": iters_per_step,
+           "cg_iters_per_blob": {"min": int(last.min()), "mean": float(last.mean()), "max": int(last.max())},
+           "launch_config": cfg, "tuned_best_solve_ms": tuned_ms, "gpu_launches": launches,
+           "clocks": clk.summary(),
+           "roofline": {"bound": "hbm", "kernel": "whole step (cg_batch_kernel dominant)",
+                        "achieved": model / (ms / 1e3) / 1e9, "peak": peak, "unit": "GB/s",
+                        "frac": model / (ms / 1e3) / 1e9 / peak, "peak_source": peak_kind,
+                        "traffic": (model * ratio) if (ratio := profiled_batch_traffic_ratio()) else None,
+                        "traffic_note": "DRAM bytes per step scaled from the 64-blob ncu capture by model bytes",
+                        "bytes_per_step_model_cg": model, "bytes_per_step_format_cg": fmt,
+                        "achieved_format": fmt / (ms / 1e3) / 1e9}}
+    if not args.no_fp64_sample:
+        # plain FP64 GPU path, one blob at a time (the reference's order): a stratified sample of the
+        # blobs sorted by size, scaled to the whole ensemble
+        order = sorted(range(args.blobs), key=lambda b: cells[b])
+        pick = order[len(order) // 16::len(order) // 8][:8] if len(order) >= 8 else order
+        tsum = 0.0
+        for b in pick:
+            f = lib.Blob(meshes[b], precision="fp64", **PHYS)
+            f.update(1)
+            tsum += f.update_timed(2, FLUSH_BYTES)["ms"] / 2
+            f.close()
+        est = tsum * len(order) / len(pick)
+        out["fp64_path_sampled"] = {"value": sz["nodes"] / (est / 1e3), "ms_per_step_est": est,
+                                    "sample_blobs": len(pick), "method": "FP64 single-blob path, blob by blob, "
+                                    "stratified sample scaled to all blobs"}
+        out["speedup_vs_fp64_path"] = out["value"] / out["fp64_path_sampled"]["value"]
+    if not args.no_e2e:
+        # end to end through the C ABI: every blob's host positions in, one step, every blob's positions out
+        pos = [bt.pos(b) for b in range(args.blobs)]
+        ke = max(2, k // 4)
+        t0 = time.perf_counter()
+        for _ in range(ke):
+            for b in range(args.blobs):
+                bt.set_state(b, pos=pos[b])
+            bt.update(1)
+            pos = [bt.pos(b) for b in range(args.blobs)]
+        e2e_s = time.perf_counter() - t0
+        nb = 24 * sum(m.n_nodes for m in meshes)
+        out["e2e"] = {"value": ws * sz["nodes"] * ke / e2e_s, "unit": "node-steps/s", "h2d_bytes_per_step": nb,
+                      "d2h_bytes_per_step": nb, "steps": ke}
+    bt.close()
+    return out
+
+
 def cpu_sample(n: int, threads: int, budget_s: float, max_steps: int, warmup: int = 1):
     """Time the oracle (reference algorithm, release optimisation, OpenMP) on the same workload."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
@@ -273,6 +383,15 @@ def main():
     ap.add_argument("--cells", type=int, default=N_CELLS)
     ap.add_argument("--error-steps", type=int, default=100)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", choices=["both", "single", "batch"], default="both",
+                    help="single: the 40^3 blob (headline); batch: the replica ensemble; both: both in one line")
+    ap.add_argument("--blobs", type=int, default=256)
+    ap.add_argument("--batch-steps", type=int, default=10)
+    ap.add_argument("--no-tune", action="store_true", help="batch: fixed launch configuration (--cg-threads, --tpn)")
+    ap.add_argument("--cg-threads", type=int, default=128)
+    ap.add_argument("--tpn", type=int, default=1)
+    ap.add_argument("--no-fp64-sample", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
     args.headline = "fp64" if args.precision == "fp64" else "mixed"
@@ -297,6 +416,23 @@ def main():
         return
 
     pick_device(local)
+    if args.workload == "batch":
+        if ws > 1:
+            if rank == 0:
+                print(json.dumps({"metric": "node-steps/s", "unavailable": "the batch workload runs on one GPU"}))
+            return
+        b = run_batch(args, ws)
+        line = {"metric": "node-steps/s", "value": b["value"], "unit": "node-steps/s", "n_gpus": ws,
+                "steps": b["steps"], "warmup": args.warmup, "ms_per_step": b["ms_per_step"],
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
+                "data": "synthetic (seeded Kuhn-cube ensemble)",
+                "config": {"workload": b["workload"], "blobs": b["blobs"], "nodes": b["nodes"], "tets": b["tets"],
+                           "l2": "flushed before every timed step (256 MiB scratch write)",
+                           "parallelism": "replicas x1"},
+                "clocks": b["clocks"], "e2e": b.get("e2e"), "gpu_launches": b["gpu_launches"],
+                "roofline": b["roofline"], "batched": b}
+        print(json.dumps(line), flush=True)
+        return
     res = run_gpu_arm(args, ws, rank, local)
     if rank != 0:
         return
@@ -329,6 +465,11 @@ def main():
         line["speedup_vs_fp64_path"] = head["value"] / f["value"]
     if "error" in res:
         line["error"] = res["error"]
+    if args.workload == "both" and ws == 1:
+        k = args.steps
+        args.steps = args.batch_steps
+        line["batched"] = run_batch(args, ws)
+        args.steps = k
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_sample(args.cells, os.cpu_count() or 1, budget_s=20.0, max_steps=3)
         line["cpu_baseline"].pop("seconds")
