@@ -144,8 +144,15 @@ __global__ void __launch_bounds__(SOLVE_PREP_THREADS)
 // ---------------------------------------------------------------------------
 // the blob
 // ---------------------------------------------------------------------------
+struct ffea_gpu_adjoint {
+    ffea_gpu_blob *blob;  // null once the blob is destroyed
+};
+
 struct ffea_gpu_blob {
-    virtual ~ffea_gpu_blob() = default;
+    ffea_gpu_adjoint *adj_handle = nullptr;  // the adjoint reserved on this blob, if any
+    virtual ~ffea_gpu_blob() {
+        if (adj_handle) adj_handle->blob = nullptr;
+    }
     HostModel h;
     ffea_gpu_params p{};
     uint32_t rng_host[6] = {12345, 12345, 12345, 12345, 12345, 12345};
@@ -164,6 +171,11 @@ struct ffea_gpu_blob {
     virtual int cg_profile(double *ns, int n) = 0;
     virtual int get_matrix_values(std::vector<double> &val_sell) = 0;
     virtual int solve_static(const double *rhs, double *x, int *iterations) = 0;
+    virtual int adj_init(int window, int every) = 0;
+    virtual int adj_forward(int *done) = 0;
+    virtual int adj_backward(const double *dl_dx, double *dG, double *dE, double *dA, double *dB,
+                             double *dl_dx0) = 0;
+    virtual void adj_release() = 0;
 };
 
 namespace {
@@ -201,6 +213,14 @@ struct BlobImpl final : ffea_gpu_blob {
     cudaEvent_t ev[FFEA_GPU_NUM_PHASES + 1] = {};
     bool record_phases = false;
     double *staging = nullptr;  // pinned host buffer, 3*N doubles, for state copies
+    // adjoint window (ffea_gpu_adjoint_*): checkpoints every `adj_every` steps, one segment recomputed
+    std::unique_ptr<Arena> adj_mem;
+    int adj_window = 0, adj_every = 0, adj_done = -1;
+    double *ck_pos = nullptr, *ck_det = nullptr, *seg_pos = nullptr, *lam = nullptr, *eg = nullptr,
+           *gtheta = nullptr, *coef = nullptr, *adj_part_d = nullptr, *fin_pos = nullptr, *fin_det = nullptr;
+    uint32_t *ck_rng = nullptr, *seg_rng = nullptr, *fin_rng = nullptr;
+    R *seg_v = nullptr;
+    float2 *adj_part_f = nullptr;
 
     ~BlobImpl() override {
         if (staging) cudaFreeHost(staging);
@@ -297,8 +317,9 @@ struct BlobImpl final : ffea_gpu_blob {
         if (mixed) {
             CK(mem.alloc(&diag, 4 * (size_t)N));
             CK(mem.alloc(&dpos, (size_t)N));
-            nmodes = rigid_modes(h, p, xc, modes);
         }
+        // rigid modes: the mixed CG deflates them; both paths' adjoints project them out
+        nmodes = rigid_modes(h, p, xc, modes);
         const int maxg = Launch<R>::cg_max_grid(device);
         if (maxg <= 0) {
             g_last_error = "cg kernel cannot be made resident";
@@ -340,11 +361,10 @@ struct BlobImpl final : ffea_gpu_blob {
         return FFEA_GPU_OK;
     }
 
-    int launch_step() {
-        const bool nomass = p.solver == FFEA_GPU_NOMASS_CG;
+    ElemArgs<R> elem_args(int recompute) {
         ElemArgs<R> ea{};
         ea.T = h.T;
-        ea.nomass = nomass;
+        ea.nomass = p.solver == FFEA_GPU_NOMASS_CG;
         ea.calc_noise = p.calc_noise;
         ea.kT = (R)p.kT;
         ea.dt = (R)p.dt;
@@ -359,21 +379,54 @@ struct BlobImpl final : ffea_gpu_blob {
         ea.rng_state = rng_state;
         ea.chunk_jump = chunk_jump;
         ea.lane_jump = lane_jump;
+        ea.recompute = recompute;
         ea.st = st;
+        return ea;
+    }
+
+    int launch_assemble() {
+        AsmArgs<R> aa{};
+        aa.N = h.N;
+        aa.slice_ptr = slice_ptr; aa.rowlen = rowlen; aa.bcol = bcol; aa.diagk = diagk;
+        aa.src_ptr = src_ptr; aa.src = src;
+        aa.geom = geom; aa.A = A; aa.B = B;
+        aa.drag = (p.calc_stokes == 1) ? drag : nullptr;
+        aa.val = val; aa.dinv = dinv; aa.diag = diag; aa.st = st;
+        CK(Launch<R>::assemble(aa, stream));
+        return FFEA_GPU_OK;
+    }
+
+    // the CG of a step, opened by the gather's (or the adjoint gather's) block sums in `init`
+    int launch_cg(const double *init, int n_init) {
+        const bool nomass = p.solver == FFEA_GPU_NOMASS_CG;
+        CgArgs<R> ca{};
+        ca.N = h.N;
+        ca.block3 = nomass;
+        ca.check_last = nomass;
+        ca.slice_ptr = slice_ptr; ca.rowlen = rowlen; ca.bcol = bcol;
+        ca.val = val; ca.dinv = dinv;
+        ca.x = x; ca.r = r; ca.q = q; ca.pbuf0 = pbuf0; ca.pbuf1 = pbuf1; ca.diag = diag;
+        ca.init_partials = init; ca.n_init = n_init; ca.init_stride = gather_blocks;
+        ca.partials = partials; ca.stride = partial_stride;
+        ca.gb = gb; ca.st = st;
+        ca.imax = p.max_iterations_cg;
+        ca.eps2 = p.epsilon2;
+        ca.limit_ns = 2000000000ull;
+        ca.history = history; ca.hist_cap = hist_cap; ca.tpn = tpn; ca.phase_ns = phase_ns;
+        CK(cudaMemsetAsync(phase_ns, 0, FFEA_GPU_CG_PHASES * sizeof(unsigned long long), stream));
+        ca.dpos = dpos; ca.nmodes = nomass ? nmodes : 0;
+        for (int i = 0; i < 36; ++i) ca.modes[i] = modes[i];
+        CK(Launch<R>::cg(ca, cg_grid, stream));
+        return FFEA_GPU_OK;
+    }
+
+    int launch_step() {
+        const bool nomass = p.solver == FFEA_GPU_NOMASS_CG;
         int rc = mark(0);
         if (rc) return rc;
-        CK(Launch<R>::element(ea, stream));
+        CK(Launch<R>::element(elem_args(0), stream));
         if ((rc = mark(1))) return rc;
-        if (nomass) {
-            AsmArgs<R> aa{};
-            aa.N = h.N;
-            aa.slice_ptr = slice_ptr; aa.rowlen = rowlen; aa.bcol = bcol; aa.diagk = diagk;
-            aa.src_ptr = src_ptr; aa.src = src;
-            aa.geom = geom; aa.A = A; aa.B = B;
-            aa.drag = (p.calc_stokes == 1) ? drag : nullptr;
-            aa.val = val; aa.dinv = dinv; aa.diag = diag; aa.st = st;
-            CK(Launch<R>::assemble(aa, stream));
-        }
+        if (nomass && (rc = launch_assemble())) return rc;
         if ((rc = mark(2))) return rc;
         GatherArgs<R> ga{};
         ga.N = h.N;
@@ -387,26 +440,7 @@ struct BlobImpl final : ffea_gpu_blob {
         ga.xc[0] = xc[0]; ga.xc[1] = xc[1]; ga.xc[2] = xc[2];
         CK(Launch<R>::gather(ga, gather_blocks, stream));
         if ((rc = mark(3))) return rc;
-        if (p.solver != FFEA_GPU_MASSLUMPED) {
-            CgArgs<R> ca{};
-            ca.N = h.N;
-            ca.block3 = nomass;
-            ca.check_last = nomass;
-            ca.slice_ptr = slice_ptr; ca.rowlen = rowlen; ca.bcol = bcol;
-            ca.val = val; ca.dinv = dinv;
-            ca.x = x; ca.r = r; ca.q = q; ca.pbuf0 = pbuf0; ca.pbuf1 = pbuf1; ca.diag = diag;
-            ca.init_partials = init_partials; ca.n_init = gather_blocks; ca.init_stride = gather_blocks;
-            ca.partials = partials; ca.stride = partial_stride;
-            ca.gb = gb; ca.st = st;
-            ca.imax = p.max_iterations_cg;
-            ca.eps2 = p.epsilon2;
-            ca.limit_ns = 2000000000ull;
-            ca.history = history; ca.hist_cap = hist_cap; ca.tpn = tpn; ca.phase_ns = phase_ns;
-            CK(cudaMemsetAsync(phase_ns, 0, FFEA_GPU_CG_PHASES * sizeof(unsigned long long), stream));
-            ca.dpos = dpos; ca.nmodes = nomass ? nmodes : 0;
-            for (int i = 0; i < 36; ++i) ca.modes[i] = modes[i];
-            CK(Launch<R>::cg(ca, cg_grid, stream));
-        }
+        if (p.solver != FFEA_GPU_MASSLUMPED && (rc = launch_cg(init_partials, gather_blocks))) return rc;
         if ((rc = mark(4))) return rc;
         EulerArgs<R> eu{};
         eu.N = h.N; eu.nomass = nomass; eu.dt = p.dt; eu.x = x;
@@ -546,7 +580,7 @@ struct BlobImpl final : ffea_gpu_blob {
         int rc;
         if (pos && (rc = put(pos, px, py, pz))) return rc;
         if (vel && (rc = put(vel, vx, vy, vz))) return rc;
-        if (pos && std::is_same<R, float>::value) {
+        if (pos) {
             // the rigid modes must vanish at the pinned nodes' current positions
             for (int k = 0; k < N; ++k)
                 for (int c = 0; c < 3; ++c) h.pos[3 * (size_t)k + c] = pos[3 * (size_t)h.node_of[k] + c];
@@ -706,6 +740,252 @@ struct BlobImpl final : ffea_gpu_blob {
                 for (int c = 0; c < 3; ++c) xout[3 * (size_t)h.node_of[k] + c] = staging[3 * (size_t)k + c];
             return FFEA_GPU_OK;
         }
+    }
+
+    // ---- adjoint window ---------------------------------------------------------------------
+    int adj_init(int window, int every) override {
+        if (p.solver != FFEA_GPU_NOMASS_CG) {
+            g_last_error = "the adjoint covers the CG_nomass solver";
+            return FFEA_GPU_EINPUT;
+        }
+        if (window <= 0 || every <= 0) {
+            g_last_error = "adjoint window and checkpoint interval must be positive";
+            return FFEA_GPU_EINPUT;
+        }
+        adj_release();
+        adj_mem.reset(new Arena());
+        const int N = h.N, T = h.T, nck = (window + every - 1) / every, seg = std::min(every, window);
+        Arena &m = *adj_mem;
+        CK(m.alloc(&ck_pos, 3 * (size_t)N * nck));
+        CK(m.alloc(&ck_det, (size_t)T * nck));
+        CK(m.alloc(&ck_rng, 6 * (size_t)nck));
+        CK(m.alloc(&seg_pos, 3 * (size_t)N * seg));
+        CK(m.alloc(&seg_v, 4 * (size_t)N * seg));
+        CK(m.alloc(&seg_rng, 6 * (size_t)seg));
+        CK(m.alloc(&lam, 4 * (size_t)N));
+        CK(m.alloc(&eg, 12 * (size_t)T));
+        CK(m.alloc(&gtheta, 4 * (size_t)T));
+        CK(m.alloc(&coef, 6));
+        CK(m.alloc(&adj_part_d, (size_t)ADJ_MOMENTS * gather_blocks));
+        CK(m.alloc(&adj_part_f, (size_t)ADJ_MOMENTS * gather_blocks));
+        CK(m.alloc(&fin_pos, 3 * (size_t)N));
+        CK(m.alloc(&fin_det, (size_t)T));
+        CK(m.alloc(&fin_rng, 6));
+        adj_window = window;
+        adj_every = every;
+        adj_done = -1;
+        return FFEA_GPU_OK;
+    }
+
+    void adj_release() override {
+        adj_mem.reset();
+        adj_window = adj_every = 0;
+        adj_done = -1;
+    }
+
+    // device copies of the state a step depends on: positions (SoA), stream state, last determinants
+    int save_state(double *pos3, uint32_t *rng, double *det) {
+        const size_t N = h.N;
+        CK(cudaMemcpyAsync(pos3, px, N * sizeof(double), cudaMemcpyDeviceToDevice, stream));
+        CK(cudaMemcpyAsync(pos3 + N, py, N * sizeof(double), cudaMemcpyDeviceToDevice, stream));
+        CK(cudaMemcpyAsync(pos3 + 2 * N, pz, N * sizeof(double), cudaMemcpyDeviceToDevice, stream));
+        if (rng) CK(cudaMemcpyAsync(rng, rng_state, 6 * sizeof(uint32_t), cudaMemcpyDeviceToDevice, stream));
+        if (det) CK(cudaMemcpyAsync(det, last_det, h.T * sizeof(double), cudaMemcpyDeviceToDevice, stream));
+        return FFEA_GPU_OK;
+    }
+
+    int load_state(const double *pos3, const uint32_t *rng, const double *det) {
+        const size_t N = h.N;
+        CK(cudaMemcpyAsync(px, pos3, N * sizeof(double), cudaMemcpyDeviceToDevice, stream));
+        CK(cudaMemcpyAsync(py, pos3 + N, N * sizeof(double), cudaMemcpyDeviceToDevice, stream));
+        CK(cudaMemcpyAsync(pz, pos3 + 2 * N, N * sizeof(double), cudaMemcpyDeviceToDevice, stream));
+        if (rng) CK(cudaMemcpyAsync(rng_state, rng, 6 * sizeof(uint32_t), cudaMemcpyDeviceToDevice, stream));
+        if (det) CK(cudaMemcpyAsync(last_det, det, h.T * sizeof(double), cudaMemcpyDeviceToDevice, stream));
+        return FFEA_GPU_OK;
+    }
+
+    int clear_flags() {
+        DevStatus s{};
+        int rc = read_status(s);
+        if (rc) return rc;
+        s.inversions = s.cg_fail = s.nonfinite = s.timeout = s.abort = 0;
+        s.steps_done = 0;
+        CK(cudaMemcpyAsync(st, &s, sizeof(DevStatus), cudaMemcpyHostToDevice, stream));
+        return FFEA_GPU_OK;
+    }
+
+    // the window's forward pass: `adj_window` steps from the current state, a checkpoint every
+    // `adj_every` steps (positions, stream state, last determinants before the step)
+    int adj_forward(int *done) override {
+        if (!adj_mem) return FFEA_GPU_EINPUT;
+        int rc = clear_flags();
+        if (rc) return rc;
+        const size_t N = h.N;
+        for (int n = 0; n < adj_window; ++n) {
+            if (n % adj_every == 0) {
+                const int c = n / adj_every;
+                if ((rc = save_state(ck_pos + 3 * N * c, ck_rng + 6 * c, ck_det + (size_t)h.T * c))) return rc;
+            }
+            if ((rc = launch_step())) return rc;
+        }
+        DevStatus s{};
+        if ((rc = read_status(s))) return rc;
+        if (done) *done = s.steps_done;
+        adj_done = s.steps_done;
+        return status_code(s);
+    }
+
+    // one backward step at stored positions and stream state: lambda <- lambda + d(dt v)/dx^T lambda,
+    // gtheta += d(dt v)/dtheta^T lambda
+    int adj_step(const R *v_step) {
+        constexpr bool mixed = std::is_same<R, float>::value;
+        CK(Launch<R>::element(elem_args(1), stream));
+        int rc = launch_assemble();
+        if (rc) return rc;
+        AdjGatherArgs<R> ag{};
+        ag.N = h.N;
+        ag.dt = p.dt;
+        ag.lam = lam;
+        ag.pinned = pinned;
+        ag.px = px; ag.py = py; ag.pz = pz;
+        for (int c = 0; c < 3; ++c) ag.xc[c] = xc[c];
+        ag.dinv = dinv;
+        ag.diag = mixed ? diag : nullptr;
+        ag.f = f; ag.r = r; ag.x = x;
+        ag.dpos = mixed ? dpos : nullptr;
+        ag.partials_d = mixed ? nullptr : adj_part_d;
+        ag.partials_f = mixed ? adj_part_f : nullptr;
+        ag.stride = gather_blocks;
+        ag.gb = gb;
+        ag.st = st;
+        CK(AdjLaunch<R>::gather(ag, gather_blocks, stream));
+        AdjModesArgs am{};
+        am.partials_d = mixed ? nullptr : adj_part_d;
+        am.partials_f = mixed ? adj_part_f : nullptr;
+        am.stride = gather_blocks;
+        am.nb = gather_blocks;
+        am.nmodes = nmodes;
+        for (int i = 0; i < 36; ++i) am.modes[i] = modes[i];
+        am.coef = coef;
+        CK(AdjLaunch<R>::modes(am, stream));
+        if (mixed) {
+            // cg_mixed_kernel projects the right-hand side itself from the moments
+            if ((rc = launch_cg(reinterpret_cast<const double *>(adj_part_f), gather_blocks))) return rc;
+        } else {
+            AdjApplyArgs<R> aa{};
+            aa.N = h.N;
+            aa.px = px; aa.py = py; aa.pz = pz;
+            for (int c = 0; c < 3; ++c) aa.xc[c] = xc[c];
+            aa.coef = coef;
+            aa.dinv = dinv;
+            aa.r = r;
+            aa.f = f;
+            aa.partials = init_partials;
+            aa.stride = gather_blocks;
+            aa.st = st;
+            CK(AdjLaunch<R>::apply(aa, gather_blocks, stream));
+            if ((rc = launch_cg(init_partials, gather_blocks))) return rc;
+        }
+        AdjElemArgs<R> ae{};
+        ae.T = h.T;
+        ae.calc_noise = p.calc_noise;
+        ae.kT = p.kT;
+        ae.dt = p.dt;
+        ae.tet = tet;
+        ae.px = px; ae.py = py; ae.pz = pz;
+        ae.jinv = jinv; ae.G = G; ae.E = E; ae.A = A; ae.B = B; ae.vol0 = vol0;
+        ae.rng_state = rng_state; ae.chunk_jump = chunk_jump; ae.lane_jump = lane_jump;
+        ae.mu = x;
+        ae.v = v_step;
+        ae.nmodes = nmodes;
+        for (int c = 0; c < 3; ++c) ae.xc[c] = xc[c];
+        ae.coef = coef;
+        ae.eg = eg;
+        ae.gtheta = gtheta;
+        ae.st = st;
+        CK(AdjLaunch<R>::elem(ae, stream));
+        AdjNodeArgs<R> an{};
+        an.N = h.N;
+        an.inc_ptr = inc_ptr; an.inc = inc;
+        an.eg = eg;
+        an.v = v_step;
+        an.dinv = dinv;
+        an.diag = mixed ? diag : nullptr;
+        an.nmodes = nmodes;
+        an.coef = coef;
+        an.lam = lam;
+        an.st = st;
+        CK(AdjLaunch<R>::node(an, stream));
+        return FFEA_GPU_OK;
+    }
+
+    int adj_backward(const double *dl_dx, double *dG, double *dE, double *dA, double *dB,
+                     double *dl_dx0) override {
+        if (!adj_mem || adj_done != adj_window) {
+            g_last_error = "run the adjoint window's forward pass first";
+            return FFEA_GPU_EINPUT;
+        }
+        const int N = h.N, T = h.T;
+        // dL/dx_final on vertex rows: a midpoint's share goes half to each edge end
+        std::vector<double> l4(4 * (size_t)N, 0.0);
+        for (int k = 0; k < N; ++k)
+            for (int c = 0; c < 3; ++c) l4[4 * (size_t)k + c] = dl_dx[3 * (size_t)h.node_of[k] + c];
+        for (size_t m = 0; m < h.mid_nodes.size(); ++m)
+            for (int c = 0; c < 3; ++c) {
+                const double gm = 0.5 * dl_dx[3 * (size_t)h.mid_nodes[m] + c];
+                l4[4 * (size_t)h.mid_a[m] + c] += gm;
+                l4[4 * (size_t)h.mid_b[m] + c] += gm;
+            }
+        CK(cudaMemcpyAsync(lam, l4.data(), l4.size() * sizeof(double), cudaMemcpyHostToDevice, stream));
+        CK(cudaMemsetAsync(gtheta, 0, 4 * (size_t)T * sizeof(double), stream));
+        DevStatus s0{};
+        int rc = read_status(s0);
+        if (rc) return rc;
+        if ((rc = save_state(fin_pos, fin_rng, fin_det))) return rc;
+        if ((rc = clear_flags())) return rc;
+        const size_t N3 = 3 * (size_t)N, N4 = 4 * (size_t)N;
+        const int nseg = (adj_window + adj_every - 1) / adj_every;
+        for (int sg = nseg - 1; sg >= 0 && !rc; --sg) {
+            const int c0 = sg * adj_every, len = std::min(adj_every, adj_window - c0);
+            if ((rc = load_state(ck_pos + N3 * sg, ck_rng + 6 * sg, ck_det + (size_t)T * sg))) break;
+            for (int j = 0; j < len && !rc; ++j) {  // recompute the segment, keeping x_n, v_n, stream states
+                if ((rc = save_state(seg_pos + N3 * j, seg_rng + 6 * j, nullptr))) break;
+                if ((rc = launch_step())) break;
+                cudaError_t e = cudaMemcpyAsync(seg_v + N4 * j, x, N4 * sizeof(R), cudaMemcpyDeviceToDevice, stream);
+                if (e != cudaSuccess) rc = cuda_fail(e, "segment velocity copy");
+            }
+            for (int j = len - 1; j >= 0 && !rc; --j) {
+                if ((rc = load_state(seg_pos + N3 * j, seg_rng + 6 * j, nullptr))) break;
+                rc = adj_step(seg_v + N4 * j);
+            }
+        }
+        DevStatus s{};
+        if (!rc) rc = read_status(s);
+        if (!rc) rc = status_code(s);
+        if (!rc) {
+            std::vector<double> gt(4 * (size_t)T);
+            CK(cudaMemcpyAsync(gt.data(), gtheta, gt.size() * sizeof(double), cudaMemcpyDeviceToHost, stream));
+            CK(cudaMemcpyAsync(l4.data(), lam, l4.size() * sizeof(double), cudaMemcpyDeviceToHost, stream));
+            CK(cudaStreamSynchronize(stream));
+            for (int e = 0; e < T; ++e) {
+                if (dG) dG[e] = gt[4 * (size_t)e];
+                if (dE) dE[e] = gt[4 * (size_t)e + 1];
+                if (dA) dA[e] = gt[4 * (size_t)e + 2];
+                if (dB) dB[e] = gt[4 * (size_t)e + 3];
+            }
+            if (dl_dx0) {
+                for (int i = 0; i < 3 * h.n_all; ++i) dl_dx0[i] = 0.0;
+                for (int k = 0; k < N; ++k)
+                    for (int c = 0; c < 3; ++c) dl_dx0[3 * (size_t)h.node_of[k] + c] = l4[4 * (size_t)k + c];
+            }
+        }
+        // the blob continues from the end of the window
+        int rc2 = load_state(fin_pos, fin_rng, fin_det);
+        if (!rc2) {
+            CK(cudaMemcpyAsync(st, &s0, sizeof(DevStatus), cudaMemcpyHostToDevice, stream));
+            CK(cudaStreamSynchronize(stream));
+        }
+        return rc ? rc : rc2;
     }
 
     // Blob::make_measurements energies (src/Blob.cpp:1066-1125), evaluated on the host from device state
@@ -982,6 +1262,44 @@ int ffea_gpu_blob_get_rhs(ffea_gpu_blob *b, double *rhs) {
 int ffea_gpu_blob_solve_static(ffea_gpu_blob *b, const double *rhs, double *x, int *iterations) {
     if (!b || !rhs || !x) return FFEA_GPU_EINPUT;
     return b->solve_static(rhs, x, iterations);
+}
+
+int ffea_gpu_adjoint_create(ffea_gpu_blob *b, int window_steps, int checkpoint_every, ffea_gpu_adjoint **out) {
+    if (!b || !out) return FFEA_GPU_EINPUT;
+    *out = nullptr;
+    if (b->adj_handle) {
+        g_last_error = "this blob already has an adjoint";
+        return FFEA_GPU_EINPUT;
+    }
+    int rc = b->adj_init(window_steps, checkpoint_every);
+    if (rc) return rc;
+    *out = new (std::nothrow) ffea_gpu_adjoint{b};
+    if (!*out) {
+        b->adj_release();
+        return FFEA_GPU_ENOMEM;
+    }
+    b->adj_handle = *out;
+    return FFEA_GPU_OK;
+}
+
+int ffea_gpu_adjoint_forward(ffea_gpu_adjoint *a, int *steps_done) {
+    if (!a || !a->blob) return FFEA_GPU_EINPUT;
+    return a->blob->adj_forward(steps_done);
+}
+
+int ffea_gpu_adjoint_backward(ffea_gpu_adjoint *a, const double *dl_dx_final, double *dl_dG, double *dl_dE,
+                              double *dl_dA, double *dl_dB, double *dl_dx_initial) {
+    if (!a || !a->blob || !dl_dx_final) return FFEA_GPU_EINPUT;
+    return a->blob->adj_backward(dl_dx_final, dl_dG, dl_dE, dl_dA, dl_dB, dl_dx_initial);
+}
+
+void ffea_gpu_adjoint_destroy(ffea_gpu_adjoint *a) {
+    if (!a) return;
+    if (a->blob) {
+        a->blob->adj_release();
+        a->blob->adj_handle = nullptr;
+    }
+    delete a;
 }
 
 const char *ffea_gpu_last_error(void) { return g_last_error.c_str(); }

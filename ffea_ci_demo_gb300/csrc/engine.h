@@ -7,6 +7,7 @@
 #pragma once
 
 #include "batch_types.cuh"
+#include "kernels_adjoint.cuh"
 
 namespace ffea {
 
@@ -23,8 +24,20 @@ struct Launch {
     static cudaError_t euler(const EulerArgs<R> &a, cudaStream_t s);
 };
 
+// launchers of the adjoint kernels (kernels_adjoint.cuh)
+template <class R>
+struct AdjLaunch {
+    static cudaError_t gather(const AdjGatherArgs<R> &a, int blocks, cudaStream_t s);
+    static cudaError_t modes(const AdjModesArgs &a, cudaStream_t s);
+    static cudaError_t apply(const AdjApplyArgs<R> &a, int blocks, cudaStream_t s);
+    static cudaError_t elem(const AdjElemArgs<R> &a, cudaStream_t s);
+    static cudaError_t node(const AdjNodeArgs<R> &a, cudaStream_t s);
+};
+
 extern template struct Launch<double>;
 extern template struct Launch<float>;
+extern template struct AdjLaunch<double>;
+extern template struct AdjLaunch<float>;
 
 cudaError_t launch_finish_step(uint32_t *rng_state, const MrgJump *step_jump, DevStatus *st, cudaStream_t s);
 

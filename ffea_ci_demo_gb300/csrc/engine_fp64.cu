@@ -8,6 +8,7 @@
 namespace ffea {
 
 template struct Launch<double>;
+template struct AdjLaunch<double>;
 
 __global__ void finish_step_kernel(uint32_t *rng_state, const MrgJump *step_jump, DevStatus *st) {
     if (threadIdx.x != 0 || blockIdx.x != 0 || st->abort) return;

@@ -77,4 +77,40 @@ cudaError_t Launch<R>::euler(const EulerArgs<R> &a, cudaStream_t s) {
     return cudaGetLastError();
 }
 
+template <class R>
+cudaError_t AdjLaunch<R>::gather(const AdjGatherArgs<R> &a, int blocks, cudaStream_t s) {
+    adj_gather_kernel<R><<<blocks, 256, 0, s>>>(a);
+    count_launch();
+    return cudaGetLastError();
+}
+
+template <class R>
+cudaError_t AdjLaunch<R>::modes(const AdjModesArgs &a, cudaStream_t s) {
+    adj_modes_kernel<R><<<1, 256, 0, s>>>(a);
+    count_launch();
+    return cudaGetLastError();
+}
+
+template <class R>
+cudaError_t AdjLaunch<R>::apply(const AdjApplyArgs<R> &a, int blocks, cudaStream_t s) {
+    adj_apply_kernel<R><<<blocks, 256, 0, s>>>(a);
+    count_launch();
+    return cudaGetLastError();
+}
+
+template <class R>
+cudaError_t AdjLaunch<R>::elem(const AdjElemArgs<R> &a, cudaStream_t s) {
+    if (a.T <= 0) return cudaSuccess;
+    elem_vjp_kernel<R><<<(a.T + 127) / 128, 128, 0, s>>>(a);
+    count_launch();
+    return cudaGetLastError();
+}
+
+template <class R>
+cudaError_t AdjLaunch<R>::node(const AdjNodeArgs<R> &a, cudaStream_t s) {
+    node_vjp_kernel<R><<<(a.N + 255) / 256, 256, 0, s>>>(a);
+    count_launch();
+    return cudaGetLastError();
+}
+
 }  // namespace ffea

@@ -7,6 +7,7 @@
 namespace ffea {
 
 template struct Launch<float>;
+template struct AdjLaunch<float>;
 
 cudaError_t BatchLaunch::schedule(BlobCgDesc *desc, const int *blob_iters, int nblobs, int ncta, int *cta_blob,
                                   const DevStatus *st, cudaStream_t s) {

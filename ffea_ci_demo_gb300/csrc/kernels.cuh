@@ -46,6 +46,7 @@ struct ElemArgs {
     const int *elem_off;           // batch: first element of each blob
     const MrgJump *chunk_jump;     // ceil(T/32): A^(7*32*c)
     const MrgJump *lane_jump;      // 32: A^(7*l)
+    int recompute;                 // 1: re-evaluation at stored positions (no inversion test, last_det kept)
     DevStatus *st;
 };
 
@@ -87,7 +88,7 @@ __global__ void __launch_bounds__(128) element_kernel(ElemArgs<R> g) {
     d[10] = J[2][0] * J[0][1] - J[2][1] * J[0][0];
     d[11] = J[1][1] * J[0][0] - J[1][0] * J[0][1];
     double det = J[0][0] * d[1] + J[1][0] * d[2] + J[2][0] * d[3];
-    const double last = g.last_det[e];
+    const double last = g.recompute ? det : g.last_det[e];
     double vold;
     if (last * det < 0) {
         // inverted: the reference returns before updating vol and dividing dpsi; the step is void
@@ -95,7 +96,7 @@ __global__ void __launch_bounds__(128) element_kernel(ElemArgs<R> g) {
         atomicExch(&g.st->abort, 1);
         return;
     }
-    g.last_det[e] = det;
+    if (!g.recompute) g.last_det[e] = det;
     vold = (1.0 / 6.0) * fabs(det);
     det = 1.0 / det;
     d[1] *= det; d[2] *= det; d[3] *= det;

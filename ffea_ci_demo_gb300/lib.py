@@ -96,6 +96,10 @@ def load():
         "ffea_gpu_blob_get_elements": (C.c_int, [vp, dp, dp, dp]),
         "ffea_gpu_blob_get_rhs": (C.c_int, [vp, dp]),
         "ffea_gpu_blob_solve_static": (C.c_int, [vp, dp, dp, ip]),
+        "ffea_gpu_adjoint_create": (C.c_int, [vp, C.c_int, C.c_int, C.POINTER(vp)]),
+        "ffea_gpu_adjoint_forward": (C.c_int, [vp, ip]),
+        "ffea_gpu_adjoint_backward": (C.c_int, [vp, dp, dp, dp, dp, dp, dp]),
+        "ffea_gpu_adjoint_destroy": (None, [vp]),
         "ffea_gpu_batch_create": (C.c_int, [vp, C.c_int, C.POINTER(Params), C.POINTER(vp)]),
         "ffea_gpu_batch_destroy": (None, [vp]),
         "ffea_gpu_batch_sizes": (C.c_int, [vp, ip, ip, ip, C.POINTER(C.c_longlong)]),
@@ -330,6 +334,52 @@ class Blob:
         o = np.empty((self.n_nodes, 3))
         _check(self._lib.ffea_gpu_blob_get_rhs(self._h, _p(o)), "get_rhs")
         return o
+
+
+class Adjoint:
+    """Reverse-mode derivative of a window of CG_nomass steps of a ``Blob``.
+
+    ``forward()`` runs the window (checkpointing every ``checkpoint_every`` steps); ``backward(dl_dx)``
+    takes dL/d(final positions) and returns dL/d(G, E, A, B) per element (meso units) and
+    dL/d(initial positions)."""
+
+    def __init__(self, blob: "Blob", window_steps: int, checkpoint_every: int):
+        self._lib = load()
+        self.blob = blob  # the blob stays alive while its adjoint is
+        self._h = C.c_void_p()
+        _check(self._lib.ffea_gpu_adjoint_create(blob._h, int(window_steps), int(checkpoint_every),
+                                                 C.byref(self._h)), "adjoint_create")
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) and self._h.value:
+            self._lib.ffea_gpu_adjoint_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        self.close()
+
+    def forward(self) -> int:
+        done = C.c_int(0)
+        _check(self._lib.ffea_gpu_adjoint_forward(self._h, C.byref(done)), "adjoint_forward")
+        return done.value
+
+    def backward(self, dl_dx_final: np.ndarray) -> dict:
+        g = np.ascontiguousarray(dl_dx_final, np.float64).reshape(-1)
+        ne, nn = self.blob.n_elem, self.blob.n_nodes
+        out = {k: np.zeros(ne) for k in ("G", "E", "A", "B")}
+        out["x0"] = np.zeros((nn, 3))
+        _check(self._lib.ffea_gpu_adjoint_backward(self._h, _p(g), _p(out["G"]), _p(out["E"]), _p(out["A"]),
+                                                   _p(out["B"]), _p(out["x0"])), "adjoint_backward")
+        return out
+
+
+def meso_to_si_gradients(g: dict) -> dict:
+    """Chain rule from dL/d(G, E, A, B) (meso) to the SI material columns of ``Mesh.material``:
+    shear/bulk modulus and shear/bulk viscosity (A = eta_s/(P t), B = eta_b/(P t) - 2/3 eta_s,
+    G = G_SI/P, E = K_SI/P, as the reference's load_material_params converts them)."""
+    P, t = 8.4305832688784826e8, 3.7302915560886126e-13
+    return {"shear_mod": g["G"] / P, "bulk_mod": g["E"] / P,
+            "shear_visc": g["A"] / (P * t) - (2.0 / 3.0) * g["B"], "bulk_visc": g["B"] / (P * t)}
 
 
 def _mesh_struct(mesh: Mesh, keep: list) -> MeshStruct:

@@ -206,6 +206,31 @@ int ffea_gpu_blob_get_rhs(ffea_gpu_blob *blob, double *rhs);
 int ffea_gpu_blob_solve_static(ffea_gpu_blob *blob, const double *rhs, double *x, int *iterations);
 
 /* ---------------------------------------------------------------------------
+ * Adjoint of a window of CG_nomass steps (the reference has no derivative code;
+ * this differentiates the step of ffea_gpu_blob_step).
+ *
+ * create: reserves checkpoint storage on `blob` for a window of window_steps steps
+ *   with a checkpoint (positions, stream state, element determinants) every
+ *   checkpoint_every steps. One adjoint per blob. Destroying the blob first
+ *   leaves the adjoint inert (its calls return FFEA_GPU_EINPUT); destroy it after.
+ * forward: runs the window from the blob's current state (as ffea_gpu_blob_step),
+ *   storing the checkpoints; the blob ends at the window's last state.
+ * backward: given dL/dx_final (3 * num_nodes, reference node order, midpoints
+ *   allowed), recomputes each segment from its checkpoint with the same noise
+ *   draws and runs the reverse sweep: one adjoint CG solve with the step's
+ *   viscosity matrix per step, plus the hand-written element derivative. Writes
+ *   dL/dG, dL/dE, dL/dA, dL/dB per element (meso units, the parameters of
+ *   ffea_gpu_mesh; any may be NULL) and dL/dx_initial (3 * num_nodes, may be
+ *   NULL). The blob is left at the window's last state.
+ * ------------------------------------------------------------------------- */
+typedef struct ffea_gpu_adjoint ffea_gpu_adjoint;
+int ffea_gpu_adjoint_create(ffea_gpu_blob *blob, int window_steps, int checkpoint_every, ffea_gpu_adjoint **out);
+int ffea_gpu_adjoint_forward(ffea_gpu_adjoint *adj, int *steps_done);
+int ffea_gpu_adjoint_backward(ffea_gpu_adjoint *adj, const double *dl_dx_final, double *dl_dG, double *dl_dE,
+                              double *dl_dA, double *dl_dB, double *dl_dx_initial);
+void ffea_gpu_adjoint_destroy(ffea_gpu_adjoint *adj);
+
+/* ---------------------------------------------------------------------------
  * Replica batch: many independent blobs of uneven size advanced together.
  *
  * The reference advances the blobs of a World one after another with the same
