@@ -12,6 +12,10 @@ A second workload (`--workload batch`, and the "batched" object of the default l
 replica ensemble: 256 Kuhn cubes with cells per side log-uniform in [8, 32] (seeded), per-blob
 G ~ U[1e8, 1e9] Pa and K = 3.9 G, all advanced by one graph-captured step (mixed precision).
 
+The "adjoint" object times the gradient of a 200-step window of a 20^3-cell cube with lognormal
+per-element moduli (checkpoints every 20 steps): seconds per step of gradient and its cost relative
+to the forward window.
+
 Metric: node-steps/s = vertex nodes x steps / time (whole job, all GPUs).
 Default arm: the mixed-precision GPU path (headline), with the plain FP64
 GPU path timed beside it. `--impl reference` times the reference algorithm on
@@ -346,6 +350,45 @@ def run_batch(args, ws) -> dict:
     return out
 
 
+def run_adjoint(args) -> dict:
+    """Configuration 3: gradient of a 200-step window (checkpoints every 20) of a 20^3-cell cube with
+    lognormal per-element moduli, noise frozen (replayed), loss |x_K - target|^2; cost against the
+    forward window."""
+    import numpy as np
+
+    from ffea_ci_demo_gb300 import build, lib
+    from ffea_ci_demo_gb300.mesh import kuhn_cube
+
+    build.build()
+    n, steps, every = 20, args.adjoint_steps, 20
+    mesh = kuhn_cube(n, side=5.0 * n, seed=12345)
+    rng = np.random.default_rng(2025)
+    mesh.material[:, 3] = rng.lognormal(np.log(5e8), 0.3, mesh.n_elem)
+    mesh.material[:, 4] = rng.lognormal(np.log(5e8), 0.3, mesh.n_elem)
+    s = mesh.scale / MESO_LENGTH
+    target = mesh.pos * s + rng.normal(0.0, 0.01, size=mesh.pos.shape)
+    out = {"workload": f"kuhn-cube-{n}: {mesh.n_elem} tets, {(n + 1) ** 3} nodes, G and K lognormal(ln 5e8, 0.3), "
+                       f"NoMassCG, dt=1e-12 s, kT=4.11e-21 J (noise replayed), {steps}-step window, checkpoint every "
+                       f"{every}, loss |x_K - target|^2", "steps": steps, "checkpoint_every": every}
+    for prec in ("mixed", "fp64"):
+        blob = lib.Blob(mesh, precision=prec, **PHYS)
+        blob.update(2)
+        adj = lib.Adjoint(blob, steps, every)
+        t0 = time.perf_counter()
+        adj.forward()
+        t1 = time.perf_counter()
+        d = blob.pos() - target
+        g = adj.backward(2.0 * d)
+        t2 = time.perf_counter()
+        fwd, bwd = t1 - t0, t2 - t1
+        out[prec] = {"forward_s": fwd, "backward_s": bwd, "grad_s_per_step": (fwd + bwd) / steps,
+                     "gradient_cost_over_forward": (fwd + bwd) / fwd, "backward_over_forward": bwd / fwd,
+                     "finite_gradients": bool(all(np.isfinite(g[k]).all() for k in ("G", "E", "A", "B")))}
+        adj.close()
+        blob.close()
+    return out
+
+
 def cpu_sample(n: int, threads: int, budget_s: float, max_steps: int, warmup: int = 1):
     """Time the oracle (reference algorithm, release optimisation, OpenMP) on the same workload."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
@@ -392,6 +435,8 @@ def main():
     ap.add_argument("--tpn", type=int, default=1)
     ap.add_argument("--no-fp64-sample", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--adjoint-steps", type=int, default=200)
+    ap.add_argument("--no-adjoint", action="store_true")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
     args.headline = "fp64" if args.precision == "fp64" else "mixed"
@@ -470,6 +515,8 @@ def main():
         args.steps = args.batch_steps
         line["batched"] = run_batch(args, ws)
         args.steps = k
+        if not args.no_adjoint:
+            line["adjoint"] = run_adjoint(args)
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_sample(args.cells, os.cpu_count() or 1, budget_s=20.0, max_steps=3)
         line["cpu_baseline"].pop("seconds")
