@@ -398,6 +398,10 @@ int check_batch_params(const ffea_gpu_params *p) {
         g_last_error = "a batch runs the CG_nomass solver in mixed precision";
         return FFEA_GPU_EINPUT;
     }
+    if (p->calc_stokes == 1 && p->calc_noise == 1) {
+        g_last_error = "a batch does not draw Stokes noise (calc_stokes with calc_noise)";
+        return FFEA_GPU_EINPUT;
+    }
     return FFEA_GPU_OK;
 }
 

@@ -205,6 +205,11 @@ struct BlobImpl final : ffea_gpu_blob {
     GridBarrier *gb;
     int cg_grid = 0, gather_blocks = 0, partial_stride = 0, tpn = 4;
     float4 *dpos = nullptr;  // mixed path: node offsets from the reference point
+    // Stokes noise (calc_stokes with calc_noise)
+    MrgJump *sn_chunk_jump = nullptr, *sn_lane_jump = nullptr;
+    int *sn_node_orig = nullptr, *sn_mid_orig = nullptr, *sn_lin_ptr = nullptr;
+    double *sn_mid_drag = nullptr;
+    int4 *sn_lin_ev = nullptr;
     int nmodes = 0;
     double modes[36] = {}, xc[3] = {};
     double *history = nullptr;
@@ -352,9 +357,37 @@ struct BlobImpl final : ffea_gpu_blob {
         for (int l = 0; l < 32; ++l) lj[l] = jump_pow(7ull * l);
         CK(mem.upload(&chunk_jump, cj));
         CK(mem.upload(&lane_jump, lj));
-        // a step consumes 7 draws per element when noise is on, none otherwise
-        std::vector<MrgJump> sj(1, jump_pow(p.calc_noise == 1 ? 7ull * (uint64_t)T : 0ull));
+        // a step consumes 7 draws per element when noise is on (and 3 per node of the reference numbering
+        // with Stokes drag), none otherwise
+        const bool snoise = p.calc_noise == 1 && p.calc_stokes == 1;
+        const uint64_t draws = p.calc_noise == 1 ? 7ull * (uint64_t)T + (snoise ? 3ull * (uint64_t)h.n_all : 0ull) : 0ull;
+        std::vector<MrgJump> sj(1, jump_pow(draws));
         CK(mem.upload(&step_jump, sj));
+        if (snoise) {
+            // node i of the reference numbering draws 3 numbers starting 7T + 3i after the step's state
+            const int nch = (h.n_all + 31) / 32;
+            std::vector<MrgJump> ncj(nch), nlj(32);
+            const Mat3 a96 = mat_pow(MRG_A1, 96, MRG_M1), b96 = mat_pow(MRG_A2, 96, MRG_M2);
+            Mat3 ca7 = mat_pow(MRG_A1, 7ull * (uint64_t)T, MRG_M1), cb7 = mat_pow(MRG_A2, 7ull * (uint64_t)T, MRG_M2);
+            for (int c = 0; c < nch; ++c) {
+                ncj[c] = to_jump(ca7, cb7);
+                ca7 = mat_mul(a96, ca7, MRG_M1);
+                cb7 = mat_mul(b96, cb7, MRG_M2);
+            }
+            for (int l = 0; l < 32; ++l) nlj[l] = jump_pow(3ull * l);
+            CK(mem.upload(&sn_chunk_jump, ncj));
+            CK(mem.upload(&sn_lane_jump, nlj));
+            CK(mem.upload(&sn_node_orig, h.node_of));
+            std::vector<double> mdrag(h.mid_nodes.size());
+            for (size_t m = 0; m < h.mid_nodes.size(); ++m) mdrag[m] = h.drag_all[h.mid_nodes[m]];
+            CK(mem.upload(&sn_mid_orig, h.mid_nodes));
+            CK(mem.upload(&sn_mid_drag, mdrag));
+            CK(mem.upload(&sn_lin_ptr, h.lin_ptr));
+            std::vector<int4> ev(h.lin_ev.size() / 4);
+            for (size_t k = 0; k < ev.size(); ++k)
+                ev[k] = make_int4(h.lin_ev[4 * k], h.lin_ev[4 * k + 1], h.lin_ev[4 * k + 2], -1);
+            CK(mem.upload(&sn_lin_ev, ev));
+        }
         std::vector<uint32_t> rs(rng_host, rng_host + 6);
         CK(mem.upload(&rng_state, rs));
         CK(cudaDeviceSynchronize());
@@ -438,6 +471,21 @@ struct BlobImpl final : ffea_gpu_blob {
         ga.partials = init_partials; ga.stride = gather_blocks; ga.st = st; ga.gb = gb;
         ga.dpos = dpos; ga.px = px; ga.py = py; ga.pz = pz; ga.diag = diag;
         ga.xc[0] = xc[0]; ga.xc[1] = xc[1]; ga.xc[2] = xc[2];
+        if (sn_lin_ptr) {
+            StokesNoise &sn = ga.sn;
+            sn.on = 1;
+            sn.kT = p.kT;
+            sn.dt = p.dt;
+            sn.rng_state = rng_state;
+            sn.chunk_jump = sn_chunk_jump;
+            sn.lane_jump = sn_lane_jump;
+            sn.node_orig = sn_node_orig;
+            sn.node_drag = drag;
+            sn.mid_orig = sn_mid_orig;
+            sn.mid_drag = sn_mid_drag;
+            sn.lin_ptr = sn_lin_ptr;
+            sn.lin_ev = sn_lin_ev;
+        }
         CK(Launch<R>::gather(ga, gather_blocks, stream));
         if ((rc = mark(3))) return rc;
         if (p.solver != FFEA_GPU_MASSLUMPED && (rc = launch_cg(init_partials, gather_blocks))) return rc;

@@ -153,6 +153,10 @@ struct HostModel {
     std::vector<unsigned> src;
     // mass matrix values (solver CG), SELL scalar over the same pattern; lumped inverse masses
     std::vector<double> mass_sell, inv_mass;
+    // Stokes noise: per vertex, the linearise events of its elements (element order), each holding up to
+    // three midpoints (index into mid_nodes, -1 once the midpoint's force has been moved)
+    std::vector<int> lin_ptr;
+    std::vector<int> lin_ev;  // 4 per event (the fourth unused)
 };
 
 // calc_shape_function_derivatives_and_volume's determinant and mat3_invert, in the reference's order
@@ -194,10 +198,6 @@ inline int build_model(const ffea_gpu_mesh *mesh, const ffea_gpu_params *p, Host
     }
     if (T >= (1 << 28)) {
         g_last_error = "too many elements (limit 2^28)";
-        return FFEA_GPU_EINPUT;
-    }
-    if (p->calc_stokes == 1 && p->calc_noise == 1) {
-        g_last_error = "Stokes noise (calc_stokes = 1 with calc_noise = 1) is not supported yet";
         return FFEA_GPU_EINPUT;
     }
     if (p->calc_stokes == 1 && !mesh->stokes_radius) {
@@ -274,6 +274,36 @@ inline int build_model(const ffea_gpu_mesh *mesh, const ffea_gpu_params *p, Host
         for (int i = 0; i < n; ++i) h.drag_all[i] = 6.0 * FFEA_PI * p->stokes_visc * mesh->stokes_radius[i];
         h.drag.resize(N);
         for (int k = 0; k < N; ++k) h.drag[k] = h.drag_all[h.node_of[k]];
+    }
+    if (p->calc_stokes == 1 && p->calc_noise == 1) {
+        // Blob::linearise_force (src/Blob.cpp:781-799) walks the elements in order: each vertex gains half of
+        // the three midpoints at it, then the element's six midpoints are zeroed, so a midpoint's force goes
+        // to its edge ends once, through the first element that holds it
+        static const int at_vertex[4][3] = {{4, 5, 6}, {4, 7, 8}, {5, 7, 9}, {6, 8, 9}};
+        std::vector<int> mid_id(n, -1);
+        for (size_t m = 0; m < h.mid_nodes.size(); ++m) mid_id[h.mid_nodes[m]] = (int)m;
+        std::vector<char> moved(n, 0);
+        std::vector<std::vector<int>> ev(N);
+        for (int e = 0; e < T; ++e) {
+            const int *t = &h.tets10[10 * (size_t)e];
+            for (int j = 0; j < 4; ++j) {
+                int q[3];
+                bool live = false;
+                for (int k = 0; k < 3; ++k) {
+                    const int x = t[at_vertex[j][k]];
+                    q[k] = moved[x] ? -1 : mid_id[x];
+                    live = live || q[k] >= 0;
+                }
+                if (!live) continue;
+                auto &v = ev[h.lin_of[t[j]]];
+                v.insert(v.end(), {q[0], q[1], q[2], -1});
+            }
+            for (int k = 4; k < 10; ++k) moved[t[k]] = 1;
+        }
+        h.lin_ptr.assign(N + 1, 0);
+        for (int a = 0; a < N; ++a) h.lin_ptr[a + 1] = h.lin_ptr[a] + (int)ev[a].size() / 4;
+        h.lin_ev.reserve(4 * (size_t)h.lin_ptr[N]);
+        for (int a = 0; a < N; ++a) h.lin_ev.insert(h.lin_ev.end(), ev[a].begin(), ev[a].end());
     }
     rest_state(h);
     // incidence: element order, vertex slots (Blob::calculate_node_element_connectivity)

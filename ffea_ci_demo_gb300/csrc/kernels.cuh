@@ -295,6 +295,55 @@ __global__ void __launch_bounds__(128) assemble_kernel(AsmArgs<R> g) {
 // ---------------------------------------------------------------------------
 // force gather (Blob::aggregate_forces_and_solve :3152-3158) + solver set-up
 // ---------------------------------------------------------------------------
+struct StokesNoise {
+    int on;
+    double kT, dt;
+    const uint32_t *rng_state;     // the step's stream state
+    const MrgJump *chunk_jump;     // A^(7T + 96 c): first draw of node chunk c (reference numbering)
+    const MrgJump *lane_jump;      // A^(3 l)
+    const int *node_orig;          // vertex -> reference node index
+    const double *node_drag;       // vertex Stokes drag
+    const int *mid_orig;           // midpoint -> reference node index
+    const double *mid_drag;
+    const int *lin_ptr;            // per vertex: its linearise events, in element order
+    const int4 *lin_ev;            // up to three live midpoints (-1: already moved) summed into the vertex
+};
+
+// force[i] -= RAND(-.5,.5) * sqrt(24 kT drag / dt), three components, for reference node i
+// (Blob::aggregate_forces_and_solve, src/Blob.cpp:3190-3219)
+template <class R>
+__device__ __forceinline__ void stokes_noise_sub(const StokesNoise &sn, int i, double drag, R (&F)[3]) {
+    uint32_t base[6], s6[6];
+#pragma unroll
+    for (int k = 0; k < 6; ++k) s6[k] = sn.rng_state[k];
+    mrg_apply(sn.chunk_jump[i >> 5], s6, base);
+    mrg_apply(sn.lane_jump[i & 31], base, s6);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        const double r = mrg_rand_half(s6);
+        F[c] -= (R)(r * sqrt((24 * sn.kT * drag) / (sn.dt)));
+    }
+}
+
+// the vertex's share of Blob::linearise_force (src/Blob.cpp:781-799): for each element holding the vertex,
+// in element order, force += 0.5 * (f_m1 + f_m2 + f_m3) over that element's three midpoints at the vertex
+// that still carry force (a midpoint's force is moved by the first element holding it, then zeroed)
+template <class R>
+__device__ __forceinline__ void stokes_linearise(const StokesNoise &sn, int a, R (&F)[3]) {
+    for (int k = sn.lin_ptr[a]; k < sn.lin_ptr[a + 1]; ++k) {
+        const int4 ev = sn.lin_ev[k];
+        const int m[3] = {ev.x, ev.y, ev.z};
+        R fm[3][3];
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+            fm[j][0] = fm[j][1] = fm[j][2] = (R)0;
+            if (m[j] >= 0) stokes_noise_sub<R>(sn, sn.mid_orig[m[j]], sn.mid_drag[m[j]], fm[j]);
+        }
+#pragma unroll
+        for (int c = 0; c < 3; ++c) F[c] += (R)0.5 * (fm[0][c] + fm[1][c] + fm[2][c]);
+    }
+}
+
 template <class R>
 struct GatherArgs {
     int N;
@@ -316,6 +365,9 @@ struct GatherArgs {
     const double *px, *py, *pz;
     double xc[3];
     const R *diag;
+    // Stokes noise (calc_stokes and calc_noise): 3 draws per node of the reference numbering, after the
+    // elements' 7T, in node order; a midpoint's force is moved to its edge ends by linearise events
+    StokesNoise sn;
 };
 
 template <class R>
@@ -339,6 +391,12 @@ __global__ void __launch_bounds__(256) gather_kernel(GatherArgs<R> g) {
             F0 -= (R)(g.vx[a] * dr);
             F1 -= (R)(g.vy[a] * dr);
             F2 -= (R)(g.vz[a] * dr);
+        }
+        if (g.sn.on) {
+            R F[3] = {F0, F1, F2};
+            stokes_noise_sub<R>(g.sn, g.sn.node_orig[a], g.sn.node_drag[a], F);
+            stokes_linearise<R>(g.sn, a, F);
+            F0 = F[0]; F1 = F[1]; F2 = F[2];
         }
         if (g.pinned[a]) { F0 = 0; F1 = 0; F2 = 0; }
         g.f[4 * a] = (double)F0;

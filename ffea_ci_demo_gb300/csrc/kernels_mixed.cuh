@@ -69,6 +69,12 @@ __global__ void __launch_bounds__(256) gather_mixed_kernel(GatherArgs<R> g) {
             F1 -= (float)(g.vy[a] * dr);
             F2 -= (float)(g.vz[a] * dr);
         }
+        if (g.sn.on) {
+            float F[3] = {F0, F1, F2};
+            stokes_noise_sub<float>(g.sn, g.sn.node_orig[a], g.sn.node_drag[a], F);
+            stokes_linearise<float>(g.sn, a, F);
+            F0 = F[0]; F1 = F[1]; F2 = F[2];
+        }
         if (g.pinned[a]) { F0 = 0; F1 = 0; F2 = 0; }
         g.f[4 * a] = F0; g.f[4 * a + 1] = F1; g.f[4 * a + 2] = F2;
         if (g.mode == 1) {

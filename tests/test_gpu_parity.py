@@ -236,3 +236,34 @@ def test_larger_cube_fp64_matches_oracle(gpu, oracle_built):
     b.update(4)
     assert disp_err(b.pos(), o.pos(), sheared(m, 0.01)) < 1e-8
     assert np.array_equal(b.rng_state(), o.rng_state())
+
+
+@pytest.mark.parametrize("name,kw,exact", [
+    ("cube3_nomass_pin_stokes", dict(solver="CG_nomass", dt=1e-12), False),
+    ("cube3_lumped_pin_stokes", dict(solver="masslumped", dt=1e-14), True),
+    ("cube3_cg_pin_stokes", dict(solver="CG", dt=1e-14), False),
+])
+def test_stokes_noise_matches_reference(gpu, name, kw, exact):
+    """Stokes drag with noise: 3 draws per node (midpoints included) after the elements' draws, midpoint
+    forces moved to their edge ends by the reference's element-order linearisation, pins zeroed."""
+    g = load(name)
+    m = case_mesh(3, 7, [0, 1, 5, 66])
+    b = gpu_blob(m, 0.02, kT=4.11e-21, calc_noise=1, calc_stokes=1, **kw)
+    b.update(1)
+    assert np.array_equal(b.rhs(), g["step1_rhs"])
+    b.update(int(g["steps"]) - 1)
+    assert np.array_equal(b.rng_state(), g["final_rng"])
+    if exact:
+        assert np.array_equal(b.pos(), g["final_pos"]) and np.array_equal(b.vel(), g["final_vel"])
+    else:
+        assert disp_err(b.pos(), g["final_pos"], sheared(m, 0.02)) < 1e-8
+
+
+def test_stokes_noise_mixed_precision(gpu):
+    m = case_mesh(4, 3, [0, 2])
+    out = {}
+    for prec in ("fp64", "mixed"):
+        b = gpu_blob(m, 0.02, solver="CG_nomass", precision=prec, kT=4.11e-21, calc_noise=1, calc_stokes=1)
+        b.update(20)
+        out[prec] = b.pos()
+    assert disp_err(out["mixed"], out["fp64"], sheared(m, 0.02)) < 1e-5
