@@ -26,6 +26,7 @@ UNITS = {
     "engine_mixed.cu": [],
     "blob.cu": [],
     "batch.cu": [],
+    "world.cu": [],
     "io.cu": [],
 }
 

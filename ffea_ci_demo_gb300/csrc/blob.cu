@@ -27,6 +27,7 @@
 #include <type_traits>
 
 #include "engine.h"
+#include "blob_iface.h"
 #include "host_model.h"
 #include "kernels_mixed.cuh"
 
@@ -141,43 +142,6 @@ __global__ void __launch_bounds__(SOLVE_PREP_THREADS)
 
 }  // namespace
 
-// ---------------------------------------------------------------------------
-// the blob
-// ---------------------------------------------------------------------------
-struct ffea_gpu_adjoint {
-    ffea_gpu_blob *blob;  // null once the blob is destroyed
-};
-
-struct ffea_gpu_blob {
-    ffea_gpu_adjoint *adj_handle = nullptr;  // the adjoint reserved on this blob, if any
-    virtual ~ffea_gpu_blob() {
-        if (adj_handle) adj_handle->blob = nullptr;
-    }
-    HostModel h;
-    ffea_gpu_params p{};
-    uint32_t rng_host[6] = {12345, 12345, 12345, 12345, 12345, 12345};
-    virtual int init() = 0;
-    virtual int step(int nsteps, int *done) = 0;
-    virtual int step_timed(int nsteps, long long flush_bytes, int *done, double *step_ms, double *phase_ms) = 0;
-    virtual int get_state(double *pos, double *vel, double *force) = 0;
-    virtual int set_state(const double *pos, const double *vel) = 0;
-    virtual int set_rng(const uint32_t s[6]) = 0;
-    virtual int get_rng(uint32_t s[6]) = 0;
-    virtual int measure(double *se, double *ke) = 0;
-    virtual int cg_iters(int *last, long long *total) = 0;
-    virtual int get_elements(double *nf, double *vol, double *visc) = 0;
-    virtual int get_rhs(double *rhs) = 0;
-    virtual int cg_history(double *res2, int max_entries, int *count) = 0;
-    virtual int cg_profile(double *ns, int n) = 0;
-    virtual int get_matrix_values(std::vector<double> &val_sell) = 0;
-    virtual int solve_static(const double *rhs, double *x, int *iterations) = 0;
-    virtual int adj_init(int window, int every) = 0;
-    virtual int adj_forward(int *done) = 0;
-    virtual int adj_backward(const double *dl_dx, double *dG, double *dE, double *dA, double *dB,
-                             double *dl_dx0) = 0;
-    virtual void adj_release() = 0;
-};
-
 namespace {
 
 template <class R>
@@ -205,6 +169,11 @@ struct BlobImpl final : ffea_gpu_blob {
     GridBarrier *gb;
     int cg_grid = 0, gather_blocks = 0, partial_stride = 0, tpn = 4;
     float4 *dpos = nullptr;  // mixed path: node offsets from the reference point
+    // measurements: densities, reference positions of vertices and midpoints (SoA), per-block sums
+    R *rho = nullptr;
+    double *p0 = nullptr, *m0 = nullptr, *meas_part = nullptr, *meas_out = nullptr;
+    int *mid_a = nullptr, *mid_b = nullptr;
+    int meas_blocks = 0;
     // Stokes noise (calc_stokes with calc_noise)
     MrgJump *sn_chunk_jump = nullptr, *sn_lane_jump = nullptr;
     int *sn_node_orig = nullptr, *sn_mid_orig = nullptr, *sn_lin_ptr = nullptr;
@@ -277,6 +246,23 @@ struct BlobImpl final : ffea_gpu_blob {
         CK(mem.upload(&A, cast_vec<R>(h.A)));
         CK(mem.upload(&B, cast_vec<R>(h.B)));
         CK(mem.upload(&vol0, cast_vec<R>(h.vol0)));
+        CK(mem.upload(&rho, cast_vec<R>(h.rho)));
+        {
+            const int M = (int)h.mid_nodes.size();
+            std::vector<double> q0(3 * (size_t)N), qm(3 * (size_t)std::max(M, 1));
+            for (int k = 0; k < N; ++k)
+                for (int c = 0; c < 3; ++c) q0[(size_t)c * N + k] = h.pos[3 * (size_t)k + c];
+            for (int m = 0; m < M; ++m)
+                for (int c = 0; c < 3; ++c)
+                    qm[(size_t)c * M + m] = .5 * (h.pos[3 * (size_t)h.mid_a[m] + c] + h.pos[3 * (size_t)h.mid_b[m] + c]);
+            CK(mem.upload(&p0, q0));
+            CK(mem.upload(&m0, qm));
+            CK(mem.upload(&mid_a, h.mid_a));
+            CK(mem.upload(&mid_b, h.mid_b));
+            meas_blocks = (std::max({T, N, M}) + 255) / 256;
+            CK(mem.alloc(&meas_part, (size_t)MEASURE_NV * meas_blocks));
+            CK(mem.alloc(&meas_out, (size_t)MEASURE_NV));
+        }
         CK(mem.upload(&last_det, h.last_det));
         CK(mem.alloc(&ef, 12 * (size_t)T));
         CK(mem.alloc(&geom, 16 * (size_t)T));
@@ -360,22 +346,11 @@ struct BlobImpl final : ffea_gpu_blob {
         // a step consumes 7 draws per element when noise is on (and 3 per node of the reference numbering
         // with Stokes drag), none otherwise
         const bool snoise = p.calc_noise == 1 && p.calc_stokes == 1;
-        const uint64_t draws = p.calc_noise == 1 ? 7ull * (uint64_t)T + (snoise ? 3ull * (uint64_t)h.n_all : 0ull) : 0ull;
-        std::vector<MrgJump> sj(1, jump_pow(draws));
-        CK(mem.upload(&step_jump, sj));
+        CK(mem.alloc(&step_jump, 1));
         if (snoise) {
-            // node i of the reference numbering draws 3 numbers starting 7T + 3i after the step's state
-            const int nch = (h.n_all + 31) / 32;
-            std::vector<MrgJump> ncj(nch), nlj(32);
-            const Mat3 a96 = mat_pow(MRG_A1, 96, MRG_M1), b96 = mat_pow(MRG_A2, 96, MRG_M2);
-            Mat3 ca7 = mat_pow(MRG_A1, 7ull * (uint64_t)T, MRG_M1), cb7 = mat_pow(MRG_A2, 7ull * (uint64_t)T, MRG_M2);
-            for (int c = 0; c < nch; ++c) {
-                ncj[c] = to_jump(ca7, cb7);
-                ca7 = mat_mul(a96, ca7, MRG_M1);
-                cb7 = mat_mul(b96, cb7, MRG_M2);
-            }
+            CK(mem.alloc(&sn_chunk_jump, (size_t)(h.n_all + 31) / 32));
+            std::vector<MrgJump> nlj(32);
             for (int l = 0; l < 32; ++l) nlj[l] = jump_pow(3ull * l);
-            CK(mem.upload(&sn_chunk_jump, ncj));
             CK(mem.upload(&sn_lane_jump, nlj));
             CK(mem.upload(&sn_node_orig, h.node_of));
             std::vector<double> mdrag(h.mid_nodes.size());
@@ -388,6 +363,8 @@ struct BlobImpl final : ffea_gpu_blob {
                 ev[k] = make_int4(h.lin_ev[4 * k], h.lin_ev[4 * k + 1], h.lin_ev[4 * k + 2], -1);
             CK(mem.upload(&sn_lin_ev, ev));
         }
+        int lrc = set_rng_layout(element_draws() + stokes_draws(), element_draws());
+        if (lrc) return lrc;
         std::vector<uint32_t> rs(rng_host, rng_host + 6);
         CK(mem.upload(&rng_state, rs));
         CK(cudaDeviceSynchronize());
@@ -790,6 +767,26 @@ struct BlobImpl final : ffea_gpu_blob {
         }
     }
 
+    // the step's stream advance, and where the Stokes draws start (node i of the reference numbering draws
+    // 3 numbers from stokes_base + 3i after the step's state)
+    int set_rng_layout(unsigned long long step_draws, unsigned long long stokes_base) override {
+        std::vector<MrgJump> sj(1, jump_pow(step_draws));
+        CK(cudaMemcpy(step_jump, sj.data(), sizeof(MrgJump), cudaMemcpyHostToDevice));
+        if (sn_chunk_jump) {
+            const int nch = (h.n_all + 31) / 32;
+            std::vector<MrgJump> ncj(nch);
+            const Mat3 a96 = mat_pow(MRG_A1, 96, MRG_M1), b96 = mat_pow(MRG_A2, 96, MRG_M2);
+            Mat3 ca = mat_pow(MRG_A1, stokes_base, MRG_M1), cb = mat_pow(MRG_A2, stokes_base, MRG_M2);
+            for (int c = 0; c < nch; ++c) {
+                ncj[c] = to_jump(ca, cb);
+                ca = mat_mul(a96, ca, MRG_M1);
+                cb = mat_mul(b96, cb, MRG_M2);
+            }
+            CK(cudaMemcpy(sn_chunk_jump, ncj.data(), ncj.size() * sizeof(MrgJump), cudaMemcpyHostToDevice));
+        }
+        return FFEA_GPU_OK;
+    }
+
     // ---- adjoint window ---------------------------------------------------------------------
     int adj_init(int window, int every) override {
         if (p.solver != FFEA_GPU_NOMASS_CG) {
@@ -1037,51 +1034,56 @@ struct BlobImpl final : ffea_gpu_blob {
     }
 
     // Blob::make_measurements energies (src/Blob.cpp:1066-1125), evaluated on the host from device state
+    // Blob::make_measurements on the device: out = strain energy, kinetic energy, centroid (3) of all nodes,
+    // RMSD of all nodes from the reference positions (meso units)
+    int measurements(double out[MEASURE_NV]) override {
+        MeasureArgs<R> ma{};
+        ma.T = h.T;
+        ma.N = h.N;
+        ma.M = (int)h.mid_nodes.size();
+        ma.inertial = p.solver != FFEA_GPU_NOMASS_CG;
+        ma.tet = tet;
+        ma.px = px; ma.py = py; ma.pz = pz; ma.vx = vx; ma.vy = vy; ma.vz = vz;
+        ma.jinv = jinv; ma.G = G; ma.E = E; ma.vol0 = vol0; ma.rho = rho;
+        ma.p0 = p0; ma.mid_a = mid_a; ma.mid_b = mid_b; ma.m0 = m0;
+        ma.partials = meas_part;
+        CK(Launch<R>::measure(ma, meas_blocks, meas_out, stream));
+        double s6[MEASURE_NV];
+        CK(cudaMemcpyAsync(s6, meas_out, sizeof s6, cudaMemcpyDeviceToHost, stream));
+        CK(cudaStreamSynchronize(stream));
+        const double n = (double)std::max(h.n_all, 1);
+        out[0] = s6[0];
+        out[1] = s6[1];
+        out[2] = s6[2] / n;
+        out[3] = s6[3] / n;
+        out[4] = s6[4] / n;
+        out[5] = sqrt(s6[5] / n);
+        return FFEA_GPU_OK;
+    }
+
     int measure(double *se, double *ke) override {
-        const int N = h.N, T = h.T;
-        std::vector<double> P(3 * (size_t)h.n_all), V(3 * (size_t)h.n_all);
-        int rc = get_state(P.data(), V.data(), nullptr);
+        double o[MEASURE_NV];
+        int rc = measurements(o);
         if (rc) return rc;
-        double kenergy = 0.0, senergy = 0.0;
-        for (int e = 0; e < T; ++e) {
-            const int *t = &h.tets10[10 * (size_t)e];
-            double J[3][3];
-            for (int rr = 0; rr < 3; ++rr)
-                for (int c = 0; c < 3; ++c) J[rr][c] = P[3 * (size_t)t[rr + 1] + c] - P[3 * (size_t)t[0] + c];
-            double d1 = J[2][2] * J[1][1] - J[2][1] * J[1][2];
-            double d2 = J[2][1] * J[0][2] - J[2][2] * J[0][1];
-            double d3 = J[1][2] * J[0][1] - J[1][1] * J[0][2];
-            const double det = J[0][0] * d1 + J[1][0] * d2 + J[2][0] * d3;
-            const double vol = (1.0 / 6.0) * fabs(det);
-            const double *Ji = &h.jinv[9 * (size_t)e];
-            double F[3][3];
-            for (int i = 0; i < 3; ++i)
-                for (int j = 0; j < 3; ++j) {
-                    F[i][j] = 0;
-                    for (int k = 0; k < 3; ++k) F[i][j] += J[k][i] * Ji[3 * j + k];
-                }
-            if (p.solver != FFEA_GPU_NOMASS_CG) {
-                double v[12], tmp[12] = {0};
-                for (int a = 0; a < 4; ++a)
-                    for (int i = 0; i < 3; ++i) v[4 * i + a] = V[3 * (size_t)t[a] + i];
-                for (int k = 0; k < 12; k += 4)
-                    for (int i = 0; i < 4; ++i)
-                        for (int j = 0; j < 4; ++j) tmp[i + k] += (i == j ? .1 : .05) * v[j + k];
-                for (int i = 0; i < 12; ++i) tmp[i] = tmp[i] * (h.vol0[e] * h.rho[e]);
-                double s = 0;
-                for (int i = 0; i < 12; ++i) s += v[i] * tmp[i];
-                kenergy += s;
-            }
-            const double C = h.E[e] - (2.0 / 3.0) * h.G[e];
-            const double t1 = vol / h.vol0[e];
-            const double ff = F[0][0] * F[0][0] + F[1][1] * F[1][1] + F[2][2] * F[2][2] + F[0][1] * F[0][1] +
-                              F[1][0] * F[1][0] + F[0][2] * F[0][2] + F[2][0] * F[2][0] + F[1][2] * F[1][2] +
-                              F[2][1] * F[2][1];
-            senergy += h.vol0[e] * (h.G[e] * (ff - 3) + 0.5 * C * (t1 * t1 - 1) - (C + 2 * h.G[e]) * log(t1));
-        }
-        (void)N;
-        if (ke) *ke = kenergy * 0.5;
-        if (se) *se = senergy * 0.5;
+        if (se) *se = o[0];
+        if (ke) *ke = o[1];
+        return FFEA_GPU_OK;
+    }
+
+    // Blob::set_pos_0: the current positions become the RMSD reference
+    int set_rmsd_reference() override {
+        const int N = h.N, M = (int)h.mid_nodes.size();
+        std::vector<double> q(3 * (size_t)N), qm(3 * (size_t)std::max(M, 1));
+        CK(cudaMemcpyAsync(q.data(), px, N * sizeof(double), cudaMemcpyDeviceToHost, stream));
+        CK(cudaMemcpyAsync(q.data() + N, py, N * sizeof(double), cudaMemcpyDeviceToHost, stream));
+        CK(cudaMemcpyAsync(q.data() + 2 * (size_t)N, pz, N * sizeof(double), cudaMemcpyDeviceToHost, stream));
+        CK(cudaStreamSynchronize(stream));
+        for (int m = 0; m < M; ++m)
+            for (int c = 0; c < 3; ++c)
+                qm[(size_t)c * M + m] = .5 * (q[(size_t)c * N + h.mid_a[m]] + q[(size_t)c * N + h.mid_b[m]]);
+        CK(cudaMemcpyAsync(p0, q.data(), q.size() * sizeof(double), cudaMemcpyHostToDevice, stream));
+        CK(cudaMemcpyAsync(m0, qm.data(), qm.size() * sizeof(double), cudaMemcpyHostToDevice, stream));
+        CK(cudaStreamSynchronize(stream));
         return FFEA_GPU_OK;
     }
 };
@@ -1196,6 +1198,16 @@ int ffea_gpu_blob_measure(ffea_gpu_blob *b, double *se, double *ke) {
     return b->measure(se, ke);
 }
 
+int ffea_gpu_blob_measurements(ffea_gpu_blob *b, double out[6]) {
+    if (!b || !out) return FFEA_GPU_EINPUT;
+    return b->measurements(out);
+}
+
+int ffea_gpu_blob_set_rmsd_reference(ffea_gpu_blob *b) {
+    if (!b) return FFEA_GPU_EINPUT;
+    return b->set_rmsd_reference();
+}
+
 int ffea_gpu_blob_cg_iterations(ffea_gpu_blob *b, int *last, long long *total) {
     if (!b) return FFEA_GPU_EINPUT;
     return b->cg_iters(last, total);
@@ -1213,6 +1225,13 @@ int ffea_gpu_blob_cg_profile(ffea_gpu_blob *b, double *ns, int n) {
         return FFEA_GPU_OK;
     }
     return b->cg_profile(ns, n);
+}
+
+int ffea_gpu_blob_counts(ffea_gpu_blob *b, int *num_nodes, int *num_elements) {
+    if (!b) return FFEA_GPU_EINPUT;
+    if (num_nodes) *num_nodes = b->h.n_all;
+    if (num_elements) *num_elements = b->h.T;
+    return FFEA_GPU_OK;
 }
 
 int ffea_gpu_blob_sizes(ffea_gpu_blob *b, int *nl, int *ne, long long *nb) {

@@ -22,6 +22,8 @@ struct Launch {
     static int cg_max_grid(int device);
     static int cg_threads();
     static cudaError_t euler(const EulerArgs<R> &a, cudaStream_t s);
+    // measure_kernel over max(T, N, M) threads in `blocks` blocks, then the final sum into out[6]
+    static cudaError_t measure(const MeasureArgs<R> &a, int blocks, double *out, cudaStream_t s);
 };
 
 // launchers of the adjoint kernels (kernels_adjoint.cuh)

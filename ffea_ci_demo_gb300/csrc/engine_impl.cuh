@@ -78,6 +78,14 @@ cudaError_t Launch<R>::euler(const EulerArgs<R> &a, cudaStream_t s) {
 }
 
 template <class R>
+cudaError_t Launch<R>::measure(const MeasureArgs<R> &a, int blocks, double *out, cudaStream_t s) {
+    measure_kernel<R><<<blocks, 256, 0, s>>>(a);
+    measure_final_kernel<R><<<1, 256, 0, s>>>(a.partials, blocks, out);
+    count_launch(2);
+    return cudaGetLastError();
+}
+
+template <class R>
 cudaError_t AdjLaunch<R>::gather(const AdjGatherArgs<R> &a, int blocks, cudaStream_t s) {
     adj_gather_kernel<R><<<blocks, 256, 0, s>>>(a);
     count_launch();

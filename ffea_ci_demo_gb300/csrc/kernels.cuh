@@ -732,6 +732,109 @@ __global__ void __launch_bounds__(256) euler_kernel(EulerArgs<R> g) {
     }
 }
 
+// ---------------------------------------------------------------------------
+// measurements (Blob::make_measurements, src/Blob.cpp:1066-1202): strain energy, kinetic energy
+// (inertial solvers), centroid of all nodes and the RMSD from the reference positions, as per-block
+// FP64 sums in a fixed order (measure_kernel) and one block that adds them up (measure_final_kernel)
+// ---------------------------------------------------------------------------
+constexpr int MEASURE_NV = 6;  // strain energy, kinetic energy, sum x, sum y, sum z, sum |x - x0|^2
+
+template <class R>
+struct MeasureArgs {
+    int T, N, M;              // elements, vertices, midpoints
+    int inertial;
+    const int4 *tet;
+    const double *px, *py, *pz, *vx, *vy, *vz;
+    const R *jinv, *G, *E, *vol0, *rho;
+    const double *p0;         // 3 x N, SoA: reference positions of the vertices
+    const int *mid_a, *mid_b; // midpoint edge ends (vertex indices)
+    const double *m0;         // 3 x M, SoA: reference positions of the midpoints
+    double *partials;         // MEASURE_NV rows of gridDim.x
+};
+
+template <class R>
+__global__ void __launch_bounds__(256) measure_kernel(MeasureArgs<R> g) {
+    __shared__ double smem[MEASURE_NV * 32];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double acc[MEASURE_NV] = {0, 0, 0, 0, 0, 0};
+    if (i < g.T) {
+        const int4 t = g.tet[i];
+        const int nd[4] = {t.x, t.y, t.z, t.w};
+        double J[3][3];
+        for (int r = 0; r < 3; ++r) {
+            J[r][0] = g.px[nd[r + 1]] - g.px[nd[0]];
+            J[r][1] = g.py[nd[r + 1]] - g.py[nd[0]];
+            J[r][2] = g.pz[nd[r + 1]] - g.pz[nd[0]];
+        }
+        const double d1 = J[2][2] * J[1][1] - J[2][1] * J[1][2];
+        const double d2 = J[2][1] * J[0][2] - J[2][2] * J[0][1];
+        const double d3 = J[1][2] * J[0][1] - J[1][1] * J[0][2];
+        const double det = J[0][0] * d1 + J[1][0] * d2 + J[2][0] * d3;
+        const double vol = (1.0 / 6.0) * fabs(det);
+        double F[3][3];
+        for (int a = 0; a < 3; ++a)
+            for (int b = 0; b < 3; ++b) {
+                F[a][b] = 0;
+                for (int k = 0; k < 3; ++k) F[a][b] += J[k][a] * (double)g.jinv[(size_t)(3 * b + k) * g.T + i];
+            }
+        const double Gs = g.G[i], Es = g.E[i], v0 = g.vol0[i];
+        if (g.inertial) {
+            double v[12], tmp[12] = {0};
+            for (int a = 0; a < 4; ++a) {
+                v[a] = g.vx[nd[a]]; v[4 + a] = g.vy[nd[a]]; v[8 + a] = g.vz[nd[a]];
+            }
+            for (int k = 0; k < 12; k += 4)
+                for (int a = 0; a < 4; ++a)
+                    for (int b = 0; b < 4; ++b) tmp[a + k] += (a == b ? .1 : .05) * v[b + k];
+            const double m = v0 * (double)g.rho[i];
+            double s = 0;
+            for (int k = 0; k < 12; ++k) s += v[k] * (tmp[k] * m);
+            acc[1] = s;
+        }
+        const double C = Es - (2.0 / 3.0) * Gs;
+        const double t1 = vol / v0;
+        const double ff = F[0][0] * F[0][0] + F[1][1] * F[1][1] + F[2][2] * F[2][2] + F[0][1] * F[0][1] +
+                          F[1][0] * F[1][0] + F[0][2] * F[0][2] + F[2][0] * F[2][0] + F[1][2] * F[1][2] +
+                          F[2][1] * F[2][1];
+        acc[0] = v0 * (Gs * (ff - 3) + 0.5 * C * (t1 * t1 - 1) - (C + 2 * Gs) * log(t1));
+    }
+    if (i < g.N) {
+        const double x = g.px[i], y = g.py[i], z = g.pz[i];
+        const double dx = x - g.p0[i], dy = y - g.p0[g.N + i], dz = z - g.p0[2 * (size_t)g.N + i];
+        acc[2] += x; acc[3] += y; acc[4] += z;
+        acc[5] += dx * dx + dy * dy + dz * dz;
+    }
+    if (i < g.M) {
+        const int a = g.mid_a[i], b = g.mid_b[i];
+        const double x = .5 * (g.px[a] + g.px[b]), y = .5 * (g.py[a] + g.py[b]), z = .5 * (g.pz[a] + g.pz[b]);
+        const double dx = x - g.m0[i], dy = y - g.m0[g.M + i], dz = z - g.m0[2 * (size_t)g.M + i];
+        acc[2] += x; acc[3] += y; acc[4] += z;
+        acc[5] += dx * dx + dy * dy + dz * dz;
+    }
+    block_sum<MEASURE_NV>(acc, smem);
+    if (threadIdx.x == 0)
+        for (int k = 0; k < MEASURE_NV; ++k) g.partials[k * gridDim.x + blockIdx.x] = acc[k];
+}
+
+// one block: the totals of measure_kernel's partials, halved energies (the reference's 1/2)
+template <class R>
+__global__ void __launch_bounds__(256) measure_final_kernel(const double *partials, int nb, double *out) {
+    __shared__ double s[MEASURE_NV];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int k = wid; k < MEASURE_NV; k += nw) {
+        double t = 0.0;
+        for (int b = lane; b < nb; b += 32) t += partials[k * nb + b];
+        t = warp_sum(t);
+        if (lane == 0) s[k] = t;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        out[0] = 0.5 * s[0];
+        out[1] = 0.5 * s[1];
+        for (int k = 2; k < MEASURE_NV; ++k) out[k] = s[k];
+    }
+}
+
 // closes a step: RNG advance and step counter (one thread), after euler_kernel
 __global__ void finish_step_kernel(uint32_t *rng_state, const MrgJump *step_jump, DevStatus *st);
 

@@ -88,7 +88,10 @@ def load():
         "ffea_gpu_blob_set_state": (C.c_int, [vp, dp, dp]),
         "ffea_gpu_blob_measure": (C.c_int, [vp, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
         "ffea_gpu_blob_cg_iterations": (C.c_int, [vp, ip, C.POINTER(C.c_longlong)]),
+        "ffea_gpu_blob_measurements": (C.c_int, [vp, dp]),
+        "ffea_gpu_blob_set_rmsd_reference": (C.c_int, [vp]),
         "ffea_gpu_blob_sizes": (C.c_int, [vp, ip, ip, C.POINTER(C.c_longlong)]),
+        "ffea_gpu_blob_counts": (C.c_int, [vp, ip, ip]),
         "ffea_gpu_blob_cg_history": (C.c_int, [vp, dp, C.c_int, ip]),
         "ffea_gpu_blob_cg_profile": (C.c_int, [vp, dp, C.c_int]),
         "ffea_gpu_blob_get_pattern": (C.c_int, [vp, dp, dp, dp, dp, C.POINTER(C.c_longlong)]),
@@ -100,6 +103,11 @@ def load():
         "ffea_gpu_adjoint_forward": (C.c_int, [vp, ip]),
         "ffea_gpu_adjoint_backward": (C.c_int, [vp, dp, dp, dp, dp, dp, dp]),
         "ffea_gpu_adjoint_destroy": (None, [vp]),
+        "ffea_gpu_world_load": (C.c_int, [C.c_char_p, C.c_int, C.POINTER(vp)]),
+        "ffea_gpu_world_run": (C.c_int, [vp, C.POINTER(C.c_longlong)]),
+        "ffea_gpu_world_num_blobs": (C.c_int, [vp]),
+        "ffea_gpu_world_blob": (vp, [vp, C.c_int]),
+        "ffea_gpu_world_destroy": (None, [vp]),
         "ffea_gpu_batch_create": (C.c_int, [vp, C.c_int, C.POINTER(Params), C.POINTER(vp)]),
         "ffea_gpu_batch_destroy": (None, [vp]),
         "ffea_gpu_batch_sizes": (C.c_int, [vp, ip, ip, ip, C.POINTER(C.c_longlong)]),
@@ -211,6 +219,9 @@ class Blob:
         return cls(_handle=h, _n=(n, t), rng_state=rng_state)
 
     def close(self) -> None:
+        if getattr(self, "_borrowed", False):
+            self._h = C.c_void_p()
+            return
         if getattr(self, "_h", None) and self._h.value:
             self._lib.ffea_gpu_blob_destroy(self._h)
             self._h = C.c_void_p()
@@ -279,6 +290,15 @@ class Blob:
         se, ke = C.c_double(), C.c_double()
         _check(self._lib.ffea_gpu_blob_measure(self._h, C.byref(se), C.byref(ke)), "measure")
         return se.value, ke.value
+
+    def measurements(self) -> dict:
+        """Blob::make_measurements on the device (meso units)."""
+        o = np.zeros(6)
+        _check(self._lib.ffea_gpu_blob_measurements(self._h, _p(o)), "measurements")
+        return {"strain_energy": o[0], "kinetic_energy": o[1], "centroid": o[2:5].copy(), "rmsd": o[5]}
+
+    def set_rmsd_reference(self) -> None:
+        _check(self._lib.ffea_gpu_blob_set_rmsd_reference(self._h), "set_rmsd_reference")
 
     def cg_iterations(self) -> tuple[int, int]:
         last, total = C.c_int(), C.c_longlong()
@@ -371,6 +391,42 @@ class Adjoint:
         _check(self._lib.ffea_gpu_adjoint_backward(self._h, _p(g), _p(out["G"]), _p(out["E"]), _p(out["A"]),
                                                    _p(out["B"]), _p(out["x0"])), "adjoint_backward")
         return out
+
+
+class World:
+    """A reference ``.ffea`` script run on the GPU (blob-step path only): ``World(script).run()`` writes the
+    trajectory, measurement and checkpoint files the reference writes."""
+
+    def __init__(self, script: str, precision: str = "fp64"):
+        self._lib = load()
+        self._h = C.c_void_p()
+        _check(self._lib.ffea_gpu_world_load(str(script).encode(), PRECISIONS[precision], C.byref(self._h)),
+               "world_load")
+
+    def run(self) -> int:
+        last = C.c_longlong(0)
+        _check(self._lib.ffea_gpu_world_run(self._h, C.byref(last)), f"world_run (stopped at step {last.value})")
+        return last.value
+
+    def blob(self, i: int = 0) -> "Blob":
+        """The i-th blob (owned by the World: valid while the World is)."""
+        h = self._lib.ffea_gpu_world_blob(self._h, i)
+        if not h:
+            raise IndexError(i)
+        b = Blob.__new__(Blob)
+        b._lib, b._h, b._borrowed = self._lib, C.c_void_p(h), True
+        n, t = C.c_int(), C.c_int()
+        _check(self._lib.ffea_gpu_blob_counts(b._h, C.byref(n), C.byref(t)), "blob_counts")
+        b.n_nodes, b.n_elem = n.value, t.value
+        return b
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) and self._h.value:
+            self._lib.ffea_gpu_world_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        self.close()
 
 
 def meso_to_si_gradients(g: dict) -> dict:

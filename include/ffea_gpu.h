@@ -140,6 +140,14 @@ int ffea_gpu_blob_set_state(ffea_gpu_blob *blob, const double *pos, const double
 /* Blob::make_measurements energies (src/Blob.cpp:1066-1125), meso units. */
 int ffea_gpu_blob_measure(ffea_gpu_blob *blob, double *strain_energy, double *kinetic_energy);
 
+/* All of Blob::make_measurements (src/Blob.cpp:1066-1202), reduced on the device in FP64:
+ * out[0] strain energy, out[1] kinetic energy (0 for CG_nomass), out[2..4] centroid of all nodes,
+ * out[5] RMSD of all nodes from the reference positions (meso units). The reference positions are
+ * the positions at creation until ffea_gpu_blob_set_rmsd_reference (Blob::set_pos_0) replaces
+ * them with the current ones. */
+int ffea_gpu_blob_measurements(ffea_gpu_blob *blob, double out[6]);
+int ffea_gpu_blob_set_rmsd_reference(ffea_gpu_blob *blob);
+
 /* CG iterations of the last step and in total (0 for masslumped). */
 int ffea_gpu_blob_cg_iterations(ffea_gpu_blob *blob, int *last, long long *total);
 
@@ -154,6 +162,9 @@ int ffea_gpu_blob_cg_history(ffea_gpu_blob *blob, double *res2, int max_entries,
  * (FP64 path only). n_phases is 10. */
 #define FFEA_GPU_CG_PHASES 10
 int ffea_gpu_blob_cg_profile(ffea_gpu_blob *blob, double *phase_ns, int n_phases);
+
+/* Nodes of the reference numbering (vertices and midpoints) and elements of the blob. */
+int ffea_gpu_blob_counts(ffea_gpu_blob *blob, int *num_nodes, int *num_elements);
 
 /* Problem sizes: vertex nodes, elements, matrix 3x3 blocks. */
 int ffea_gpu_blob_sizes(ffea_gpu_blob *blob, int *num_linear_nodes, int *num_elements, long long *num_blocks);
@@ -279,6 +290,29 @@ int ffea_gpu_batch_set_config(ffea_gpu_batch *batch, int cg_threads, int threads
  * threads per row (1, 2, 4, 8) and keeps the fastest; positions, velocities and RNG states are not
  * changed. *best_ms (may be NULL) gets the best mean solve time. */
 int ffea_gpu_batch_tune(ffea_gpu_batch *batch, int solves, double *best_ms);
+
+/* ---------------------------------------------------------------------------
+ * .ffea script front-end: a World with the blob-step path only
+ * (World::init / World::run, src/World.cpp:54-620, 1747-2059).
+ *
+ * load: reads the script's <param> and <system> blocks (one conformation per
+ *   blob), builds each blob from its structure files, applies centroid /
+ *   rotation / velocity and the move into the simulation box, sets the RMSD
+ *   reference, seeds the stream from rng_seed (or, with restart = 1, from
+ *   checkpoint_in and the trajectory's last complete frame) and opens the
+ *   trajectory and measurement files. Features outside the path (calc_ssint,
+ *   calc_steric, calc_es, kinetics, springs, preComp, ctforces, rods, several
+ *   conformations, STATIC blobs) are refused with FFEA_GPU_EINPUT.
+ * run: steps step_initial .. num_steps; every `check` steps the stream state
+ *   goes to checkpoint_out before the forces, then the positions to the
+ *   trajectory (.ftj) and the measurements (.fm), as the reference writes them.
+ * ------------------------------------------------------------------------- */
+typedef struct ffea_gpu_world ffea_gpu_world;
+int ffea_gpu_world_load(const char *ffea_script, int precision, ffea_gpu_world **out);
+int ffea_gpu_world_run(ffea_gpu_world *world, long long *last_step);
+int ffea_gpu_world_num_blobs(ffea_gpu_world *world);
+ffea_gpu_blob *ffea_gpu_world_blob(ffea_gpu_world *world, int index);
+void ffea_gpu_world_destroy(ffea_gpu_world *world);
 
 /* Last CUDA error text for FFEA_GPU_ECUDA (static storage). */
 const char *ffea_gpu_last_error(void);

@@ -1,0 +1,144 @@
+""".ffea script front-end (ffea_gpu_world_*): World::init / World::run for the blob-step path.
+
+* A script run must follow exactly the trajectory of the same blob stepped through the C ABI
+  from the World's initial placement with the World's seed (bit-exact, FP64), write the
+  checkpoint state the reference would (six (rand() + rand()) mod m seeds from rng_seed, then
+  7 draws per element per step), and a frame / measurement row every `check` steps.
+* A restart from the checkpoint and the trajectory's last frame continues the same stream;
+  positions agree within the trajectory's 7 printed digits (the reference's own restart
+  test allows 5e-4).
+* Equipartition, as the reference's physics test checks it: the mean strain energy over the
+  measurement file is (3N - 6) kT / 2 within 3%.
+"""
+import ctypes as C
+import os
+import shutil
+
+import numpy as np
+import pytest
+
+import pyoracle as po
+from ffea_ci_demo_gb300 import build, lib
+from ffea_ci_demo_gb300.mesh import kuhn_cube, write_script, write_structure
+
+M1, M2 = 4294967087, 4294944443
+
+
+def seeds_from(rng_seed):
+    """World::init's package seed: srand(rng_seed), then (rand() + rand()) % m1 (x3) and % m2 (x3)."""
+    libc = C.CDLL(None)
+    libc.srand(C.c_uint(rng_seed))
+    return np.array([(libc.rand() + libc.rand()) % (M1 if k < 3 else M2) for k in range(6)], np.uint32)
+
+
+def make_script(tmp, name, n=2, **kw):
+    m = kuhn_cube(n, side=10.0, seed=4)
+    paths = write_structure(m, str(tmp), name)
+    path = os.path.join(str(tmp), name + ".ffea")
+    write_script(path, paths, scale=1e-9, **kw)
+    return m, paths, path
+
+
+def read_fm(path):
+    with open(path) as f:
+        lines = f.read().split("\n")
+    k = lines.index("Measurements:")
+    head = lines[k + 1].split()
+    rows = [list(map(float, ln.split())) for ln in lines[k + 2:] if ln.strip()]
+    return head, np.array(rows)
+
+
+def frames(path):
+    with open(path) as f:
+        txt = f.read()
+    return [int(ln.split("step")[1]) for ln in txt.split("\n") if ln.startswith("Blob 0, Conformation 0, step")]
+
+
+def test_script_refusals(tmp_path):
+    build.build()
+    _, paths, path = make_script(tmp_path, "c")
+    txt = open(path).read()
+    L = lib.load()
+    h = C.c_void_p()
+    for old, new in (("<calc_steric = 0>", "<calc_steric = 1>"), ("<calc_es = 0>", "<calc_es = 1>"),
+                     ("<calc_ssint = 0>", ""), ("<num_conformations = (1)>", "<num_conformations = (2)>"),
+                     ("<kT = ", "<colour = blue>\n\t<kT = ")):
+        bad = os.path.join(str(tmp_path), "bad.ffea")
+        with open(bad, "w") as f:
+            f.write(txt.replace(old, new))
+        assert L.ffea_gpu_world_load(bad.encode(), 0, C.byref(h)) == lib.EINPUT, (old, new)
+        assert lib.last_error()
+
+
+@pytest.mark.gpu
+def test_world_run_matches_blob_and_reference_seeding(gpu, oracle_built, tmp_path):
+    m, paths, path = make_script(tmp_path, "w", num_steps=20, check=5, rng_seed=777, kT=4.11e-21, calc_noise=1,
+                                 dt=1e-12)
+    w = lib.World(path)
+    x0 = w.blob(0).pos()
+    w.run()
+    xw = w.blob(0).pos()
+    seed = seeds_from(777)
+    b = lib.Blob.from_files(paths["node"], paths["top"], paths["mat"], paths["stokes"], paths["pin"], 1e-9,
+                            solver="CG_nomass", rng_state=seed, dt=1e-12, kT=4.11e-21, epsilon=1e-10, calc_noise=1,
+                            calc_stokes=0, max_iterations_cg=10000)
+    b.set_state(pos=x0)
+    b.update(21)  # steps 0..num_steps inclusive, as World::run
+    assert np.array_equal(xw, b.pos())
+    # the checkpoint holds the stream before step 20's forces: the seed advanced by 20 x 7T draws
+    o = po.OracleRng()
+    o.set_state(seed)
+    for _ in range(20 * 7 * m.n_elem):
+        o.rand_u01()
+    line = open(os.path.join(str(tmp_path), "w.fcp")).read().split("\n")
+    assert line[0].startswith("RNGStreams dedicated to the thermal stress:")
+    assert np.array_equal(np.array(line[1].split(), np.uint32), o.get_state())
+    assert frames(os.path.join(str(tmp_path), "w.ftj")) == [0, 5, 10, 15, 20]
+    head, rows = read_fm(os.path.join(str(tmp_path), "w.fm"))
+    assert head == ["Time", "StrainEnergy", "Centroid[0]", "Centroid[1]", "Centroid[2]", "RMSD"]
+    assert rows.shape == (5, 6) and rows[0, 5] == 0.0 and rows[-1, 5] > 0.0
+    # the system centroid sits at the centre of the simulation box (move_into_box)
+    assert np.allclose(rows[0, 2:5], rows[0, 2:5].mean(), rtol=1e-6)
+
+
+@pytest.mark.gpu
+def test_world_restart_continues_the_stream(gpu, tmp_path):
+    _, _, full = make_script(tmp_path, "full", num_steps=20, check=5, rng_seed=99)
+    wa = lib.World(full)
+    wa.run()
+    xa = wa.blob(0).pos()
+    ra = open(os.path.join(str(tmp_path), "full.fcp")).read()
+    _, _, first = make_script(tmp_path, "part", num_steps=10, check=5, rng_seed=99)
+    lib.World(first).run()
+    shutil.copy(os.path.join(str(tmp_path), "part.fcp"), os.path.join(str(tmp_path), "part_in.fcp"))
+    txt = open(first).read().replace("<restart = 0>", "<restart = 1>").replace(
+        "<num_steps = 10>", "<num_steps = 20>\n\t<checkpoint_in = part_in.fcp>\n\t<checkpoint_out = part.fcp>")
+    with open(first, "w") as f:
+        f.write(txt)
+    wb = lib.World(first)
+    wb.run()
+    xb = wb.blob(0).pos()
+    assert open(os.path.join(str(tmp_path), "part.fcp")).read() == ra
+    assert np.abs(xb - xa).max() <= 5e-4 * np.abs(xa).max()
+    assert frames(os.path.join(str(tmp_path), "part.ftj")) == [0, 5, 10, 15, 20]
+    assert read_fm(os.path.join(str(tmp_path), "part.fm"))[1].shape[0] == 5
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_equipartition_of_strain_energy(gpu, tmp_path, precision):
+    n = 2
+    steps, check = 120000, 300
+    _, _, path = make_script(tmp_path, "eq", n=n, num_steps=steps, check=check, rng_seed=2024, dt=1e-14,
+                             kT=4.11e-21, calc_noise=1, epsilon=1e-6)
+    import time
+    t0 = time.perf_counter()
+    lib.World(path, precision=precision).run()
+    print(f"{precision}: {(time.perf_counter() - t0) / steps * 1e6:.1f} us per step (27-node blob)")
+    head, rows = read_fm(os.path.join(str(tmp_path), "eq.fm"))
+    se = rows[40:, head.index("StrainEnergy")]
+    nodes = (n + 1) ** 3
+    want = 4.11e-21 * (3 * nodes - 6) / 2
+    dev = abs(se.mean() / want - 1)
+    print(precision, "equipartition: mean strain energy / (3N-6)kT/2 - 1 =", dev, "samples", se.size)
+    assert dev < 0.03
