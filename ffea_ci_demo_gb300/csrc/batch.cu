@@ -41,7 +41,7 @@ struct ffea_gpu_batch {
     int4 *tet;
     float *jinv, *G, *E, *A, *B, *vol0, *ef, *geom;
     double *last_det;
-    int *inc_ptr, *inc, *pinned, *slice_ptr, *rowlen, *bcol, *diagk, *src_ptr;
+    int *inc_ptr, *inc, *pinned, *slice_ptr, *rowlen, *bcol, *diagk, *src_ptr, *grp_slice;
     unsigned *src;
     double *drag = nullptr;
     float *val, *dinv, *diag;
@@ -184,6 +184,7 @@ int ffea_gpu_batch::init() {
     CK(mem.upload(&rowlen, h.rowlen));
     CK(mem.upload(&bcol, h.bcol));
     CK(mem.upload(&diagk, h.diagk));
+    CK(mem.upload(&grp_slice, h.grp_slice));
     CK(mem.upload(&src_ptr, h.src_ptr));
     CK(mem.upload(&src, h.src));
     if (!h.drag.empty()) CK(mem.upload(&drag, h.drag));
@@ -318,6 +319,7 @@ int ffea_gpu_batch::launch_forces() {
     CK(Launch<float>::element(ea, stream));
     AsmArgs<float> aa{};
     aa.N = h.N;
+    aa.nslots = h.nslots; aa.grp_slice = grp_slice;
     aa.slice_ptr = slice_ptr; aa.rowlen = rowlen; aa.bcol = bcol; aa.diagk = diagk;
     aa.src_ptr = src_ptr; aa.src = src;
     aa.geom = geom; aa.A = A; aa.B = B;

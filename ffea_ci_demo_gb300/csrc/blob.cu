@@ -155,7 +155,7 @@ struct BlobImpl final : ffea_gpu_blob {
     R *jinv, *G, *E, *A, *B, *vol0, *ef, *geom;
     double *last_det;
     int *inc_ptr, *inc, *pinned;
-    int *slice_ptr, *rowlen, *bcol, *diagk, *src_ptr;
+    int *slice_ptr, *rowlen, *bcol, *diagk, *src_ptr, *grp_slice;
     unsigned *src;
     double *drag = nullptr;
     R *val, *dinv;
@@ -273,6 +273,7 @@ struct BlobImpl final : ffea_gpu_blob {
         CK(mem.upload(&rowlen, h.rowlen));
         CK(mem.upload(&bcol, h.bcol));
         CK(mem.upload(&diagk, h.diagk));
+        CK(mem.upload(&grp_slice, h.grp_slice));
         CK(mem.upload(&src_ptr, h.src_ptr));
         CK(mem.upload(&src, h.src));
         if (!h.drag.empty()) CK(mem.upload(&drag, h.drag));
@@ -397,6 +398,7 @@ struct BlobImpl final : ffea_gpu_blob {
     int launch_assemble() {
         AsmArgs<R> aa{};
         aa.N = h.N;
+        aa.nslots = h.nslots; aa.grp_slice = grp_slice;
         aa.slice_ptr = slice_ptr; aa.rowlen = rowlen; aa.bcol = bcol; aa.diagk = diagk;
         aa.src_ptr = src_ptr; aa.src = src;
         aa.geom = geom; aa.A = A; aa.B = B;

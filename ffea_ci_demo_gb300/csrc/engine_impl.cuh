@@ -25,8 +25,8 @@ cudaError_t Launch<R>::element(const ElemArgs<R> &a, cudaStream_t s) {
 
 template <class R>
 cudaError_t Launch<R>::assemble(const AsmArgs<R> &a, cudaStream_t s) {
-    if (a.N <= 0) return cudaSuccess;
-    assemble_kernel<R><<<(a.N + ASM_THREADS - 1) / ASM_THREADS, ASM_THREADS, 0, s>>>(a);
+    if (a.N <= 0 || a.nslots <= 0) return cudaSuccess;
+    assemble_kernel<R><<<(unsigned)((a.nslots + ASM_THREADS - 1) / ASM_THREADS), ASM_THREADS, 0, s>>>(a);
     count_launch();
     return cudaGetLastError();
 }

@@ -148,6 +148,7 @@ struct HostModel {
     int nslices = 0;
     long long nslots = 0;
     std::vector<int> slice_ptr, rowlen, bcol, diagk;
+    std::vector<int> grp_slice;  // slice of each group of 32 slots
     std::vector<std::vector<int>> nbr;  // sorted neighbours per vertex
     std::vector<int> src_ptr;
     std::vector<unsigned> src;
@@ -347,6 +348,9 @@ inline int build_model(const ffea_gpu_mesh *mesh, const ffea_gpu_params *p, Host
         h.slice_ptr[s + 1] = h.slice_ptr[s] + 32 * w;
     }
     h.nslots = h.slice_ptr[h.nslices];
+    h.grp_slice.assign((size_t)(h.nslots / 32), 0);
+    for (int s = 0; s < h.nslices; ++s)
+        for (int gidx = h.slice_ptr[s] / 32; gidx < h.slice_ptr[s + 1] / 32; ++gidx) h.grp_slice[gidx] = s;
     if (h.nslots >= (1ll << 31)) {
         g_last_error = "matrix too large for 32-bit slot indices";
         return FFEA_GPU_EINPUT;

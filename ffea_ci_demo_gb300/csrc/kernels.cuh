@@ -231,6 +231,8 @@ __global__ void __launch_bounds__(128) element_kernel(ElemArgs<R> g) {
 template <class R>
 struct AsmArgs {
     int N;
+    long long nslots;       // 32 x the slices' widths
+    const int *grp_slice;   // slice of each group of 32 slots
     const int *slice_ptr, *rowlen, *bcol, *diagk;
     const int *src_ptr;
     const unsigned *src;    // (element << 4) | (slot_a << 2) | slot_b ; 0xffffffff = identity
@@ -244,52 +246,54 @@ struct AsmArgs {
 
 constexpr unsigned SRC_IDENTITY = 0xffffffffu;
 
+// One thread per matrix slot (3x3 block): the slot's sources summed from zero in registration order,
+// so each FP64 value rounds as sum_all_sources' does; the diagonal slot of a row also gives the Jacobi
+// inverse. Padding slots past a row's length are never read and are skipped.
 template <class R>
 __global__ void __launch_bounds__(128) assemble_kernel(AsmArgs<R> g) {
-    const int a = blockIdx.x * blockDim.x + threadIdx.x;
-    if (a >= g.N || g.st->abort) return;
-    const int s = a >> 5, lane = a & 31;
-    const int base = g.slice_ptr[s];
-    const int len = g.rowlen[a];
-    const int dk = g.diagk[a];
-    R *vbase = g.val + 9 * (size_t)base + lane;
-    for (int k = 0; k < len; ++k) {
-        const int slot = base + 32 * k + lane;
-        R v[9];
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (t >= g.nslots || g.st->abort) return;
+    const int s = g.grp_slice[t >> 5];
+    const int lane = (int)(t & 31);
+    const int a = 32 * s + lane;
+    if (a >= g.N) return;
+    const int k = (int)((t >> 5) - (g.slice_ptr[s] >> 5));
+    if (k >= g.rowlen[a]) return;
+    const long long slot = t;
+    R v[9];
 #pragma unroll
-        for (int c = 0; c < 9; ++c) v[c] = (R)0.0;
-        for (int q = g.src_ptr[slot]; q < g.src_ptr[slot + 1]; ++q) {
-            const unsigned code = g.src[q];
-            if (code == SRC_IDENTITY) {
-                v[0] += (R)1; v[4] += (R)1; v[8] += (R)1;
-                continue;
-            }
-            const int e = (int)(code >> 4), pa = (code >> 2) & 3, pb = code & 3;
-            const R *gm = g.geom + 16 * (size_t)e;
-            R dpsi[12];
-#pragma unroll
-            for (int m = 0; m < 12; ++m) dpsi[m] = gm[m];
-            const R vol = gm[12], A = g.A[e], B = g.B[e];
-#pragma unroll
-            for (int i = 0; i < 3; ++i)
-#pragma unroll
-                for (int j = 0; j < 3; ++j) v[3 * i + j] += visc_entry<R>(dpsi, A, B, vol, pa + 4 * i, pb + 4 * j);
+    for (int c = 0; c < 9; ++c) v[c] = (R)0.0;
+    for (int q = g.src_ptr[slot]; q < g.src_ptr[slot + 1]; ++q) {
+        const unsigned code = g.src[q];
+        if (code == SRC_IDENTITY) {
+            v[0] += (R)1; v[4] += (R)1; v[8] += (R)1;
+            continue;
         }
-        if (k == dk) {
-            if (g.drag) {
-                const R dr = (R)g.drag[a];
-                v[0] += dr; v[4] += dr; v[8] += dr;
-            }
-            // calc_inverse_diagonal (src/SparseMatrixFixedPattern.cpp:305-312)
-            g.dinv[4 * a] = (R)1.0 / v[0];
-            g.dinv[4 * a + 1] = (R)1.0 / v[4];
-            g.dinv[4 * a + 2] = (R)1.0 / v[8];
-            if (g.diag) { g.diag[4 * a] = v[0]; g.diag[4 * a + 1] = v[4]; g.diag[4 * a + 2] = v[8]; }
-        }
-        R *vp = vbase + (size_t)32 * 9 * k;
+        const int e = (int)(code >> 4), pa = (code >> 2) & 3, pb = code & 3;
+        const R *gm = g.geom + 16 * (size_t)e;
+        R dpsi[12];
 #pragma unroll
-        for (int c = 0; c < 9; ++c) vp[32 * c] = v[c];
+        for (int m = 0; m < 12; ++m) dpsi[m] = gm[m];
+        const R vol = gm[12], A = g.A[e], B = g.B[e];
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int j = 0; j < 3; ++j) v[3 * i + j] += visc_entry<R>(dpsi, A, B, vol, pa + 4 * i, pb + 4 * j);
     }
+    if (k == g.diagk[a]) {
+        if (g.drag) {
+            const R dr = (R)g.drag[a];
+            v[0] += dr; v[4] += dr; v[8] += dr;
+        }
+        // calc_inverse_diagonal (src/SparseMatrixFixedPattern.cpp:305-312)
+        g.dinv[4 * a] = (R)1.0 / v[0];
+        g.dinv[4 * a + 1] = (R)1.0 / v[4];
+        g.dinv[4 * a + 2] = (R)1.0 / v[8];
+        if (g.diag) { g.diag[4 * a] = v[0]; g.diag[4 * a + 1] = v[4]; g.diag[4 * a + 2] = v[8]; }
+    }
+    R *vp = g.val + 9 * (size_t)g.slice_ptr[s] + 32 * 9 * (size_t)k + lane;
+#pragma unroll
+    for (int c = 0; c < 9; ++c) vp[32 * c] = v[c];
 }
 
 // ---------------------------------------------------------------------------

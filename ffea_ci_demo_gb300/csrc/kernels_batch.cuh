@@ -137,8 +137,7 @@ __global__ void __launch_bounds__(BATCH_MAX_THREADS) cg_batch_kernel(const __gri
     if (!ok) return;
     grid_sum_df<MIXED_GATHER_NP>(spart, gsz, gsz, s_sc);
     const double f2 = s_sc[0];
-    if (threadIdx.x == 0) mixed_setup(s_desc, s_sc, s_A6, s_tau, s_Om, &s_beta, &s_conv);
-    __syncthreads();
+    mixed_setup(s_desc, s_sc, s_A6, s_tau, s_Om, &s_beta, &s_conv);
     // r = f^ (projected), initial r.z
     float acc0[1] = {0.f};
     BATCH_NODE_LOOP(row0, nrows, rank, gsz, a) {

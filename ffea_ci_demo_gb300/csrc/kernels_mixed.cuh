@@ -112,58 +112,75 @@ __global__ void __launch_bounds__(256) gather_mixed_kernel(GatherArgs<R> g) {
     }
 }
 
-// thread 0 of every block: G = Z^T D Z from the moments, its inverse, and the coefficients of the
-// projection of the right-hand side (kept out of line: it runs once per solve)
+// The whole block, once per solve: G = Z^T D Z from the moments M, G^{-1} by Gauss-Jordan on the augmented
+// [G | I] in shared memory (one thread per entry, one pivot at a time), A6 = modes^T G^{-1} modes, and
+// (tau, Omega) of D Z c0 with c0 = G^{-1} Z^T f. Every thread of the block must call it; the results are
+// in shared memory after it returns.
 template <class A>
-__device__ __noinline__ void mixed_setup(const A &g, const double *s_sc, double *s_A6, float *s_tau,
-                                         float *s_Om, float *s_beta, int *s_conv) {
-        const int k = g.nmodes;
-        double M[6][6];
-        int idx = 7;
-        for (int i = 0; i < 6; ++i)
-            for (int j = i; j < 6; ++j, ++idx) M[i][j] = M[j][i] = s_sc[idx];
-        double G[36], Ginv[36];
+__device__ void mixed_setup(const A &g, const double *s_sc, double *s_A6, float *s_tau, float *s_Om, float *s_beta,
+                            int *s_conv) {
+    __shared__ double sM[36], sAug[6][12], sF[6], sV[6], sC[6], sPiv;
+    const int t = threadIdx.x, k = g.nmodes;
+    if (t < 36) {
+        const int i = t / 6, j = t % 6, lo = i < j ? i : j, hi = i < j ? j : i;
+        // packed upper triangle: row lo starts at 7 + lo*6 - lo*(lo-1)/2
+        sM[t] = s_sc[7 + lo * 6 - (lo * (lo - 1)) / 2 + (hi - lo)];
+    }
+    __syncthreads();
+    if (t < 36) {
+        const int i = t / 6, j = t % 6;
+        double sum = 0.0;
+        if (i < k && j < k)
+            for (int p = 0; p < 6; ++p)
+                for (int q = 0; q < 6; ++q) sum += g.modes[6 * i + p] * sM[6 * p + q] * g.modes[6 * j + q];
+        sAug[i][j] = sum;
+        sAug[i][6 + j] = (i == j) ? 1.0 : 0.0;
+    }
+    __syncthreads();
+    for (int col = 0; col < k; ++col) {
+        if (t == 0) sPiv = sAug[col][col];
+        __syncthreads();
+        if (t < 12) sAug[col][t] /= sPiv;
+        __syncthreads();
+        if (t < 6) sF[t] = sAug[t][col];
+        __syncthreads();
+        if (t < 72) {
+            const int i = t / 12, j = t % 12;
+            if (i != col && i < k) sAug[i][j] -= sF[i] * sAug[col][j];
+        }
+        __syncthreads();
+    }
+    if (t < 36) {
+        const int p = t / 6, q = t % 6;
+        double sum = 0.0;
         for (int i = 0; i < k; ++i)
-            for (int j = 0; j < k; ++j) {
-                double sum = 0.0;
-                for (int p = 0; p < 6; ++p)
-                    for (int q = 0; q < 6; ++q) sum += g.modes[6 * i + p] * M[p][q] * g.modes[6 * j + q];
-                G[6 * i + j] = sum;
-                Ginv[6 * i + j] = (i == j) ? 1.0 : 0.0;
-            }
-        for (int col = 0; col < k; ++col) {  // Gauss-Jordan on the SPD Gram matrix
-            const double piv = G[6 * col + col];
-            for (int j = 0; j < k; ++j) { G[6 * col + j] /= piv; Ginv[6 * col + j] /= piv; }
-            for (int i = 0; i < k; ++i) {
-                if (i == col) continue;
-                const double fct = G[6 * i + col];
-                for (int j = 0; j < k; ++j) { G[6 * i + j] -= fct * G[6 * col + j]; Ginv[6 * i + j] -= fct * Ginv[6 * col + j]; }
-            }
-        }
-        // A6 = modes^T G^{-1} modes: maps the moments (S1, S2) of a vector v to the (tau, Omega) of
-        // D Z G^{-1} Z^T D v, and S . A6 S = v^T D Z G^{-1} Z^T D v
-        for (int p = 0; p < 6; ++p)
-            for (int q = 0; q < 6; ++q) {
-                double sum = 0.0;
-                for (int i = 0; i < k; ++i)
-                    for (int j = 0; j < k; ++j) sum += g.modes[6 * i + p] * Ginv[6 * i + j] * g.modes[6 * j + q];
-                s_A6[6 * p + q] = sum;
-            }
-        // c0 = G^{-1} Z^T f; tau, Omega of D Z c0
-        double v[6], tau[3] = {0, 0, 0}, Om[3] = {0, 0, 0};
-        for (int i = 0; i < k; ++i) {
-            const double *m = g.modes + 6 * i;
-            v[i] = m[0] * s_sc[1] + m[1] * s_sc[2] + m[2] * s_sc[3] + m[3] * s_sc[4] + m[4] * s_sc[5] + m[5] * s_sc[6];
-        }
-        for (int i = 0; i < k; ++i) {
-            double c = 0.0;
-            for (int j = 0; j < k; ++j) c += Ginv[6 * i + j] * v[j];
-            for (int t = 0; t < 3; ++t) { tau[t] += c * g.modes[6 * i + t]; Om[t] += c * g.modes[6 * i + 3 + t]; }
-        }
-        for (int t = 0; t < 3; ++t) { s_tau[t] = (float)tau[t]; s_Om[t] = (float)Om[t]; }
+            for (int j = 0; j < k; ++j) sum += g.modes[6 * i + p] * sAug[i][6 + j] * g.modes[6 * j + q];
+        s_A6[t] = sum;
+    }
+    if (t < 6) {
+        const double *m = g.modes + 6 * t;
+        sV[t] = (t < k) ? m[0] * s_sc[1] + m[1] * s_sc[2] + m[2] * s_sc[3] + m[3] * s_sc[4] + m[4] * s_sc[5] +
+                              m[5] * s_sc[6]
+                        : 0.0;
+    }
+    __syncthreads();
+    if (t < 6) {
+        double c = 0.0;
+        for (int j = 0; j < k; ++j) c += sAug[t][6 + j] * sV[j];
+        sC[t] = (t < k) ? c : 0.0;
+    }
+    __syncthreads();
+    if (t < 6) {
+        double sum = 0.0;
+        for (int i = 0; i < k; ++i) sum += sC[i] * g.modes[6 * i + t];
+        if (t < 3) s_tau[t] = (float)sum; else s_Om[t - 3] = (float)sum;
+    }
+    if (t == 0) {
         *s_beta = 0.f;
         *s_conv = 0;
     }
+    __syncthreads();
+}
 
 template <class R>
 __global__ void __launch_bounds__(1024, 1) cg_mixed_kernel(const __grid_constant__ CgArgs<R> g) {
@@ -181,8 +198,7 @@ __global__ void __launch_bounds__(1024, 1) cg_mixed_kernel(const __grid_constant
     // set-up: G = Z^T D Z from the moments M, projected right-hand side
     grid_sum_df<MIXED_GATHER_NP>(reinterpret_cast<const float2 *>(g.init_partials), g.init_stride, g.n_init, s_sc);
     const double f2 = s_sc[0];
-    if (threadIdx.x == 0) mixed_setup(g, s_sc, s_A6, s_tau, s_Om, &s_beta, &s_conv);
-    __syncthreads();
+    mixed_setup(g, s_sc, s_A6, s_tau, s_Om, &s_beta, &s_conv);
     float acc0[1] = {0.f};
     FFEA_NODE_LOOP(g, a) {
         float r0 = g.r[4 * a], r1 = g.r[4 * a + 1], r2 = g.r[4 * a + 2];
