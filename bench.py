@@ -12,7 +12,8 @@ A second workload (`--workload batch`, and the "batched" object of the default l
 replica ensemble: 256 Kuhn cubes with cells per side log-uniform in [8, 32] (seeded), per-blob
 G ~ U[1e8, 1e9] Pa and K = 3.9 G, all advanced by one graph-captured step (mixed precision).
 
-The "adjoint" object times the gradient of a 200-step window of a 20^3-cell cube with lognormal
+The "scale" object runs the 64^3-cell cube (1,572,864 tets), CG_nomass and mass-lumped, mixed
+against FP64. The "adjoint" object times the gradient of a 200-step window of a 20^3-cell cube with lognormal
 per-element moduli (checkpoints every 20 steps): seconds per step of gradient and its cost relative
 to the forward window.
 
@@ -389,6 +390,59 @@ def run_adjoint(args) -> dict:
     return out
 
 
+def run_scale(args) -> dict:
+    """Configuration 4: the 64^3-cell cube (1,572,864 tets, 274,625 nodes, side 320 nm), CG_nomass and
+    mass-lumped, mixed precision against the plain FP64 path: node-steps/s, HBM GB/s of the CG, CG
+    iterations per step, and the mixed path's kT = 0 position error against the FP64 path."""
+    import numpy as np
+
+    from ffea_ci_demo_gb300 import build, lib
+    from ffea_ci_demo_gb300.mesh import apply_shear, counts, kuhn_cube
+
+    build.build()
+    n = args.scale_cells
+    mesh = kuhn_cube(n, side=5.0 * n, seed=12345)
+    c = counts(n)
+    N = c["N"]
+    peak, peak_kind = measured_peak()
+    out = {"workload": f"kuhn-cube-{n}: {c['T']} tets, {N} nodes, side {5 * n} nm, kT=4.11e-21 J",
+           "cells_per_side": n, "tets": c["T"], "nodes": N}
+    for solver, dt in (("CG_nomass", 1e-12), ("masslumped", args.scale_lumped_dt)):
+        res = {"dt": dt}
+        for prec in ("mixed", "fp64"):
+            b = lib.Blob(mesh, precision=prec, **dict(PHYS, solver=solver, dt=dt))
+            b.update(2)
+            it0 = b.cg_iterations()[1]
+            k = args.scale_steps
+            t = b.update_timed(k, FLUSH_BYTES)
+            it = (b.cg_iterations()[1] - it0) / k
+            r = {"value": N * k / (t["ms"] / 1e3), "ms_per_step": t["ms"] / k, "cg_iters_per_step": it,
+                 "phase_ms_per_step": {q: v / k for q, v in t["phase_ms"].items()}}
+            if solver == "CG_nomass":
+                p = 4 if prec == "mixed" else 8
+                cg_ms = t["phase_ms"]["cg"] / k
+                model = it * cg_bytes_per_iteration(n, p)
+                r["roofline_cg"] = {"achieved": model / (cg_ms / 1e3) / 1e9, "peak": peak, "unit": "GB/s",
+                                    "frac": model / (cg_ms / 1e3) / 1e9 / peak, "peak_source": peak_kind}
+            res[prec] = r
+            b.close()
+        res["speedup_mixed_vs_fp64"] = res["mixed"]["value"] / res["fp64"]["value"]
+        # kT = 0 error of the mixed path against the FP64 path (same initial shear)
+        p0 = apply_shear(mesh, 0.02, seed=3) * (mesh.scale / MESO_LENGTH)
+        xs = {}
+        for prec in ("fp64", "mixed"):
+            b = lib.Blob(mesh, precision=prec, **dict(PHYS, solver=solver, dt=dt, kT=0.0, calc_noise=0))
+            b.set_state(pos=p0)
+            b.update(args.scale_error_steps)
+            xs[prec] = b.pos()
+            b.close()
+        res["kT0_error"] = {"steps": args.scale_error_steps,
+                            "max_abs_disp_err_rel_to_max_disp":
+                                float(np.abs(xs["mixed"] - xs["fp64"]).max() / np.abs(xs["fp64"] - p0).max())}
+        out[solver] = res
+    return out
+
+
 def cpu_sample(n: int, threads: int, budget_s: float, max_steps: int, warmup: int = 1):
     """Time the oracle (reference algorithm, release optimisation, OpenMP) on the same workload."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
@@ -436,6 +490,11 @@ def main():
     ap.add_argument("--no-fp64-sample", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--adjoint-steps", type=int, default=200)
+    ap.add_argument("--no-scale", action="store_true")
+    ap.add_argument("--scale-cells", type=int, default=64)
+    ap.add_argument("--scale-steps", type=int, default=5)
+    ap.add_argument("--scale-error-steps", type=int, default=20)
+    ap.add_argument("--scale-lumped-dt", type=float, default=1e-12)
     ap.add_argument("--no-adjoint", action="store_true")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
@@ -517,6 +576,8 @@ def main():
         args.steps = k
         if not args.no_adjoint:
             line["adjoint"] = run_adjoint(args)
+        if not args.no_scale:
+            line["scale"] = run_scale(args)
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_sample(args.cells, os.cpu_count() or 1, budget_s=20.0, max_steps=3)
         line["cpu_baseline"].pop("seconds")

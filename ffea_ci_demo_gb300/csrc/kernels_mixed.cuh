@@ -117,7 +117,7 @@ __global__ void __launch_bounds__(256) gather_mixed_kernel(GatherArgs<R> g) {
 // (tau, Omega) of D Z c0 with c0 = G^{-1} Z^T f. Every thread of the block must call it; the results are
 // in shared memory after it returns.
 template <class A>
-__device__ void mixed_setup(const A &g, const double *s_sc, double *s_A6, float *s_tau, float *s_Om, float *s_beta,
+__device__ __noinline__ void mixed_setup(const A &g, const double *s_sc, double *s_A6, float *s_tau, float *s_Om, float *s_beta,
                             int *s_conv) {
     __shared__ double sM[36], sAug[6][12], sF[6], sV[6], sC[6], sPiv;
     const int t = threadIdx.x, k = g.nmodes;
