@@ -28,6 +28,7 @@
 
 #include "engine.h"
 #include "blob_iface.h"
+#include "ctforces.h"
 #include "host_model.h"
 #include "kernels_mixed.cuh"
 
@@ -174,6 +175,12 @@ struct BlobImpl final : ffea_gpu_blob {
     double *p0 = nullptr, *m0 = nullptr, *meas_part = nullptr, *meas_out = nullptr;
     int *mid_a = nullptr, *mid_b = nullptr;
     int meas_blocks = 0;
+    // constant forces (ctforces file): per vertex / midpoint linear forces, surface faces and sets
+    Arena ctf_mem;
+    double *ctf_node = nullptr, *ctf_mid = nullptr, *ctf_ff = nullptr;
+    int *vface_ptr = nullptr, *vface = nullptr, *mface_ptr = nullptr, *mface = nullptr;
+    SurfArgs surf{};
+    bool lin_from_ctf = false, has_ctf = false;
     // Stokes noise (calc_stokes with calc_noise)
     MrgJump *sn_chunk_jump = nullptr, *sn_lane_jump = nullptr;
     int *sn_node_orig = nullptr, *sn_mid_orig = nullptr, *sn_lin_ptr = nullptr;
@@ -358,11 +365,8 @@ struct BlobImpl final : ffea_gpu_blob {
             for (size_t m = 0; m < h.mid_nodes.size(); ++m) mdrag[m] = h.drag_all[h.mid_nodes[m]];
             CK(mem.upload(&sn_mid_orig, h.mid_nodes));
             CK(mem.upload(&sn_mid_drag, mdrag));
-            CK(mem.upload(&sn_lin_ptr, h.lin_ptr));
-            std::vector<int4> ev(h.lin_ev.size() / 4);
-            for (size_t k = 0; k < ev.size(); ++k)
-                ev[k] = make_int4(h.lin_ev[4 * k], h.lin_ev[4 * k + 1], h.lin_ev[4 * k + 2], -1);
-            CK(mem.upload(&sn_lin_ev, ev));
+            int lrc0 = upload_linearise(mem);
+            if (lrc0) return lrc0;
         }
         int lrc = set_rng_layout(element_draws() + stokes_draws(), element_draws());
         if (lrc) return lrc;
@@ -450,9 +454,9 @@ struct BlobImpl final : ffea_gpu_blob {
         ga.partials = init_partials; ga.stride = gather_blocks; ga.st = st; ga.gb = gb;
         ga.dpos = dpos; ga.px = px; ga.py = py; ga.pz = pz; ga.diag = diag;
         ga.xc[0] = xc[0]; ga.xc[1] = xc[1]; ga.xc[2] = xc[2];
-        if (sn_lin_ptr) {
-            StokesNoise &sn = ga.sn;
-            sn.on = 1;
+        {
+            NodeForces &sn = ga.sn;
+            sn.noise = sn_chunk_jump != nullptr;
             sn.kT = p.kT;
             sn.dt = p.dt;
             sn.rng_state = rng_state;
@@ -462,9 +466,16 @@ struct BlobImpl final : ffea_gpu_blob {
             sn.node_drag = drag;
             sn.mid_orig = sn_mid_orig;
             sn.mid_drag = sn_mid_drag;
+            sn.node_ctf = ctf_node;
+            sn.mid_ctf = ctf_mid;
+            sn.vface_ptr = vface_ptr; sn.vface = vface;
+            sn.mface_ptr = mface_ptr; sn.mface = mface;
+            sn.ff = ctf_ff;
             sn.lin_ptr = sn_lin_ptr;
             sn.lin_ev = sn_lin_ev;
+            sn.on = sn.noise || sn.lin_ptr != nullptr;
         }
+        if (surf.nsets > 0) CK(launch_surface_forces(surf, stream));
         CK(Launch<R>::gather(ga, gather_blocks, stream));
         if ((rc = mark(3))) return rc;
         if (p.solver != FFEA_GPU_MASSLUMPED && (rc = launch_cg(init_partials, gather_blocks))) return rc;
@@ -769,6 +780,118 @@ struct BlobImpl final : ffea_gpu_blob {
         }
     }
 
+    int upload_linearise(Arena &m) {
+        CK(m.upload(&sn_lin_ptr, h.lin_ptr));
+        std::vector<int4> ev(h.lin_ev.size() / 4);
+        for (size_t k = 0; k < ev.size(); ++k)
+            ev[k] = make_int4(h.lin_ev[4 * k], h.lin_ev[4 * k + 1], h.lin_ev[4 * k + 2], -1);
+        CK(m.upload(&sn_lin_ev, ev));
+        return FFEA_GPU_OK;
+    }
+
+    int load_ctforces(const char *ctf_file, const char *surf_file, int blob_index) override {
+        CtfModel cm;
+        std::string err;
+        int rc = ffea::host::load_ctforces(ctf_file, surf_file, blob_index, h.n_all, cm, err);
+        if (rc) {
+            g_last_error = err;
+            return rc;
+        }
+        const int N = h.N, M = (int)h.mid_nodes.size(), n = h.n_all;
+        std::vector<int> mid_id(n, -1);
+        for (int m = 0; m < M; ++m) mid_id[h.mid_nodes[m]] = m;
+        bool mid_force = false, any_lin = false;
+        std::vector<double> vn(3 * (size_t)N, 0.0), vm(3 * (size_t)std::max(M, 1), 0.0);
+        for (int k = 0; k < N; ++k)
+            for (int c = 0; c < 3; ++c) vn[3 * (size_t)k + c] = cm.lin[3 * (size_t)h.node_of[k] + c];
+        for (int m = 0; m < M; ++m) {
+            for (int c = 0; c < 3; ++c) vm[3 * (size_t)m + c] = cm.lin[3 * (size_t)h.mid_nodes[m] + c];
+            mid_force = mid_force || cm.has_lin[h.mid_nodes[m]];
+        }
+        for (int i = 0; i < n; ++i) any_lin = any_lin || cm.has_lin[i];
+        if (lin_from_ctf) {  // the replay lived with the previous constant forces
+            sn_lin_ptr = nullptr;
+            sn_lin_ev = nullptr;
+            lin_from_ctf = false;
+        }
+        ctf_mem.clear();
+        ctf_node = ctf_mid = ctf_ff = nullptr;
+        vface_ptr = vface = mface_ptr = mface = nullptr;
+        surf = SurfArgs{};
+        if (any_lin) {
+            CK(ctf_mem.upload(&ctf_node, vn));
+            if (mid_force) CK(ctf_mem.upload(&ctf_mid, vm));
+        }
+        const int nsets = (int)cm.set_ptr.size() - 1;
+        if (nsets > 0) {
+            const int nf = (int)cm.face_nodes.size() / 3;
+            std::vector<int2> corner(3 * (size_t)nf);
+            for (int f = 0; f < nf; ++f)
+                for (int k = 0; k < 3; ++k) {
+                    const int x = cm.face_nodes[3 * (size_t)f + k];
+                    corner[3 * (size_t)f + k] = h.lin_of[x] >= 0 ? make_int2(h.lin_of[x], h.lin_of[x])
+                                                                 : make_int2(h.mid_a[mid_id[x]], h.mid_b[mid_id[x]]);
+                }
+            // sets holding each face (set order); faces holding each node (face order), forced faces only
+            std::vector<std::vector<int>> fs(nf), vf(N), mf(M);
+            for (int s2 = 0; s2 < nsets; ++s2)
+                for (int k = cm.set_ptr[s2]; k < cm.set_ptr[s2 + 1]; ++k) fs[cm.set_faces[k]].push_back(s2);
+            for (int f = 0; f < nf; ++f) {
+                if (fs[f].empty()) continue;
+                for (int k = 0; k < 3; ++k) {
+                    const int x = cm.face_nodes[3 * (size_t)f + k];
+                    if (h.lin_of[x] >= 0) vf[h.lin_of[x]].push_back(f);
+                    else { mf[mid_id[x]].push_back(f); mid_force = true; }
+                }
+            }
+            auto csr = [](const std::vector<std::vector<int>> &v, std::vector<int> &ptr, std::vector<int> &idx) {
+                ptr.assign(v.size() + 1, 0);
+                for (size_t i = 0; i < v.size(); ++i) ptr[i + 1] = ptr[i] + (int)v[i].size();
+                idx.clear();
+                for (const auto &x : v) idx.insert(idx.end(), x.begin(), x.end());
+                if (idx.empty()) idx.push_back(0);
+            };
+            std::vector<int> fsp, fsi, vfp, vfi, mfp, mfi;
+            csr(fs, fsp, fsi);
+            csr(vf, vfp, vfi);
+            csr(mf, mfp, mfi);
+            int *d_set_ptr, *d_set_faces, *d_fsp, *d_fsi;
+            int2 *d_corner;
+            double *d_setF, *d_total;
+            CK(ctf_mem.upload(&d_set_ptr, cm.set_ptr));
+            CK(ctf_mem.upload(&d_set_faces, cm.set_faces));
+            CK(ctf_mem.upload(&d_setF, cm.set_force));
+            CK(ctf_mem.upload(&d_corner, corner));
+            CK(ctf_mem.upload(&d_fsp, fsp));
+            CK(ctf_mem.upload(&d_fsi, fsi));
+            CK(ctf_mem.alloc(&d_total, (size_t)nsets));
+            CK(ctf_mem.alloc(&ctf_ff, 3 * (size_t)nf));
+            CK(ctf_mem.upload(&vface_ptr, vfp));
+            CK(ctf_mem.upload(&vface, vfi));
+            if (M > 0) {
+                CK(ctf_mem.upload(&mface_ptr, mfp));
+                CK(ctf_mem.upload(&mface, mfi));
+            }
+            surf.nsets = nsets;
+            surf.nfaces = nf;
+            surf.set_ptr = d_set_ptr; surf.set_faces = d_set_faces; surf.set_force = d_setF;
+            surf.corner = d_corner;
+            surf.face_set_ptr = d_fsp; surf.face_set = d_fsi;
+            surf.px = px; surf.py = py; surf.pz = pz;
+            surf.set_total = d_total; surf.ff = ctf_ff;
+            surf.st = st;
+        }
+        // midpoints that carry force need the linearisation replay (already there with Stokes noise)
+        if (mid_force && !sn_lin_ptr) {
+            build_linearise_events(h);
+            int lrc = upload_linearise(ctf_mem);
+            if (lrc) return lrc;
+            lin_from_ctf = true;
+        }
+        has_ctf = any_lin || nsets > 0;
+        return FFEA_GPU_OK;
+    }
+
     // the step's stream advance, and where the Stokes draws start (node i of the reference numbering draws
     // 3 numbers from stokes_base + 3i after the step's state)
     int set_rng_layout(unsigned long long step_draws, unsigned long long stokes_base) override {
@@ -797,6 +920,10 @@ struct BlobImpl final : ffea_gpu_blob {
         }
         if (window <= 0 || every <= 0) {
             g_last_error = "adjoint window and checkpoint interval must be positive";
+            return FFEA_GPU_EINPUT;
+        }
+        if (has_ctf) {
+            g_last_error = "the adjoint does not differentiate constant forces";
             return FFEA_GPU_EINPUT;
         }
         adj_release();
@@ -1198,6 +1325,12 @@ int ffea_gpu_blob_set_state(ffea_gpu_blob *b, const double *pos, const double *v
 int ffea_gpu_blob_measure(ffea_gpu_blob *b, double *se, double *ke) {
     if (!b) return FFEA_GPU_EINPUT;
     return b->measure(se, ke);
+}
+
+int ffea_gpu_blob_load_ctforces(ffea_gpu_blob *b, const char *ctforces_file, const char *surface_file,
+                                int blob_index) {
+    if (!b || !ctforces_file || blob_index < 0) return FFEA_GPU_EINPUT;
+    return b->load_ctforces(ctforces_file, surface_file, blob_index);
 }
 
 int ffea_gpu_blob_measurements(ffea_gpu_blob *b, double out[6]) {

@@ -45,6 +45,8 @@ struct ffea_gpu_blob {
     // several blobs on one stream (the reference's single-thread order over a World's blobs): each step
     // advances the blob's stream by step_draws, and its Stokes draws start stokes_base after its elements'
     virtual int set_rng_layout(unsigned long long step_draws, unsigned long long stokes_base) = 0;
+    // constant forces of the reference's ctforces file for this blob (Blob::load_ctforces)
+    virtual int load_ctforces(const char *ctforces_file, const char *surface_file, int blob_index) = 0;
     // draws of one step: 7 per element (noise on) and 3 per node of the reference numbering (Stokes noise)
     unsigned long long element_draws() const { return p.calc_noise == 1 ? 7ull * (unsigned long long)h.T : 0ull; }
     unsigned long long stokes_draws() const {

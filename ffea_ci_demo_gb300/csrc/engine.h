@@ -42,6 +42,8 @@ extern template struct AdjLaunch<double>;
 extern template struct AdjLaunch<float>;
 
 cudaError_t launch_finish_step(uint32_t *rng_state, const MrgJump *step_jump, DevStatus *st, cudaStream_t s);
+// the constant surface forces of a step (surf_set_kernel, then surf_face_kernel)
+cudaError_t launch_surface_forces(const SurfArgs &a, cudaStream_t s);
 
 // launchers of the batch kernels (mixed precision; instantiated in engine_mixed.cu)
 struct BatchLaunch {

@@ -19,6 +19,38 @@ __global__ void finish_step_kernel(uint32_t *rng_state, const MrgJump *step_jump
     st->steps_done += 1;
 }
 
+// one thread per set: the sum of its faces' areas in file order (totalArea of apply_ctforces)
+__global__ void __launch_bounds__(128) surf_set_kernel(SurfArgs g) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= g.nsets || g.st->abort) return;
+    double total = 0.0;
+    for (int k = g.set_ptr[s]; k < g.set_ptr[s + 1]; ++k) total += face_area(g, g.set_faces[k]);
+    g.set_total[s] = total;
+}
+
+// one thread per face: its force from every set holding it, in set order (Face::add_force_to_node)
+__global__ void __launch_bounds__(128) surf_face_kernel(SurfArgs g) {
+    const int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= g.nfaces || g.st->abort) return;
+    double out[3] = {0.0, 0.0, 0.0};
+    if (g.face_set_ptr[f] < g.face_set_ptr[f + 1]) {
+        const double area = face_area(g, f);
+        for (int k = g.face_set_ptr[f]; k < g.face_set_ptr[f + 1]; ++k) {
+            const int s = g.face_set[k];
+            const double w = area / (3 * g.set_total[s]);
+            for (int c = 0; c < 3; ++c) out[c] += w * g.set_force[3 * (size_t)s + c];
+        }
+    }
+    for (int c = 0; c < 3; ++c) g.ff[3 * (size_t)f + c] = out[c];
+}
+
+cudaError_t launch_surface_forces(const SurfArgs &a, cudaStream_t s) {
+    surf_set_kernel<<<(a.nsets + 127) / 128, 128, 0, s>>>(a);
+    surf_face_kernel<<<(a.nfaces + 127) / 128, 128, 0, s>>>(a);
+    count_launch(2);
+    return cudaGetLastError();
+}
+
 static std::atomic<long long> g_launches{0};
 void count_launch(int n) { g_launches += n; }
 long long launch_count() { return g_launches.load(); }

@@ -105,8 +105,10 @@ inline MrgJump jump_pow(uint64_t n) { return to_jump(mat_pow(MRG_A1, n, MRG_M1),
 // ---------------------------------------------------------------------------
 struct Arena {
     std::vector<void *> ptrs;
-    ~Arena() {
+    ~Arena() { clear(); }
+    void clear() {
         for (void *p : ptrs) cudaFree(p);
+        ptrs.clear();
     }
     template <class T>
     cudaError_t alloc(T **out, size_t n) {
@@ -188,6 +190,41 @@ inline void rest_state(HostModel &h) {
         const double id = 1.0 / det;
         for (int k = 0; k < 9; ++k) inv[k] *= id;
     }
+}
+
+// The vertex side of Blob::linearise_force, replayed once: per vertex, in element order, the (up to three)
+// midpoints whose force the vertex receives (a midpoint's force moves through the first element holding it).
+inline void build_linearise_events(HostModel &h) {
+    const int n = h.n_all, N = h.N, T = h.T;
+    // Blob::linearise_force (src/Blob.cpp:781-799) walks the elements in order: each vertex gains half of
+    // the three midpoints at it, then the element's six midpoints are zeroed, so a midpoint's force goes
+    // to its edge ends once, through the first element that holds it
+    static const int at_vertex[4][3] = {{4, 5, 6}, {4, 7, 8}, {5, 7, 9}, {6, 8, 9}};
+    std::vector<int> mid_id(n, -1);
+    for (size_t m = 0; m < h.mid_nodes.size(); ++m) mid_id[h.mid_nodes[m]] = (int)m;
+    std::vector<char> moved(n, 0);
+    std::vector<std::vector<int>> ev(N);
+    for (int e = 0; e < T; ++e) {
+        const int *t = &h.tets10[10 * (size_t)e];
+        for (int j = 0; j < 4; ++j) {
+            int q[3];
+            bool live = false;
+            for (int k = 0; k < 3; ++k) {
+                const int x = t[at_vertex[j][k]];
+                q[k] = moved[x] ? -1 : mid_id[x];
+                live = live || q[k] >= 0;
+            }
+            if (!live) continue;
+            auto &v = ev[h.lin_of[t[j]]];
+            v.insert(v.end(), {q[0], q[1], q[2], -1});
+        }
+        for (int k = 4; k < 10; ++k) moved[t[k]] = 1;
+    }
+    h.lin_ptr.assign(N + 1, 0);
+    for (int a = 0; a < N; ++a) h.lin_ptr[a + 1] = h.lin_ptr[a] + (int)ev[a].size() / 4;
+    h.lin_ev.clear();
+    h.lin_ev.reserve(4 * (size_t)h.lin_ptr[N]);
+    for (int a = 0; a < N; ++a) h.lin_ev.insert(h.lin_ev.end(), ev[a].begin(), ev[a].end());
 }
 
 inline int build_model(const ffea_gpu_mesh *mesh, const ffea_gpu_params *p, HostModel &h) {
@@ -276,36 +313,7 @@ inline int build_model(const ffea_gpu_mesh *mesh, const ffea_gpu_params *p, Host
         h.drag.resize(N);
         for (int k = 0; k < N; ++k) h.drag[k] = h.drag_all[h.node_of[k]];
     }
-    if (p->calc_stokes == 1 && p->calc_noise == 1) {
-        // Blob::linearise_force (src/Blob.cpp:781-799) walks the elements in order: each vertex gains half of
-        // the three midpoints at it, then the element's six midpoints are zeroed, so a midpoint's force goes
-        // to its edge ends once, through the first element that holds it
-        static const int at_vertex[4][3] = {{4, 5, 6}, {4, 7, 8}, {5, 7, 9}, {6, 8, 9}};
-        std::vector<int> mid_id(n, -1);
-        for (size_t m = 0; m < h.mid_nodes.size(); ++m) mid_id[h.mid_nodes[m]] = (int)m;
-        std::vector<char> moved(n, 0);
-        std::vector<std::vector<int>> ev(N);
-        for (int e = 0; e < T; ++e) {
-            const int *t = &h.tets10[10 * (size_t)e];
-            for (int j = 0; j < 4; ++j) {
-                int q[3];
-                bool live = false;
-                for (int k = 0; k < 3; ++k) {
-                    const int x = t[at_vertex[j][k]];
-                    q[k] = moved[x] ? -1 : mid_id[x];
-                    live = live || q[k] >= 0;
-                }
-                if (!live) continue;
-                auto &v = ev[h.lin_of[t[j]]];
-                v.insert(v.end(), {q[0], q[1], q[2], -1});
-            }
-            for (int k = 4; k < 10; ++k) moved[t[k]] = 1;
-        }
-        h.lin_ptr.assign(N + 1, 0);
-        for (int a = 0; a < N; ++a) h.lin_ptr[a + 1] = h.lin_ptr[a] + (int)ev[a].size() / 4;
-        h.lin_ev.reserve(4 * (size_t)h.lin_ptr[N]);
-        for (int a = 0; a < N; ++a) h.lin_ev.insert(h.lin_ev.end(), ev[a].begin(), ev[a].end());
-    }
+    if (p->calc_stokes == 1 && p->calc_noise == 1) build_linearise_events(h);
     rest_state(h);
     // incidence: element order, vertex slots (Blob::calculate_node_element_connectivity)
     h.inc_ptr.assign(N + 1, 0);

@@ -299,24 +299,33 @@ __global__ void __launch_bounds__(128) assemble_kernel(AsmArgs<R> g) {
 // ---------------------------------------------------------------------------
 // force gather (Blob::aggregate_forces_and_solve :3152-3158) + solver set-up
 // ---------------------------------------------------------------------------
-struct StokesNoise {
-    int on;
+// Forces on nodes other than the elements' (Blob::apply_ctforces, src/Blob.cpp:1676-1743; the Stokes part of
+// aggregate_forces_and_solve, :3172-3224; linearise_force, :781-799), on the reference numbering:
+// constant linear forces (before the element contributions), constant surface forces (after them, face by face),
+// Stokes noise (3 draws per node after the elements' 7T), and the move of midpoint forces to their edge ends.
+struct NodeForces {
+    int on;                        // any of the below
+    int noise;                     // Stokes noise
     double kT, dt;
     const uint32_t *rng_state;     // the step's stream state
-    const MrgJump *chunk_jump;     // A^(7T + 96 c): first draw of node chunk c (reference numbering)
+    const MrgJump *chunk_jump;     // A^(base + 96 c): first draw of node chunk c (reference numbering)
     const MrgJump *lane_jump;      // A^(3 l)
     const int *node_orig;          // vertex -> reference node index
     const double *node_drag;       // vertex Stokes drag
     const int *mid_orig;           // midpoint -> reference node index
     const double *mid_drag;
-    const int *lin_ptr;            // per vertex: its linearise events, in element order
+    const double *node_ctf, *mid_ctf;      // 3 per vertex / midpoint: constant linear forces (or null)
+    const int *vface_ptr, *vface;          // surface faces holding each vertex, in face order (or null)
+    const int *mface_ptr, *mface;          // the same for midpoints
+    const double *ff;                      // 3 per face: this step's constant surface force at each corner
+    const int *lin_ptr;            // per vertex: its linearise events, in element order (or null)
     const int4 *lin_ev;            // up to three live midpoints (-1: already moved) summed into the vertex
 };
 
 // force[i] -= RAND(-.5,.5) * sqrt(24 kT drag / dt), three components, for reference node i
 // (Blob::aggregate_forces_and_solve, src/Blob.cpp:3190-3219)
 template <class R>
-__device__ __forceinline__ void stokes_noise_sub(const StokesNoise &sn, int i, double drag, R (&F)[3]) {
+__device__ __forceinline__ void stokes_noise_sub(const NodeForces &sn, int i, double drag, R (&F)[3]) {
     uint32_t base[6], s6[6];
 #pragma unroll
     for (int k = 0; k < 6; ++k) s6[k] = sn.rng_state[k];
@@ -329,11 +338,31 @@ __device__ __forceinline__ void stokes_noise_sub(const StokesNoise &sn, int i, d
     }
 }
 
+// force[node] += face force of every surface face holding the node, in face order
+template <class R>
+__device__ __forceinline__ void surface_add(const NodeForces &sn, const int *ptr, const int *faces, int i,
+                                            R (&F)[3]) {
+    for (int k = ptr[i]; k < ptr[i + 1]; ++k) {
+        const double *f = sn.ff + 3 * (size_t)faces[k];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) F[c] += (R)f[c];
+    }
+}
+
+// the force a midpoint carries into linearise_force: its constant forces, then its noise
+template <class R>
+__device__ __forceinline__ void midpoint_force(const NodeForces &sn, int m, R (&f)[3]) {
+#pragma unroll
+    for (int c = 0; c < 3; ++c) f[c] = sn.mid_ctf ? (R)sn.mid_ctf[3 * (size_t)m + c] : (R)0;
+    if (sn.mface_ptr) surface_add<R>(sn, sn.mface_ptr, sn.mface, m, f);
+    if (sn.noise) stokes_noise_sub<R>(sn, sn.mid_orig[m], sn.mid_drag[m], f);
+}
+
 // the vertex's share of Blob::linearise_force (src/Blob.cpp:781-799): for each element holding the vertex,
 // in element order, force += 0.5 * (f_m1 + f_m2 + f_m3) over that element's three midpoints at the vertex
 // that still carry force (a midpoint's force is moved by the first element holding it, then zeroed)
 template <class R>
-__device__ __forceinline__ void stokes_linearise(const StokesNoise &sn, int a, R (&F)[3]) {
+__device__ __forceinline__ void midpoint_linearise(const NodeForces &sn, int a, R (&F)[3]) {
     for (int k = sn.lin_ptr[a]; k < sn.lin_ptr[a + 1]; ++k) {
         const int4 ev = sn.lin_ev[k];
         const int m[3] = {ev.x, ev.y, ev.z};
@@ -341,12 +370,52 @@ __device__ __forceinline__ void stokes_linearise(const StokesNoise &sn, int a, R
 #pragma unroll
         for (int j = 0; j < 3; ++j) {
             fm[j][0] = fm[j][1] = fm[j][2] = (R)0;
-            if (m[j] >= 0) stokes_noise_sub<R>(sn, sn.mid_orig[m[j]], sn.mid_drag[m[j]], fm[j]);
+            if (m[j] >= 0) midpoint_force<R>(sn, m[j], fm[j]);
         }
 #pragma unroll
         for (int c = 0; c < 3; ++c) F[c] += (R)0.5 * (fm[0][c] + fm[1][c] + fm[2][c]);
     }
 }
+
+// one step's constant surface forces (CTF 3 of Blob::apply_ctforces): each set's force spread over its faces in
+// proportion to their current areas, area_j / (3 sum_k area_k) of it at each corner of face j
+struct SurfArgs {
+    int nsets, nfaces;
+    const int *set_ptr, *set_faces;
+    const double *set_force;       // 3 per set
+    const int2 *corner;            // 3 per face: vertex rows (a, b) of the corner at (x_a + x_b) / 2
+    const int *face_set_ptr, *face_set;
+    const double *px, *py, *pz;
+    double *set_total;             // per set
+    double *ff;                    // 3 per face
+    const DevStatus *st;
+};
+
+// Face::get_area (src/Face.cpp:169-187) at the current positions
+__device__ __forceinline__ double face_area(const SurfArgs &g, int f) {
+    double p[3][3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const int2 c = g.corner[3 * f + k];
+        p[k][0] = .5 * (g.px[c.x] + g.px[c.y]);
+        p[k][1] = .5 * (g.py[c.x] + g.py[c.y]);
+        p[k][2] = .5 * (g.pz[c.x] + g.pz[c.y]);
+    }
+    double a[3], b[3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        a[i] = p[1][i] - p[0][i];
+        b[i] = p[2][i] - p[0][i];
+    }
+    const double t0 = a[1] * b[2] - a[2] * b[1], t1 = a[2] * b[0] - a[0] * b[2], t2 = a[0] * b[1] - a[1] * b[0];
+    // magnitude (include/mat_vec_fns_II.h:326-333) is an `omp simd` reduction: built with GCC it sums two
+    // lanes, (t0^2 + t2^2) + t1^2
+    const double r = (t0 * t0 + t2 * t2) + t1 * t1;
+    return .5 * sqrt(r);
+}
+
+__global__ void __launch_bounds__(128) surf_set_kernel(SurfArgs g);
+__global__ void __launch_bounds__(128) surf_face_kernel(SurfArgs g);
 
 template <class R>
 struct GatherArgs {
@@ -371,7 +440,7 @@ struct GatherArgs {
     const R *diag;
     // Stokes noise (calc_stokes and calc_noise): 3 draws per node of the reference numbering, after the
     // elements' 7T, in node order; a midpoint's force is moved to its edge ends by linearise events
-    StokesNoise sn;
+    NodeForces sn;
 };
 
 template <class R>
@@ -383,12 +452,22 @@ __global__ void __launch_bounds__(256) gather_kernel(GatherArgs<R> g) {
     const bool live = a < g.N && !g.st->abort;
     if (live) {
         R F0 = 0, F1 = 0, F2 = 0;
+        if (g.sn.node_ctf) {  // constant linear forces come first (apply_ctforces runs before the elements)
+            F0 = (R)g.sn.node_ctf[3 * (size_t)a];
+            F1 = (R)g.sn.node_ctf[3 * (size_t)a + 1];
+            F2 = (R)g.sn.node_ctf[3 * (size_t)a + 2];
+        }
         for (int m = g.inc_ptr[a]; m < g.inc_ptr[a + 1]; ++m) {
             const int es = g.inc[m];
             const R *c = g.ef + 12 * (size_t)(es >> 2) + 3 * (es & 3);
             F0 += c[0];
             F1 += c[1];
             F2 += c[2];
+        }
+        if (g.sn.vface_ptr) {
+            R F[3] = {F0, F1, F2};
+            surface_add<R>(g.sn, g.sn.vface_ptr, g.sn.vface, a, F);
+            F0 = F[0]; F1 = F[1]; F2 = F[2];
         }
         if (g.drag) {  // inertial Stokes drag (src/Blob.cpp:3186-3188)
             const double dr = g.drag[a];
@@ -398,8 +477,8 @@ __global__ void __launch_bounds__(256) gather_kernel(GatherArgs<R> g) {
         }
         if (g.sn.on) {
             R F[3] = {F0, F1, F2};
-            stokes_noise_sub<R>(g.sn, g.sn.node_orig[a], g.sn.node_drag[a], F);
-            stokes_linearise<R>(g.sn, a, F);
+            if (g.sn.noise) stokes_noise_sub<R>(g.sn, g.sn.node_orig[a], g.sn.node_drag[a], F);
+            if (g.sn.lin_ptr) midpoint_linearise<R>(g.sn, a, F);
             F0 = F[0]; F1 = F[1]; F2 = F[2];
         }
         if (g.pinned[a]) { F0 = 0; F1 = 0; F2 = 0; }

@@ -56,12 +56,22 @@ __global__ void __launch_bounds__(256) gather_mixed_kernel(GatherArgs<R> g) {
     for (int i = 0; i < MIXED_GATHER_NP; ++i) acc[i] = df32{0.f, 0.f};
     if (a < g.N && !g.st->abort) {
         float F0 = 0, F1 = 0, F2 = 0;
+        if (g.sn.node_ctf) {
+            F0 = (float)g.sn.node_ctf[3 * (size_t)a];
+            F1 = (float)g.sn.node_ctf[3 * (size_t)a + 1];
+            F2 = (float)g.sn.node_ctf[3 * (size_t)a + 2];
+        }
         for (int m = g.inc_ptr[a]; m < g.inc_ptr[a + 1]; ++m) {
             const int es = g.inc[m];
             const R *c = g.ef + 12 * (size_t)(es >> 2) + 3 * (es & 3);
             F0 += c[0];
             F1 += c[1];
             F2 += c[2];
+        }
+        if (g.sn.vface_ptr) {
+            float F[3] = {F0, F1, F2};
+            surface_add<float>(g.sn, g.sn.vface_ptr, g.sn.vface, a, F);
+            F0 = F[0]; F1 = F[1]; F2 = F[2];
         }
         if (g.drag) {
             const double dr = g.drag[a];
@@ -71,8 +81,8 @@ __global__ void __launch_bounds__(256) gather_mixed_kernel(GatherArgs<R> g) {
         }
         if (g.sn.on) {
             float F[3] = {F0, F1, F2};
-            stokes_noise_sub<float>(g.sn, g.sn.node_orig[a], g.sn.node_drag[a], F);
-            stokes_linearise<float>(g.sn, a, F);
+            if (g.sn.noise) stokes_noise_sub<float>(g.sn, g.sn.node_orig[a], g.sn.node_drag[a], F);
+            if (g.sn.lin_ptr) midpoint_linearise<float>(g.sn, a, F);
             F0 = F[0]; F1 = F[1]; F2 = F[2];
         }
         if (g.pinned[a]) { F0 = 0; F1 = 0; F2 = 0; }

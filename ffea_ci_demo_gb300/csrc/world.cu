@@ -10,9 +10,11 @@
 // World::make_measurements / write_measurements_to_file :4598-4692). restart = 1 resumes from the
 // checkpoint and the last complete trajectory frame (:300-425, :690-860).
 //
-// Everything outside the path is refused with FFEA_GPU_EINPUT and a message: surface-surface and
+// Constant forces (calc_ctforces = 1, <interactions><ctforces><ctforces_fname>) are loaded per blob
+// with its surface file, as Blob::init does (src/Blob.cpp:188-190, read_and_build_system :2266-2290).
+// Everything else outside the path is refused with FFEA_GPU_EINPUT and a message: surface-surface and
 // steric interactions (calc_ssint, calc_steric must be set to 0), electrostatics, kinetics, springs,
-// pre-computed potentials, constant forces, rods, several conformations, STATIC/FROZEN blobs.
+// pre-computed potentials, rotational constant forces, rods, several conformations, STATIC/FROZEN blobs.
 //
 // The reference's threads each own a stream; this engine reproduces its single-thread order, in which
 // one stream serves every blob: per step, the elements of blob 0, 1, ... draw 7 numbers each, then
@@ -109,7 +111,7 @@ std::string join_dir(const std::string &dir, const std::string &f) {
 }
 
 struct BlobSpec {
-    std::string nodes, topology, material, stokes, pin, motion_state = "DYNAMIC";
+    std::string nodes, topology, material, stokes, pin, surface, motion_state = "DYNAMIC";
     int solver = FFEA_GPU_NOMASS_CG;
     double scale = 0.0;  // metres per file unit
     bool set_centroid = false, set_velocity = false;
@@ -131,7 +133,8 @@ struct ffea_gpu_world {
     int check = 10000, restart = 0;
     long long rng_seed = 0;
     bool seed_set = false;
-    int move_into_box = 1, es_N[3] = {-1, -1, -1};
+    int move_into_box = 1, es_N[3] = {-1, -1, -1}, calc_ctforces = 0;
+    std::string ctforces_fname;
     double ssint_cutoff = 3e-9 / M_LENGTH;
     std::string script, dir, traj_fname, meas_fname, ockpt_fname, ickpt_fname;
     std::vector<BlobSpec> spec;
@@ -164,7 +167,7 @@ int ffea_gpu_world::read_params(const std::vector<std::string> &lines) {
     p.precision = precision;
     int calc_ssint = 1, calc_steric = 1;
     // keys of features this engine leaves out: they must be 0 (or absent)
-    static const char *must_be_zero[] = {"calc_es", "calc_kinetics", "calc_springs", "calc_preComp", "calc_ctforces",
+    static const char *must_be_zero[] = {"calc_es", "calc_kinetics", "calc_springs", "calc_preComp",
                                          "sticky_wall_xz", "calc_steric_rod", "calc_vdw_rod", "num_rods",
                                          "num_interfaces", "force_pbc"};
     // keys that only configure those features (or output we do not write): accepted and ignored
@@ -196,6 +199,10 @@ int ffea_gpu_world::read_params(const std::vector<std::string> &lines) {
         else if (k == "es_N_z") es_N[2] = atoi(v.c_str());
         else if (k == "calc_ssint" || k == "calc_vdw") calc_ssint = atoi(v.c_str());
         else if (k == "calc_steric") calc_steric = atoi(v.c_str());
+        else if (k == "calc_ctforces") {
+            calc_ctforces = atoi(v.c_str());
+            if (calc_ctforces != 0 && calc_ctforces != 1) return fail("'calc_ctforces' must be 0 or 1");
+        }
         else if (k == "num_blobs" || k == "num_conformations") {
             for (double x : tuple_values(v))
                 if (k == "num_conformations" && x != 1.0) return fail("several conformations per blob are outside this engine");
@@ -228,12 +235,26 @@ int ffea_gpu_world::read_params(const std::vector<std::string> &lines) {
 
 // read_and_build_system's reading of <system> (src/World.cpp:2300-2700), one conformation per blob
 int ffea_gpu_world::read_system(const std::vector<std::string> &lines) {
-    int depth_blob = 0, depth_conf = 0;
+    int depth_blob = 0, depth_conf = 0, depth_inter = 0, depth_ctf = 0, ctf_fields = 0;
     BlobSpec cur;
     for (const auto &ln : lines) {
         std::string k, v;
         parse_tag(ln, k, v);
         if (k == "system" || k == "/system") continue;
+        // <interactions>: only its <ctforces> block is read, and only with calc_ctforces = 1 (the blocks of
+        // springs and pre-computed potentials belong to features that must be off)
+        if (!depth_blob && k == "interactions") { depth_inter = 1; continue; }
+        if (!depth_blob && k == "/interactions") { depth_inter = 0; continue; }
+        if (depth_inter) {
+            if (k == "ctforces") depth_ctf = 1;
+            else if (k == "/ctforces") depth_ctf = 0;
+            else if (depth_ctf && calc_ctforces) {
+                ++ctf_fields;
+                if (k != "ctforces_fname") return fail("ctforces_fname not provided in <ctforces> block");
+                ctforces_fname = join_dir(dir, v);
+            }
+            continue;
+        }
         if (k == "blob") { depth_blob = 1; cur = BlobSpec(); continue; }
         if (k == "/blob") {
             if (cur.scale <= 0) return fail("blob " + std::to_string(spec.size()) + ": scale not set");
@@ -252,7 +273,8 @@ int ffea_gpu_world::read_system(const std::vector<std::string> &lines) {
             else if (k == "stokes") cur.stokes = join_dir(dir, v);
             else if (k == "pin") cur.pin = join_dir(dir, v);
             else if (k == "motion_state") cur.motion_state = v;
-            else if (k == "surface" || k == "vdw" || k == "ssint" || k == "beads" || k == "binding_sites") continue;
+            else if (k == "surface") cur.surface = join_dir(dir, v);
+            else if (k == "vdw" || k == "ssint" || k == "beads" || k == "binding_sites") continue;
             else return fail("unsupported conformation key '" + k + "'");
             continue;
         }
@@ -285,6 +307,11 @@ int ffea_gpu_world::read_system(const std::vector<std::string> &lines) {
         }
     }
     if (spec.empty()) return fail("no <blob> in <system>");
+    if (calc_ctforces) {
+        if (ctf_fields != 1) return fail("only a single field is allowed in the <ctforces> block");
+        std::ifstream probe(ctforces_fname);
+        if (!probe) return fail("ctforces_fname: " + ctforces_fname + " could not be opened");
+    }
     return FFEA_GPU_OK;
 }
 
@@ -303,6 +330,9 @@ int ffea_gpu_world::build() {
         if (rc) return rc;
         blobs.push_back(b);
         n_all.push_back(b->h.n_all);
+        if (calc_ctforces &&
+            (rc = b->load_ctforces(ctforces_fname.c_str(), s.surface.empty() ? nullptr : s.surface.c_str(), i)))
+            return rc;
         pos[i].resize(3 * (size_t)b->h.n_all);
         vel[i].assign(3 * (size_t)b->h.n_all, 0.0);
         if ((rc = ffea_gpu_blob_get_state(b, pos[i].data(), nullptr, nullptr))) return rc;

@@ -89,6 +89,7 @@ def load():
         "ffea_gpu_blob_measure": (C.c_int, [vp, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
         "ffea_gpu_blob_cg_iterations": (C.c_int, [vp, ip, C.POINTER(C.c_longlong)]),
         "ffea_gpu_blob_measurements": (C.c_int, [vp, dp]),
+        "ffea_gpu_blob_load_ctforces": (C.c_int, [vp, C.c_char_p, C.c_char_p, C.c_int]),
         "ffea_gpu_blob_set_rmsd_reference": (C.c_int, [vp]),
         "ffea_gpu_blob_sizes": (C.c_int, [vp, ip, ip, C.POINTER(C.c_longlong)]),
         "ffea_gpu_blob_counts": (C.c_int, [vp, ip, ip]),
@@ -290,6 +291,12 @@ class Blob:
         se, ke = C.c_double(), C.c_double()
         _check(self._lib.ffea_gpu_blob_measure(self._h, C.byref(se), C.byref(ke)), "measure")
         return se.value, ke.value
+
+    def load_ctforces(self, ctforces_file: str, surface_file: str | None = None, blob_index: int = 0) -> None:
+        """The reference's constant forces (linear on nodes, linear over surface faces) for this blob."""
+        _check(self._lib.ffea_gpu_blob_load_ctforces(self._h, str(ctforces_file).encode(),
+                                                     None if surface_file is None else str(surface_file).encode(),
+                                                     int(blob_index)), "load_ctforces")
 
     def measurements(self) -> dict:
         """Blob::make_measurements on the device (meso units)."""

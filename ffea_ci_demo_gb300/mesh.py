@@ -68,23 +68,34 @@ def kuhn_cube(n: int, side: float = 20.0, *, jitter: float = 0.05, seed: int = 1
     """
     if n < 1:
         raise ValueError("n must be >= 1")
-    h = side / n
-    m = n + 1
-    g = np.arange(m, dtype=np.float64) * h
-    z, y, x = np.meshgrid(g, g, g, indexing="ij")
+    return kuhn_box(n, n, n, side / n, jitter=jitter, seed=seed, density=density, shear_mod=shear_mod,
+                    bulk_mod=bulk_mod, shear_visc=shear_visc, bulk_visc=bulk_visc, dielectric=dielectric,
+                    scale=scale, stokes_radius=stokes_radius)
+
+
+def kuhn_box(nx: int, ny: int, nz: int, h: float, *, jitter: float = 0.05, seed: int = 12345,
+             density: float = 1500.0, shear_mod: float = 5.7e8, bulk_mod: float = 2.2e9,
+             shear_visc: float = 1e-3, bulk_visc: float = 1e-3, dielectric: float = 1.0,
+             scale: float = 1e-9, stokes_radius: float | None = None) -> Mesh:
+    """Box of nx x ny x nz cubic cells of edge ``h`` (file units), 6 Kuhn tets per cell, numbered as
+    :func:`kuhn_cube` (vertices x fastest, then midpoints in first-appearance order)."""
+    if min(nx, ny, nz) < 1:
+        raise ValueError("cell counts must be >= 1")
+    mx, my, mz = nx + 1, ny + 1, nz + 1
+    z, y, x = np.meshgrid(np.arange(mz) * h, np.arange(my) * h, np.arange(mx) * h, indexing="ij")
     pos_lin = np.stack([x.ravel(), y.ravel(), z.ravel()], axis=1)
     rng = np.random.default_rng(seed)
     d = rng.uniform(-jitter * h, jitter * h, size=pos_lin.shape)
-    ijk = np.stack(np.meshgrid(np.arange(m), np.arange(m), np.arange(m), indexing="ij"), -1)
+    ijk = np.stack(np.meshgrid(np.arange(mz), np.arange(my), np.arange(mx), indexing="ij"), -1)
     ijk = ijk.reshape(-1, 3)[:, ::-1]  # (i, j, k) with x fastest, matching pos_lin
-    interior = np.all((ijk > 0) & (ijk < n), axis=1)
+    interior = np.all((ijk > 0) & (ijk < np.array([nx, ny, nz])), axis=1)
     pos_lin[interior] += d[interior]
 
     def vid(i, j, k):
-        return i + m * (j + m * k)
+        return i + mx * (j + my * k)
 
     # 6 tets per cell, orientation made positive (det > 0)
-    cells = np.stack(np.meshgrid(np.arange(n), np.arange(n), np.arange(n), indexing="ij"), -1)
+    cells = np.stack(np.meshgrid(np.arange(nz), np.arange(ny), np.arange(nx), indexing="ij"), -1)
     cells = cells.reshape(-1, 3)[:, ::-1]  # x fastest over cells
     tets4 = []
     for perm in itertools.permutations(range(3)):
@@ -102,7 +113,7 @@ def kuhn_cube(n: int, side: float = 20.0, *, jitter: float = 0.05, seed: int = 1
             t4[:, t, a] = vid(c[:, 0], c[:, 1], c[:, 2])
     t4 = t4.reshape(-1, 4)
     T = t4.shape[0]
-    N = m ** 3
+    N = mx * my * mz
 
     # unique edges -> midpoint nodes, numbered in first-appearance order
     e_all = np.stack([np.stack([t4[:, a], t4[:, b]], 1) for a, b in MID_EDGES], 1)  # (T,6,2)
@@ -189,15 +200,86 @@ def write_structure(mesh: Mesh, directory: str, name: str, pos: np.ndarray | Non
     return paths
 
 
+def surface_faces(mesh: Mesh) -> np.ndarray:
+    """The blob's surface as FFEA surface faces: rows ``element n0 n1 n2`` (global node ids).
+
+    Every tetrahedron face that belongs to one element only is split, as FFEA's second-order surface is,
+    into its four triangles through the edge midpoints: the three corner triangles (vertex, two
+    midpoints) and the central one. The corners of each boundary face are ordered so that its normal
+    points out of the element, and the four triangles keep that orientation. Faces come in element
+    order, then by the element's vertex they are opposite to (0..3)."""
+    t = np.asarray(mesh.tets, np.int64)
+    T = t.shape[0]
+    mid = {frozenset(e): 4 + k for k, e in enumerate(MID_EDGES)}
+    keys = {}
+    for o in range(4):
+        tri = np.sort(np.delete(t[:, :4], o, axis=1), axis=1)
+        for e in range(T):
+            k = tuple(tri[e])
+            keys[k] = keys.get(k, 0) + 1
+    out = []
+    p = mesh.pos
+    for e in range(T):
+        for o in range(4):
+            loc = [a for a in range(4) if a != o]
+            if keys[tuple(sorted(int(t[e, a]) for a in loc))] != 1:
+                continue
+            a, b, c = loc
+            n = np.cross(p[t[e, b]] - p[t[e, a]], p[t[e, c]] - p[t[e, a]])
+            if np.dot(n, p[t[e, o]] - p[t[e, a]]) > 0:
+                b, c = c, b
+            mab, mbc, mca = mid[frozenset((a, b))], mid[frozenset((b, c))], mid[frozenset((c, a))]
+            for tri in ((a, mab, mca), (b, mbc, mab), (c, mca, mbc), (mab, mbc, mca)):
+                out.append([e] + [int(t[e, k]) for k in tri])
+    return np.array(out, np.int32).reshape(-1, 4)
+
+
+def faces_on_plane(mesh: Mesh, faces: np.ndarray, axis: int, value: float, tol: float = 1e-9) -> np.ndarray:
+    """Indices of the surface faces whose three nodes lie on the plane x[axis] = value."""
+    c = mesh.pos[faces[:, 1:], axis]
+    return np.nonzero(np.all(np.abs(c - value) <= tol, axis=1))[0].astype(np.int32)
+
+
+def write_surface(path: str, faces: np.ndarray) -> None:
+    """An FFEA surface file (Blob::load_surface, src/Blob.cpp:2089-2170)."""
+    with open(path, "w") as f:
+        f.write(f"ffea surface file\nnum_surface_faces {faces.shape[0]}\nfaces:\n")
+        np.savetxt(f, np.asarray(faces, np.int64), fmt="%d")
+
+
+def write_ctforces(path: str, linear=(), surface=()) -> None:
+    """An FFEA constant-forces file (Blob::load_ctforces, src/Blob.cpp:2478-2805).
+
+    ``linear``: (F [N], (dx, dy, dz), blob, conformation, node or "all") per force;
+    ``surface``: (F [N], (dx, dy, dz), blob, conformation, [face indices]) per set of faces."""
+    lines = ["ffea ctforces file", f"num_ctforces {len(linear) + len(surface)}"]
+    if linear:
+        lines.append(f"num_linear_forces {len(linear)}")
+    if surface:
+        lines.append(f"num_linear_surface_forces {len(surface)}")
+    if linear:
+        lines.append("linear forces:")
+        for F, d, b, c, n in linear:
+            lines.append(f"{F!r} {d[0]!r} {d[1]!r} {d[2]!r} {b} {c} {n}")
+    if surface:
+        lines.append("linear surface forces:")
+        for F, d, b, c, fs in surface:
+            lines.append(f"{F!r} {d[0]!r} {d[1]!r} {d[2]!r} {b} {c} " + " ".join(str(int(x)) for x in fs))
+    with open(path, "w") as f:
+        f.write("\n".join(lines) + "\n")
+
+
 def write_script(path: str, structure: dict, *, solver: str = "CG_nomass", scale: float = 1e-9,
                  dt: float = 1e-12, kT: float = 4.11e-21, epsilon: float = 1e-10,
                  max_iterations_cg: int = 10000, calc_noise: int = 1, calc_stokes: int = 0,
                  stokes_visc: float = 1e-3, rng_seed: int = 12345, num_steps: int = 1000,
-                 check: int | None = None) -> None:
+                 check: int | None = None, ctforces: str | None = None, surface: str | None = None) -> None:
     """Write a single-blob ``.ffea`` script with every non-hot-path force off.
 
     ``calc_ssint`` and ``calc_steric`` default to 1 in the reference
     (src/SimulationParams.cpp:39,44), so they are set to 0 explicitly.
+    ``ctforces`` (a constant-forces file) sets ``calc_ctforces = 1`` with an ``<interactions>`` block;
+    ``surface`` adds the conformation's surface file.
     """
     check = num_steps if check is None else check
     d = os.path.dirname(os.path.abspath(path))
@@ -216,7 +298,7 @@ def write_script(path: str, structure: dict, *, solver: str = "CG_nomass", scale
         f"\t<calc_stokes = {calc_stokes}>",
         f"\t<stokes_visc = {stokes_visc!r}>",
         "\t<calc_ssint = 0>", "\t<calc_steric = 0>", "\t<calc_es = 0>", "\t<calc_kinetics = 0>",
-        "\t<calc_preComp = 0>", "\t<calc_springs = 0>", "\t<calc_ctforces = 0>",
+        "\t<calc_preComp = 0>", "\t<calc_springs = 0>", f"\t<calc_ctforces = {int(ctforces is not None)}>",
         "\t<num_blobs = 1>", "\t<num_conformations = (1)>", "\t<num_states = (1)>",
         "</param>", "", "<system>", "\t<blob>", "\t\t<conformation>",
         "\t\t\t<motion_state = DYNAMIC>",
@@ -225,10 +307,14 @@ def write_script(path: str, structure: dict, *, solver: str = "CG_nomass", scale
         f"\t\t\t<material = {rel['mat']}>",
         f"\t\t\t<stokes = {rel['stokes']}>",
         f"\t\t\t<pin = {rel['pin']}>",
+    ] + ([f"\t\t\t<surface = {os.path.relpath(surface, d)}>"] if surface else []) + [
         "\t\t</conformation>",
         f"\t\t<solver = {solver}>",
         f"\t\t<scale = {scale!r}>",
-        "\t</blob>", "</system>", "",
+        "\t</blob>",
+    ] + (["\t<interactions>", "\t\t<ctforces>", f"\t\t\t<ctforces_fname = {os.path.relpath(ctforces, d)}>",
+          "\t\t</ctforces>", "\t</interactions>"] if ctforces else []) + [
+        "</system>", "",
     ]
     with open(path, "w") as f:
         f.write("\n".join(lines))

@@ -140,6 +140,15 @@ int ffea_gpu_blob_set_state(ffea_gpu_blob *blob, const double *pos, const double
 /* Blob::make_measurements energies (src/Blob.cpp:1066-1125), meso units. */
 int ffea_gpu_blob_measure(ffea_gpu_blob *blob, double *strain_energy, double *kinetic_energy);
 
+/* Constant forces of the reference's ctforces file for blob `blob_index` (Blob::load_ctforces,
+ * src/Blob.cpp:2478-2805; applied as Blob::apply_ctforces, :1676-1743): linear forces on nodes (added
+ * before the element forces) and linear surface forces spread over sets of faces of `surface_file`
+ * (the blob's .surf; may be NULL without surface forces) in proportion to their current areas (added
+ * after the element forces, face by face). Rotational forces return FFEA_GPU_EINPUT. Replaces any
+ * constant forces loaded before. */
+int ffea_gpu_blob_load_ctforces(ffea_gpu_blob *blob, const char *ctforces_file, const char *surface_file,
+                                int blob_index);
+
 /* All of Blob::make_measurements (src/Blob.cpp:1066-1202), reduced on the device in FP64:
  * out[0] strain energy, out[1] kinetic energy (0 for CG_nomass), out[2..4] centroid of all nodes,
  * out[5] RMSD of all nodes from the reference positions (meso units). The reference positions are

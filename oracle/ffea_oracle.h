@@ -108,6 +108,18 @@ void orc_blob_get_rng_state(const orc_blob *b, int stream, uint32_t out[6]);
 void orc_blob_set_rng_state(orc_blob *b, int stream, const uint32_t s[6]);
 /* Blob::make_measurements energies: strain energy and kinetic energy (meso) */
 void orc_blob_measure(const orc_blob *b, double *strain_energy, double *kinetic_energy);
+/*
+ * Constant forces of this blob (Blob::load_ctforces, src/Blob.cpp:2478-2805), as read from the file:
+ *   linear forces (CTF 1): n_lin entries in file order, node lin_node[i], force magnitude and direction
+ *     lin_fd[4i..4i+3] = (F [N], dx, dy, dz), "all" already expanded to one entry per node;
+ *   linear surface forces (CTF 3): n_sets sets, set s holding set_size[s] faces (concatenated in set_faces)
+ *     and set_fd[4s..4s+3] = (F [N], dx, dy, dz);
+ *   the surface: n_faces faces of three nodes each (face_nodes), as in the .surf file.
+ * Returns ORC_OK, or ORC_EINPUT for an index out of range or a zero direction.
+ */
+int orc_blob_set_ctforces(orc_blob *b, int n_lin, const int *lin_node, const double *lin_fd, int n_sets,
+                          const int *set_size, const int *set_faces, const double *set_fd, int n_faces,
+                          const int *face_nodes);
 
 #ifdef __cplusplus
 }

@@ -23,6 +23,7 @@
 #define MESO_VOLUME 4.913e-30
 #define MESO_TIME 3.7302915560886126e-13
 #define MESO_PRESSURE 8.4305832688784826e8
+#define MESO_FORCE 2.4364705882352941e-11
 #define FFEA_PI 3.141592653589793238462643383279502884197169399375105820974944592307816406286208998628034825342117067982148
 
 typedef struct { int col; double val; } orc_entry; /* sparse_entry, include/SparseMatrixTypes.h:31-35 */
@@ -61,6 +62,11 @@ struct orc_blob {
     orc_rng *rng;
     int last_iters;
     long long total_iters;
+    /* constant forces (Blob::load_ctforces, src/Blob.cpp:2478-2805): ctf_l_nodes / ctf_l_forces,
+     * ctf_sl_surfsize / ctf_sl_faces / ctf_sl_forces, and the surface faces with their Face::force */
+    int n_lctf, n_sets, n_faces;
+    int *lctf_node, *set_size, *set_faces, *face_nodes;
+    double *lctf_f, *set_f, *face_f, *face_area;
 };
 
 static void *xcalloc(size_t n, size_t sz) { return calloc(n ? n : 1, sz ? sz : 1); }
@@ -192,8 +198,50 @@ static void elem_fluct_stress(const orc_blob *b, int e, double S[3][3], orc_rng 
 }
 
 /* Blob::update_internal_forces, src/Blob.cpp:400-491 */
+/* Face::get_area, src/Face.cpp:169-187: half the length of (n1 - n0) x (n2 - n0) */
+static double face_get_area(const orc_blob *b, int f) {
+    const double *p0 = b->pos + 3 * (size_t)b->face_nodes[3 * f], *p1 = b->pos + 3 * (size_t)b->face_nodes[3 * f + 1],
+                 *p2 = b->pos + 3 * (size_t)b->face_nodes[3 * f + 2];
+    double a[3], c[3], t[3];
+    for (int i = 0; i < 3; ++i) {
+        a[i] = p1[i] - p0[i];
+        c[i] = p2[i] - p0[i];
+    }
+    t[0] = a[1] * c[2] - a[2] * c[1];
+    t[1] = a[2] * c[0] - a[0] * c[2];
+    t[2] = a[0] * c[1] - a[1] * c[0];
+    /* magnitude, include/mat_vec_fns_II.h:326-333: an `omp simd` sum reduction, which GCC (-O2 -fopenmp,
+     * two double lanes) evaluates as (t0^2 + t2^2) + t1^2; checked against the reference's header built so */
+    const double r = (t[0] * t[0] + t[2] * t[2]) + t[1] * t[1];
+    return .5 * sqrt(r);
+}
+
+/* Blob::apply_ctforces, src/Blob.cpp:1676-1741 (CTF 1 and CTF 3; rotational forces are not loaded) */
+static void apply_ctforces(orc_blob *b) {
+    for (int i = 0; i < b->n_lctf; ++i)
+        for (int c = 0; c < 3; ++c) b->force[3 * (size_t)b->lctf_node[i] + c] += b->lctf_f[3 * i + c];
+    int aux = 0;
+    for (int s = 0; s < b->n_sets; ++s) {
+        double total = 0;
+        for (int j = 0; j < b->set_size[s]; ++j) {
+            b->face_area[j] = face_get_area(b, b->set_faces[aux + j]);
+            total += b->face_area[j];
+        }
+        for (int j = 0; j < b->set_size[s]; ++j) {
+            const double w = b->face_area[j] / (3 * total);
+            double tr[3];
+            for (int c = 0; c < 3; ++c) tr[c] = w * b->set_f[3 * s + c]; /* resize2 */
+            double *ff = b->face_f + 9 * (size_t)b->set_faces[aux + j];
+            for (int k = 0; k < 3; ++k) /* Face::add_force_to_node(0..2, traction) */
+                for (int c = 0; c < 3; ++c) ff[3 * k + c] += tr[c];
+        }
+        aux += b->set_size[s];
+    }
+}
+
 int orc_blob_update_internal_forces(orc_blob *b) {
     int num_inversions = 0;
+    apply_ctforces(b);
     const int nomass = b->solver == ORC_NOMASS_CG;
 #pragma omp parallel num_threads(b->nthreads) reduction(+ : num_inversions)
     {
@@ -413,6 +461,7 @@ static void lumped_solve(orc_blob *b, double *x) {
 void orc_blob_zero_forces(orc_blob *b) {
     memset(b->node_force, 0, sizeof(double) * 30 * (size_t)b->T);
     memset(b->force, 0, sizeof(double) * 3 * (size_t)b->n);
+    if (b->face_f) memset(b->face_f, 0, sizeof(double) * 9 * (size_t)b->n_faces);
 }
 
 /* tetra_element_linear::linearise_element, src/tetra_element_linear.cpp:553-577 */
@@ -439,6 +488,10 @@ static int aggregate_forces_and_solve(orc_blob *b) {
             b->force[3 * i + 2] += b->contrib[m][2];
         }
     }
+    /* surface forces onto nodes, face order (a face's fourth, opposite node always receives zero here) */
+    for (int f = 0; f < b->n_faces; ++f)
+        for (int k = 0; k < 3; ++k)
+            for (int c = 0; c < 3; ++c) b->force[3 * (size_t)b->face_nodes[3 * f + k] + c] += b->face_f[9 * f + 3 * k + c];
     if (b->calc_stokes == 1) {
         const int nomass = b->solver == ORC_NOMASS_CG;
         if (!nomass || b->calc_noise == 1) {
@@ -974,7 +1027,8 @@ void orc_blob_destroy(orc_blob *b) {
                     b->tet, b->rho, b->A, b->B, b->G, b->E, b->vol0, b->vol, b->last_det, b->jinv0, b->dpsi,
                     b->visc, b->node_force, b->F, b->stress_mag, b->cptr, b->contrib, b->contrib_es, b->key,
                     b->entry, b->sptr, b->src, b->diag, b->precond, b->r, b->p, b->z, b->q, b->f, b->work_in,
-                    b->work_out, b->mkey, b->mentry, b->d, b->s, b->inv_m, b->rng};
+                    b->work_out, b->mkey, b->mentry, b->d, b->s, b->inv_m, b->rng, b->lctf_node, b->set_size,
+                    b->set_faces, b->face_nodes, b->lctf_f, b->set_f, b->face_f, b->face_area};
     for (size_t i = 0; i < sizeof(ptrs) / sizeof(ptrs[0]); ++i) free(ptrs[i]);
     free(b);
 }
@@ -1085,4 +1139,55 @@ void orc_blob_measure(const orc_blob *b, double *strain, double *kinetic) {
     }
     *kinetic = ke * 0.5;
     *strain = se * 0.5;
+}
+
+/* F * normalize(d) / mesoDimensions::force, as Blob::load_ctforces stores each force (src/Blob.cpp:2600-2606) */
+static int ctf_convert(const double *fd, double out[3]) {
+    double sum = 0; /* normalize, include/mat_vec_fns_II.h:188-198 */
+    for (int i = 0; i < 3; ++i) sum += fd[1 + i] * fd[1 + i];
+    if (sum == 0) return ORC_EINPUT;
+    sum = sqrt(sum);
+    for (int i = 0; i < 3; ++i) out[i] = fd[0] * (fd[1 + i] / sum) / MESO_FORCE;
+    return ORC_OK;
+}
+
+int orc_blob_set_ctforces(orc_blob *b, int n_lin, const int *lin_node, const double *lin_fd, int n_sets,
+                          const int *set_size, const int *set_faces, const double *set_fd, int n_faces,
+                          const int *face_nodes) {
+    int tot = 0, maxs = 0;
+    for (int i = 0; i < n_lin; ++i)
+        if (lin_node[i] < 0 || lin_node[i] >= b->n) return ORC_EINPUT;
+    for (int s = 0; s < n_sets; ++s) {
+        if (set_size[s] < 0) return ORC_EINPUT;
+        tot += set_size[s];
+        if (set_size[s] > maxs) maxs = set_size[s];
+    }
+    for (int j = 0; j < tot; ++j)
+        if (set_faces[j] < 0 || set_faces[j] >= n_faces) return ORC_EINPUT;
+    for (int j = 0; j < 3 * n_faces; ++j)
+        if (face_nodes[j] < 0 || face_nodes[j] >= b->n) return ORC_EINPUT;
+    free(b->lctf_node); free(b->lctf_f); free(b->set_size); free(b->set_faces); free(b->set_f);
+    free(b->face_nodes); free(b->face_f); free(b->face_area);
+    b->n_lctf = n_lin;
+    b->n_sets = n_sets;
+    b->n_faces = n_faces;
+    b->lctf_node = xcalloc(n_lin, sizeof(int));
+    b->lctf_f = xcalloc(3 * (size_t)n_lin, sizeof(double));
+    b->set_size = xcalloc(n_sets, sizeof(int));
+    b->set_faces = xcalloc(tot, sizeof(int));
+    b->set_f = xcalloc(3 * (size_t)n_sets, sizeof(double));
+    b->face_nodes = xcalloc(3 * (size_t)n_faces, sizeof(int));
+    b->face_f = xcalloc(9 * (size_t)n_faces, sizeof(double));
+    b->face_area = xcalloc(maxs, sizeof(double));
+    for (int i = 0; i < n_lin; ++i) {
+        b->lctf_node[i] = lin_node[i];
+        if (ctf_convert(lin_fd + 4 * i, b->lctf_f + 3 * i)) return ORC_EINPUT;
+    }
+    for (int s = 0; s < n_sets; ++s) {
+        b->set_size[s] = set_size[s];
+        if (ctf_convert(set_fd + 4 * s, b->set_f + 3 * s)) return ORC_EINPUT;
+    }
+    if (tot) memcpy(b->set_faces, set_faces, sizeof(int) * tot);
+    if (n_faces) memcpy(b->face_nodes, face_nodes, sizeof(int) * 3 * (size_t)n_faces);
+    return ORC_OK;
 }

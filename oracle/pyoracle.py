@@ -82,6 +82,7 @@ def port_lib(fast: bool = False):
         "blob_get_rng_state": [C.c_void_p, C.c_int, _up],
         "blob_set_rng_state": [C.c_void_p, C.c_int, _up],
         "blob_measure": [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double)],
+        "blob_set_ctforces": [C.c_void_p, C.c_int, _ip, _dp, C.c_int, _ip, _ip, _dp, C.c_int, _ip],
     }.items():
         getattr(lib, P + name).argtypes = args
     lib.orc_blob_total_cg_iters.argtypes = [C.c_void_p]
@@ -140,6 +141,7 @@ def ref_lib():
         "blob_get_inv_mass": [C.c_void_p, _dp],
         "blob_get_rng_state": [C.c_void_p, C.c_int, _up],
         "blob_measure": [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double)],
+        "blob_set_ctforces": [C.c_void_p, C.c_int, _ip, _dp, C.c_int, _ip, _ip, _dp, C.c_int, _ip],
     }.items():
         getattr(lib, "ref_" + name).argtypes = args
     lib._typed = True
@@ -227,6 +229,77 @@ class _BlobBase:
         s, k = C.c_double(), C.c_double()
         self._f("blob_measure")(self._h, C.byref(s), C.byref(k))
         return s.value, k.value
+
+    def set_ctforces(self, ctf: dict, faces: np.ndarray | None = None) -> None:
+        """Constant forces from :func:`read_ctforces`; ``faces`` (F, 4) rows ``element n0 n1 n2`` of the
+        blob's surface file (:func:`read_surface`)."""
+        faces = np.zeros((0, 4), np.int32) if faces is None else np.asarray(faces, np.int32)
+        arg = faces[:, 1:] if self._p == "orc_" else faces
+        i32 = lambda a: np.ascontiguousarray(a, np.int32) if len(a) else np.zeros(1, np.int32)
+        f64 = lambda a: np.ascontiguousarray(a, np.float64).ravel() if len(a) else np.zeros(4)
+        st = self._f("blob_set_ctforces")(
+            self._h, len(ctf["lin_node"]), i32(ctf["lin_node"]), f64(ctf["lin_fd"]), len(ctf["set_size"]),
+            i32(ctf["set_size"]), i32(ctf["set_faces"]), f64(ctf["set_fd"]), faces.shape[0],
+            i32(np.ascontiguousarray(arg).ravel()))
+        if st != 0:
+            raise ValueError(f"set_ctforces failed (status {st})")
+
+
+def read_ctforces(path: str, blob_index: int, n_nodes: int) -> dict:
+    """The entries of one blob (conformation 0) of a constant-forces file, as Blob::load_ctforces
+    (src/Blob.cpp:2478-2805) selects them: linear forces in file order with "all" expanded over the
+    nodes, and the linear surface-force sets. Forces stay as (F [N], dx, dy, dz); rotational forces
+    are rejected."""
+    lines = []
+    for ln in open(path).read().split("\n"):
+        ln = ln.strip()
+        if ln:
+            lines.append(ln)
+    head = {}
+    at = 1
+    while at < len(lines) and ":" not in lines[at]:
+        w = lines[at].split()
+        head[w[0]] = int(w[1])
+        at += 1
+    nl, nr, ns = (head.get(k, 0) for k in ("num_linear_forces", "num_rot_forces", "num_linear_surface_forces"))
+    out = {"lin_node": [], "lin_fd": [], "set_size": [], "set_faces": [], "set_fd": []}
+    if lines[at].startswith("linear forces:"):
+        at += 1
+    for ln in lines[at:at + nl]:
+        w = ln.split()
+        if int(w[4]) != blob_index or int(w[5]) != 0:
+            continue
+        fd = [float(x) for x in w[:4]]
+        nodes = range(n_nodes) if w[6] == "all" else [int(w[6])]
+        for n in nodes:
+            out["lin_node"].append(n)
+            out["lin_fd"].append(fd)
+    at += nl
+    if nr:
+        at += 1
+        if any(int(ln.split()[8]) == blob_index for ln in lines[at:at + nr]):
+            raise ValueError("rotational constant forces are not restated")
+        at += nr
+    if ns:
+        at += 1
+        for ln in lines[at:at + ns]:
+            w = ln.split()
+            if int(w[4]) != blob_index or int(w[5]) != 0:
+                continue
+            out["set_fd"].append([float(x) for x in w[:4]])
+            out["set_size"].append(len(w) - 6)
+            out["set_faces"].extend(int(x) for x in w[6:])
+    return {"lin_node": np.array(out["lin_node"], np.int32), "lin_fd": np.array(out["lin_fd"], np.float64),
+            "set_size": np.array(out["set_size"], np.int32), "set_faces": np.array(out["set_faces"], np.int32),
+            "set_fd": np.array(out["set_fd"], np.float64)}
+
+
+def read_surface(path: str) -> np.ndarray:
+    """Faces of an FFEA surface file (Blob::load_surface, src/Blob.cpp:2089-2170): rows element n0 n1 n2."""
+    with open(path) as f:
+        lines = f.read().split("\n")
+    nf = int(lines[1].split()[1])
+    return np.array([[int(x) for x in ln.split()] for ln in lines[3:3 + nf]], np.int32).reshape(nf, 4)
 
 
 def _mesh_args(mesh):

@@ -32,6 +32,7 @@
 #include <vector>
 
 #include "FFEA_return_codes.h"
+#include "Face.h"
 #include "RngStream.h"
 #include "SimulationParams.h"
 #include "Solver.h"
@@ -67,6 +68,11 @@ struct RefBlob {
     SimulationParams params;
     std::shared_ptr<std::vector<RngStream>> rng;
     int nthreads = 1;
+    // constant forces: Blob's ctf_* members and its surface (include/Blob.h)
+    std::vector<Face> surface;
+    int num_l_ctf = 0, num_slsets_ctf = 0;
+    std::vector<int> ctf_l_nodes, ctf_sl_faces, ctf_sl_surfsize;
+    std::vector<scalar> ctf_l_forces, ctf_sl_forces;
 };
 }  // namespace
 
@@ -167,8 +173,77 @@ void *ref_blob_create(int n_nodes, const double *pos, double scale_m, int n_elem
 
 void ref_blob_destroy(void *h) { delete static_cast<RefBlob *>(h); }
 
+/* the same arguments as orc_blob_set_ctforces, plus the element of each face (face4: element, n0, n1, n2) */
+int ref_blob_set_ctforces(void *h, int n_lin, const int *lin_node, const double *lin_fd, int n_sets,
+                          const int *set_size, const int *set_faces, const double *set_fd, int n_faces,
+                          const int *face4) {
+    RefBlob *b = static_cast<RefBlob *>(h);
+    try {
+        b->surface = std::vector<Face>(n_faces);
+        b->params.num_blobs = 1;
+        for (int i = 0; i < n_faces; ++i) {
+            const int *f = face4 + 4 * i;
+            tetra_element_linear &el = b->elem[f[0]];
+            const int n_op = el.get_opposite_node(el.what_node_is_this(f[1]), el.what_node_is_this(f[2]),
+                                                  el.what_node_is_this(f[3]));
+            if (n_op == -1) return 3;
+            b->surface[i].init(i, &b->node[f[1]], &b->node[f[2]], &b->node[f[3]], el.n[n_op], nullptr, b->params);
+        }
+        auto conv = [](const double *fd, scalar *out) {
+            arr3 d = {fd[1], fd[2], fd[3]};
+            normalize(d);
+            out[0] = fd[0] * d[0] / mesoDimensions::force;
+            out[1] = fd[0] * d[1] / mesoDimensions::force;
+            out[2] = fd[0] * d[2] / mesoDimensions::force;
+        };
+        b->num_l_ctf = n_lin;
+        b->ctf_l_nodes.assign(lin_node, lin_node + n_lin);
+        b->ctf_l_forces.assign(3 * (size_t)n_lin, 0.0);
+        for (int i = 0; i < n_lin; ++i) conv(lin_fd + 4 * i, &b->ctf_l_forces[3 * i]);
+        b->num_slsets_ctf = n_sets;
+        b->ctf_sl_surfsize.assign(set_size, set_size + n_sets);
+        int tot = 0;
+        for (int s = 0; s < n_sets; ++s) tot += set_size[s];
+        b->ctf_sl_faces.assign(set_faces, set_faces + tot);
+        b->ctf_sl_forces.assign(3 * (size_t)n_sets, 0.0);
+        for (int s = 0; s < n_sets; ++s) conv(set_fd + 4 * s, &b->ctf_sl_forces[3 * s]);
+    } catch (FFEAException &) {
+        return 3;
+    }
+    return 0;
+}
+
+/* Blob::apply_ctforces, src/Blob.cpp:1676-1741 (CTF 1 and CTF 3) */
+static void apply_ctforces(RefBlob *b) {
+    auto &force = b->force;
+    for (int i = 0; i < b->num_l_ctf; i++) {
+        force[b->ctf_l_nodes[i]][0] += b->ctf_l_forces[3 * i];
+        force[b->ctf_l_nodes[i]][1] += b->ctf_l_forces[3 * i + 1];
+        force[b->ctf_l_nodes[i]][2] += b->ctf_l_forces[3 * i + 2];
+    }
+    int auxndx = 0;
+    std::vector<scalar> faceAreas;
+    for (int i = 0; i < b->num_slsets_ctf; i++) {
+        scalar totalArea = 0;
+        for (int j = 0; j < b->ctf_sl_surfsize[i]; j++) {
+            faceAreas.push_back(b->surface[b->ctf_sl_faces[auxndx + j]].get_area());
+            totalArea += faceAreas[j];
+        }
+        for (int j = 0; j < b->ctf_sl_surfsize[i]; j++) {
+            arr3 traction;
+            resize2(faceAreas[j] / (3 * totalArea), arr_view<scalar, 3>(b->ctf_sl_forces, 3 * i), traction);
+            b->surface[b->ctf_sl_faces[auxndx + j]].add_force_to_node(0, traction);
+            b->surface[b->ctf_sl_faces[auxndx + j]].add_force_to_node(1, traction);
+            b->surface[b->ctf_sl_faces[auxndx + j]].add_force_to_node(2, traction);
+        }
+        auxndx += b->ctf_sl_surfsize[i];
+        faceAreas.clear();
+    }
+}
+
 static int update_internal_forces(RefBlob *b) {
     int num_inversions = 0;
+    apply_ctforces(b);
     const bool nomass = b->solver_kind == 0;
 #pragma omp parallel num_threads(b->nthreads) reduction(+ : num_inversions)
     {
@@ -211,6 +286,13 @@ static int update_positions(RefBlob *b) {
             force[n][0] += (*node[n].force_contributions[m])[0];
             force[n][1] += (*node[n].force_contributions[m])[1];
             force[n][2] += (*node[n].force_contributions[m])[2];
+        }
+    for (size_t n = 0; n < b->surface.size(); ++n)
+        for (int i = 0; i < 4; i++) {
+            const int sni = b->surface[n].n[i]->index;
+            force[sni][0] += b->surface[n].force[i][0];
+            force[sni][1] += b->surface[n].force[i][1];
+            force[sni][2] += b->surface[n].force[i][2];
         }
     const SimulationParams &params = b->params;
     if (params.calc_stokes == 1 && (!nomass || params.calc_noise == 1)) {
@@ -266,6 +348,7 @@ int ref_blob_step(void *h, int nsteps) {
     for (int s = 0; s < nsteps; ++s) {
         for (auto &el : b->elem) el.zero_force();
         for (auto &f : b->force) f = {0, 0, 0};
+        for (auto &fc : b->surface) fc.zero_force();
         if (update_internal_forces(b)) return 1;
         int st = update_positions(b);
         if (st) return st;

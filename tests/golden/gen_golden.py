@@ -27,7 +27,8 @@ sys.path.insert(0, ROOT)
 sys.path.insert(0, os.path.join(ROOT, "oracle"))
 
 import pyoracle as po  # noqa: E402
-from ffea_ci_demo_gb300.mesh import apply_shear, kuhn_cube  # noqa: E402
+from ffea_ci_demo_gb300.mesh import (apply_shear, faces_on_plane, kuhn_cube, surface_faces,  # noqa: E402
+                                     write_ctforces, write_surface)
 
 MESO_LENGTH = 1.7e-10
 
@@ -69,6 +70,35 @@ def gen_rng():
                         known_answer=known, **{k: v for k, v in states.items()})
 
 
+def ctf_case(m, directory, name="ctf"):
+    """Constant-force inputs for a Kuhn cube of side 20 (file units): linear forces on a vertex (twice),
+    on a midpoint and on every node; two sets of surface faces, the top face z = 20 and half of the x = 0
+    face together with three top faces (so three faces carry both sets). Writes ``name``.ctforces and
+    ``name``.surf into ``directory`` and returns their paths."""
+    faces = surface_faces(m)
+    top = faces_on_plane(m, faces, 2, 20.0)
+    side = faces_on_plane(m, faces, 0, 0.0)
+    ctf = os.path.join(directory, name + ".ctforces")
+    surf = os.path.join(directory, name + ".surf")
+    write_surface(surf, faces)
+    write_ctforces(ctf, linear=[(2e-12, (1.0, 2.0, 3.0), 0, 0, 9), (5e-12, (0.0, 0.0, -1.0), 0, 0, m.n_linear + 7),
+                                (3e-13, (1.0, 0.0, 0.0), 0, 0, "all"), (1e-12, (-1.0, 0.5, 0.0), 0, 0, 9),
+                                (4e-12, (0.0, 1.0, 0.0), 1, 0, 3)],
+                   surface=[(2e-11, (0.0, 0.0, 1.0), 0, 0, top),
+                            (1e-11, (0.3, -1.0, 0.2), 0, 0, np.concatenate([side[: len(side) // 2], top[:3]])),
+                            (1e-11, (1.0, 0.0, 0.0), 1, 0, top)])
+    return ctf, surf
+
+
+def file_digest(*paths):
+    import hashlib
+    h = hashlib.sha256()
+    for p in paths:
+        with open(p, "rb") as f:
+            h.update(f.read())
+    return h.hexdigest()
+
+
 def digest(*arrays):
     """sha256 of the arrays' bytes: pins large integer structures without storing them."""
     import hashlib
@@ -78,10 +108,13 @@ def digest(*arrays):
     return h.hexdigest()
 
 
-def dump_blob(name, m, pos0, steps, full=True, **kw):
+def dump_blob(name, m, pos0, steps, full=True, ctf=None, **kw):
     b = po.RefBlob(m, **kw)
     b.set_pos(pos0)
     out = {"n": m.n_nodes, "T": m.n_elem, "steps": steps}
+    if ctf is not None:
+        b.set_ctforces(po.read_ctforces(ctf[0], 0, m.n_nodes), po.read_surface(ctf[1]))
+        out["ctf_sha256"] = file_digest(*ctf)
     rest = b.rest()
     out["jinv0"] = rest["jinv0"]
     out["mat"] = rest["mat"]
@@ -144,6 +177,16 @@ def main():
               calc_noise=1, calc_stokes=1)
     dump_blob("cube3_cg_pin_stokes", m3, sheared(m3), 10, solver="CG", dt=1e-14, kT=4.11e-21,
               calc_noise=1, calc_stokes=1)
+    # constant linear and surface forces (with the pins, drag and noise of the previous cases)
+    import tempfile
+    with tempfile.TemporaryDirectory() as d:
+        ctf = ctf_case(m3, d)
+        common = dict(kT=4.11e-21, calc_noise=1, calc_stokes=1, ctf=ctf)
+        dump_blob("cube3_nomass_ctf", m3, sheared(m3), 10, solver="CG_nomass", dt=1e-12, **common)
+        dump_blob("cube3_lumped_ctf", m3, sheared(m3), 10, solver="masslumped", dt=1e-14, **common)
+        dump_blob("cube3_cg_ctf", m3, sheared(m3), 10, solver="CG", dt=1e-14, **common)
+        dump_blob("cube3_nomass_ctf_kT0", m3, sheared(m3), 20, solver="CG_nomass", dt=1e-12, kT=0.0, calc_noise=0,
+                  calc_stokes=1, ctf=ctf)
     # the CPU-runnable benchmark cube: 6^3 cells, 1296 tets, 1000 steps
     m6 = case_mesh(6, seed=12345)
     for solver in ("masslumped", "CG"):

@@ -12,7 +12,7 @@ import numpy as np
 import pytest
 
 import pyoracle as po
-from gen_golden import case_mesh, digest, sheared
+from gen_golden import case_mesh, ctf_case, digest, file_digest, sheared
 
 GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 
@@ -60,6 +60,14 @@ CASES = {
                                 dict(solver="masslumped", dt=1e-14, kT=4.11e-21, calc_noise=1, calc_stokes=1)),
     "cube3_cg_pin_stokes": (lambda: case_mesh(3, 7, [0, 1, 5, 66]), 0.02,
                             dict(solver="CG", dt=1e-14, kT=4.11e-21, calc_noise=1, calc_stokes=1)),
+    "cube3_nomass_ctf": (lambda: case_mesh(3, 7, [0, 1, 5, 66]), 0.02,
+                         dict(solver="CG_nomass", dt=1e-12, kT=4.11e-21, calc_noise=1, calc_stokes=1)),
+    "cube3_lumped_ctf": (lambda: case_mesh(3, 7, [0, 1, 5, 66]), 0.02,
+                         dict(solver="masslumped", dt=1e-14, kT=4.11e-21, calc_noise=1, calc_stokes=1)),
+    "cube3_cg_ctf": (lambda: case_mesh(3, 7, [0, 1, 5, 66]), 0.02,
+                     dict(solver="CG", dt=1e-14, kT=4.11e-21, calc_noise=1, calc_stokes=1)),
+    "cube3_nomass_ctf_kT0": (lambda: case_mesh(3, 7, [0, 1, 5, 66]), 0.02,
+                             dict(solver="CG_nomass", dt=1e-12, kT=0.0, calc_noise=0, calc_stokes=1)),
     "cube6_masslumped_kT0_1000": (lambda: case_mesh(6, 12345), 0.02,
                                   dict(solver="masslumped", dt=1e-14, kT=0.0, calc_noise=0)),
     "cube6_masslumped_noise_1000": (lambda: case_mesh(6, 12345), 0.0,
@@ -75,12 +83,16 @@ CASES = {
 
 
 @pytest.mark.parametrize("name", sorted(CASES))
-def test_oracle_matches_reference_golden(oracle_built, name):
+def test_oracle_matches_reference_golden(oracle_built, name, tmp_path):
     make, strain, kw = CASES[name]
     g = load(name)
     m = make()
     b = po.OracleBlob(m, threads=1, **kw)
     b.set_pos(sheared(m, strain))
+    if "ctf_sha256" in g:  # constant forces: the same files the reference was given
+        ctf = ctf_case(m, str(tmp_path))
+        assert file_digest(*ctf) == str(g["ctf_sha256"])
+        b.set_ctforces(po.read_ctforces(ctf[0], 0, m.n_nodes), po.read_surface(ctf[1]))
     solver = kw["solver"]
     c = b.contrib()
     if "contrib_ptr" in g:
