@@ -169,6 +169,7 @@ struct BlobImpl final : ffea_gpu_blob {
     DevStatus *st;
     GridBarrier *gb;
     int cg_grid = 0, gather_blocks = 0, partial_stride = 0, tpn = 4;
+    int cg_npb = 0;  // mixed path: rows per block of the owned-rows CG (0: cg_mixed_kernel)
     float4 *dpos = nullptr;  // mixed path: node offsets from the reference point
     // measurements: densities, reference positions of vertices and midpoints (SoA), per-block sums
     R *rho = nullptr;
@@ -331,6 +332,15 @@ struct BlobImpl final : ffea_gpu_blob {
         tpn = 8;
         while (tpn > 1 && (long long)N * tpn > lanes) tpn >>= 1;
         partial_stride = cg_grid;
+        // mixed path: each block keeps a run of rows in shared memory when they fit (FFEA_GPU_CG_OWN=0 turns
+        // this off); the run is a multiple of a warp's rows so that a warp's rows share a SELL slice
+        if (mixed) {
+            const char *own = getenv("FFEA_GPU_CG_OWN");
+            const int maxrows = (own && own[0] == '0') ? 0 : Launch<R>::cg_own_max_rows(device);
+            const int align = 32 / tpn, rows = (N + cg_grid - 1) / cg_grid;
+            const int npb = (rows + align - 1) / align * align;
+            cg_npb = (maxrows > 0 && npb <= maxrows) ? npb : 0;
+        }
         CK(mem.alloc(&partials, (mixed ? MIXED_PARTIAL_ROWS : 3) * (size_t)partial_stride));
         CK(mem.alloc(&st, 1));
         hist_cap = std::min(std::max(p.max_iterations_cg, 1), 1 << 20);
@@ -432,6 +442,7 @@ struct BlobImpl final : ffea_gpu_blob {
         CK(cudaMemsetAsync(phase_ns, 0, FFEA_GPU_CG_PHASES * sizeof(unsigned long long), stream));
         ca.dpos = dpos; ca.nmodes = nomass ? nmodes : 0;
         for (int i = 0; i < 36; ++i) ca.modes[i] = modes[i];
+        ca.npb = cg_npb;
         CK(Launch<R>::cg(ca, cg_grid, stream));
         return FFEA_GPU_OK;
     }

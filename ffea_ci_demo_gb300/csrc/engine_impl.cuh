@@ -59,13 +59,46 @@ int Launch<R>::cg_max_grid(int device) {
 }
 
 template <class R>
+int Launch<R>::cg_own_max_rows(int device) {
+    if constexpr (std::is_same<R, float>::value) {
+        int optin = 0, nsm = 0;
+        if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device) != cudaSuccess ||
+            cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device) != cudaSuccess)
+            return 0;
+        cudaFuncAttributes fa{};
+        if (cudaFuncGetAttributes(&fa, cg_mixed_own_kernel<R>) != cudaSuccess) return 0;
+        const int dyn = optin - (int)fa.sharedSizeBytes;
+        if (dyn <= 0 || cudaFuncSetAttribute(cg_mixed_own_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             dyn) != cudaSuccess)
+            return 0;
+        const int rows = dyn / (int)own_smem_bytes(1);
+        int per_sm = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, cg_mixed_own_kernel<R>, CG_THREADS,
+                                                          own_smem_bytes(rows)) != cudaSuccess || per_sm < 1)
+            return 0;
+        return rows;
+    } else {
+        (void)device;
+        return 0;
+    }
+}
+
+template <class R>
 cudaError_t Launch<R>::cg(const CgArgs<R> &a, int grid, cudaStream_t s) {
     CgArgs<R> args = a;
     void *params[] = {&args};
     const void *fn;
-    if constexpr (std::is_same<R, float>::value) fn = (const void *)cg_mixed_kernel<R>;
-    else fn = (const void *)cg_kernel<R>;
-    cudaError_t e = cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(CG_THREADS), params, 0, s);
+    size_t smem = 0;
+    if constexpr (std::is_same<R, float>::value) {
+        fn = (const void *)cg_mixed_kernel<R>;
+        if (a.npb > 0) {
+            fn = (const void *)cg_mixed_own_kernel<R>;
+            smem = own_smem_bytes(a.npb);
+        }
+    } else {
+        fn = (const void *)cg_kernel<R>;
+    }
+    cudaError_t e = cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(CG_THREADS), params, smem, s);
     count_launch();
     return e;
 }

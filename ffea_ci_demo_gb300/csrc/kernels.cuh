@@ -542,6 +542,7 @@ struct CgArgs {
     const float4 *dpos;
     int nmodes;
     double modes[36];
+    int npb;              // cg_mixed_own_kernel: rows owned by each block (a multiple of 32 / tpn)
 };
 
 // p at node b for this iteration: p_new = beta p_old + D^{-1} r (vec3_scale_and_add with the

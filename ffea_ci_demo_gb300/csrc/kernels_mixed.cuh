@@ -356,4 +356,298 @@ __global__ void __launch_bounds__(1024, 1) cg_mixed_kernel(const __grid_constant
     }
 }
 
+// Block reduction of NV FP32 per-thread values straight into the per-block partial rows: FP32 within
+// each warp, then warp i sums value i over the warps in double-float and its lane 0 stores the pair.
+// NV <= 32. The caller must pass a __syncthreads() before smem is written again.
+template <int NV>
+__device__ __forceinline__ void block_reduce_store(const float (&v)[NV], float *smem, float2 *partials, int stride,
+                                                   int row0) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+    for (int i = 0; i < NV; ++i) {
+        const float w = warp_sum_f(v[i]);
+        if (lane == 0) smem[i * 32 + wid] = w;
+    }
+    __syncthreads();
+    if (wid < NV) {
+        df32 t = {lane < nw ? smem[wid * 32 + lane] : 0.f, 0.f};
+        t = warp_sum_df(t);
+        if (lane == 0) partials[(row0 + wid) * stride + blockIdx.x] = make_float2(t.hi, t.lo);
+    }
+}
+
+// grid_sum_df with each lane's loads issued eight at a time before their sums: the same fixed order, the
+// partials' L2 latency paid once per 256 blocks.
+template <int NV>
+__device__ __forceinline__ void grid_sum_df8(const float2 *partials, int stride, int nb, double *s_out) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int i = wid; i < NV; i += nw) {
+        df32 t = {0.f, 0.f};
+        for (int b0 = 0; b0 < nb; b0 += 256) {
+            float2 q[8];
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+                const int b = b0 + lane + 32 * j;
+                q[j] = (b < nb) ? __ldcg(partials + i * stride + b) : make_float2(0.f, 0.f);
+            }
+#pragma unroll
+            for (int j = 0; j < 8; ++j) t = df_add(t, df32{q[j].x, q[j].y});
+        }
+        t = warp_sum_df(t);
+        if (lane == 0) s_out[i] = (double)t.hi + (double)t.lo;
+    }
+    __syncthreads();
+}
+
+// Row a of q = V p for cg_mixed_own_kernel: p at a neighbour b is formed from the preconditioned residual
+// z_b and the previous direction, both stored as float4 per node (two 16-byte loads per neighbour).
+__device__ __forceinline__ void spmv_row_z(const CgArgs<float> &g, const float4 *z4, const float4 *p4, float beta,
+                                           bool first, int a, int sub, bool valid, float &q0, float &q1, float &q2) {
+    q0 = 0.f; q1 = 0.f; q2 = 0.f;
+    const int tpn = g.tpn;
+    if (valid) {
+        const int s = a >> 5, lane = a & 31;
+        const int base = __ldg(g.slice_ptr + s);
+        const int len = __ldg(g.rowlen + a);
+        if (g.block3) {
+            const float *v = g.val + 9 * (size_t)base + lane;
+            int k = sub;
+            int bn = (k < len) ? __ldg(g.bcol + base + 32 * k + lane) : 0;
+#pragma unroll 1
+            for (; k < len; k += tpn) {
+                const int b = bn;
+                if (k + tpn < len) bn = __ldg(g.bcol + base + 32 * (k + tpn) + lane);
+                const float *vk = v + (size_t)32 * 9 * k;
+                const float v0 = __ldg(vk), v1 = __ldg(vk + 32), v2 = __ldg(vk + 64), v3 = __ldg(vk + 96),
+                            v4 = __ldg(vk + 128), v5 = __ldg(vk + 160), v6 = __ldg(vk + 192), v7 = __ldg(vk + 224),
+                            v8 = __ldg(vk + 256);
+                const float4 z = z4[b];
+                float p0 = z.x, p1 = z.y, p2 = z.z;
+                if (!first) {
+                    const float4 po = p4[b];
+                    p0 = fmaf(beta, po.x, p0); p1 = fmaf(beta, po.y, p1); p2 = fmaf(beta, po.z, p2);
+                }
+                q0 = fmaf(v0, p0, q0); q0 = fmaf(v1, p1, q0); q0 = fmaf(v2, p2, q0);
+                q1 = fmaf(v3, p0, q1); q1 = fmaf(v4, p1, q1); q1 = fmaf(v5, p2, q1);
+                q2 = fmaf(v6, p0, q2); q2 = fmaf(v7, p1, q2); q2 = fmaf(v8, p2, q2);
+            }
+        } else {
+            const float *v = g.val + base + lane;
+            for (int k = sub; k < len; k += tpn) {
+                const int b = __ldg(g.bcol + base + 32 * k + lane);
+                const float m = __ldg(v + 32 * k);
+                const float4 z = z4[b];
+                float p0 = z.x, p1 = z.y, p2 = z.z;
+                if (!first) {
+                    const float4 po = p4[b];
+                    p0 = fmaf(beta, po.x, p0); p1 = fmaf(beta, po.y, p1); p2 = fmaf(beta, po.z, p2);
+                }
+                q0 = fmaf(m, p0, q0);
+                q1 = fmaf(m, p1, q1);
+                q2 = fmaf(m, p2, q2);
+            }
+        }
+    }
+    for (int o = 1; o < tpn; o <<= 1) {
+        q0 += __shfl_xor_sync(0xffffffffu, q0, o);
+        q1 += __shfl_xor_sync(0xffffffffu, q1, o);
+        q2 += __shfl_xor_sync(0xffffffffu, q2, o);
+    }
+}
+
+// Bytes of dynamic shared memory cg_mixed_own_kernel needs for npb owned rows: x, r, q, p, D^{-1}, D, d.
+constexpr int OWN_FIELDS = 21;
+__host__ __device__ constexpr size_t own_smem_bytes(int npb) { return (size_t)OWN_FIELDS * npb * sizeof(float); }
+
+// The mixed CG of cg_mixed_kernel with each block owning a fixed run of npb rows: the rows' x, r, q, p,
+// D^{-1}, D and offsets stay in shared memory for the whole solve, the block computes its own rows' SpMV,
+// and only what other blocks read goes to global memory: z = D^{-1} r (in the q buffer) and the search
+// direction (double-buffered). The arithmetic is the same as cg_mixed_kernel's: p = z + beta p_old is
+// formed identically by the owner and by every block that reads row b as a neighbour.
+template <class R>
+__global__ void __launch_bounds__(1024, 1) cg_mixed_own_kernel(const __grid_constant__ CgArgs<R> g) {
+    static_assert(sizeof(R) == sizeof(float), "the owned-rows CG is the mixed path's");
+    extern __shared__ float sn[];
+    __shared__ float smemf[MIXED_A_NP * 32];
+    __shared__ double s_sc[MIXED_GATHER_NP];
+    __shared__ double s_A6[36];
+    __shared__ float s_alpha, s_beta, s_tau[3], s_Om[3];
+    __shared__ double s_delta;
+    __shared__ int s_conv;
+    DevStatus *st = g.st;
+    if (st->abort) return;
+    const bool defl = g.nmodes > 0;
+    unsigned long long tm = (blockIdx.x == 0 && threadIdx.x == 0) ? globaltimer_ns() : 0ull;
+    float2 *partials = reinterpret_cast<float2 *>(g.partials);
+    const int npb = g.npb, a0 = blockIdx.x * npb;
+    const int nloc = max(0, min(npb, g.N - a0));
+    float *sx = sn, *sr = sn + 3 * npb, *sq = sn + 6 * npb, *sp = sn + 9 * npb, *sdi = sn + 12 * npb,
+          *sdg = sn + 15 * npb, *sd = sn + 18 * npb;
+    float4 *z4 = reinterpret_cast<float4 *>(g.q);
+    grid_sum_df8<MIXED_GATHER_NP>(reinterpret_cast<const float2 *>(g.init_partials), g.init_stride, g.n_init, s_sc);
+    const double f2 = s_sc[0];
+    mixed_setup(g, s_sc, s_A6, s_tau, s_Om, &s_beta, &s_conv);
+    float acc0[1] = {0.f};
+    for (int l = threadIdx.x; l < nloc; l += blockDim.x) {
+        const int a = a0 + l;
+        float r0 = g.r[4 * a], r1 = g.r[4 * a + 1], r2 = g.r[4 * a + 2];
+        const float i0 = g.dinv[4 * a], i1 = g.dinv[4 * a + 1], i2 = g.dinv[4 * a + 2];
+        if (defl) {
+            const float4 d = g.dpos[a];
+            const float D0 = g.diag[4 * a], D1 = g.diag[4 * a + 1], D2 = g.diag[4 * a + 2];
+            r0 -= D0 * (s_tau[0] + (s_Om[1] * d.z - s_Om[2] * d.y));
+            r1 -= D1 * (s_tau[1] + (s_Om[2] * d.x - s_Om[0] * d.z));
+            r2 -= D2 * (s_tau[2] + (s_Om[0] * d.y - s_Om[1] * d.x));
+            sdg[l] = D0; sdg[npb + l] = D1; sdg[2 * npb + l] = D2;
+            sd[l] = d.x; sd[npb + l] = d.y; sd[2 * npb + l] = d.z;
+        }
+        sr[l] = r0; sr[npb + l] = r1; sr[2 * npb + l] = r2;
+        sdi[l] = i0; sdi[npb + l] = i1; sdi[2 * npb + l] = i2;
+        sx[l] = 0.f; sx[npb + l] = 0.f; sx[2 * npb + l] = 0.f;
+        const float z0 = i0 * r0, z1 = i1 * r1, z2 = i2 * r2;
+        z4[a] = make_float4(z0, z1, z2, 0.f);
+        acc0[0] += r0 * z0 + r1 * z1 + r2 * z2;
+    }
+    const int row0 = MIXED_A_NP + MIXED_B_NP;
+    block_reduce_store<1>(acc0, smemf, partials, g.stride, row0);
+    bool ok = grid_sync(g.gb, st, g.limit_ns);
+    if (ok) {
+        grid_sum_df8<1>(partials + row0 * g.stride, 0, gridDim.x, s_sc);
+        if (threadIdx.x == 0) s_delta = s_sc[0];
+        __syncthreads();
+    }
+    const float4 *pold = reinterpret_cast<const float4 *>(g.pbuf0);
+    float4 *pnew = reinterpret_cast<float4 *>(g.pbuf1);
+    const int tpn = g.tpn, gpb = blockDim.x / tpn, grp = threadIdx.x / tpn, sub = threadIdx.x % tpn;
+    const int npass = (nloc + gpb - 1) / gpb;
+    FFEA_MARK(g, tm, 0);
+    int it = 0;
+    for (; ok && it < g.imax; ++it) {
+        const bool first = it == 0;
+        const float beta = s_beta;
+        // phase A: q = V p over the block's rows (p formed on the fly); p.q; moments of D p
+        float acc[MIXED_A_NP];
+#pragma unroll
+        for (int i = 0; i < MIXED_A_NP; ++i) acc[i] = 0.f;
+        for (int ps = 0; ps < npass; ++ps) {
+            const int l = ps * gpb + grp;
+            const bool valid = l < nloc;
+            float q0, q1, q2;
+            spmv_row_z(g, z4, pold, beta, first, a0 + l, sub, valid, q0, q1, q2);
+            if (!valid || sub != 0) continue;
+            const float z0 = sdi[l] * sr[l], z1 = sdi[npb + l] * sr[npb + l], z2 = sdi[2 * npb + l] * sr[2 * npb + l];
+            float p0 = z0, p1 = z1, p2 = z2;
+            if (!first) {
+                p0 = fmaf(beta, sp[l], z0); p1 = fmaf(beta, sp[npb + l], z1); p2 = fmaf(beta, sp[2 * npb + l], z2);
+            }
+            sp[l] = p0; sp[npb + l] = p1; sp[2 * npb + l] = p2;
+            sq[l] = q0; sq[npb + l] = q1; sq[2 * npb + l] = q2;
+            pnew[a0 + l] = make_float4(p0, p1, p2, 0.f);
+            acc[0] += p0 * q0 + p1 * q1 + p2 * q2;
+            if (defl) {
+                const float dx = sd[l], dy = sd[npb + l], dz = sd[2 * npb + l];
+                const float e0 = sdg[l] * p0, e1 = sdg[npb + l] * p1, e2 = sdg[2 * npb + l] * p2;
+                acc[1] += e0; acc[2] += e1; acc[3] += e2;
+                acc[4] += dy * e2 - dz * e1;
+                acc[5] += dz * e0 - dx * e2;
+                acc[6] += dx * e1 - dy * e0;
+            }
+        }
+        FFEA_MARK(g, tm, 1);
+        block_reduce_store<MIXED_A_NP>(acc, smemf, partials, g.stride, 0);
+        FFEA_MARK(g, tm, 2);
+        if (!(ok = grid_sync(g.gb, st, g.limit_ns))) break;
+        FFEA_MARK(g, tm, 3);
+        grid_sum_df8<MIXED_A_NP>(partials, g.stride, gridDim.x, s_sc);
+        if (threadIdx.x < 32) {
+            const int ln = threadIdx.x;
+            double tO = 0.0;
+            if (defl && ln < 6) {
+#pragma unroll
+                for (int qq = 0; qq < 6; ++qq) tO += s_A6[6 * ln + qq] * s_sc[1 + qq];
+            }
+            double prod = (ln < 6) ? tO * s_sc[1 + ln] : 0.0;
+#pragma unroll
+            for (int o = 4; o > 0; o >>= 1) prod += __shfl_xor_sync(0xffffffffu, prod, o);
+            if (ln < 6) {
+                if (ln < 3) s_tau[ln] = (float)tO; else s_Om[ln - 3] = (float)tO;
+            }
+            if (ln == 0) s_alpha = (float)s_delta / (float)(s_sc[0] + prod);
+        }
+        __syncthreads();
+        FFEA_MARK(g, tm, 4);
+        const float alpha = s_alpha;
+        const float t0 = s_tau[0], t1 = s_tau[1], t2 = s_tau[2], O0 = s_Om[0], O1 = s_Om[1], O2 = s_Om[2];
+        // phase B: x += alpha p ; r -= alpha (q + D (tau + Omega x d)) ; z = D^{-1} r ; r.r ; r.z
+        float acc2[MIXED_B_NP] = {0.f, 0.f};
+        for (int l = threadIdx.x; l < nloc; l += blockDim.x) {
+            float p[3], qv[3], rv[3];
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                p[c] = sp[c * npb + l];
+                qv[c] = sq[c * npb + l];
+                sx[c * npb + l] += alpha * p[c];
+            }
+            if (defl) {
+                const float dx = sd[l], dy = sd[npb + l], dz = sd[2 * npb + l];
+                qv[0] += sdg[l] * (t0 + (O1 * dz - O2 * dy));
+                qv[1] += sdg[npb + l] * (t1 + (O2 * dx - O0 * dz));
+                qv[2] += sdg[2 * npb + l] * (t2 + (O0 * dy - O1 * dx));
+            }
+            float z[3];
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                rv[c] = sr[c * npb + l] - alpha * qv[c];
+                sr[c * npb + l] = rv[c];
+                z[c] = sdi[c * npb + l] * rv[c];
+            }
+            z4[a0 + l] = make_float4(z[0], z[1], z[2], 0.f);
+            acc2[0] += rv[0] * rv[0] + rv[1] * rv[1] + rv[2] * rv[2];
+            acc2[1] += rv[0] * z[0] + rv[1] * z[1] + rv[2] * z[2];
+        }
+        FFEA_MARK(g, tm, 5);
+        block_reduce_store<MIXED_B_NP>(acc2, smemf, partials, g.stride, MIXED_A_NP);
+        FFEA_MARK(g, tm, 6);
+        if (!(ok = grid_sync(g.gb, st, g.limit_ns))) break;
+        FFEA_MARK(g, tm, 7);
+        grid_sum_df8<MIXED_B_NP>(partials + MIXED_A_NP * g.stride, g.stride, gridDim.x, s_sc);
+        if (threadIdx.x == 0) {
+            s_conv = (g.check_last || it + 1 < g.imax) && (f2 == 0.0 || s_sc[0] < g.eps2 * f2);
+            if (blockIdx.x == 0 && it < g.hist_cap) g.history[it] = (f2 == 0.0) ? 0.0 : s_sc[0] / f2;
+            const double delta_old = s_delta;
+            s_delta = s_sc[1];
+            s_beta = (float)s_delta / (float)delta_old;
+        }
+        __syncthreads();
+        FFEA_MARK(g, tm, 8);
+        if (s_conv) {
+            ++it;
+            break;
+        }
+        const float4 *t = pold; pold = pnew; pnew = const_cast<float4 *>(t);
+    }
+    // the solution (and residual) back to global memory
+    for (int l = threadIdx.x; l < nloc; l += blockDim.x) {
+        const int a = a0 + l;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            g.x[4 * a + c] = sx[c * npb + l];
+            g.r[4 * a + c] = sr[c * npb + l];
+        }
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        if (!ok) {
+            st->abort = 1;
+        } else if (!s_conv) {
+            st->cg_fail = 1;
+            st->abort = 1;
+            st->last_iters = g.imax;
+            st->total_iters += g.imax;
+        } else {
+            st->last_iters = it;
+            st->total_iters += it;
+        }
+    }
+}
+
 }  // namespace ffea
