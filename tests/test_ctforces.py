@@ -24,6 +24,7 @@ from ffea_ci_demo_gb300 import lib
 from ffea_ci_demo_gb300.mesh import (faces_on_plane, kuhn_box, surface_faces, write_ctforces, write_script,
                                      write_structure, write_surface)
 from gen_golden import case_mesh, ctf_case, file_digest, sheared
+from fe import linear_fe_extension
 from test_world import seeds_from
 
 GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
@@ -142,46 +143,6 @@ def test_script_with_constant_forces_matches_blob(gpu, tmp_path):
         f.write("\n".join(ln for ln in txt.split("\n") if "<surface =" not in ln))
     with pytest.raises(lib.FFEAError):
         lib.World(script)
-
-
-def linear_fe_extension(mesh, f_ext, pinned, G, K):
-    """Static small-strain extension of the mesh's linear tetrahedra (Lame mu = G, lambda = K - 2G/3, the
-    small-strain limit of the reference's shear and bulk stresses) under the vertex forces f_ext (N),
-    with the pinned vertices held: the displacement of every vertex (m)."""
-    import scipy.sparse as sp
-    import scipy.sparse.linalg as spla
-    nv = mesh.n_linear
-    t4 = mesh.tets[:, :4]
-    P = mesh.pos[:nv] * mesh.scale
-    lam = K - 2.0 * G / 3.0
-    D = np.zeros((6, 6))
-    D[:3, :3] = lam
-    D[np.arange(3), np.arange(3)] += 2.0 * G
-    D[np.arange(3, 6), np.arange(3, 6)] = G
-    rows, cols, vals = [], [], []
-    for e in range(t4.shape[0]):
-        Mx = np.hstack([np.ones((4, 1)), P[t4[e]]])
-        g = np.linalg.inv(Mx)[1:, :]
-        V = abs(np.linalg.det(Mx)) / 6.0
-        B = np.zeros((6, 12))
-        for a in range(4):
-            gx, gy, gz = g[:, a]
-            B[0, 3 * a], B[1, 3 * a + 1], B[2, 3 * a + 2] = gx, gy, gz
-            B[3, 3 * a], B[3, 3 * a + 1] = gy, gx
-            B[4, 3 * a + 1], B[4, 3 * a + 2] = gz, gy
-            B[5, 3 * a], B[5, 3 * a + 2] = gz, gx
-        idx = (3 * t4[e][:, None] + np.arange(3)).ravel()
-        rows.append(np.repeat(idx, 12))
-        cols.append(np.tile(idx, 12))
-        vals.append((V * B.T @ D @ B).ravel())
-    Kg = sp.csr_matrix((np.concatenate(vals), (np.concatenate(rows), np.concatenate(cols))), shape=(3 * nv,) * 2)
-    free = np.ones(3 * nv, bool)
-    pv = pinned[pinned < nv]
-    for c in range(3):
-        free[3 * pv + c] = False
-    u = np.zeros(3 * nv)
-    u[free] = spla.spsolve(Kg[free][:, free].tocsc(), f_ext[:nv].ravel()[free])
-    return u.reshape(-1, 3)
 
 
 @pytest.mark.gpu

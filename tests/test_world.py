@@ -9,6 +9,11 @@
   test allows 5e-4).
 * Equipartition, as the reference's physics test checks it: the mean strain energy over the
   measurement file is (3N - 6) kT / 2 within 3%.
+* Mode variances: over the same run's trajectory, the variance of each of the 3N - 6 internal normal
+  modes of the small-strain stiffness (tests/fe.py) is the Boltzmann value kT / lambda_k. Each mode's
+  ratio carries a sampling error sqrt(2 / n_eff) (n_eff from its autocorrelation): every mode lies within
+  5 of those errors, and the mean ratio over the modes within 3% (the harmonic approximation and the
+  Euler step, dt / tau <= 2%, each bias it by about 1%).
 """
 import ctypes as C
 import os
@@ -18,6 +23,7 @@ import numpy as np
 import pytest
 
 import pyoracle as po
+from fe import mode_variance_ratios
 from ffea_ci_demo_gb300 import build, lib
 from ffea_ci_demo_gb300.mesh import kuhn_cube, write_script, write_structure
 
@@ -52,6 +58,22 @@ def frames(path):
     with open(path) as f:
         txt = f.read()
     return [int(ln.split("step")[1]) for ln in txt.split("\n") if ln.startswith("Blob 0, Conformation 0, step")]
+
+
+def read_ftj(path, n_take):
+    """Positions (m) of the first n_take nodes of blob 0 in every frame of a trajectory file."""
+    out = []
+    with open(path) as f:
+        lines = f.read().split("\n")
+    i = 0
+    while i < len(lines):
+        if lines[i].startswith("Blob 0, Conformation 0, step"):
+            rows = lines[i + 2:i + 2 + n_take]
+            out.append([[float(x) for x in r.split()[:3]] for r in rows])
+            i += 2 + n_take
+        else:
+            i += 1
+    return np.array(out)
 
 
 def test_script_refusals(tmp_path):
@@ -129,7 +151,7 @@ def test_world_restart_continues_the_stream(gpu, tmp_path):
 def test_equipartition_of_strain_energy(gpu, tmp_path, precision):
     n = 2
     steps, check = 120000, 300
-    _, _, path = make_script(tmp_path, "eq", n=n, num_steps=steps, check=check, rng_seed=2024, dt=1e-14,
+    m, _, path = make_script(tmp_path, "eq", n=n, num_steps=steps, check=check, rng_seed=2024, dt=1e-14,
                              kT=4.11e-21, calc_noise=1, epsilon=1e-6)
     import time
     t0 = time.perf_counter()
@@ -142,3 +164,12 @@ def test_equipartition_of_strain_energy(gpu, tmp_path, precision):
     dev = abs(se.mean() / want - 1)
     print(precision, "equipartition: mean strain energy / (3N-6)kT/2 - 1 =", dev, "samples", se.size)
     assert dev < 0.03
+    # mode variances over the trajectory frames (the first 40 dropped, as above)
+    frames = read_ftj(os.path.join(str(tmp_path), "eq.ftj"), nodes)[40:]
+    ratio, neff = mode_variance_ratios(frames, m.pos[:nodes] * 1e-9, m.tets[:, :4], 5.7e8, 2.2e9, 4.11e-21)
+    z = (ratio - 1) / np.sqrt(2.0 / neff)
+    print(precision, f"mode variances: {ratio.size} modes, mean ratio {ratio.mean():.4f}, range "
+          f"[{ratio.min():.3f}, {ratio.max():.3f}], n_eff {neff.min():.0f}-{neff.max():.0f}, max |z| {np.abs(z).max():.2f}")
+    assert ratio.size == 3 * nodes - 6
+    assert np.abs(z).max() < 5.0
+    assert abs(ratio.mean() - 1) < 0.03
