@@ -169,7 +169,7 @@ struct BlobImpl final : ffea_gpu_blob {
     DevStatus *st;
     GridBarrier *gb;
     int cg_grid = 0, gather_blocks = 0, partial_stride = 0, tpn = 4;
-    int cg_npb = 0;  // mixed path: rows per block of the owned-rows CG (0: cg_mixed_kernel)
+    int cg_npb = 0;  // rows per block of the owned-rows CG kernels (0: cg_kernel / cg_mixed_kernel)
     float4 *dpos = nullptr;  // mixed path: node offsets from the reference point
     // measurements: densities, reference positions of vertices and midpoints (SoA), per-block sums
     R *rho = nullptr;
@@ -332,9 +332,9 @@ struct BlobImpl final : ffea_gpu_blob {
         tpn = 8;
         while (tpn > 1 && (long long)N * tpn > lanes) tpn >>= 1;
         partial_stride = cg_grid;
-        // mixed path: each block keeps a run of rows in shared memory when they fit (FFEA_GPU_CG_OWN=0 turns
-        // this off); the run is a multiple of a warp's rows so that a warp's rows share a SELL slice
-        if (mixed) {
+        // each block keeps a run of rows in shared memory when they fit (FFEA_GPU_CG_OWN=0 turns this off);
+        // the run is a multiple of a warp's rows so that a warp's rows share a SELL slice
+        {
             const char *own = getenv("FFEA_GPU_CG_OWN");
             const int maxrows = (own && own[0] == '0') ? 0 : Launch<R>::cg_own_max_rows(device);
             const int align = 32 / tpn, rows = (N + cg_grid - 1) / cg_grid;

@@ -58,29 +58,31 @@ int Launch<R>::cg_max_grid(int device) {
     return nsm * per_sm;
 }
 
+// the most rows per block an owned-rows CG kernel (bytes_per_row of dynamic shared memory each) can hold
+template <class K>
+static int own_max_rows(K kernel, int device, int bytes_per_row) {
+    int optin = 0;
+    if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device) != cudaSuccess) return 0;
+    cudaFuncAttributes fa{};
+    if (cudaFuncGetAttributes(&fa, kernel) != cudaSuccess) return 0;
+    const int dyn = optin - (int)fa.sharedSizeBytes;
+    if (dyn <= 0 || cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn) != cudaSuccess)
+        return 0;
+    const int rows = dyn / bytes_per_row;
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, CG_THREADS, (size_t)rows * bytes_per_row) !=
+            cudaSuccess ||
+        per_sm < 1)
+        return 0;
+    return rows;
+}
+
 template <class R>
 int Launch<R>::cg_own_max_rows(int device) {
-    if constexpr (std::is_same<R, float>::value) {
-        int optin = 0, nsm = 0;
-        if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device) != cudaSuccess ||
-            cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device) != cudaSuccess)
-            return 0;
-        cudaFuncAttributes fa{};
-        if (cudaFuncGetAttributes(&fa, cg_mixed_own_kernel<R>) != cudaSuccess) return 0;
-        const int dyn = optin - (int)fa.sharedSizeBytes;
-        if (dyn <= 0 || cudaFuncSetAttribute(cg_mixed_own_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             dyn) != cudaSuccess)
-            return 0;
-        const int rows = dyn / (int)own_smem_bytes(1);
-        int per_sm = 0;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, cg_mixed_own_kernel<R>, CG_THREADS,
-                                                          own_smem_bytes(rows)) != cudaSuccess || per_sm < 1)
-            return 0;
-        return rows;
-    } else {
-        (void)device;
-        return 0;
-    }
+    if constexpr (std::is_same<R, float>::value)
+        return own_max_rows(cg_mixed_own_kernel<R>, device, (int)own_smem_bytes(1));
+    else
+        return own_max_rows(cg_own_kernel<R>, device, (int)own_smem_bytes_d(1));
 }
 
 template <class R>
@@ -97,6 +99,10 @@ cudaError_t Launch<R>::cg(const CgArgs<R> &a, int grid, cudaStream_t s) {
         }
     } else {
         fn = (const void *)cg_kernel<R>;
+        if (a.npb > 0) {
+            fn = (const void *)cg_own_kernel<R>;
+            smem = own_smem_bytes_d(a.npb);
+        }
     }
     cudaError_t e = cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(CG_THREADS), params, smem, s);
     count_launch();

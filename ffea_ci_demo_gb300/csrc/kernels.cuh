@@ -785,6 +785,204 @@ __global__ void __launch_bounds__(1024, 1) cg_kernel(const __grid_constant__ CgA
     }
 }
 
+// Row a of q = V p for cg_own_kernel (FP64): the direction at neighbour b read as two 16-byte loads; the
+// products are fused in the same order as spmv_row.
+template <class R>
+__device__ __forceinline__ void spmv_row_pd(const CgArgs<R> &g, const double2 *p2, int a, int sub, bool valid, R &q0,
+                                            R &q1, R &q2) {
+    q0 = 0.0; q1 = 0.0; q2 = 0.0;
+    const int tpn = g.tpn;
+    if (valid) {
+        const int s = a >> 5, lane = a & 31;
+        const int base = __ldg(g.slice_ptr + s);
+        const int len = __ldg(g.rowlen + a);
+        if (g.block3) {
+            const R *v = g.val + 9 * (size_t)base + lane;
+            int k = sub;
+            int bn = (k < len) ? __ldg(g.bcol + base + 32 * k + lane) : 0;
+#pragma unroll 1
+            for (; k < len; k += tpn) {
+                const int b = bn;
+                if (k + tpn < len) bn = __ldg(g.bcol + base + 32 * (k + tpn) + lane);
+                const R *vk = v + (size_t)32 * 9 * k;
+                const R v0 = __ldg(vk), v1 = __ldg(vk + 32), v2 = __ldg(vk + 64), v3 = __ldg(vk + 96),
+                        v4 = __ldg(vk + 128), v5 = __ldg(vk + 160), v6 = __ldg(vk + 192), v7 = __ldg(vk + 224),
+                        v8 = __ldg(vk + 256);
+                const double2 pa = p2[2 * b], pb = p2[2 * b + 1];
+                const R p0 = pa.x, p1 = pa.y, p2v = pb.x;
+                q0 = fma(v0, p0, q0); q0 = fma(v1, p1, q0); q0 = fma(v2, p2v, q0);
+                q1 = fma(v3, p0, q1); q1 = fma(v4, p1, q1); q1 = fma(v5, p2v, q1);
+                q2 = fma(v6, p0, q2); q2 = fma(v7, p1, q2); q2 = fma(v8, p2v, q2);
+            }
+        } else {
+            const R *v = g.val + base + lane;
+            for (int k = sub; k < len; k += tpn) {
+                const int b = __ldg(g.bcol + base + 32 * k + lane);
+                const R m = __ldg(v + 32 * k);
+                const double2 pa = p2[2 * b], pb = p2[2 * b + 1];
+                q0 = fma(m, (R)pa.x, q0);
+                q1 = fma(m, (R)pa.y, q1);
+                q2 = fma(m, (R)pb.x, q2);
+            }
+        }
+    }
+    for (int o = 1; o < tpn; o <<= 1) {
+        q0 += __shfl_xor_sync(0xffffffffu, q0, o);
+        q1 += __shfl_xor_sync(0xffffffffu, q1, o);
+        q2 += __shfl_xor_sync(0xffffffffu, q2, o);
+    }
+}
+
+// Bytes of dynamic shared memory cg_own_kernel needs for npb owned rows: x, r, q, p (FP64).
+__host__ __device__ constexpr size_t own_smem_bytes_d(int npb) { return (size_t)12 * npb * sizeof(double); }
+
+// The FP64 CG of cg_kernel with each block owning a fixed run of npb rows: their x, r, q and p stay in
+// shared memory for the whole solve and the block computes its own rows' SpMV, so the residual and
+// direction updates touch global memory only to publish p for the other blocks' SpMV (in the pbuf0 buffer,
+// 32 bytes per node). Every value is computed by the same expression as in cg_kernel; only the grouping of
+// the cross-node sums changes.
+template <class R>
+__global__ void __launch_bounds__(1024, 1) cg_own_kernel(const __grid_constant__ CgArgs<R> g) {
+    static_assert(sizeof(R) == sizeof(double), "the FP64 owned-rows CG");
+    extern __shared__ double snd[];
+    __shared__ double smem[2 * CG_MAX_THREADS];
+    __shared__ double s_sc[4];
+    __shared__ R s_alpha, s_beta;
+    __shared__ double s_delta;
+    __shared__ int s_conv;
+    DevStatus *st = g.st;
+    if (st->abort) return;
+    unsigned long long tm = (blockIdx.x == 0 && threadIdx.x == 0) ? globaltimer_ns() : 0ull;
+    const int npb = g.npb, a0 = blockIdx.x * npb;
+    const int nloc = max(0, min(npb, g.N - a0));
+    double *sx = snd, *sr = snd + 3 * npb, *sq = snd + 6 * npb, *sp = snd + 9 * npb;
+    double2 *p2 = reinterpret_cast<double2 *>(g.pbuf0);
+    // p = z = D^{-1} r  (conjugate_gradient_residual_assume_x_zero, src/NoMassCGSolver.cpp:196-220)
+    for (int l = threadIdx.x; l < nloc; l += blockDim.x) {
+        const int a = a0 + l;
+        R z[3];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            const R r = g.r[4 * a + c];
+            sr[c * npb + l] = r;
+            sx[c * npb + l] = 0.0;
+            z[c] = __ldg(g.dinv + 4 * a + c) * r;
+            sp[c * npb + l] = z[c];
+        }
+        p2[2 * a] = make_double2(z[0], z[1]);
+        p2[2 * a + 1] = make_double2(z[2], 0.0);
+    }
+    grid_sum_d<2>(g.init_partials, g.init_stride, g.n_init, s_sc);
+    const double f2 = s_sc[0];
+    if (threadIdx.x == 0) { s_delta = s_sc[1]; s_conv = 0; }
+    bool ok = grid_sync(g.gb, st, g.limit_ns);
+    const int tpn = g.tpn, gpb = blockDim.x / tpn, grp = threadIdx.x / tpn, sub = threadIdx.x % tpn;
+    const int npass = (nloc + gpb - 1) / gpb;
+    FFEA_MARK(g, tm, 0);
+    int it = 0;
+    for (; ok && it < g.imax; ++it) {
+        // q = V p ; pTq   (get_alpha_denominator :253-266)
+        double acc1[1] = {0.0};
+        for (int ps = 0; ps < npass; ++ps) {
+            const int l = ps * gpb + grp;
+            const bool valid = l < nloc;
+            R q0, q1, q2;
+            spmv_row_pd(g, p2, a0 + l, sub, valid, q0, q1, q2);
+            if (!valid || sub != 0) continue;
+            sq[l] = q0; sq[npb + l] = q1; sq[2 * npb + l] = q2;
+            acc1[0] += (double)fma(sp[2 * npb + l], q2, fma(sp[npb + l], q1, sp[l] * q0));
+        }
+        FFEA_MARK(g, tm, 1);
+        double out1[1];
+        block_sum_smem<1>(acc1, smem, out1);
+        if (threadIdx.x == 0) g.partials[blockIdx.x] = out1[0];
+        FFEA_MARK(g, tm, 2);
+        if (!(ok = grid_sync(g.gb, st, g.limit_ns))) break;
+        FFEA_MARK(g, tm, 3);
+        grid_sum_d<1>(g.partials, 0, gridDim.x, s_sc);
+        if (threadIdx.x == 0) s_alpha = (R)(s_delta / s_sc[0]);
+        __syncthreads();
+        FFEA_MARK(g, tm, 4);
+        const R alpha = s_alpha, malpha = -s_alpha;
+        // x += alpha p ; r += (-alpha) q ; |r|^2 ; r.z   (vec3_add_to_scaled, residual2, apply_preconditioner)
+        double acc2[2] = {0.0, 0.0};
+        for (int l = threadIdx.x; l < nloc; l += blockDim.x) {
+            const int a = a0 + l;
+            R r[3], z[3];
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                sx[c * npb + l] = fma(alpha, sp[c * npb + l], sx[c * npb + l]);
+                r[c] = fma(malpha, sq[c * npb + l], sr[c * npb + l]);
+                sr[c * npb + l] = r[c];
+                z[c] = __ldg(g.dinv + 4 * a + c) * r[c];
+            }
+            acc2[0] += (double)fma(r[2], r[2], fma(r[1], r[1], r[0] * r[0]));
+            acc2[1] += (double)fma(r[2], z[2], fma(r[1], z[1], r[0] * z[0]));
+        }
+        FFEA_MARK(g, tm, 5);
+        double out2[2];
+        block_sum_smem<2>(acc2, smem, out2);
+        if (threadIdx.x == 0) {
+            g.partials[g.stride + blockIdx.x] = out2[0];
+            g.partials[2 * g.stride + blockIdx.x] = out2[1];
+        }
+        FFEA_MARK(g, tm, 6);
+        if (!(ok = grid_sync(g.gb, st, g.limit_ns))) break;
+        FFEA_MARK(g, tm, 7);
+        grid_sum_d<2>(g.partials + g.stride, g.stride, gridDim.x, s_sc);
+        if (threadIdx.x == 0) {
+            const double res2 = (f2 == 0.0) ? 0.0 : s_sc[0] / f2;
+            if (blockIdx.x == 0 && it < g.hist_cap) g.history[it] = res2;
+            s_conv = (g.check_last || it + 1 < g.imax) && res2 < g.eps2;
+            const double delta_old = s_delta;
+            s_delta = s_sc[1];
+            s_beta = (R)(s_delta / delta_old);
+        }
+        __syncthreads();
+        FFEA_MARK(g, tm, 8);
+        if (s_conv) {
+            ++it;
+            break;
+        }
+        // p = beta p + z   (vec3_scale_and_add :202-212), published for the next SpMV
+        const R beta = s_beta;
+        for (int l = threadIdx.x; l < nloc; l += blockDim.x) {
+            const int a = a0 + l;
+            R pv[3];
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                pv[c] = fma(beta, sp[c * npb + l], __ldg(g.dinv + 4 * a + c) * sr[c * npb + l]);
+                sp[c * npb + l] = pv[c];
+            }
+            p2[2 * a] = make_double2(pv[0], pv[1]);
+            p2[2 * a + 1] = make_double2(pv[2], 0.0);
+        }
+        if (!(ok = grid_sync(g.gb, st, g.limit_ns))) break;
+        FFEA_MARK(g, tm, 9);
+    }
+    for (int l = threadIdx.x; l < nloc; l += blockDim.x) {
+        const int a = a0 + l;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            g.x[4 * a + c] = sx[c * npb + l];
+            g.r[4 * a + c] = sr[c * npb + l];
+        }
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        if (!ok) {
+            st->abort = 1;
+        } else if (!s_conv) {
+            st->cg_fail = 1;
+            st->abort = 1;
+            st->last_iters = g.imax;
+            st->total_iters += g.imax;
+        } else {
+            st->last_iters = it;
+            st->total_iters += it;
+        }
+    }
+}
+
 // ---------------------------------------------------------------------------
 // Euler update (Blob::euler_integrate :3249-3279), non-finite check, RNG advance
 // ---------------------------------------------------------------------------
