@@ -47,6 +47,7 @@ struct ffea_gpu_batch {
     float *val, *dinv, *diag;
     double *f;
     float *x, *r, *q, *pbuf0, *pbuf1;
+    float4 *zbuf = nullptr;
     float4 *dpos;
     int *elem_blob, *d_elem_off;
     uint32_t *rng_states;
@@ -197,6 +198,7 @@ int ffea_gpu_batch::init() {
     CK(mem.alloc(&q, 4 * (size_t)N));
     CK(mem.alloc(&pbuf0, 4 * (size_t)N));
     CK(mem.alloc(&pbuf1, 4 * (size_t)N));
+    CK(mem.alloc(&zbuf, (size_t)N));
     CK(mem.alloc(&dpos, (size_t)N));
     std::vector<int> eb(T);
     for (int b = 0; b < nblobs; ++b)
@@ -353,7 +355,7 @@ int ffea_gpu_batch::launch_cg_only() {
     ca.tpn = tpn;
     ca.slice_ptr = slice_ptr; ca.rowlen = rowlen; ca.bcol = bcol;
     ca.val = val; ca.dinv = dinv; ca.diag = diag;
-    ca.x = x; ca.r = r; ca.q = q; ca.pbuf0 = pbuf0; ca.pbuf1 = pbuf1;
+    ca.x = x; ca.r = r; ca.q = q; ca.pbuf0 = pbuf0; ca.pbuf1 = pbuf1; ca.z = zbuf;
     ca.dpos = dpos;
     ca.px = px; ca.py = py; ca.pz = pz;
     ca.desc = desc;

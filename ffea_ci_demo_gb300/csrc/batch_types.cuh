@@ -23,6 +23,7 @@ struct BatchCgArgs {
     const int *slice_ptr, *rowlen, *bcol;
     const float *val, *dinv, *diag;
     float *x, *r, *q, *pbuf0, *pbuf1;
+    float4 *z;             // D^{-1} r, read by the SpMV of the blob's other rows
     float4 *dpos;
     const double *px, *py, *pz;
     const BlobCgDesc *desc;

@@ -138,18 +138,24 @@ __global__ void __launch_bounds__(BATCH_MAX_THREADS) cg_batch_kernel(const __gri
     grid_sum_df<MIXED_GATHER_NP>(spart, gsz, gsz, s_sc);
     const double f2 = s_sc[0];
     mixed_setup(s_desc, s_sc, s_A6, s_tau, s_Om, &s_beta, &s_conv);
-    // r = f^ (projected), initial r.z
+    // r = f^ (projected), z = D^{-1} r, initial r.z
+    float4 *r4 = reinterpret_cast<float4 *>(g.r), *x4 = reinterpret_cast<float4 *>(g.x),
+           *q4 = reinterpret_cast<float4 *>(g.q);
+    const float4 *dinv4 = reinterpret_cast<const float4 *>(g.dinv), *diag4 = reinterpret_cast<const float4 *>(g.diag);
     float acc0[1] = {0.f};
     BATCH_NODE_LOOP(row0, nrows, rank, gsz, a) {
-        float r0 = g.r[4 * a], r1 = g.r[4 * a + 1], r2 = g.r[4 * a + 2];
+        float4 r = r4[a];
         if (defl) {
-            const float4 d = g.dpos[a];
-            r0 -= g.diag[4 * a] * (s_tau[0] + (s_Om[1] * d.z - s_Om[2] * d.y));
-            r1 -= g.diag[4 * a + 1] * (s_tau[1] + (s_Om[2] * d.x - s_Om[0] * d.z));
-            r2 -= g.diag[4 * a + 2] * (s_tau[2] + (s_Om[0] * d.y - s_Om[1] * d.x));
-            g.r[4 * a] = r0; g.r[4 * a + 1] = r1; g.r[4 * a + 2] = r2;
+            const float4 d = g.dpos[a], D = __ldg(diag4 + a);
+            r.x -= D.x * (s_tau[0] + (s_Om[1] * d.z - s_Om[2] * d.y));
+            r.y -= D.y * (s_tau[1] + (s_Om[2] * d.x - s_Om[0] * d.z));
+            r.z -= D.z * (s_tau[2] + (s_Om[0] * d.y - s_Om[1] * d.x));
+            r4[a] = r;
         }
-        acc0[0] += r0 * (g.dinv[4 * a] * r0) + r1 * (g.dinv[4 * a + 1] * r1) + r2 * (g.dinv[4 * a + 2] * r2);
+        const float4 di = __ldg(dinv4 + a);
+        const float z0 = di.x * r.x, z1 = di.y * r.y, z2 = di.z * r.z;
+        g.z[a] = make_float4(z0, z1, z2, 0.f);
+        acc0[0] += r.x * z0 + r.y * z1 + r.z * z2;
     }
     const int rowz = MIXED_A_NP + MIXED_B_NP;
     {
@@ -164,28 +170,33 @@ __global__ void __launch_bounds__(BATCH_MAX_THREADS) cg_batch_kernel(const __gri
         if (threadIdx.x == 0) s_delta = s_sc[0];
         __syncthreads();
     }
-    float *pold = g.pbuf0, *pnew = g.pbuf1;
+    const float4 *pold = reinterpret_cast<const float4 *>(g.pbuf0);
+    float4 *pnew = reinterpret_cast<float4 *>(g.pbuf1);
     int it = 0;
     for (; ok && it < g.imax; ++it) {
         const bool first = it == 0;
         const float beta = s_beta;
-        // phase A: q = V p with p formed on the fly; p.q; moments of D p
+        // phase A: q = V p with p = z + beta p_old formed on the fly; p.q; moments of D p
         float acc[MIXED_A_NP];
 #pragma unroll
         for (int i = 0; i < MIXED_A_NP; ++i) acc[i] = 0.f;
         {
             BATCH_ROW_LOOP(g.tpn, row0, nrows, rank, gsz, a, sub, valid) {
                 float q0, q1, q2;
-                spmv_row<true>(g, pold, beta, first, a, sub, valid, q0, q1, q2);
+                spmv_row_z(g, g.z, pold, beta, first, a, sub, valid, q0, q1, q2);
                 if (!valid || sub != 0) continue;
-                float p0, p1, p2;
-                p_on_the_fly(g, pold, beta, first, a, p0, p1, p2);
-                pnew[4 * a] = p0; pnew[4 * a + 1] = p1; pnew[4 * a + 2] = p2;
-                g.q[4 * a] = q0; g.q[4 * a + 1] = q1; g.q[4 * a + 2] = q2;
+                const float4 z = g.z[a];
+                float p0 = z.x, p1 = z.y, p2 = z.z;
+                if (!first) {
+                    const float4 po = pold[a];
+                    p0 = fmaf(beta, po.x, p0); p1 = fmaf(beta, po.y, p1); p2 = fmaf(beta, po.z, p2);
+                }
+                pnew[a] = make_float4(p0, p1, p2, 0.f);
+                q4[a] = make_float4(q0, q1, q2, 0.f);
                 acc[0] += p0 * q0 + p1 * q1 + p2 * q2;
                 if (defl) {
-                    const float4 d = g.dpos[a];
-                    const float e0 = g.diag[4 * a] * p0, e1 = g.diag[4 * a + 1] * p1, e2 = g.diag[4 * a + 2] * p2;
+                    const float4 d = g.dpos[a], D = __ldg(diag4 + a);
+                    const float e0 = D.x * p0, e1 = D.y * p1, e2 = D.z * p2;
                     acc[1] += e0; acc[2] += e1; acc[3] += e2;
                     acc[4] += d.y * e2 - d.z * e1;
                     acc[5] += d.z * e0 - d.x * e2;
@@ -223,19 +234,22 @@ __global__ void __launch_bounds__(BATCH_MAX_THREADS) cg_batch_kernel(const __gri
         // phase B: x += alpha p ; r -= alpha (q + D (tau + Omega x d)) ; r.r ; r.z
         float acc2[MIXED_B_NP] = {0.f, 0.f};
         BATCH_NODE_LOOP(row0, nrows, rank, gsz, a) {
-#pragma unroll
-            for (int c = 0; c < 3; ++c) g.x[4 * a + c] += alpha * pnew[4 * a + c];
-            float q0 = g.q[4 * a], q1 = g.q[4 * a + 1], q2 = g.q[4 * a + 2];
+            const float4 p = pnew[a], r = r4[a], di = __ldg(dinv4 + a);
+            float4 x = x4[a], q = q4[a];
+            x.x += alpha * p.x; x.y += alpha * p.y; x.z += alpha * p.z;
+            x4[a] = x;
             if (defl) {
-                const float4 d = g.dpos[a];
-                q0 += g.diag[4 * a] * (t0 + (O1 * d.z - O2 * d.y));
-                q1 += g.diag[4 * a + 1] * (t1 + (O2 * d.x - O0 * d.z));
-                q2 += g.diag[4 * a + 2] * (t2 + (O0 * d.y - O1 * d.x));
+                const float4 d = g.dpos[a], D = __ldg(diag4 + a);
+                q.x += D.x * (t0 + (O1 * d.z - O2 * d.y));
+                q.y += D.y * (t1 + (O2 * d.x - O0 * d.z));
+                q.z += D.z * (t2 + (O0 * d.y - O1 * d.x));
             }
-            const float r0 = g.r[4 * a] - alpha * q0, r1 = g.r[4 * a + 1] - alpha * q1, r2 = g.r[4 * a + 2] - alpha * q2;
-            g.r[4 * a] = r0; g.r[4 * a + 1] = r1; g.r[4 * a + 2] = r2;
+            const float r0 = r.x - alpha * q.x, r1 = r.y - alpha * q.y, r2 = r.z - alpha * q.z;
+            r4[a] = make_float4(r0, r1, r2, 0.f);
+            const float z0 = di.x * r0, z1 = di.y * r1, z2 = di.z * r2;
+            g.z[a] = make_float4(z0, z1, z2, 0.f);
             acc2[0] += r0 * r0 + r1 * r1 + r2 * r2;
-            acc2[1] += r0 * (g.dinv[4 * a] * r0) + r1 * (g.dinv[4 * a + 1] * r1) + r2 * (g.dinv[4 * a + 2] * r2);
+            acc2[1] += r0 * z0 + r1 * z1 + r2 * z2;
         }
         {
             df32 o[MIXED_B_NP];
@@ -256,7 +270,7 @@ __global__ void __launch_bounds__(BATCH_MAX_THREADS) cg_batch_kernel(const __gri
             ++it;
             break;
         }
-        float *t = pold; pold = pnew; pnew = t;
+        const float4 *t = pold; pold = pnew; pnew = const_cast<float4 *>(t);
     }
     if (rank == 0 && threadIdx.x == 0) {
         if (!ok) {

@@ -399,10 +399,11 @@ __device__ __forceinline__ void grid_sum_df8(const float2 *partials, int stride,
     __syncthreads();
 }
 
-// Row a of q = V p for cg_mixed_own_kernel: p at a neighbour b is formed from the preconditioned residual
+// Row a of q = V p for cg_mixed_own_kernel and cg_batch_kernel: p at a neighbour b is formed from the preconditioned residual
 // z_b and the previous direction, both stored as float4 per node (two 16-byte loads per neighbour).
-__device__ __forceinline__ void spmv_row_z(const CgArgs<float> &g, const float4 *z4, const float4 *p4, float beta,
-                                           bool first, int a, int sub, bool valid, float &q0, float &q1, float &q2) {
+template <class A>
+__device__ __forceinline__ void spmv_row_z(const A &g, const float4 *z4, const float4 *p4, float beta, bool first,
+                                           int a, int sub, bool valid, float &q0, float &q1, float &q2) {
     q0 = 0.f; q1 = 0.f; q2 = 0.f;
     const int tpn = g.tpn;
     if (valid) {
