@@ -160,6 +160,23 @@ def profiled_batch_traffic_ratio():
     return None
 
 
+_PINNED = []
+
+
+def host_array(shape):
+    """A float64 host array in page-locked memory (torch's pinned allocator) for the end-to-end runs, or
+    ordinary memory if that is not available; returns the array and which it is."""
+    import numpy as np
+    try:
+        import torch
+
+        t = torch.empty(shape, dtype=torch.float64, pin_memory=True)
+        _PINNED.append(t)  # the array below is a view of t's memory: keep t alive
+        return t.numpy(), "pinned"
+    except Exception:  # noqa: BLE001 - any failure to pin falls back to pageable memory
+        return np.empty(shape), "pageable"
+
+
 def cg_bytes_per_iteration(n: int, p: int) -> float:
     """Compulsory bytes of one CG iteration by the per-unit model: nnz (p + 4) + (R + 1) 4 + 8 R p."""
     from ffea_ci_demo_gb300.mesh import counts
@@ -224,20 +241,23 @@ def run_gpu_arm(args, ws, rank, local) -> dict | None:
                      "cg_iters_per_step": iters / steps, "launches": launches, "clocks": clk.summary(),
                      "blocks": nb}
         if prec == args.headline:
-            # end to end through the C ABI: host positions in, one step, host positions out
-            pos_host = blob.pos()
+            # end to end through the C ABI: every node's host position (the reference's layout, midpoints
+            # included, in pinned host memory) in, one step, every position out
+            pos_host, mem_kind = host_array((blob.n_nodes, 3))
+            blob.pos(out=pos_host)
             k = max(3, steps // 2)
             barrier()
             t0 = time.perf_counter()
             for _ in range(k):
                 blob.set_state(pos=pos_host)
                 blob.update(1)
-                pos_host = blob.pos()
+                blob.pos(out=pos_host)
             t1 = time.perf_counter()
             barrier()
             e2e_s = max_over_ranks(t1 - t0)
-            out[prec]["e2e"] = {"value": ws * N * k / e2e_s, "unit": "node-steps/s", "h2d_bytes_per_step": 24 * N,
-                                "d2h_bytes_per_step": 24 * N, "steps": k}
+            nbytes = 24 * blob.n_nodes
+            out[prec]["e2e"] = {"value": ws * N * k / e2e_s, "unit": "node-steps/s", "h2d_bytes_per_step": nbytes,
+                                "d2h_bytes_per_step": nbytes, "steps": k, "host_memory": mem_kind}
         blob.close()
     # kT = 0 error of the mixed path against the FP64 path (same initial shear)
     if args.precision == "both" and args.error_steps > 0:
@@ -334,19 +354,20 @@ def run_batch(args, ws) -> dict:
                                     "stratified sample scaled to all blobs"}
         out["speedup_vs_fp64_path"] = out["value"] / out["fp64_path_sampled"]["value"]
     if not args.no_e2e:
-        # end to end through the C ABI: every blob's host positions in, one step, every blob's positions out
-        pos = [bt.pos(b) for b in range(args.blobs)]
+        # end to end through the C ABI: every blob's host positions (pinned host memory) in, one step, every
+        # blob's positions out
+        pos, mem_kind = host_array((sum(m.n_nodes for m in meshes), 3))
+        bt.positions(out=pos)
         ke = max(2, k // 4)
         t0 = time.perf_counter()
         for _ in range(ke):
-            for b in range(args.blobs):
-                bt.set_state(b, pos=pos[b])
+            bt.set_positions(pos)
             bt.update(1)
-            pos = [bt.pos(b) for b in range(args.blobs)]
+            bt.positions(out=pos)
         e2e_s = time.perf_counter() - t0
         nb = 24 * sum(m.n_nodes for m in meshes)
         out["e2e"] = {"value": ws * sz["nodes"] * ke / e2e_s, "unit": "node-steps/s", "h2d_bytes_per_step": nb,
-                      "d2h_bytes_per_step": nb, "steps": ke}
+                      "d2h_bytes_per_step": nb, "steps": ke, "host_memory": mem_kind}
     bt.close()
     return out
 

@@ -58,7 +58,11 @@ struct ffea_gpu_batch {
     int *cta_blob, *blob_iters;
     float2 *partials;
     std::vector<BlobCgDesc> hdesc;
-    double *staging = nullptr;  // pinned, 3 x the largest blob's vertex count
+    // every blob's node state in the reference layout on the device (the blobs' n_all x 3 arrays back to
+    // back), the vertex row of each vertex node and the source rows of every node (see BlobImpl)
+    double *aos = nullptr;
+    int *d_node_of = nullptr;
+    int2 *ref_src = nullptr;
     int max_rows = 0, max_elems = 0;
     // launch configuration (ffea_gpu_batch_tune)
     int cg_threads = 256, tpn = 4, ncta = 0, ncta_cap = 0;
@@ -72,7 +76,6 @@ struct ffea_gpu_batch {
         if (graph) cudaGraphDestroy(graph);
         if (ev0) cudaEventDestroy(ev0);
         if (ev1) cudaEventDestroy(ev1);
-        if (staging) cudaFreeHost(staging);
         if (stream) cudaStreamDestroy(stream);
     }
 
@@ -105,10 +108,16 @@ struct ffea_gpu_batch {
         if (s.nonfinite) return FFEA_GPU_ENAN;
         return FFEA_GPU_OK;
     }
-    int upload_desc() {
-        CK(cudaMemcpyAsync(desc, hdesc.data(), hdesc.size() * sizeof(BlobCgDesc), cudaMemcpyHostToDevice, stream));
+    int upload_desc(int only = -1) {
+        const size_t b0 = only < 0 ? 0 : (size_t)only, nb = only < 0 ? hdesc.size() : 1;
+        CK(cudaMemcpyAsync(desc + b0, hdesc.data() + b0, nb * sizeof(BlobCgDesc), cudaMemcpyHostToDevice, stream));
         CK(cudaStreamSynchronize(stream));
         return FFEA_GPU_OK;
+    }
+    // the rigid modes of blob b after its host positions changed (they must vanish at its pinned nodes)
+    void refresh_modes(int b) {
+        BlobCgDesc &d = hdesc[b];
+        d.nmodes = rigid_modes(h, p, d.xc, d.modes, d.row0, d.nrows);
     }
 };
 
@@ -149,7 +158,6 @@ int ffea_gpu_batch::init() {
         max_rows = std::max(max_rows, row_off[b + 1] - row_off[b]);
         max_elems = std::max(max_elems, elem_off[b + 1] - elem_off[b]);
     }
-    CK(cudaHostAlloc((void **)&staging, 3 * (size_t)std::max(max_rows, 1) * sizeof(double), cudaHostAllocDefault));
     std::vector<double> tmp(N);
     auto up3 = [&](double **dst, int c) -> cudaError_t {
         for (int k = 0; k < N; ++k) tmp[k] = h.pos[3 * (size_t)k + c];
@@ -158,6 +166,14 @@ int ffea_gpu_batch::init() {
     CK(up3(&px, 0));
     CK(up3(&py, 1));
     CK(up3(&pz, 2));
+    {
+        std::vector<int2> src(std::max(h.n_all, 1), make_int2(-1, -1));
+        for (int k = 0; k < N; ++k) src[h.node_of[k]] = make_int2(k, k);
+        for (size_t m = 0; m < h.mid_nodes.size(); ++m) src[h.mid_nodes[m]] = make_int2(h.mid_a[m], h.mid_b[m]);
+        CK(mem.upload(&ref_src, src));
+        CK(mem.upload(&d_node_of, h.node_of));
+        CK(mem.alloc(&aos, 3 * (size_t)std::max(h.n_all, 1)));
+    }
     CK(mem.alloc(&vx, N));
     CK(mem.alloc(&vy, N));
     CK(mem.alloc(&vz, N));
@@ -591,30 +607,14 @@ int ffea_gpu_batch_step_timed(ffea_gpu_batch *bt, int nsteps, long long flush_by
     return ffea_gpu_batch::status_code(s);
 }
 
-int ffea_gpu_batch_get_state(ffea_gpu_batch *bt, int blob, double *pos, double *vel) {
-    if (!bt || blob < 0 || blob >= bt->nblobs) return FFEA_GPU_EINPUT;
-    const HostModel &h = bt->h;
-    const int r0 = bt->row_off[blob], nr = bt->row_off[blob + 1] - r0, n0 = bt->nall_off[blob];
-    const int n = bt->nall_off[blob + 1] - n0;
-    double *stg = bt->staging;
+// blobs [b0, b1) in the reference layout: assembled on the device, one copy out
+static int batch_get_range(ffea_gpu_batch *bt, int b0, int b1, double *pos, double *vel) {
+    const int n0 = bt->nall_off[b0], n = bt->nall_off[b1] - n0;
     auto fill = [&](double *out, const double *dx, const double *dy, const double *dz, bool mids) -> int {
-        CK(cudaMemcpyAsync(stg, dx + r0, nr * sizeof(double), cudaMemcpyDeviceToHost, bt->stream));
-        CK(cudaMemcpyAsync(stg + nr, dy + r0, nr * sizeof(double), cudaMemcpyDeviceToHost, bt->stream));
-        CK(cudaMemcpyAsync(stg + 2 * (size_t)nr, dz + r0, nr * sizeof(double), cudaMemcpyDeviceToHost, bt->stream));
+        CK(launch_aos_gather(dx, dy, dz, bt->ref_src + n0, n, mids ? 1 : 0, bt->aos + 3 * (size_t)n0, bt->stream));
+        CK(cudaMemcpyAsync(out, bt->aos + 3 * (size_t)n0, 3 * (size_t)n * sizeof(double), cudaMemcpyDeviceToHost,
+                           bt->stream));
         CK(cudaStreamSynchronize(bt->stream));
-        for (int i = 0; i < 3 * n; ++i) out[i] = 0.0;
-        for (int k = 0; k < nr; ++k) {
-            const size_t i = 3 * (size_t)(h.node_of[r0 + k] - n0);
-            out[i] = stg[k];
-            out[i + 1] = stg[nr + k];
-            out[i + 2] = stg[2 * (size_t)nr + k];
-        }
-        if (mids)
-            for (int m = bt->mid_off[blob]; m < bt->mid_off[blob + 1]; ++m) {
-                const size_t i = 3 * (size_t)(h.mid_nodes[m] - n0);
-                const size_t a = 3 * (size_t)(h.node_of[h.mid_a[m]] - n0), c = 3 * (size_t)(h.node_of[h.mid_b[m]] - n0);
-                for (int d = 0; d < 3; ++d) out[i + d] = .5 * (out[a + d] + out[c + d]);
-            }
         return FFEA_GPU_OK;
     };
     int rc;
@@ -623,21 +623,16 @@ int ffea_gpu_batch_get_state(ffea_gpu_batch *bt, int blob, double *pos, double *
     return FFEA_GPU_OK;
 }
 
-int ffea_gpu_batch_set_state(ffea_gpu_batch *bt, int blob, const double *pos, const double *vel) {
-    if (!bt || blob < 0 || blob >= bt->nblobs) return FFEA_GPU_EINPUT;
+// blobs [b0, b1) from the reference layout: one copy in, the vertex rows picked out on the device; then the
+// host's copy of the positions and the blobs' rigid modes
+static int batch_set_range(ffea_gpu_batch *bt, int b0, int b1, const double *pos, const double *vel) {
     HostModel &h = bt->h;
-    const int r0 = bt->row_off[blob], nr = bt->row_off[blob + 1] - r0, n0 = bt->nall_off[blob];
-    double *stg = bt->staging;
+    const int n0 = bt->nall_off[b0], n = bt->nall_off[b1] - n0;
+    const int r0 = bt->row_off[b0], nr = bt->row_off[b1] - r0;
     auto put = [&](const double *in, double *dx, double *dy, double *dz) -> int {
-        for (int k = 0; k < nr; ++k) {
-            const size_t i = 3 * (size_t)(h.node_of[r0 + k] - n0);
-            stg[k] = in[i];
-            stg[nr + k] = in[i + 1];
-            stg[2 * (size_t)nr + k] = in[i + 2];
-        }
-        CK(cudaMemcpyAsync(dx + r0, stg, nr * sizeof(double), cudaMemcpyHostToDevice, bt->stream));
-        CK(cudaMemcpyAsync(dy + r0, stg + nr, nr * sizeof(double), cudaMemcpyHostToDevice, bt->stream));
-        CK(cudaMemcpyAsync(dz + r0, stg + 2 * (size_t)nr, nr * sizeof(double), cudaMemcpyHostToDevice, bt->stream));
+        CK(cudaMemcpyAsync(bt->aos + 3 * (size_t)n0, in, 3 * (size_t)n * sizeof(double), cudaMemcpyHostToDevice,
+                           bt->stream));
+        CK(launch_aos_scatter(bt->aos, bt->d_node_of + r0, nr, dx + r0, dy + r0, dz + r0, bt->stream));
         CK(cudaStreamSynchronize(bt->stream));
         return FFEA_GPU_OK;
     };
@@ -645,14 +640,32 @@ int ffea_gpu_batch_set_state(ffea_gpu_batch *bt, int blob, const double *pos, co
     if (pos && (rc = put(pos, bt->px, bt->py, bt->pz))) return rc;
     if (vel && (rc = put(vel, bt->vx, bt->vy, bt->vz))) return rc;
     if (pos) {
-        // the rigid modes must vanish at the pinned nodes' current positions
-        for (int k = 0; k < nr; ++k)
-            for (int c = 0; c < 3; ++c) h.pos[3 * (size_t)(r0 + k) + c] = pos[3 * (size_t)(h.node_of[r0 + k] - n0) + c];
-        BlobCgDesc &d = bt->hdesc[blob];
-        d.nmodes = rigid_modes(h, bt->p, d.xc, d.modes, d.row0, d.nrows);
-        return bt->upload_desc();
+        for (int k = r0; k < r0 + nr; ++k)
+            for (int c = 0; c < 3; ++c) h.pos[3 * (size_t)k + c] = pos[3 * (size_t)(h.node_of[k] - n0) + c];
+        for (int b = b0; b < b1; ++b) bt->refresh_modes(b);
+        return bt->upload_desc(b1 - b0 == 1 ? b0 : -1);
     }
     return FFEA_GPU_OK;
+}
+
+int ffea_gpu_batch_get_state(ffea_gpu_batch *bt, int blob, double *pos, double *vel) {
+    if (!bt || blob < 0 || blob >= bt->nblobs) return FFEA_GPU_EINPUT;
+    return batch_get_range(bt, blob, blob + 1, pos, vel);
+}
+
+int ffea_gpu_batch_set_state(ffea_gpu_batch *bt, int blob, const double *pos, const double *vel) {
+    if (!bt || blob < 0 || blob >= bt->nblobs) return FFEA_GPU_EINPUT;
+    return batch_set_range(bt, blob, blob + 1, pos, vel);
+}
+
+int ffea_gpu_batch_get_states(ffea_gpu_batch *bt, double *pos, double *vel) {
+    if (!bt) return FFEA_GPU_EINPUT;
+    return batch_get_range(bt, 0, bt->nblobs, pos, vel);
+}
+
+int ffea_gpu_batch_set_states(ffea_gpu_batch *bt, const double *pos, const double *vel) {
+    if (!bt) return FFEA_GPU_EINPUT;
+    return batch_set_range(bt, 0, bt->nblobs, pos, vel);
 }
 
 int ffea_gpu_batch_set_rng_state(ffea_gpu_batch *bt, int blob, const uint32_t s[6]) {

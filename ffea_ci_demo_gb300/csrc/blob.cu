@@ -195,6 +195,11 @@ struct BlobImpl final : ffea_gpu_blob {
     cudaEvent_t ev[FFEA_GPU_NUM_PHASES + 1] = {};
     bool record_phases = false;
     double *staging = nullptr;  // pinned host buffer, 3*N doubles, for state copies
+    // node state in the reference's layout on the device: n_all x 3 doubles, the vertex row of each vertex
+    // node, and the source rows of every reference node (vertex (k, k), midpoint (a, b), else (-1, -1))
+    double *aos = nullptr;
+    int *d_node_of = nullptr;
+    int2 *ref_src = nullptr;
     // adjoint window (ffea_gpu_adjoint_*): checkpoints every `adj_every` steps, one segment recomputed
     std::unique_ptr<Arena> adj_mem;
     int adj_window = 0, adj_every = 0, adj_done = -1;
@@ -237,6 +242,14 @@ struct BlobImpl final : ffea_gpu_blob {
         CK(up3(&px, 0));
         CK(up3(&py, 1));
         CK(up3(&pz, 2));
+        {
+            std::vector<int2> src(std::max(h.n_all, 1), make_int2(-1, -1));
+            for (int k = 0; k < N; ++k) src[h.node_of[k]] = make_int2(k, k);
+            for (size_t m = 0; m < h.mid_nodes.size(); ++m) src[h.mid_nodes[m]] = make_int2(h.mid_a[m], h.mid_b[m]);
+            CK(mem.upload(&ref_src, src));
+            CK(mem.upload(&d_node_of, h.node_of));
+            CK(mem.alloc(&aos, 3 * (size_t)std::max(h.n_all, 1)));
+        }
         CK(mem.alloc(&vx, N));
         CK(mem.alloc(&vy, N));
         CK(mem.alloc(&vz, N));
@@ -577,24 +590,12 @@ struct BlobImpl final : ffea_gpu_blob {
 
     int get_state(double *pos, double *vel, double *force) override {
         const int N = h.N, n = h.n_all;
+        // the reference layout is assembled on the device (midpoints as linearise_element leaves them) and
+        // copied out in one transfer
         auto fill = [&](double *out, const double *dx, const double *dy, const double *dz, bool mids) -> int {
-            CK(cudaMemcpyAsync(staging, dx, N * sizeof(double), cudaMemcpyDeviceToHost, stream));
-            CK(cudaMemcpyAsync(staging + N, dy, N * sizeof(double), cudaMemcpyDeviceToHost, stream));
-            CK(cudaMemcpyAsync(staging + 2 * (size_t)N, dz, N * sizeof(double), cudaMemcpyDeviceToHost, stream));
+            CK(launch_aos_gather(dx, dy, dz, ref_src, n, mids ? 1 : 0, aos, stream));
+            CK(cudaMemcpyAsync(out, aos, 3 * (size_t)n * sizeof(double), cudaMemcpyDeviceToHost, stream));
             CK(cudaStreamSynchronize(stream));
-            for (int i = 0; i < 3 * n; ++i) out[i] = 0.0;
-            for (int k = 0; k < N; ++k) {
-                const int i = h.node_of[k];
-                out[3 * (size_t)i] = staging[k];
-                out[3 * (size_t)i + 1] = staging[N + k];
-                out[3 * (size_t)i + 2] = staging[2 * (size_t)N + k];
-            }
-            if (mids)
-                for (size_t m = 0; m < h.mid_nodes.size(); ++m) {
-                    const int i = h.mid_nodes[m], a = h.node_of[h.mid_a[m]], b = h.node_of[h.mid_b[m]];
-                    for (int c = 0; c < 3; ++c)
-                        out[3 * (size_t)i + c] = .5 * (out[3 * (size_t)a + c] + out[3 * (size_t)b + c]);
-                }
             return FFEA_GPU_OK;
         };
         int rc;
@@ -613,16 +614,10 @@ struct BlobImpl final : ffea_gpu_blob {
 
     int set_state(const double *pos, const double *vel) override {
         const int N = h.N;
+        // one transfer of the reference-layout array, the vertex rows picked out on the device
         auto put = [&](const double *in, double *dx, double *dy, double *dz) -> int {
-            for (int k = 0; k < N; ++k) {
-                const size_t i = 3 * (size_t)h.node_of[k];
-                staging[k] = in[i];
-                staging[N + k] = in[i + 1];
-                staging[2 * (size_t)N + k] = in[i + 2];
-            }
-            CK(cudaMemcpyAsync(dx, staging, N * sizeof(double), cudaMemcpyHostToDevice, stream));
-            CK(cudaMemcpyAsync(dy, staging + N, N * sizeof(double), cudaMemcpyHostToDevice, stream));
-            CK(cudaMemcpyAsync(dz, staging + 2 * (size_t)N, N * sizeof(double), cudaMemcpyHostToDevice, stream));
+            CK(cudaMemcpyAsync(aos, in, 3 * (size_t)h.n_all * sizeof(double), cudaMemcpyHostToDevice, stream));
+            CK(launch_aos_scatter(aos, d_node_of, N, dx, dy, dz, stream));
             CK(cudaStreamSynchronize(stream));
             return FFEA_GPU_OK;
         };

@@ -51,6 +51,52 @@ cudaError_t launch_surface_forces(const SurfArgs &a, cudaStream_t s) {
     return cudaGetLastError();
 }
 
+__global__ void __launch_bounds__(256) aos_scatter_kernel(const double *aos, const int *node_of, int N, double *px,
+                                                          double *py, double *pz) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= N) return;
+    const double *q = aos + 3 * (size_t)node_of[k];
+    px[k] = q[0];
+    py[k] = q[1];
+    pz[k] = q[2];
+}
+
+// Blob::linearise_elements leaves every midpoint at .5 * (x_a + x_b) (tetra_element_linear::linearise_element,
+// src/tetra_element_linear.cpp:553-577); a vertex is copied as is
+__global__ void __launch_bounds__(256) aos_gather_kernel(const double *px, const double *py, const double *pz,
+                                                         const int2 *src, int n_all, int mids, double *aos) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_all) return;
+    const int2 ab = src[i];
+    double o0 = 0.0, o1 = 0.0, o2 = 0.0;
+    if (ab.x >= 0 && ab.x == ab.y) {
+        o0 = px[ab.x]; o1 = py[ab.x]; o2 = pz[ab.x];
+    } else if (ab.x >= 0 && mids) {
+        o0 = .5 * (px[ab.x] + px[ab.y]);
+        o1 = .5 * (py[ab.x] + py[ab.y]);
+        o2 = .5 * (pz[ab.x] + pz[ab.y]);
+    }
+    aos[3 * (size_t)i] = o0;
+    aos[3 * (size_t)i + 1] = o1;
+    aos[3 * (size_t)i + 2] = o2;
+}
+
+cudaError_t launch_aos_scatter(const double *aos, const int *node_of, int N, double *px, double *py, double *pz,
+                               cudaStream_t s) {
+    if (N <= 0) return cudaSuccess;
+    aos_scatter_kernel<<<(N + 255) / 256, 256, 0, s>>>(aos, node_of, N, px, py, pz);
+    count_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t launch_aos_gather(const double *px, const double *py, const double *pz, const int2 *src, int n_all,
+                              int mids, double *aos, cudaStream_t s) {
+    if (n_all <= 0) return cudaSuccess;
+    aos_gather_kernel<<<(n_all + 255) / 256, 256, 0, s>>>(px, py, pz, src, n_all, mids, aos);
+    count_launch();
+    return cudaGetLastError();
+}
+
 static std::atomic<long long> g_launches{0};
 void count_launch(int n) { g_launches += n; }
 long long launch_count() { return g_launches.load(); }

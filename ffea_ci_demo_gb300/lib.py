@@ -116,6 +116,8 @@ def load():
         "ffea_gpu_batch_step": (C.c_int, [vp, C.c_int, ip]),
         "ffea_gpu_batch_step_timed": (C.c_int, [vp, C.c_int, C.c_longlong, ip, C.POINTER(C.c_double)]),
         "ffea_gpu_batch_get_state": (C.c_int, [vp, C.c_int, dp, dp]),
+        "ffea_gpu_batch_get_states": (C.c_int, [vp, dp, dp]),
+        "ffea_gpu_batch_set_states": (C.c_int, [vp, dp, dp]),
         "ffea_gpu_batch_set_state": (C.c_int, [vp, C.c_int, dp, dp]),
         "ffea_gpu_batch_set_rng_state": (C.c_int, [vp, C.c_int, dp]),
         "ffea_gpu_batch_get_rng_state": (C.c_int, [vp, C.c_int, dp]),
@@ -140,6 +142,14 @@ def _p(a):
 
 def last_error() -> str:
     return load().ffea_gpu_last_error().decode()
+
+
+def _out(out, shape):
+    if out is None:
+        return np.empty(shape)
+    if out.dtype != np.float64 or not out.flags["C_CONTIGUOUS"] or out.size != int(np.prod(shape)):
+        raise ValueError(f"out must be a C-contiguous float64 array of {int(np.prod(shape))} values")
+    return out
 
 
 def _check(rc: int, where: str) -> None:
@@ -263,13 +273,15 @@ class Blob:
         _check(self._lib.ffea_gpu_blob_get_state(self._h, _p(pos), _p(vel), _p(force)), "get_state")
         return pos, vel, force
 
-    def pos(self) -> np.ndarray:
-        o = np.empty((self.n_nodes, 3))
+    def pos(self, out: np.ndarray | None = None) -> np.ndarray:
+        """Node positions (num_nodes, 3) in the reference's order; `out` (C-contiguous float64, e.g. a view of
+        pinned host memory) is filled in place."""
+        o = _out(out, (self.n_nodes, 3))
         _check(self._lib.ffea_gpu_blob_get_state(self._h, _p(o), None, None), "get_state")
         return o
 
-    def vel(self) -> np.ndarray:
-        o = np.empty((self.n_nodes, 3))
+    def vel(self, out: np.ndarray | None = None) -> np.ndarray:
+        o = _out(out, (self.n_nodes, 3))
         _check(self._lib.ffea_gpu_blob_get_state(self._h, None, _p(o), None), "get_state")
         return o
 
@@ -514,6 +526,18 @@ class Batch:
         pa = None if pos is None else np.ascontiguousarray(pos, np.float64)
         va = None if vel is None else np.ascontiguousarray(vel, np.float64)
         _check(self._lib.ffea_gpu_batch_set_state(self._h, blob, _p(pa), _p(va)), "batch_set_state")
+
+    def positions(self, out: np.ndarray | None = None) -> np.ndarray:
+        """Every blob's node positions, back to back in blob order: (sum of node counts, 3)."""
+        o = _out(out, (int(sum(self.n_nodes)), 3))
+        _check(self._lib.ffea_gpu_batch_get_states(self._h, _p(o), None), "batch_get_states")
+        return o
+
+    def set_positions(self, pos) -> None:
+        pa = np.ascontiguousarray(pos, np.float64)
+        if pa.size != 3 * int(sum(self.n_nodes)):
+            raise ValueError("positions of every blob, back to back")
+        _check(self._lib.ffea_gpu_batch_set_states(self._h, _p(pa), None), "batch_set_states")
 
     def rng_state(self, blob: int) -> np.ndarray:
         a = np.empty(6, np.uint32)

@@ -285,6 +285,11 @@ int ffea_gpu_batch_step_timed(ffea_gpu_batch *batch, int nsteps, long long flush
 /* State of one blob in its own node order (as ffea_gpu_blob_get_state / set_state). */
 int ffea_gpu_batch_get_state(ffea_gpu_batch *batch, int blob, double *pos, double *vel);
 int ffea_gpu_batch_set_state(ffea_gpu_batch *batch, int blob, const double *pos, const double *vel);
+/* Every blob's state at once: the blobs' arrays back to back in blob order (sum of the blobs' node
+ * counts x 3 doubles each), as num_blobs calls of ffea_gpu_batch_get_state / set_state, with one host <->
+ * device transfer. */
+int ffea_gpu_batch_get_states(ffea_gpu_batch *batch, double *pos, double *vel);
+int ffea_gpu_batch_set_states(ffea_gpu_batch *batch, const double *pos, const double *vel);
 int ffea_gpu_batch_set_rng_state(ffea_gpu_batch *batch, int blob, const uint32_t state[6]);
 int ffea_gpu_batch_get_rng_state(ffea_gpu_batch *batch, int blob, uint32_t state[6]);
 
