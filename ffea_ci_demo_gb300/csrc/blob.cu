@@ -170,6 +170,7 @@ struct BlobImpl final : ffea_gpu_blob {
     GridBarrier *gb;
     int cg_grid = 0, gather_blocks = 0, partial_stride = 0, tpn = 4;
     int cg_npb = 0;  // rows per block of the owned-rows CG kernels (0: cg_kernel / cg_mixed_kernel)
+    int cg_block = 1024;  // threads per CG block
     float4 *dpos = nullptr;  // mixed path: node offsets from the reference point
     // measurements: densities, reference positions of vertices and midpoints (SoA), per-block sums
     R *rho = nullptr;
@@ -338,10 +339,17 @@ struct BlobImpl final : ffea_gpu_blob {
             g_last_error = "cg kernel cannot be made resident";
             return FFEA_GPU_ECUDA;
         }
-        // one block per SM (fewer for small meshes); threads per SpMV row chosen so that every warp
+        // one block per SM (fewer for small meshes); up to 2048 rows, a single block (its barrier is a block
+        // barrier) of as few threads as give each row 8 lanes. Threads per SpMV row chosen so that every warp
         // handles its rows in one pass: tpn = the largest power of two <= 8 with N <= warps * 32 / tpn
-        cg_grid = std::max(1, std::min(maxg, (N + 255) / 256));
-        const long long lanes = (long long)cg_grid * Launch<R>::cg_threads();
+        if (N <= 2048) {
+            cg_grid = 1;
+            cg_block = std::min(Launch<R>::cg_threads(), std::max(128, (N * 8 + 31) / 32 * 32));
+        } else {
+            cg_grid = std::max(1, std::min(maxg, (N + 255) / 256));
+            cg_block = Launch<R>::cg_threads();
+        }
+        const long long lanes = (long long)cg_grid * cg_block;
         tpn = 8;
         while (tpn > 1 && (long long)N * tpn > lanes) tpn >>= 1;
         partial_stride = cg_grid;
@@ -456,7 +464,7 @@ struct BlobImpl final : ffea_gpu_blob {
         ca.dpos = dpos; ca.nmodes = nomass ? nmodes : 0;
         for (int i = 0; i < 36; ++i) ca.modes[i] = modes[i];
         ca.npb = cg_npb;
-        CK(Launch<R>::cg(ca, cg_grid, stream));
+        CK(Launch<R>::cg(ca, cg_grid, cg_block, stream));
         return FFEA_GPU_OK;
     }
 
@@ -768,7 +776,7 @@ struct BlobImpl final : ffea_gpu_blob {
             ca.eps2 = p.epsilon2;
             ca.limit_ns = 2000000000ull;
             ca.history = nullptr; ca.hist_cap = 0; ca.tpn = tpn; ca.phase_ns = sphase;
-            CK(Launch<R>::cg(ca, cg_grid, stream));
+            CK(Launch<R>::cg(ca, cg_grid, cg_block, stream));
             DevStatus ds{};
             CK(cudaMemcpy2DAsync(staging, 3 * sizeof(double), s + SS_X, 4 * sizeof(double), 3 * sizeof(double), N,
                                  cudaMemcpyDeviceToHost, stream));

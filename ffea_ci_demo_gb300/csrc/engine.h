@@ -17,8 +17,9 @@ struct Launch {
     static cudaError_t assemble(const AsmArgs<R> &a, cudaStream_t s);
     static cudaError_t gather(const GatherArgs<R> &a, int blocks, cudaStream_t s);
     static int gather_threads();
-    // persistent cooperative CG; returns the grid actually used in *grid
-    static cudaError_t cg(const CgArgs<R> &a, int grid, cudaStream_t s);
+    // persistent cooperative CG of `grid` blocks of `threads` threads (128 <= threads <= cg_threads(),
+    // a multiple of 32)
+    static cudaError_t cg(const CgArgs<R> &a, int grid, int threads, cudaStream_t s);
     static int cg_max_grid(int device);
     static int cg_threads();
     // mixed path: the most rows per block cg_mixed_own_kernel can keep in shared memory on `device`

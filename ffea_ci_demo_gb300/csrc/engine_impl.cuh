@@ -86,7 +86,7 @@ int Launch<R>::cg_own_max_rows(int device) {
 }
 
 template <class R>
-cudaError_t Launch<R>::cg(const CgArgs<R> &a, int grid, cudaStream_t s) {
+cudaError_t Launch<R>::cg(const CgArgs<R> &a, int grid, int threads, cudaStream_t s) {
     CgArgs<R> args = a;
     void *params[] = {&args};
     const void *fn;
@@ -104,7 +104,7 @@ cudaError_t Launch<R>::cg(const CgArgs<R> &a, int grid, cudaStream_t s) {
             smem = own_smem_bytes_d(a.npb);
         }
     }
-    cudaError_t e = cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(CG_THREADS), params, smem, s);
+    cudaError_t e = cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(threads), params, smem, s);
     count_launch();
     return e;
 }

@@ -357,8 +357,8 @@ __global__ void __launch_bounds__(1024, 1) cg_mixed_kernel(const __grid_constant
 }
 
 // Block reduction of NV FP32 per-thread values straight into the per-block partial rows: FP32 within
-// each warp, then warp i sums value i over the warps in double-float and its lane 0 stores the pair.
-// NV <= 32. The caller must pass a __syncthreads() before smem is written again.
+// each warp, then warp w sums values w, w + (warps), ... over the warps in double-float and its lane 0
+// stores the pairs. The caller must pass a __syncthreads() before smem is written again.
 template <int NV>
 __device__ __forceinline__ void block_reduce_store(const float (&v)[NV], float *smem, float2 *partials, int stride,
                                                    int row0) {
@@ -369,10 +369,10 @@ __device__ __forceinline__ void block_reduce_store(const float (&v)[NV], float *
         if (lane == 0) smem[i * 32 + wid] = w;
     }
     __syncthreads();
-    if (wid < NV) {
-        df32 t = {lane < nw ? smem[wid * 32 + lane] : 0.f, 0.f};
+    for (int i = wid; i < NV; i += nw) {
+        df32 t = {lane < nw ? smem[i * 32 + lane] : 0.f, 0.f};
         t = warp_sum_df(t);
-        if (lane == 0) partials[(row0 + wid) * stride + blockIdx.x] = make_float2(t.hi, t.lo);
+        if (lane == 0) partials[(row0 + i) * stride + blockIdx.x] = make_float2(t.hi, t.lo);
     }
 }
 
