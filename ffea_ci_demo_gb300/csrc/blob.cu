@@ -339,10 +339,12 @@ struct BlobImpl final : ffea_gpu_blob {
             g_last_error = "cg kernel cannot be made resident";
             return FFEA_GPU_ECUDA;
         }
-        // one block per SM (fewer for small meshes); up to 2048 rows, a single block (its barrier is a block
-        // barrier) of as few threads as give each row 8 lanes. Threads per SpMV row chosen so that every warp
-        // handles its rows in one pass: tpn = the largest power of two <= 8 with N <= warps * 32 / tpn
-        if (N <= 2048) {
+        // one block per SM (fewer for small meshes). A mixed blob of up to 2048 rows runs in a single block (its
+        // barrier is a block barrier); an FP64 one only up to 256 rows, since its SpMV is bound by the FP64
+        // units of the SMs it runs on. A single block has as few threads as give each row 8 lanes. Threads per
+        // SpMV row chosen so that every warp handles its rows in one pass: tpn = the largest power of two <= 8
+        // with N <= warps * 32 / tpn
+        if (N <= (mixed ? 2048 : 256)) {
             cg_grid = 1;
             cg_block = std::min(Launch<R>::cg_threads(), std::max(128, (N * 8 + 31) / 32 * 32));
         } else {
