@@ -148,3 +148,30 @@ def test_batch_tuner_keeps_state():
         p0 = m.pos * (m.scale / MESO_LENGTH)
         d = np.abs(bt.pos(b) - ref.pos(b)).max()
         assert d <= 1e-5 * np.abs(ref.pos(b) - p0).max(), b
+
+
+@pytest.mark.gpu
+def test_batch_bulk_state_matches_per_blob_calls():
+    """ffea_gpu_batch_get_states / set_states: every blob's reference-layout array back to back, the same values
+    as the per-blob calls (midpoints included), and a bulk set moves each blob as the per-blob set does."""
+    meshes = [case_mesh(n, s) for n, s in MESHES]
+    bt = lib.Batch(meshes, kT=0.0, calc_noise=0)
+    bt.update(2)
+    allpos = bt.positions()
+    off = np.cumsum([0] + [m.n_nodes for m in meshes])
+    for b in range(len(meshes)):
+        assert np.array_equal(allpos[off[b]:off[b + 1]], bt.pos(b))
+    x0 = np.concatenate([sheared(m, 0.02) for m in meshes])
+    bt.set_positions(x0)
+    for b, m in enumerate(meshes):
+        got, want = bt.pos(b), x0[off[b]:off[b + 1]]
+        nv = m.n_linear  # vertices exactly; midpoints as the device linearises them
+        assert np.array_equal(got[:nv], want[:nv])
+        np.testing.assert_allclose(got[nv:], want[nv:], rtol=1e-14)
+    bt.update(5)
+    ref = lib.Batch(meshes, kT=0.0, calc_noise=0)
+    ref.update(2)  # the same CTA schedule as bt's
+    for b, m in enumerate(meshes):
+        ref.set_state(b, pos=sheared(m, 0.02))
+    ref.update(5)
+    assert np.array_equal(bt.positions(), ref.positions())
