@@ -67,6 +67,42 @@ def rank_info():
     return ws, rank, local
 
 
+class Replicas:
+    """The ranks of a multi-GPU run: one independent replica of the workload per rank (a blob does not shard),
+    host-side barriers and the max over ranks of a timing through gloo (no collective touches the data path).
+    A run's throughput is the units all ranks processed divided by the slowest rank's time."""
+
+    def __init__(self, world_size: int):
+        self.ws = world_size
+        self.dist = None
+        if world_size > 1:
+            import torch.distributed as dist
+
+            dist.init_process_group("gloo")
+            self.dist = dist
+
+    def barrier(self) -> None:
+        if self.dist:
+            self.dist.barrier()
+
+    def max(self, x: float) -> float:
+        if not self.dist:
+            return x
+        import torch
+
+        t = torch.tensor([x], dtype=torch.float64)
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX)
+        return float(t.item())
+
+    def throughput(self, units_per_rank: float, seconds: float) -> float:
+        return self.ws * units_per_rank / self.max(seconds)
+
+    def close(self) -> None:
+        if self.dist:
+            self.dist.destroy_process_group()
+            self.dist = None
+
+
 def pick_device(local: int) -> str:
     vis = os.environ.get("CUDA_VISIBLE_DEVICES")
     phys = vis.split(",")[local] if vis else str(local)
@@ -198,29 +234,13 @@ def run_gpu_arm(args, ws, rank, local) -> dict | None:
     from ffea_ci_demo_gb300 import build, lib
     from ffea_ci_demo_gb300.mesh import apply_shear, counts, kuhn_cube
 
-    dist = None
-    if ws > 1:
-        import torch.distributed as dist  # noqa: F811
-
-        dist.init_process_group("gloo")
+    ranks = Replicas(ws)
+    barrier, max_over_ranks = ranks.barrier, ranks.max
     build.build()
     n = args.cells
     mesh = kuhn_cube(n, side=SIDE * n / N_CELLS, seed=12345)
     N = counts(n)["N"]
     gpu = os.environ.get("CUDA_VISIBLE_DEVICES", "0")
-
-    def barrier():
-        if dist:
-            dist.barrier()
-
-    def max_over_ranks(x: float) -> float:
-        if not dist:
-            return x
-        import torch
-
-        t = torch.tensor([x], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
 
     out = {}
     for prec in (["mixed", "fp64"] if args.precision == "both" else [args.precision]):
@@ -297,8 +317,7 @@ def run_gpu_arm(args, ws, rank, local) -> dict | None:
             "note": "strain energy averaged over the second half of the run, sampled every 10 steps; at dt = 1e-12 s "
                     "the explicit Euler step is comparable to the stiffest modes' relaxation time, so both paths "
                     "(and the reference's algorithm) sit the same amount above equipartition"}
-    if dist:
-        dist.destroy_process_group()
+    ranks.close()
     return out if rank == 0 else None
 
 
