@@ -401,6 +401,68 @@ __device__ __forceinline__ void grid_sum_df8(const float2 *partials, int stride,
 
 // Row a of q = V p for cg_mixed_own_kernel and cg_batch_kernel: p at a neighbour b is formed from the preconditioned residual
 // z_b and the previous direction, both stored as float4 per node (two 16-byte loads per neighbour).
+// The same row with two blocks per trip: both blocks' loads (values, columns, z and p) issue before
+// either block's products, halving the chain of dependent L2 round trips per lane. The products are
+// accumulated in the same order as spmv_row_z, so the result is identical.
+template <class A>
+__device__ __forceinline__ void spmv_row_z2(const A &g, const float4 *z4, const float4 *p4, float beta, bool first,
+                                            int a, int sub, bool valid, float &q0, float &q1, float &q2) {
+    q0 = 0.f; q1 = 0.f; q2 = 0.f;
+    const int tpn = g.tpn;
+    if (valid) {
+        const int s = a >> 5, lane = a & 31;
+        const int base = __ldg(g.slice_ptr + s);
+        const int len = __ldg(g.rowlen + a);
+        const float *v = g.val + 9 * (size_t)base + lane;
+        int k = sub;
+#pragma unroll 1
+        for (; k + tpn < len; k += 2 * tpn) {
+            const int ba = __ldg(g.bcol + base + 32 * k + lane), bb = __ldg(g.bcol + base + 32 * (k + tpn) + lane);
+            const float *va = v + (size_t)32 * 9 * k, *vb = v + (size_t)32 * 9 * (k + tpn);
+            float wa[9], wb[9];
+#pragma unroll
+            for (int i = 0; i < 9; ++i) {
+                wa[i] = __ldg(va + 32 * i);
+                wb[i] = __ldg(vb + 32 * i);
+            }
+            const float4 za = z4[ba], zb = z4[bb];
+            float pa0 = za.x, pa1 = za.y, pa2 = za.z, pb0 = zb.x, pb1 = zb.y, pb2 = zb.z;
+            if (!first) {
+                const float4 oa = p4[ba], ob = p4[bb];
+                pa0 = fmaf(beta, oa.x, pa0); pa1 = fmaf(beta, oa.y, pa1); pa2 = fmaf(beta, oa.z, pa2);
+                pb0 = fmaf(beta, ob.x, pb0); pb1 = fmaf(beta, ob.y, pb1); pb2 = fmaf(beta, ob.z, pb2);
+            }
+            q0 = fmaf(wa[0], pa0, q0); q0 = fmaf(wa[1], pa1, q0); q0 = fmaf(wa[2], pa2, q0);
+            q1 = fmaf(wa[3], pa0, q1); q1 = fmaf(wa[4], pa1, q1); q1 = fmaf(wa[5], pa2, q1);
+            q2 = fmaf(wa[6], pa0, q2); q2 = fmaf(wa[7], pa1, q2); q2 = fmaf(wa[8], pa2, q2);
+            q0 = fmaf(wb[0], pb0, q0); q0 = fmaf(wb[1], pb1, q0); q0 = fmaf(wb[2], pb2, q0);
+            q1 = fmaf(wb[3], pb0, q1); q1 = fmaf(wb[4], pb1, q1); q1 = fmaf(wb[5], pb2, q1);
+            q2 = fmaf(wb[6], pb0, q2); q2 = fmaf(wb[7], pb1, q2); q2 = fmaf(wb[8], pb2, q2);
+        }
+        if (k < len) {
+            const int b = __ldg(g.bcol + base + 32 * k + lane);
+            const float *vk = v + (size_t)32 * 9 * k;
+            float w[9];
+#pragma unroll
+            for (int i = 0; i < 9; ++i) w[i] = __ldg(vk + 32 * i);
+            const float4 z = z4[b];
+            float p0 = z.x, p1 = z.y, p2 = z.z;
+            if (!first) {
+                const float4 po = p4[b];
+                p0 = fmaf(beta, po.x, p0); p1 = fmaf(beta, po.y, p1); p2 = fmaf(beta, po.z, p2);
+            }
+            q0 = fmaf(w[0], p0, q0); q0 = fmaf(w[1], p1, q0); q0 = fmaf(w[2], p2, q0);
+            q1 = fmaf(w[3], p0, q1); q1 = fmaf(w[4], p1, q1); q1 = fmaf(w[5], p2, q1);
+            q2 = fmaf(w[6], p0, q2); q2 = fmaf(w[7], p1, q2); q2 = fmaf(w[8], p2, q2);
+        }
+    }
+    for (int o = 1; o < tpn; o <<= 1) {
+        q0 += __shfl_xor_sync(0xffffffffu, q0, o);
+        q1 += __shfl_xor_sync(0xffffffffu, q1, o);
+        q2 += __shfl_xor_sync(0xffffffffu, q2, o);
+    }
+}
+
 template <class A>
 __device__ __forceinline__ void spmv_row_z(const A &g, const float4 *z4, const float4 *p4, float beta, bool first,
                                            int a, int sub, bool valid, float &q0, float &q1, float &q2) {
@@ -534,7 +596,8 @@ __global__ void __launch_bounds__(1024, 1) cg_mixed_own_kernel(const __grid_cons
             const int l = ps * gpb + grp;
             const bool valid = l < nloc;
             float q0, q1, q2;
-            spmv_row_z(g, z4, pold, beta, first, a0 + l, sub, valid, q0, q1, q2);
+            if (g.block3) spmv_row_z2(g, z4, pold, beta, first, a0 + l, sub, valid, q0, q1, q2);
+            else spmv_row_z(g, z4, pold, beta, first, a0 + l, sub, valid, q0, q1, q2);
             if (!valid || sub != 0) continue;
             const float z0 = sdi[l] * sr[l], z1 = sdi[npb + l] * sr[npb + l], z2 = sdi[2 * npb + l] * sr[2 * npb + l];
             float p0 = z0, p1 = z1, p2 = z2;
