@@ -187,6 +187,7 @@ struct BlobImpl final : ffea_gpu_blob {
     MrgJump *sn_chunk_jump = nullptr, *sn_lane_jump = nullptr;
     int *sn_node_orig = nullptr, *sn_mid_orig = nullptr, *sn_lin_ptr = nullptr;
     double *sn_mid_drag = nullptr;
+    R *mid_f = nullptr;  // the step's midpoint forces (3 per midpoint), when any midpoint carries force
     int4 *sn_lin_ev = nullptr;
     int nmodes = 0;
     double modes[36] = {}, xc[3] = {};
@@ -398,6 +399,7 @@ struct BlobImpl final : ffea_gpu_blob {
             for (size_t m = 0; m < h.mid_nodes.size(); ++m) mdrag[m] = h.drag_all[h.mid_nodes[m]];
             CK(mem.upload(&sn_mid_orig, h.mid_nodes));
             CK(mem.upload(&sn_mid_drag, mdrag));
+            if (!h.mid_nodes.empty()) CK(mem.alloc(&mid_f, 3 * h.mid_nodes.size()));
             int lrc0 = upload_linearise(mem);
             if (lrc0) return lrc0;
         }
@@ -510,6 +512,12 @@ struct BlobImpl final : ffea_gpu_blob {
             sn.on = sn.noise || sn.lin_ptr != nullptr;
         }
         if (surf.nsets > 0) CK(launch_surface_forces(surf, stream));
+        // midpoints that carry force: each computed once (the vertices' linearise replay reads it up to ~20 times)
+        const int M = (int)h.mid_nodes.size();
+        if (ga.sn.lin_ptr && mid_f && (ga.sn.noise || ctf_mid || mface_ptr)) {
+            CK(Launch<R>::mid_force(ga.sn, M, mid_f, st, stream));
+            ga.sn.mid_f = mid_f;
+        }
         CK(Launch<R>::gather(ga, gather_blocks, stream));
         if ((rc = mark(3))) return rc;
         if (p.solver != FFEA_GPU_MASSLUMPED && (rc = launch_cg(init_partials, gather_blocks))) return rc;
@@ -897,6 +905,7 @@ struct BlobImpl final : ffea_gpu_blob {
             surf.set_total = d_total; surf.ff = ctf_ff;
             surf.st = st;
         }
+        if (mid_force && !mid_f && M > 0) CK(mem.alloc(&mid_f, 3 * (size_t)M));
         // midpoints that carry force need the linearisation replay (already there with Stokes noise)
         if (mid_force && !sn_lin_ptr) {
             build_linearise_events(h);

@@ -16,6 +16,8 @@ struct Launch {
     static cudaError_t element(const ElemArgs<R> &a, cudaStream_t s);
     static cudaError_t assemble(const AsmArgs<R> &a, cudaStream_t s);
     static cudaError_t gather(const GatherArgs<R> &a, int blocks, cudaStream_t s);
+    // the step's midpoint forces (M midpoints) into out, for the gather's linearise replay
+    static cudaError_t mid_force(const NodeForces &sn, int M, R *out, const DevStatus *st, cudaStream_t s);
     static int gather_threads();
     // persistent cooperative CG of `grid` blocks of `threads` threads (128 <= threads <= cg_threads(),
     // a multiple of 32)

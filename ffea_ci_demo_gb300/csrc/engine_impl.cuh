@@ -43,6 +43,14 @@ cudaError_t Launch<R>::gather(const GatherArgs<R> &a, int blocks, cudaStream_t s
 }
 
 template <class R>
+cudaError_t Launch<R>::mid_force(const NodeForces &sn, int M, R *out, const DevStatus *st, cudaStream_t s) {
+    if (M <= 0) return cudaSuccess;
+    mid_force_kernel<R><<<(M + 255) / 256, 256, 0, s>>>(sn, M, out, st);
+    count_launch();
+    return cudaGetLastError();
+}
+
+template <class R>
 int Launch<R>::cg_threads() { return CG_THREADS; }
 
 template <class R>

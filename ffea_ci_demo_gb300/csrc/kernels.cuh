@@ -320,6 +320,8 @@ struct NodeForces {
     const double *ff;                      // 3 per face: this step's constant surface force at each corner
     const int *lin_ptr;            // per vertex: its linearise events, in element order (or null)
     const int4 *lin_ev;            // up to three live midpoints (-1: already moved) summed into the vertex
+    const void *mid_f;             // this step's midpoint forces (3 per midpoint, in the step's precision R) as
+                                   // midpoint_force gives them, computed once by mid_force_kernel (or null)
 };
 
 // force[i] -= RAND(-.5,.5) * sqrt(24 kT drag / dt), three components, for reference node i
@@ -370,11 +372,29 @@ __device__ __forceinline__ void midpoint_linearise(const NodeForces &sn, int a, 
 #pragma unroll
         for (int j = 0; j < 3; ++j) {
             fm[j][0] = fm[j][1] = fm[j][2] = (R)0;
-            if (m[j] >= 0) midpoint_force<R>(sn, m[j], fm[j]);
+            if (m[j] < 0) continue;
+            if (sn.mid_f) {
+                const R *mf = static_cast<const R *>(sn.mid_f) + 3 * (size_t)m[j];
+                fm[j][0] = mf[0]; fm[j][1] = mf[1]; fm[j][2] = mf[2];
+            } else {
+                midpoint_force<R>(sn, m[j], fm[j]);
+            }
         }
 #pragma unroll
         for (int c = 0; c < 3; ++c) F[c] += (R)0.5 * (fm[0][c] + fm[1][c] + fm[2][c]);
     }
+}
+
+// every midpoint's force of the step (midpoint_force) once, for the vertices' linearise replay to read
+template <class R>
+__global__ void __launch_bounds__(256) mid_force_kernel(NodeForces sn, int M, R *out, const DevStatus *st) {
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= M || st->abort) return;
+    R f[3];
+    midpoint_force<R>(sn, m, f);
+    out[3 * (size_t)m] = f[0];
+    out[3 * (size_t)m + 1] = f[1];
+    out[3 * (size_t)m + 2] = f[2];
 }
 
 // one step's constant surface forces (CTF 3 of Blob::apply_ctforces): each set's force spread over its faces in

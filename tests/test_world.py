@@ -173,3 +173,37 @@ def test_equipartition_of_strain_energy(gpu, tmp_path, precision):
     assert ratio.size == 3 * nodes - 6
     assert np.abs(z).max() < 5.0
     assert abs(ratio.mean() - 1) < 0.03
+
+
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("solver,tol", [("CG", {"KineticEnergy": 0.04, "StrainEnergy": 0.03}),
+                                        ("CG_nomass", {"StrainEnergy": 0.03})])
+def test_reference_sphere_equipartition(gpu, tmp_path, solver, tol):
+    """The reference's physics tests tests/physics/sphere_63_120_mass and _nomass on their own mesh
+    (tests/golden/sphere_63_120.npz, made by gen_sphere.py from the reference's structure files): 1e5 steps
+    of 1e-14 s with Stokes drag and noise, CG tolerance 1e-2, and the averages of the measurement rows
+    40 .. second to last (testAverages.py): kinetic energy within 4% of 3N kT / 2 and strain energy within 3%
+    of (3N - 6) kT / 2, N = 63 vertices. The reference's script leaves calc_steric at its default of 1; here
+    it is 0, as the front-end refuses surface interactions (they act only when surface faces overlap)."""
+    from ffea_ci_demo_gb300.mesh import Mesh
+
+    z = np.load(os.path.join(GOLD, "sphere_63_120.npz"))
+    m = Mesh(pos=z["pos"], tets=z["tets"], material=z["material"], stokes_radius=z["stokes_radius"],
+             pinned=z["pinned"], scale=float(z["scale"]), n_linear=int(z["n_linear"]))
+    paths = write_structure(m, str(tmp_path), "sphere")
+    path = os.path.join(str(tmp_path), "sphere.ffea")
+    write_script(path, paths, solver=solver, scale=m.scale, dt=1e-14, kT=4.11e-21, epsilon=0.01,
+                 max_iterations_cg=1000, calc_noise=1, calc_stokes=1, stokes_visc=1e-3, rng_seed=44,
+                 num_steps=100000, check=1000)
+    lib.World(path).run()
+    head, rows = read_fm(os.path.join(str(tmp_path), "sphere.fm"))
+    assert rows.shape[0] == 101
+    kT, n = 4.11e-21, 63
+    want = {"KineticEnergy": kT * 3 * n / 2, "StrainEnergy": kT * (3 * n - 6) / 2}
+    for key, t in tol.items():
+        dev = abs(rows[40:-1, head.index(key)].mean() / want[key] - 1)
+        print(solver, key, "deviation", dev, "bound", t)
+        assert dev < t, (key, dev)
