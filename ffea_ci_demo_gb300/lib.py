@@ -427,6 +427,10 @@ class World:
         _check(self._lib.ffea_gpu_world_run(self._h, C.byref(last)), f"world_run (stopped at step {last.value})")
         return last.value
 
+    @property
+    def num_blobs(self) -> int:
+        return int(self._lib.ffea_gpu_world_num_blobs(self._h))
+
     def blob(self, i: int = 0) -> "Blob":
         """The i-th blob (owned by the World: valid while the World is)."""
         h = self._lib.ffea_gpu_world_blob(self._h, i)

@@ -207,3 +207,57 @@ def test_reference_sphere_equipartition(gpu, tmp_path, solver, tol):
         dev = abs(rows[40:-1, head.index(key)].mean() / want[key] - 1)
         print(solver, key, "deviation", dev, "bound", t)
         assert dev < t, (key, dev)
+
+
+@pytest.mark.gpu
+def test_two_blob_script_shares_one_stream(gpu, oracle_built, tmp_path):
+    """Two blobs in one script: World::run's single-thread order draws blob 0's elements, then blob 1's, from
+    one stream every step. Each blob must follow the oracle stepped on its slice of that stream (FP64 CG to
+    rounding, <= 1e-8 of the displacement), and the checkpoint must hold the stream after every step's
+    7 (T0 + T1) draws."""
+    ma, mb = kuhn_cube(2, side=10.0, seed=4), kuhn_cube(3, side=12.0, seed=9)
+    pa = write_structure(ma, str(tmp_path), "a")
+    pb = write_structure(mb, str(tmp_path), "b")
+    path = os.path.join(str(tmp_path), "two.ffea")
+    write_script(path, pa, num_steps=6, check=3, rng_seed=321, dt=1e-12, calc_noise=1, kT=4.11e-21)
+    txt = open(path).read()
+    blob_b = "\t<blob>\n\t\t<conformation>\n\t\t\t<motion_state = DYNAMIC>\n" + "".join(
+        f"\t\t\t<{k} = {os.path.basename(pb[f])}>\n" for k, f in
+        (("nodes", "node"), ("topology", "top"), ("material", "mat"), ("stokes", "stokes"), ("pin", "pin"))) + \
+        "\t\t</conformation>\n\t\t<solver = CG_nomass>\n\t\t<scale = 1e-09>\n\t\t<centroid = (30.0, 0.0, 0.0)>\n\t</blob>\n"
+    txt = txt.replace("<num_blobs = 1>", "<num_blobs = 2>").replace("<num_conformations = (1)>",
+                                                                     "<num_conformations = (1,1)>")
+    txt = txt.replace("</system>", blob_b + "</system>")
+    with open(path, "w") as f:
+        f.write(txt)
+    w = lib.World(path)
+    assert w.num_blobs == 2
+    x0 = [w.blob(0).pos(), w.blob(1).pos()]
+    w.run()
+    T0, T1 = ma.n_elem, mb.n_elem
+    state = seeds_from(321)
+    kw = dict(dt=1e-12, kT=4.11e-21, calc_noise=1, epsilon=1e-10)
+    oa, ob = po.OracleBlob(ma, threads=1, **kw), po.OracleBlob(mb, threads=1, **kw)
+    oa.set_pos(x0[0])
+    ob.set_pos(x0[1])
+    g = po.OracleRng()
+    for _ in range(7):  # steps 0..6
+        g.set_state(state)
+        oa.set_rng_state(state)
+        assert oa.step(1) == 0
+        for _ in range(7 * T0):
+            g.rand_u01()
+        ob.set_rng_state(g.get_state())
+        assert ob.step(1) == 0
+        for _ in range(7 * T1):
+            g.rand_u01()
+        state = g.get_state()
+    for b, o in enumerate((oa, ob)):
+        d = np.abs(w.blob(b).pos() - o.pos()).max() / np.abs(o.pos() - x0[b]).max()
+        assert d < 1e-8, (b, d)
+    # the checkpoint written before step 6's forces: the stream after 6 steps
+    g.set_state(seeds_from(321))
+    for _ in range(6 * 7 * (T0 + T1)):
+        g.rand_u01()
+    line = open(os.path.join(str(tmp_path), "two.fcp")).read().split("\n")
+    assert np.array_equal(np.array(line[1].split(), np.uint32), g.get_state())
