@@ -171,6 +171,7 @@ struct BlobImpl final : ffea_gpu_blob {
     int cg_grid = 0, gather_blocks = 0, partial_stride = 0, tpn = 4;
     int cg_npb = 0;  // rows per block of the owned-rows CG kernels (0: cg_kernel / cg_mixed_kernel)
     int cg_block = 1024;  // threads per CG block
+    bool cg_sr = false;   // the mixed CG_nomass solve uses cg_mixed_sr_kernel
     float4 *dpos = nullptr;  // mixed path: node offsets from the reference point
     // measurements: densities, reference positions of vertices and midpoints (SoA), per-block sums
     R *rho = nullptr;
@@ -358,14 +359,21 @@ struct BlobImpl final : ffea_gpu_blob {
         partial_stride = cg_grid;
         // each block keeps a run of rows in shared memory when they fit (FFEA_GPU_CG_OWN=0 turns this off);
         // the run is a multiple of a warp's rows so that a warp's rows share a SELL slice
+        // the mixed CG_nomass solve takes one reduction per iteration (cg_mixed_sr_kernel) when its rows fit
+        // (FFEA_GPU_CG_SR=0 keeps the two-reduction kernel)
         {
-            const char *own = getenv("FFEA_GPU_CG_OWN");
+            const char *own = getenv("FFEA_GPU_CG_OWN"), *sr = getenv("FFEA_GPU_CG_SR");
             const int maxrows = (own && own[0] == '0') ? 0 : Launch<R>::cg_own_max_rows(device);
             const int align = 32 / tpn, rows = (N + cg_grid - 1) / cg_grid;
             const int npb = (rows + align - 1) / align * align;
             cg_npb = (maxrows > 0 && npb <= maxrows) ? npb : 0;
+            if (mixed && p.solver == FFEA_GPU_NOMASS_CG && !(sr && sr[0] == '0') && !(own && own[0] == '0')) {
+                const int srrows = Launch<R>::cg_sr_max_rows(device);
+                cg_sr = srrows > 0 && npb <= srrows;
+                if (cg_sr) cg_npb = npb;
+            }
         }
-        CK(mem.alloc(&partials, (mixed ? MIXED_PARTIAL_ROWS : 3) * (size_t)partial_stride));
+        CK(mem.alloc(&partials, (mixed ? std::max(MIXED_PARTIAL_ROWS, MIXED_SR_NP) : 3) * (size_t)partial_stride));
         CK(mem.alloc(&st, 1));
         hist_cap = std::min(std::max(p.max_iterations_cg, 1), 1 << 20);
         CK(mem.alloc(&history, (size_t)hist_cap));
@@ -468,6 +476,7 @@ struct BlobImpl final : ffea_gpu_blob {
         ca.dpos = dpos; ca.nmodes = nomass ? nmodes : 0;
         for (int i = 0; i < 36; ++i) ca.modes[i] = modes[i];
         ca.npb = cg_npb;
+        ca.sr = cg_sr && nomass;
         CK(Launch<R>::cg(ca, cg_grid, cg_block, stream));
         return FFEA_GPU_OK;
     }

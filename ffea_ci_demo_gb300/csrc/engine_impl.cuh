@@ -94,6 +94,14 @@ int Launch<R>::cg_own_max_rows(int device) {
 }
 
 template <class R>
+int Launch<R>::cg_sr_max_rows(int device) {
+    if constexpr (std::is_same<R, float>::value)
+        return own_max_rows(cg_mixed_sr_kernel<R>, device, (int)sr_smem_bytes(1));
+    else
+        return (void)device, 0;
+}
+
+template <class R>
 cudaError_t Launch<R>::cg(const CgArgs<R> &a, int grid, int threads, cudaStream_t s) {
     CgArgs<R> args = a;
     void *params[] = {&args};
@@ -101,7 +109,10 @@ cudaError_t Launch<R>::cg(const CgArgs<R> &a, int grid, int threads, cudaStream_
     size_t smem = 0;
     if constexpr (std::is_same<R, float>::value) {
         fn = (const void *)cg_mixed_kernel<R>;
-        if (a.npb > 0) {
+        if (a.npb > 0 && a.sr) {
+            fn = (const void *)cg_mixed_sr_kernel<R>;
+            smem = sr_smem_bytes(a.npb);
+        } else if (a.npb > 0) {
             fn = (const void *)cg_mixed_own_kernel<R>;
             smem = own_smem_bytes(a.npb);
         }

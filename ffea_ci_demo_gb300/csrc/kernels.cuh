@@ -562,7 +562,8 @@ struct CgArgs {
     const float4 *dpos;
     int nmodes;
     double modes[36];
-    int npb;              // cg_mixed_own_kernel: rows owned by each block (a multiple of 32 / tpn)
+    int npb;              // owned-rows kernels: rows owned by each block (a multiple of 32 / tpn)
+    int sr;               // mixed path, 3x3-block matrix: the single-reduction kernel (cg_mixed_sr_kernel)
 };
 
 // p at node b for this iteration: p_new = beta p_old + D^{-1} r (vec3_scale_and_add with the

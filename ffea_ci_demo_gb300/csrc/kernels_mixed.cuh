@@ -34,6 +34,8 @@ constexpr int MIXED_A_NP = 7;        // p.q, S1(Dp)(3), S2(Dp)(3)
 constexpr int MIXED_B_NP = 2;        // r.r, r.z
 // partial rows: [0, A) phase A, [A, A+B) phase B, A+B the initial r.z
 constexpr int MIXED_PARTIAL_ROWS = MIXED_A_NP + MIXED_B_NP + 1;
+// cg_mixed_sr_kernel's one reduction per iteration: r.z, r.r, z.w, z.q, p.w, S1(Dz)(3), S2(Dz)(3)
+constexpr int MIXED_SR_NP = 11;
 
 // the six basis columns phi_j of Phi_a = [I | (.) x d]: e_x, e_y, e_z, e_x x d, e_y x d, e_z x d
 __device__ __forceinline__ void phi_cols(float dx, float dy, float dz, float (&phi)[6][3]) {
@@ -710,6 +712,256 @@ __global__ void __launch_bounds__(1024, 1) cg_mixed_own_kernel(const __grid_cons
         } else {
             st->last_iters = it;
             st->total_iters += it;
+        }
+    }
+}
+
+// Row a of w = V z for cg_mixed_sr_kernel: the preconditioned residual of neighbour b read as one float4;
+// two blocks per trip, products in block order.
+template <class A>
+__device__ __forceinline__ void spmv_row_w(const A &g, const float4 *z4, int a, int sub, bool valid, float &w0,
+                                           float &w1, float &w2) {
+    w0 = 0.f; w1 = 0.f; w2 = 0.f;
+    const int tpn = g.tpn;
+    if (valid) {
+        const int s = a >> 5, lane = a & 31;
+        const int base = __ldg(g.slice_ptr + s);
+        const int len = __ldg(g.rowlen + a);
+        const float *v = g.val + 9 * (size_t)base + lane;
+        int k = sub;
+#pragma unroll 1
+        for (; k + tpn < len; k += 2 * tpn) {
+            const int ba = __ldg(g.bcol + base + 32 * k + lane), bb = __ldg(g.bcol + base + 32 * (k + tpn) + lane);
+            const float *va = v + (size_t)32 * 9 * k, *vb = v + (size_t)32 * 9 * (k + tpn);
+            float wa[9], wb[9];
+#pragma unroll
+            for (int i = 0; i < 9; ++i) {
+                wa[i] = __ldg(va + 32 * i);
+                wb[i] = __ldg(vb + 32 * i);
+            }
+            const float4 za = z4[ba], zb = z4[bb];
+            w0 = fmaf(wa[0], za.x, w0); w0 = fmaf(wa[1], za.y, w0); w0 = fmaf(wa[2], za.z, w0);
+            w1 = fmaf(wa[3], za.x, w1); w1 = fmaf(wa[4], za.y, w1); w1 = fmaf(wa[5], za.z, w1);
+            w2 = fmaf(wa[6], za.x, w2); w2 = fmaf(wa[7], za.y, w2); w2 = fmaf(wa[8], za.z, w2);
+            w0 = fmaf(wb[0], zb.x, w0); w0 = fmaf(wb[1], zb.y, w0); w0 = fmaf(wb[2], zb.z, w0);
+            w1 = fmaf(wb[3], zb.x, w1); w1 = fmaf(wb[4], zb.y, w1); w1 = fmaf(wb[5], zb.z, w1);
+            w2 = fmaf(wb[6], zb.x, w2); w2 = fmaf(wb[7], zb.y, w2); w2 = fmaf(wb[8], zb.z, w2);
+        }
+        if (k < len) {
+            const int b = __ldg(g.bcol + base + 32 * k + lane);
+            const float *vk = v + (size_t)32 * 9 * k;
+            float wk[9];
+#pragma unroll
+            for (int i = 0; i < 9; ++i) wk[i] = __ldg(vk + 32 * i);
+            const float4 z = z4[b];
+            w0 = fmaf(wk[0], z.x, w0); w0 = fmaf(wk[1], z.y, w0); w0 = fmaf(wk[2], z.z, w0);
+            w1 = fmaf(wk[3], z.x, w1); w1 = fmaf(wk[4], z.y, w1); w1 = fmaf(wk[5], z.z, w1);
+            w2 = fmaf(wk[6], z.x, w2); w2 = fmaf(wk[7], z.y, w2); w2 = fmaf(wk[8], z.z, w2);
+        }
+    }
+    for (int o = 1; o < tpn; o <<= 1) {
+        w0 += __shfl_xor_sync(0xffffffffu, w0, o);
+        w1 += __shfl_xor_sync(0xffffffffu, w1, o);
+        w2 += __shfl_xor_sync(0xffffffffu, w2, o);
+    }
+}
+
+// Bytes of dynamic shared memory cg_mixed_sr_kernel needs for npb owned rows: x, r, p, q, w, D^{-1}, D, d.
+constexpr int SR_FIELDS = 24;
+__host__ __device__ constexpr size_t sr_smem_bytes(int npb) { return (size_t)SR_FIELDS * npb * sizeof(float); }
+
+// The mixed CG with one reduction per iteration (the single-synchronisation rearrangement of Chronopoulos and
+// Gear, 1989): the SpMV is applied to z = D^{-1} r, w = V z, and the search direction's product follows from
+// q = w~ + beta q_old, p = z + beta p_old, so beta is not needed before the SpMV. One sweep computes w and all
+// the dot products the step needs (r.z, r.r, z.w, z.q_old, p_old.w and the rigid-mode moments of D z); p.q
+// is then formed from them in FP64:
+//     p.q = z.w~ + beta (z.q_old + p_old.w~) + beta^2 p_old.q_old,    w~ = w + D Z A6 Z^T D z.
+// Per iteration: one grid barrier with a reduction, and one without (the new z must be visible before the
+// SpMV). Rows are owned as in cg_mixed_own_kernel. In exact arithmetic the iterates are those of the other
+// mixed CG kernels; in FP32 they agree to rounding and converge in the same number of iterations.
+template <class R>
+__global__ void __launch_bounds__(1024, 1) cg_mixed_sr_kernel(const __grid_constant__ CgArgs<R> g) {
+    static_assert(sizeof(R) == sizeof(float), "the single-reduction CG is the mixed path's");
+    extern __shared__ float sn[];
+    __shared__ float smemf[MIXED_SR_NP * 32];
+    __shared__ double s_sc[MIXED_GATHER_NP];
+    __shared__ double s_A6[36];
+    __shared__ double s_mp[6];        // moments of D p for the current direction
+    __shared__ double s_g, s_pq;      // r.z and p.q~ of the previous iteration
+    __shared__ float s_alpha, s_beta, s_tau[3], s_Om[3], s_dummy;
+    __shared__ int s_conv, s_stop;
+    DevStatus *st = g.st;
+    if (st->abort) return;
+    const bool defl = g.nmodes > 0;
+    unsigned long long tm = (blockIdx.x == 0 && threadIdx.x == 0) ? globaltimer_ns() : 0ull;
+    float2 *partials = reinterpret_cast<float2 *>(g.partials);
+    const int npb = g.npb, a0 = blockIdx.x * npb;
+    const int nloc = max(0, min(npb, g.N - a0));
+    float *sx = sn, *sr = sn + 3 * npb, *sp = sn + 6 * npb, *sq = sn + 9 * npb, *sw = sn + 12 * npb,
+          *sdi = sn + 15 * npb, *sdg = sn + 18 * npb, *sd = sn + 21 * npb;
+    float4 *z4 = reinterpret_cast<float4 *>(g.q);
+    grid_sum_df8<MIXED_GATHER_NP>(reinterpret_cast<const float2 *>(g.init_partials), g.init_stride, g.n_init, s_sc);
+    const double f2 = s_sc[0];
+    mixed_setup(g, s_sc, s_A6, s_tau, s_Om, &s_dummy, &s_conv);
+    // r = f^ (projected), x = 0, p = q = 0, z = D^{-1} r published
+    for (int l = threadIdx.x; l < nloc; l += blockDim.x) {
+        const int a = a0 + l;
+        float r0 = g.r[4 * a], r1 = g.r[4 * a + 1], r2 = g.r[4 * a + 2];
+        const float i0 = g.dinv[4 * a], i1 = g.dinv[4 * a + 1], i2 = g.dinv[4 * a + 2];
+        if (defl) {
+            const float4 d = g.dpos[a];
+            const float D0 = g.diag[4 * a], D1 = g.diag[4 * a + 1], D2 = g.diag[4 * a + 2];
+            r0 -= D0 * (s_tau[0] + (s_Om[1] * d.z - s_Om[2] * d.y));
+            r1 -= D1 * (s_tau[1] + (s_Om[2] * d.x - s_Om[0] * d.z));
+            r2 -= D2 * (s_tau[2] + (s_Om[0] * d.y - s_Om[1] * d.x));
+            sdg[l] = D0; sdg[npb + l] = D1; sdg[2 * npb + l] = D2;
+            sd[l] = d.x; sd[npb + l] = d.y; sd[2 * npb + l] = d.z;
+        }
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            sx[c * npb + l] = 0.f;
+            sp[c * npb + l] = 0.f;
+            sq[c * npb + l] = 0.f;
+        }
+        sr[l] = r0; sr[npb + l] = r1; sr[2 * npb + l] = r2;
+        sdi[l] = i0; sdi[npb + l] = i1; sdi[2 * npb + l] = i2;
+        z4[a] = make_float4(i0 * r0, i1 * r1, i2 * r2, 0.f);
+    }
+    if (threadIdx.x < 6) s_mp[threadIdx.x] = 0.0;
+    if (threadIdx.x == 0) { s_g = 0.0; s_pq = 0.0; s_stop = 0; }
+    bool ok = grid_sync(g.gb, st, g.limit_ns);
+    const int tpn = g.tpn, gpb = blockDim.x / tpn, grp = threadIdx.x / tpn, sub = threadIdx.x % tpn;
+    const int npass = (nloc + gpb - 1) / gpb;
+    FFEA_MARK(g, tm, 0);
+    int k = 0;  // updates applied so far
+    s_conv = 0;
+    for (; ok; ++k) {
+        // w = V z over the block's rows, and the iteration's dot products
+        float acc[MIXED_SR_NP];
+#pragma unroll
+        for (int i = 0; i < MIXED_SR_NP; ++i) acc[i] = 0.f;
+        for (int ps = 0; ps < npass; ++ps) {
+            const int l = ps * gpb + grp;
+            const bool valid = l < nloc;
+            float w0, w1, w2;
+            spmv_row_w(g, z4, a0 + l, sub, valid, w0, w1, w2);
+            if (!valid || sub != 0) continue;
+            sw[l] = w0; sw[npb + l] = w1; sw[2 * npb + l] = w2;
+            const float r0 = sr[l], r1 = sr[npb + l], r2 = sr[2 * npb + l];
+            const float z0 = sdi[l] * r0, z1 = sdi[npb + l] * r1, z2 = sdi[2 * npb + l] * r2;
+            acc[0] += r0 * z0 + r1 * z1 + r2 * z2;
+            acc[1] += r0 * r0 + r1 * r1 + r2 * r2;
+            acc[2] += z0 * w0 + z1 * w1 + z2 * w2;
+            acc[3] += z0 * sq[l] + z1 * sq[npb + l] + z2 * sq[2 * npb + l];
+            acc[4] += sp[l] * w0 + sp[npb + l] * w1 + sp[2 * npb + l] * w2;
+            if (defl) {
+                const float dx = sd[l], dy = sd[npb + l], dz = sd[2 * npb + l];
+                const float e0 = sdg[l] * z0, e1 = sdg[npb + l] * z1, e2 = sdg[2 * npb + l] * z2;
+                acc[5] += e0; acc[6] += e1; acc[7] += e2;
+                acc[8] += dy * e2 - dz * e1;
+                acc[9] += dz * e0 - dx * e2;
+                acc[10] += dx * e1 - dy * e0;
+            }
+        }
+        FFEA_MARK(g, tm, 1);
+        block_reduce_store<MIXED_SR_NP>(acc, smemf, partials, g.stride, 0);
+        FFEA_MARK(g, tm, 2);
+        if (!(ok = grid_sync(g.gb, st, g.limit_ns))) break;
+        FFEA_MARK(g, tm, 3);
+        grid_sum_df8<MIXED_SR_NP>(partials, g.stride, gridDim.x, s_sc);
+        if (threadIdx.x < 32) {
+            const int ln = threadIdx.x;
+            // c = A6 m(z): the rigid-mode coefficients of D Z A6 Z^T D z, over six lanes
+            double c = 0.0;
+            if (defl && ln < 6) {
+#pragma unroll
+                for (int qq = 0; qq < 6; ++qq) c += s_A6[6 * ln + qq] * s_sc[5 + qq];
+            }
+            double mzc = (ln < 6) ? s_sc[5 + ln] * c : 0.0;   // m(z).c
+            double mpc = (ln < 6) ? s_mp[ln] * c : 0.0;       // m(p_old).c
+#pragma unroll
+            for (int o = 4; o > 0; o >>= 1) {
+                mzc += __shfl_xor_sync(0xffffffffu, mzc, o);
+                mpc += __shfl_xor_sync(0xffffffffu, mpc, o);
+            }
+            const double gam = s_sc[0], rr = s_sc[1];
+            // |r|^2/|f|^2 < epsilon2 after an update, as NoMassCGSolver::solve tests it (a zero force: x = 0 at once)
+            const bool conv = f2 == 0.0 || (k > 0 && (g.check_last || k < g.imax) && rr < g.eps2 * f2);
+            if (ln == 0 && blockIdx.x == 0 && k > 0 && k - 1 < g.hist_cap) g.history[k - 1] = (f2 == 0.0) ? 0.0 : rr / f2;
+            const bool stop = conv || k >= g.imax;
+            // the step lengths in FP32 (as cg_mixed_kernel forms them): FP64 division is slow on this GPU
+            const float beta_f = (k == 0) ? 0.f : (float)gam / (float)s_g;
+            const double beta = beta_f;
+            const double zw = s_sc[2] + mzc, pw = s_sc[4] + mpc;
+            const double pq = zw + beta * (s_sc[3] + pw) + beta * beta * s_pq;
+            __syncwarp();
+            if (ln < 6) {
+                const float cf = (float)c;
+                if (ln < 3) s_tau[ln] = cf; else s_Om[ln - 3] = cf;
+                s_mp[ln] = s_sc[5 + ln] + beta * s_mp[ln];
+            }
+            if (ln == 0) {
+                s_conv = conv;
+                s_stop = stop;
+                s_beta = beta_f;
+                s_alpha = (float)gam / (float)pq;
+                s_g = gam;
+                s_pq = pq;
+            }
+        }
+        __syncthreads();
+        FFEA_MARK(g, tm, 4);
+        if (s_stop) break;
+        const float alpha = s_alpha, beta = s_beta;
+        const float t0 = s_tau[0], t1 = s_tau[1], t2 = s_tau[2], O0 = s_Om[0], O1 = s_Om[1], O2 = s_Om[2];
+        // p = z + beta p ; q = w~ + beta q ; x += alpha p ; r -= alpha q ; z = D^{-1} r published
+        for (int l = threadIdx.x; l < nloc; l += blockDim.x) {
+            const int a = a0 + l;
+            float wv[3] = {sw[l], sw[npb + l], sw[2 * npb + l]};
+            if (defl) {
+                const float dx = sd[l], dy = sd[npb + l], dz = sd[2 * npb + l];
+                wv[0] += sdg[l] * (t0 + (O1 * dz - O2 * dy));
+                wv[1] += sdg[npb + l] * (t1 + (O2 * dx - O0 * dz));
+                wv[2] += sdg[2 * npb + l] * (t2 + (O0 * dy - O1 * dx));
+            }
+            float zn[3];
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                const float r = sr[c * npb + l], di = sdi[c * npb + l];
+                const float pv = fmaf(beta, sp[c * npb + l], di * r);
+                const float qv = fmaf(beta, sq[c * npb + l], wv[c]);
+                sp[c * npb + l] = pv;
+                sq[c * npb + l] = qv;
+                sx[c * npb + l] += alpha * pv;
+                const float rn = r - alpha * qv;
+                sr[c * npb + l] = rn;
+                zn[c] = di * rn;
+            }
+            z4[a] = make_float4(zn[0], zn[1], zn[2], 0.f);
+        }
+        FFEA_MARK(g, tm, 5);
+        if (!(ok = grid_sync(g.gb, st, g.limit_ns))) break;
+        FFEA_MARK(g, tm, 7);
+    }
+    for (int l = threadIdx.x; l < nloc; l += blockDim.x) {
+        const int a = a0 + l;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            g.x[4 * a + c] = sx[c * npb + l];
+            g.r[4 * a + c] = sr[c * npb + l];
+        }
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        if (!ok) {
+            st->abort = 1;
+        } else if (!s_conv) {
+            st->cg_fail = 1;
+            st->abort = 1;
+            st->last_iters = g.imax;
+            st->total_iters += g.imax;
+        } else {
+            st->last_iters = k;
+            st->total_iters += k;
         }
     }
 }
