@@ -172,6 +172,8 @@ struct BlobImpl final : ffea_gpu_blob {
     int cg_npb = 0;  // rows per block of the owned-rows CG kernels (0: cg_kernel / cg_mixed_kernel)
     int cg_block = 1024;  // threads per CG block
     bool cg_sr = false;   // the mixed CG_nomass solve uses cg_mixed_sr_kernel
+    int *nb_ptr = nullptr, *nb_list = nullptr;  // its blocks' neighbour blocks
+    unsigned int *nb_flags = nullptr;           // and their publication counters
     float4 *dpos = nullptr;  // mixed path: node offsets from the reference point
     // measurements: densities, reference positions of vertices and midpoints (SoA), per-block sums
     R *rho = nullptr;
@@ -372,6 +374,29 @@ struct BlobImpl final : ffea_gpu_blob {
                 cg_sr = srrows > 0 && npb <= srrows;
                 if (cg_sr) cg_npb = npb;
             }
+            if (cg_sr) {
+                // the blocks each block's SpMV reads z from: owners of the columns of its rows
+                std::vector<int> nbp(cg_grid + 1, 0), nbl;
+                std::vector<char> seen(cg_grid, 0);
+                for (int b = 0; b < cg_grid; ++b) {
+                    std::vector<int> got;
+                    for (int a = b * npb; a < std::min(N, (b + 1) * npb); ++a) {
+                        const int s0 = h.slice_ptr[a >> 5], ln = a & 31;
+                        for (int k = 0; k < h.rowlen[a]; ++k) {
+                            const int ob = h.bcol[s0 + 32 * k + ln] / npb;
+                            if (ob != b && !seen[ob]) { seen[ob] = 1; got.push_back(ob); }
+                        }
+                    }
+                    for (int ob : got) seen[ob] = 0;
+                    std::sort(got.begin(), got.end());
+                    nbl.insert(nbl.end(), got.begin(), got.end());
+                    nbp[b + 1] = (int)nbl.size();
+                }
+                if (nbl.empty()) nbl.push_back(0);
+                CK(mem.upload(&nb_ptr, nbp));
+                CK(mem.upload(&nb_list, nbl));
+                CK(mem.alloc(&nb_flags, (size_t)FLAG_STRIDE * cg_grid));
+            }
         }
         CK(mem.alloc(&partials, (mixed ? std::max(MIXED_PARTIAL_ROWS, MIXED_SR_NP) : 3) * (size_t)partial_stride));
         CK(mem.alloc(&st, 1));
@@ -477,6 +502,10 @@ struct BlobImpl final : ffea_gpu_blob {
         for (int i = 0; i < 36; ++i) ca.modes[i] = modes[i];
         ca.npb = cg_npb;
         ca.sr = cg_sr && nomass;
+        if (ca.sr) {
+            ca.nb_ptr = nb_ptr; ca.nb_list = nb_list; ca.flags = nb_flags;
+            CK(cudaMemsetAsync(nb_flags, 0, (size_t)FLAG_STRIDE * cg_grid * sizeof(unsigned int), stream));
+        }
         CK(Launch<R>::cg(ca, cg_grid, cg_block, stream));
         return FFEA_GPU_OK;
     }

@@ -564,6 +564,10 @@ struct CgArgs {
     double modes[36];
     int npb;              // owned-rows kernels: rows owned by each block (a multiple of 32 / tpn)
     int sr;               // mixed path, 3x3-block matrix: the single-reduction kernel (cg_mixed_sr_kernel)
+    // cg_mixed_sr_kernel: blocks owning a column of block b's rows (nb_ptr[b] .. nb_ptr[b + 1] in nb_list) and
+    // one publication counter per block (FLAG_STRIDE words apart, zero at launch)
+    const int *nb_ptr, *nb_list;
+    unsigned int *flags;
 };
 
 // p at node b for this iteration: p_new = beta p_old + D^{-1} r (vec3_scale_and_add with the
