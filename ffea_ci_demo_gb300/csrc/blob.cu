@@ -502,7 +502,7 @@ struct BlobImpl final : ffea_gpu_blob {
         for (int i = 0; i < 36; ++i) ca.modes[i] = modes[i];
         ca.npb = cg_npb;
         ca.sr = cg_sr && nomass;
-        if (ca.sr) {
+        if (nb_flags) {
             ca.nb_ptr = nb_ptr; ca.nb_list = nb_list; ca.flags = nb_flags;
             CK(cudaMemsetAsync(nb_flags, 0, (size_t)FLAG_STRIDE * cg_grid * sizeof(unsigned int), stream));
         }

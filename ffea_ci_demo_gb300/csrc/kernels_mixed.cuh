@@ -766,43 +766,6 @@ __device__ __forceinline__ void spmv_row_w(const A &g, const float4 *z4, int a, 
     }
 }
 
-constexpr int FLAG_STRIDE = 32;  // words between two blocks' publication counters (one 128-byte line each)
-
-// Block `blockIdx.x` has written its rows' z for round `epoch`: publish that (a release through the fence
-// and the atomic), then wait (bounded by %globaltimer) until every block owning a column of its rows has
-// published the same round, and order the block's later reads after those writes. Returns false on a
-// timeout (recorded in st) or when another block recorded one.
-__device__ __forceinline__ bool neighbour_sync(const CgArgs<float> &g, unsigned int epoch, DevStatus *st) {
-    __shared__ int s_nok;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        s_nok = 0;
-        __threadfence();
-        atomicExch(g.flags + (size_t)FLAG_STRIDE * blockIdx.x, epoch);
-    }
-    __syncthreads();
-    const int j0 = g.nb_ptr[blockIdx.x], j1 = g.nb_ptr[blockIdx.x + 1];
-    for (int j = j0 + (int)threadIdx.x; j < j1; j += blockDim.x) {
-        const volatile unsigned int *f = g.flags + (size_t)FLAG_STRIDE * g.nb_list[j];
-        const unsigned long long t0 = globaltimer_ns();
-        unsigned int polls = 0;
-        while ((int)(*f - epoch) < 0) {
-            if ((++polls & 255u) == 0u) {
-                if (globaltimer_ns() - t0 > g.limit_ns) {
-                    atomicExch(&st->timeout, 1);
-                    atomicExch(&st->abort, 1);
-                    s_nok = 1;
-                    break;
-                }
-                if (*((volatile int *)&st->timeout)) { s_nok = 1; break; }
-            }
-        }
-        __threadfence();
-    }
-    __syncthreads();
-    return s_nok == 0;
-}
-
 // Bytes of dynamic shared memory cg_mixed_sr_kernel needs for npb owned rows: x, r, p, q, w, D^{-1}, D, d.
 constexpr int SR_FIELDS = 24;
 __host__ __device__ constexpr size_t sr_smem_bytes(int npb) { return (size_t)SR_FIELDS * npb * sizeof(float); }
