@@ -614,8 +614,12 @@ def main():
     model_bytes = iters * cg_bytes_per_iteration(args.cells, p)
     fmt_bytes = iters * cg_format_bytes_per_iteration(head["blocks"], (args.cells + 1) ** 3, p)
     achieved = model_bytes / (cg_ms / 1e3) / 1e9
-    cg_name = "cg_kernel" if args.headline == "fp64" else (
-        "cg_mixed_kernel" if os.environ.get("FFEA_GPU_CG_OWN", "1").startswith("0") else "cg_mixed_own_kernel")
+    own = not os.environ.get("FFEA_GPU_CG_OWN", "1").startswith("0")
+    sr = own and not os.environ.get("FFEA_GPU_CG_SR", "1").startswith("0")
+    if args.headline == "fp64":
+        cg_name = "cg_own_kernel" if own else "cg_kernel"
+    else:
+        cg_name = "cg_mixed_sr_kernel" if sr else ("cg_mixed_own_kernel" if own else "cg_mixed_kernel")
     roofline = {"bound": "hbm", "kernel": cg_name, "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "peak_source": peak_kind, "traffic": profiled_traffic(args.headline),
                 "bytes_per_launch_model": model_bytes, "bytes_per_launch_format": fmt_bytes,
