@@ -191,6 +191,7 @@ struct BlobImpl final : ffea_gpu_blob {
     int *sn_node_orig = nullptr, *sn_mid_orig = nullptr, *sn_lin_ptr = nullptr;
     double *sn_mid_drag = nullptr;
     R *mid_f = nullptr;  // the step's midpoint forces (3 per midpoint), when any midpoint carries force
+    RotArgs rot{};       // rotational constant forces (nodes, their forces, the arrays they update)
     int4 *sn_lin_ev = nullptr;
     int nmodes = 0;
     double modes[36] = {}, xc[3] = {};
@@ -549,6 +550,7 @@ struct BlobImpl final : ffea_gpu_blob {
             sn.lin_ev = sn_lin_ev;
             sn.on = sn.noise || sn.lin_ptr != nullptr;
         }
+        if (rot.nv + rot.nm > 0) CK(launch_rot_forces(rot, stream));
         if (surf.nsets > 0) CK(launch_surface_forces(surf, stream));
         // midpoints that carry force: each computed once (the vertices' linearise replay reads it up to ~20 times)
         const int M = (int)h.mid_nodes.size();
@@ -868,9 +870,33 @@ struct BlobImpl final : ffea_gpu_blob {
             for (int c = 0; c < 3; ++c) vn[3 * (size_t)k + c] = cm.lin[3 * (size_t)h.node_of[k] + c];
         for (int m = 0; m < M; ++m) {
             for (int c = 0; c < 3; ++c) vm[3 * (size_t)m + c] = cm.lin[3 * (size_t)h.mid_nodes[m] + c];
-            mid_force = mid_force || cm.has_lin[h.mid_nodes[m]];
+            mid_force = mid_force || cm.has_lin[h.mid_nodes[m]] || !cm.rot[h.mid_nodes[m]].empty();
         }
-        for (int i = 0; i < n; ++i) any_lin = any_lin || cm.has_lin[i];
+        for (int i = 0; i < n; ++i) any_lin = any_lin || cm.has_lin[i] || !cm.rot[i].empty();
+        // rotational forces: the nodes carrying them, in vertex then midpoint order, with their forces in file order
+        std::vector<int> rv_row, rv_ptr(1, 0), rm_idx, rm_ptr(1, 0);
+        std::vector<RotEntry> rent;
+        auto add_rot = [&](int node) {
+            for (const RotCtf &r : cm.rot[node]) {
+                RotEntry e{};
+                e.F = r.F;
+                e.torque = r.torque;
+                for (int c = 0; c < 3; ++c) { e.p[c] = r.p[c]; e.d[c] = r.d[c]; }
+                rent.push_back(e);
+            }
+        };
+        for (int k = 0; k < N; ++k)
+            if (!cm.rot[h.node_of[k]].empty()) {
+                rv_row.push_back(k);
+                add_rot(h.node_of[k]);
+                rv_ptr.push_back((int)rent.size());
+            }
+        for (int m = 0; m < M; ++m)
+            if (!cm.rot[h.mid_nodes[m]].empty()) {
+                rm_idx.push_back(m);
+                add_rot(h.mid_nodes[m]);
+                rm_ptr.push_back((int)rent.size() - rv_ptr.back());
+            }
         if (lin_from_ctf) {  // the replay lived with the previous constant forces
             sn_lin_ptr = nullptr;
             sn_lin_ev = nullptr;
@@ -880,9 +906,36 @@ struct BlobImpl final : ffea_gpu_blob {
         ctf_node = ctf_mid = ctf_ff = nullptr;
         vface_ptr = vface = mface_ptr = mface = nullptr;
         surf = SurfArgs{};
+        rot = RotArgs{};
         if (any_lin) {
             CK(ctf_mem.upload(&ctf_node, vn));
             if (mid_force) CK(ctf_mem.upload(&ctf_mid, vm));
+        }
+        if (!rent.empty()) {
+            // the static linear sums stay as they are; the gather reads copies the rotational kernel rewrites
+            // for its nodes every step
+            double *lin_v = ctf_node, *lin_m = ctf_mid;
+            CK(ctf_mem.upload(&ctf_node, vn));
+            if (mid_force) CK(ctf_mem.upload(&ctf_mid, vm));
+            int *d_vrow, *d_vptr, *d_midx, *d_mptr;
+            RotEntry *d_ent;
+            if (rv_row.empty()) rv_row.push_back(0);
+            if (rm_idx.empty()) rm_idx.push_back(0);
+            CK(ctf_mem.upload(&d_vrow, rv_row));
+            CK(ctf_mem.upload(&d_vptr, rv_ptr));
+            CK(ctf_mem.upload(&d_midx, rm_idx));
+            CK(ctf_mem.upload(&d_mptr, rm_ptr));
+            CK(ctf_mem.upload(&d_ent, rent));
+            rot.nv = (int)rv_ptr.size() - 1;
+            rot.nm = (int)rm_ptr.size() - 1;
+            rot.v_row = d_vrow; rot.v_ptr = d_vptr; rot.m_idx = d_midx; rot.m_ptr = d_mptr;
+            rot.ent = d_ent;
+            rot.ent_m = d_ent + rv_ptr.back();
+            rot.mid_a = mid_a; rot.mid_b = mid_b;
+            rot.px = px; rot.py = py; rot.pz = pz;
+            rot.lin_v = lin_v; rot.lin_m = lin_m;
+            rot.out_v = ctf_node; rot.out_m = ctf_mid;
+            rot.st = st;
         }
         const int nsets = (int)cm.set_ptr.size() - 1;
         if (nsets > 0) {

@@ -1,6 +1,6 @@
 // ctforces.h -- the reference's constant-force file (Blob::load_ctforces, src/Blob.cpp:2478-2805) for one blob:
-// linear forces on nodes (CTF 1) and linear forces spread over sets of surface faces in proportion to their
-// areas (CTF 3). Rotational forces (CTF 2) are refused. Host only.
+// linear forces on nodes (CTF 1), rotational forces about an axis through a point (CTF 2), and linear forces
+// spread over sets of surface faces in proportion to their areas (CTF 3). Host only.
 #pragma once
 
 #include <cmath>
@@ -13,12 +13,23 @@
 namespace ffea {
 namespace host {
 
-constexpr double MESO_FORCE = 2.4364705882352941e-11;  // mesoDimensions::force (include/dimensions.h:37)
+constexpr double MESO_FORCE = 2.4364705882352941e-11;   // mesoDimensions::force (include/dimensions.h:37)
+constexpr double MESO_LENGTH_CTF = 1.7e-10;             // mesoDimensions::length (include/dimensions.h:31)
+
+// one rotational constant force (CTF 2) on one node: about the axis through p along the unit vector d,
+// F times (r x d) ('f') or F / |r| times (r x d) ('t'), r from the node to its nearest point on the axis
+struct RotCtf {
+    double F;
+    int torque;
+    double p[3], d[3];
+};
 
 struct CtfModel {
     // CTF 1: per node of the reference numbering, the sum of its linear forces in file order (meso)
     std::vector<double> lin;
     std::vector<char> has_lin;
+    // CTF 2: per node, its rotational forces in file order (the reference adds them after the linear ones)
+    std::vector<std::vector<RotCtf>> rot;
     // CTF 3: surface faces (3 corner nodes, reference numbering), sets of faces with their force (meso)
     std::vector<int> face_nodes;
     std::vector<double> set_force;        // 3 per set
@@ -126,13 +137,39 @@ inline int load_ctforces(const char *ctf_file, const char *surf_file, int blob_i
         }
     }
     at += n_l;
+    m.rot.assign(n_all, {});
     if (at < (int)L.size() && L[at].compare(0, 18, "rotational forces:") == 0) {
         ++at;
+        // "F type px py pz dx dy dz blob conformation node|all" (src/Blob.cpp:2652-2730): F in N, the axis point
+        // in m, type "p?" (an axis through a point; "n?" axes between nodes are not applied by the reference
+        // either, src/Blob.cpp:1697-1705) and "?f" (F (r x d)) or "?t" (F/|r| (r x d))
         for (int i = at; i < at + n_r; ++i) {
             const auto w = ctf_split(L[i]);
-            if (w.size() == 11 && atoi(w[8].c_str()) == blob_index && atoi(w[9].c_str()) == 0) {
-                err = "rotational constant forces are not supported";
+            if (w.size() != 11) { err = "invalid rotational force line: " + L[i]; return 3; }
+            if (atoi(w[8].c_str()) != blob_index || atoi(w[9].c_str()) != 0) continue;
+            const std::string &type = w[1];
+            if (type.size() < 2 || type[0] != 'p') {
+                err = "rotational forces about an axis between nodes (type 'n') are not applied by the reference";
                 return 3;
+            }
+            if (type[1] != 'f' && type[1] != 't') { err = "invalid rotational force type: " + type; return 3; }
+            RotCtf r{};
+            r.F = atof(w[0].c_str()) * (1. / MESO_FORCE);
+            r.torque = type[1] == 't';
+            double d[3] = {atof(w[5].c_str()), atof(w[6].c_str()), atof(w[7].c_str())}, sum = 0;
+            for (int c = 0; c < 3; ++c) sum += d[c] * d[c];  // normalize, include/mat_vec_fns_II.h:188-198
+            if (sum == 0) { err = "rotational force with a zero axis"; return 3; }
+            sum = std::sqrt(sum);
+            for (int c = 0; c < 3; ++c) {
+                r.d[c] = d[c] / sum;
+                r.p[c] = (1. / MESO_LENGTH_CTF) * atof(w[2 + c].c_str());  // resize(mdlm1, ctf_p)
+            }
+            if (w[10] == "all") {
+                for (int n = 0; n < n_all; ++n) m.rot[n].push_back(r);
+            } else {
+                const int n = atoi(w[10].c_str());
+                if (n < 0 || n >= n_all) { err = "rotational force on an out of range node"; return 3; }
+                m.rot[n].push_back(r);
             }
         }
     } else if (n_r > 0) { err = "expected 'rotational forces:'"; return 3; }

@@ -52,6 +52,8 @@ extern template struct AdjLaunch<float>;
 cudaError_t launch_finish_step(uint32_t *rng_state, const MrgJump *step_jump, DevStatus *st, cudaStream_t s);
 // the constant surface forces of a step (surf_set_kernel, then surf_face_kernel)
 cudaError_t launch_surface_forces(const SurfArgs &a, cudaStream_t s);
+// the step's constant node forces of the nodes with rotational forces (rot_force_kernel)
+cudaError_t launch_rot_forces(const RotArgs &a, cudaStream_t s);
 // node state in the reference's numbering and layout (n_all x 3, AoS) <-> the vertex rows (SoA):
 // scatter takes vertex k from aos[3 node_of[k] + c]; gather writes every reference node i from its source
 // rows src[i] = (a, b): a vertex (a == b), a midpoint (x_a + x_b) / 2 when `mids`, else 0 (also for a < 0)

@@ -44,6 +44,49 @@ __global__ void __launch_bounds__(128) surf_face_kernel(SurfArgs g) {
     for (int c = 0; c < 3; ++c) g.ff[3 * (size_t)f + c] = out[c];
 }
 
+// one thread per node with rotational forces: its linear sum, then each rotational force in file order
+// (Blob::apply_ctforces adds CTF 1 before CTF 2), at the node's current position (a midpoint at (x_a + x_b)/2)
+__global__ void __launch_bounds__(128) rot_force_kernel(RotArgs g) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= g.nv + g.nm || g.st->abort) return;
+    const bool vert = i < g.nv;
+    const int j = vert ? i : i - g.nv;
+    double p0[3];
+    int row, e0, e1;
+    const double *lin;
+    double *out;
+    if (vert) {
+        row = g.v_row[j];
+        p0[0] = g.px[row]; p0[1] = g.py[row]; p0[2] = g.pz[row];
+        e0 = g.v_ptr[j]; e1 = g.v_ptr[j + 1];
+        lin = g.lin_v + 3 * (size_t)row;
+        out = g.out_v + 3 * (size_t)row;
+    } else {
+        row = g.m_idx[j];
+        const int a = g.mid_a[row], b = g.mid_b[row];
+        p0[0] = .5 * (g.px[a] + g.px[b]); p0[1] = .5 * (g.py[a] + g.py[b]); p0[2] = .5 * (g.pz[a] + g.pz[b]);
+        e0 = g.m_ptr[j]; e1 = g.m_ptr[j + 1];
+        lin = g.lin_m + 3 * (size_t)row;
+        out = g.out_m + 3 * (size_t)row;
+    }
+    const RotEntry *ent = vert ? g.ent : g.ent_m;
+    double F[3] = {lin[0], lin[1], lin[2]};
+    for (int k = e0; k < e1; ++k) {
+        double f[3];
+        rot_force(ent[k], p0, f);
+        for (int c = 0; c < 3; ++c) F[c] += f[c];
+    }
+    for (int c = 0; c < 3; ++c) out[c] = F[c];
+}
+
+cudaError_t launch_rot_forces(const RotArgs &a, cudaStream_t s) {
+    const int n = a.nv + a.nm;
+    if (n <= 0) return cudaSuccess;
+    rot_force_kernel<<<(n + 127) / 128, 128, 0, s>>>(a);
+    count_launch();
+    return cudaGetLastError();
+}
+
 cudaError_t launch_surface_forces(const SurfArgs &a, cudaStream_t s) {
     surf_set_kernel<<<(a.nsets + 127) / 128, 128, 0, s>>>(a);
     surf_face_kernel<<<(a.nfaces + 127) / 128, 128, 0, s>>>(a);

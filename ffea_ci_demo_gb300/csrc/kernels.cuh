@@ -385,6 +385,68 @@ __device__ __forceinline__ void midpoint_linearise(const NodeForces &sn, int a, 
     }
 }
 
+// one rotational constant force on a node (CTF 2 of Blob::apply_ctforces, src/Blob.cpp:1684-1720)
+struct RotEntry {
+    double F;         // meso force
+    double p[3];      // a point of the axis (meso length)
+    double d[3];      // the axis' unit direction
+    int torque;       // 0: F (r x d); 1: F / |r| (r x d)
+    int pad;
+};
+
+// nodes (vertex rows, then midpoints) carrying rotational constant forces: each step their constant force is
+// the linear sum plus every rotational force in file order, evaluated at the node's current position
+struct RotArgs {
+    int nv, nm;
+    const int *v_row, *v_ptr;   // vertex row of list entry i, its forces [v_ptr[i], v_ptr[i + 1]) in ent
+    const int *m_idx, *m_ptr;   // the same for midpoints (index into the midpoint list), ptr into ent_m
+    const RotEntry *ent, *ent_m;
+    const int *mid_a, *mid_b;   // midpoint edge ends (vertex rows)
+    const double *px, *py, *pz;
+    const double *lin_v, *lin_m;  // the static linear sums (3 per vertex / midpoint)
+    double *out_v, *out_m;        // the step's constant forces (3 per vertex / midpoint)
+    const DevStatus *st;
+};
+
+__device__ __forceinline__ void cross3(const double (&u)[3], const double (&v)[3], double (&w)[3]) {
+    // arr3arr3VectorProduct, include/mat_vec_fns_II.h:369-373
+    w[0] = u[1] * v[2] - v[1] * u[2];
+    w[1] = -u[0] * v[2] + v[0] * u[2];
+    w[2] = u[0] * v[1] - v[0] * u[1];
+}
+
+// magnitude (include/mat_vec_fns_II.h:326-333): an `omp simd` sum that GCC builds as (a0^2 + a2^2) + a1^2
+__device__ __forceinline__ double magnitude3(const double (&a)[3]) { return sqrt((a[0] * a[0] + a[2] * a[2]) + a[1] * a[1]); }
+
+// the force of one rotational entry on a node at p0: r to the nearest point of the axis
+// (intersectingPointToLine, include/mat_vec_fns_II.h:755-777), then F (r x d) or F/|r| (r x d)
+__device__ __forceinline__ void rot_force(const RotEntry &e, const double (&p0)[3], double (&f)[3]) {
+    const double d[3] = {e.d[0], e.d[1], e.d[2]};
+    double p0p1[3], v2[3], p3[3];
+    for (int c = 0; c < 3; ++c) p0p1[c] = p0[c] - e.p[c];
+    cross3(p0p1, d, v2);
+    if (magnitude3(v2) < 3.0 * 2.220446049250313080847e-16) {  // ffea_const::threeErr
+        for (int c = 0; c < 3; ++c) p3[c] = p0[c];
+    } else {
+        double cp3p0[3], v1v2[3];
+        cross3(d, v2, cp3p0);
+        cross3(d, cp3p0, v1v2);
+        // detByRows (include/mat_vec_fns_II.h:379-385)
+        double cc = p0p1[0] * (d[1] * v1v2[2] - d[2] * v1v2[1]);
+        cc += p0p1[1] * (d[2] * v1v2[0] - d[0] * v1v2[2]);
+        cc += p0p1[2] * (d[0] * v1v2[1] - d[1] * v1v2[0]);
+        cc /= (v1v2[0] * v1v2[0] + v1v2[1] * v1v2[1] + v1v2[2] * v1v2[2]);
+        for (int c = 0; c < 3; ++c) p3[c] = p0[c] + cc * cp3p0[c];
+    }
+    double r[3];
+    for (int c = 0; c < 3; ++c) r[c] = p3[c] - p0[c];
+    cross3(r, d, f);
+    const double s = e.torque ? e.F / magnitude3(r) : e.F;
+    for (int c = 0; c < 3; ++c) f[c] = s * f[c];
+}
+
+__global__ void __launch_bounds__(128) rot_force_kernel(RotArgs g);
+
 // every midpoint's force of the step (midpoint_force) once, for the vertices' linearise replay to read
 template <class R>
 __global__ void __launch_bounds__(256) mid_force_kernel(NodeForces sn, int M, R *out, const DevStatus *st) {

@@ -247,20 +247,27 @@ def write_surface(path: str, faces: np.ndarray) -> None:
         np.savetxt(f, np.asarray(faces, np.int64), fmt="%d")
 
 
-def write_ctforces(path: str, linear=(), surface=()) -> None:
+def write_ctforces(path: str, linear=(), surface=(), rotational=()) -> None:
     """An FFEA constant-forces file (Blob::load_ctforces, src/Blob.cpp:2478-2805).
 
     ``linear``: (F [N], (dx, dy, dz), blob, conformation, node or "all") per force;
+    ``rotational``: (F [N], type "pf" or "pt", (px, py, pz) [m], (dx, dy, dz), blob, conformation, node or "all");
     ``surface``: (F [N], (dx, dy, dz), blob, conformation, [face indices]) per set of faces."""
-    lines = ["ffea ctforces file", f"num_ctforces {len(linear) + len(surface)}"]
+    lines = ["ffea ctforces file", f"num_ctforces {len(linear) + len(rotational) + len(surface)}"]
     if linear:
         lines.append(f"num_linear_forces {len(linear)}")
+    if rotational:
+        lines.append(f"num_rot_forces {len(rotational)}")
     if surface:
         lines.append(f"num_linear_surface_forces {len(surface)}")
     if linear:
         lines.append("linear forces:")
         for F, d, b, c, n in linear:
             lines.append(f"{F!r} {d[0]!r} {d[1]!r} {d[2]!r} {b} {c} {n}")
+    if rotational:
+        lines.append("rotational forces:")
+        for F, t, pt, d, b, c, n in rotational:
+            lines.append(f"{F!r} {t} {pt[0]!r} {pt[1]!r} {pt[2]!r} {d[0]!r} {d[1]!r} {d[2]!r} {b} {c} {n}")
     if surface:
         lines.append("linear surface forces:")
         for F, d, b, c, fs in surface:

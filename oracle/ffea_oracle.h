@@ -120,6 +120,13 @@ void orc_blob_measure(const orc_blob *b, double *strain_energy, double *kinetic_
 int orc_blob_set_ctforces(orc_blob *b, int n_lin, const int *lin_node, const double *lin_fd, int n_sets,
                           const int *set_size, const int *set_faces, const double *set_fd, int n_faces,
                           const int *face_nodes);
+/*
+ * Rotational constant forces (CTF 2) of this blob, after orc_blob_set_ctforces, in file order ("all" expanded):
+ * node rot_node[i], type rot_torque[i] (0: "pf", 1: "pt"), rot_fpd[7i..7i+6] = (F [N], px, py, pz [m], dx, dy, dz).
+ * Returns ORC_OK, or ORC_EINPUT for a node out of range or a zero axis.
+ */
+int orc_blob_set_rot_ctforces(orc_blob *b, int n_rot, const int *rot_node, const int *rot_torque,
+                              const double *rot_fpd);
 
 #ifdef __cplusplus
 }

@@ -67,6 +67,10 @@ struct orc_blob {
     int n_lctf, n_sets, n_faces;
     int *lctf_node, *set_size, *set_faces, *face_nodes;
     double *lctf_f, *set_f, *face_f, *face_area;
+    /* rotational constant forces: ctf_r_nodes, ctf_r_forces, ctf_r_axis (point, direction), ctf_r_type */
+    int n_rctf;
+    int *rctf_node, *rctf_torque;
+    double *rctf_f, *rctf_axis;
 };
 
 static void *xcalloc(size_t n, size_t sz) { return calloc(n ? n : 1, sz ? sz : 1); }
@@ -216,10 +220,51 @@ static double face_get_area(const orc_blob *b, int f) {
     return .5 * sqrt(r);
 }
 
-/* Blob::apply_ctforces, src/Blob.cpp:1676-1741 (CTF 1 and CTF 3; rotational forces are not loaded) */
+/* arr3arr3VectorProduct, include/mat_vec_fns_II.h:369-373 */
+static void cross3(const double *u, const double *v, double *w) {
+    w[0] = u[1] * v[2] - v[1] * u[2];
+    w[1] = -u[0] * v[2] + v[0] * u[2];
+    w[2] = u[0] * v[1] - v[0] * u[1];
+}
+
+/* magnitude, include/mat_vec_fns_II.h:326-333, in the order GCC builds its two-lane `omp simd` sum */
+static double magnitude3(const double *a) { return sqrt((a[0] * a[0] + a[2] * a[2]) + a[1] * a[1]); }
+
+/* CTF 2 of Blob::apply_ctforces (src/Blob.cpp:1684-1720) for one entry at node position p0:
+ * intersectingPointToLine (include/mat_vec_fns_II.h:755-777), r = p3 - p0, f = r x d, scaled by F or F/|r| */
+static void rot_force(const double *axis, double F, int torque, const double *p0, double *f) {
+    const double *p1 = axis, *d = axis + 3;
+    double p0p1[3], v2[3], p3[3], r[3];
+    for (int c = 0; c < 3; ++c) p0p1[c] = p0[c] - p1[c];
+    cross3(p0p1, d, v2);
+    if (magnitude3(v2) < 3.0 * 2.220446049250313080847e-16) {
+        for (int c = 0; c < 3; ++c) p3[c] = p0[c];
+    } else {
+        double cp3p0[3], v1v2[3], cc;
+        cross3(d, v2, cp3p0);
+        cross3(d, cp3p0, v1v2);
+        cc = p0p1[0] * (d[1] * v1v2[2] - d[2] * v1v2[1]); /* detByRows, :379-385 */
+        cc += p0p1[1] * (d[2] * v1v2[0] - d[0] * v1v2[2]);
+        cc += p0p1[2] * (d[0] * v1v2[1] - d[1] * v1v2[0]);
+        cc /= (v1v2[0] * v1v2[0] + v1v2[1] * v1v2[1] + v1v2[2] * v1v2[2]);
+        for (int c = 0; c < 3; ++c) p3[c] = p0[c] + cc * cp3p0[c];
+    }
+    for (int c = 0; c < 3; ++c) r[c] = p3[c] - p0[c];
+    cross3(r, d, f);
+    const double s = torque ? F / magnitude3(r) : F;
+    for (int c = 0; c < 3; ++c) f[c] = s * f[c];
+}
+
+/* Blob::apply_ctforces, src/Blob.cpp:1676-1741 (CTF 1, CTF 2 about axes through a point, CTF 3) */
 static void apply_ctforces(orc_blob *b) {
     for (int i = 0; i < b->n_lctf; ++i)
         for (int c = 0; c < 3; ++c) b->force[3 * (size_t)b->lctf_node[i] + c] += b->lctf_f[3 * i + c];
+    for (int i = 0; i < b->n_rctf; ++i) {
+        double f[3];
+        const int n = b->rctf_node[i];
+        rot_force(b->rctf_axis + 6 * i, b->rctf_f[i], b->rctf_torque[i], b->pos + 3 * (size_t)n, f);
+        for (int c = 0; c < 3; ++c) b->force[3 * (size_t)n + c] += f[c];
+    }
     int aux = 0;
     for (int s = 0; s < b->n_sets; ++s) {
         double total = 0;
@@ -1028,7 +1073,8 @@ void orc_blob_destroy(orc_blob *b) {
                     b->visc, b->node_force, b->F, b->stress_mag, b->cptr, b->contrib, b->contrib_es, b->key,
                     b->entry, b->sptr, b->src, b->diag, b->precond, b->r, b->p, b->z, b->q, b->f, b->work_in,
                     b->work_out, b->mkey, b->mentry, b->d, b->s, b->inv_m, b->rng, b->lctf_node, b->set_size,
-                    b->set_faces, b->face_nodes, b->lctf_f, b->set_f, b->face_f, b->face_area};
+                    b->set_faces, b->face_nodes, b->lctf_f, b->set_f, b->face_f, b->face_area, b->rctf_node,
+                    b->rctf_torque, b->rctf_f, b->rctf_axis};
     for (size_t i = 0; i < sizeof(ptrs) / sizeof(ptrs[0]); ++i) free(ptrs[i]);
     free(b);
 }
@@ -1189,5 +1235,32 @@ int orc_blob_set_ctforces(orc_blob *b, int n_lin, const int *lin_node, const dou
     }
     if (tot) memcpy(b->set_faces, set_faces, sizeof(int) * tot);
     if (n_faces) memcpy(b->face_nodes, face_nodes, sizeof(int) * 3 * (size_t)n_faces);
+    return ORC_OK;
+}
+
+int orc_blob_set_rot_ctforces(orc_blob *b, int n_rot, const int *rot_node, const int *rot_torque,
+                              const double *rot_fpd) {
+    for (int i = 0; i < n_rot; ++i)
+        if (rot_node[i] < 0 || rot_node[i] >= b->n) return ORC_EINPUT;
+    free(b->rctf_node); free(b->rctf_torque); free(b->rctf_f); free(b->rctf_axis);
+    b->n_rctf = n_rot;
+    b->rctf_node = xcalloc(n_rot, sizeof(int));
+    b->rctf_torque = xcalloc(n_rot, sizeof(int));
+    b->rctf_f = xcalloc(n_rot, sizeof(double));
+    b->rctf_axis = xcalloc(6 * (size_t)n_rot, sizeof(double));
+    for (int i = 0; i < n_rot; ++i) {
+        const double *q = rot_fpd + 7 * i;
+        double sum = 0; /* normalize(ctf_d), include/mat_vec_fns_II.h:188-198 */
+        for (int c = 0; c < 3; ++c) sum += q[4 + c] * q[4 + c];
+        if (sum == 0) return ORC_EINPUT;
+        sum = sqrt(sum);
+        b->rctf_node[i] = rot_node[i];
+        b->rctf_torque[i] = rot_torque[i];
+        b->rctf_f[i] = q[0] * (1. / MESO_FORCE); /* F * mdfm1, src/Blob.cpp:2675 */
+        for (int c = 0; c < 3; ++c) {
+            b->rctf_axis[6 * i + c] = (1. / MESO_LENGTH) * q[1 + c]; /* resize(mdlm1, ctf_p) */
+            b->rctf_axis[6 * i + 3 + c] = q[4 + c] / sum;
+        }
+    }
     return ORC_OK;
 }

@@ -83,6 +83,7 @@ def port_lib(fast: bool = False):
         "blob_set_rng_state": [C.c_void_p, C.c_int, _up],
         "blob_measure": [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double)],
         "blob_set_ctforces": [C.c_void_p, C.c_int, _ip, _dp, C.c_int, _ip, _ip, _dp, C.c_int, _ip],
+        "blob_set_rot_ctforces": [C.c_void_p, C.c_int, _ip, _ip, _dp],
     }.items():
         getattr(lib, P + name).argtypes = args
     lib.orc_blob_total_cg_iters.argtypes = [C.c_void_p]
@@ -142,6 +143,7 @@ def ref_lib():
         "blob_get_rng_state": [C.c_void_p, C.c_int, _up],
         "blob_measure": [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double)],
         "blob_set_ctforces": [C.c_void_p, C.c_int, _ip, _dp, C.c_int, _ip, _ip, _dp, C.c_int, _ip],
+        "blob_set_rot_ctforces": [C.c_void_p, C.c_int, _ip, _ip, _dp],
     }.items():
         getattr(lib, "ref_" + name).argtypes = args
     lib._typed = True
@@ -243,13 +245,20 @@ class _BlobBase:
             i32(np.ascontiguousarray(arg).ravel()))
         if st != 0:
             raise ValueError(f"set_ctforces failed (status {st})")
+        n_rot = len(ctf.get("rot_node", []))
+        st = self._f("blob_set_rot_ctforces")(self._h, n_rot, i32(ctf.get("rot_node", [])),
+                                               i32(ctf.get("rot_torque", [])),
+                                               np.ascontiguousarray(ctf["rot_fpd"], np.float64).ravel()
+                                               if n_rot else np.zeros(7))
+        if st != 0:
+            raise ValueError(f"set_rot_ctforces failed (status {st})")
 
 
 def read_ctforces(path: str, blob_index: int, n_nodes: int) -> dict:
     """The entries of one blob (conformation 0) of a constant-forces file, as Blob::load_ctforces
     (src/Blob.cpp:2478-2805) selects them: linear forces in file order with "all" expanded over the
-    nodes, and the linear surface-force sets. Forces stay as (F [N], dx, dy, dz); rotational forces
-    are rejected."""
+    nodes, rotational forces (type, then (F [N], axis point [m], axis direction)) the same way, and the
+    linear surface-force sets. Forces stay as read: (F [N], dx, dy, dz)."""
     lines = []
     for ln in open(path).read().split("\n"):
         ln = ln.strip()
@@ -275,10 +284,21 @@ def read_ctforces(path: str, blob_index: int, n_nodes: int) -> dict:
             out["lin_node"].append(n)
             out["lin_fd"].append(fd)
     at += nl
+    rot = {"rot_node": [], "rot_torque": [], "rot_fpd": []}
     if nr:
         at += 1
-        if any(int(ln.split()[8]) == blob_index for ln in lines[at:at + nr]):
-            raise ValueError("rotational constant forces are not restated")
+        for ln in lines[at:at + nr]:
+            w = ln.split()
+            if int(w[8]) != blob_index or int(w[9]) != 0:
+                continue
+            if w[1][0] != "p" or w[1][1] not in "ft":
+                raise ValueError("only rotational forces about an axis through a point are applied")
+            fpd = [float(w[0])] + [float(x) for x in w[2:8]]
+            nodes = range(n_nodes) if w[10] == "all" else [int(w[10])]
+            for n in nodes:
+                rot["rot_node"].append(n)
+                rot["rot_torque"].append(1 if w[1][1] == "t" else 0)
+                rot["rot_fpd"].append(fpd)
         at += nr
     if ns:
         at += 1
@@ -291,7 +311,9 @@ def read_ctforces(path: str, blob_index: int, n_nodes: int) -> dict:
             out["set_faces"].extend(int(x) for x in w[6:])
     return {"lin_node": np.array(out["lin_node"], np.int32), "lin_fd": np.array(out["lin_fd"], np.float64),
             "set_size": np.array(out["set_size"], np.int32), "set_faces": np.array(out["set_faces"], np.int32),
-            "set_fd": np.array(out["set_fd"], np.float64)}
+            "set_fd": np.array(out["set_fd"], np.float64),
+            "rot_node": np.array(rot["rot_node"], np.int32), "rot_torque": np.array(rot["rot_torque"], np.int32),
+            "rot_fpd": np.array(rot["rot_fpd"], np.float64).reshape(-1, 7)}
 
 
 def read_surface(path: str) -> np.ndarray:

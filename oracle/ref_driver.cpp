@@ -70,9 +70,10 @@ struct RefBlob {
     int nthreads = 1;
     // constant forces: Blob's ctf_* members and its surface (include/Blob.h)
     std::vector<Face> surface;
-    int num_l_ctf = 0, num_slsets_ctf = 0;
-    std::vector<int> ctf_l_nodes, ctf_sl_faces, ctf_sl_surfsize;
-    std::vector<scalar> ctf_l_forces, ctf_sl_forces;
+    int num_l_ctf = 0, num_r_ctf = 0, num_slsets_ctf = 0;
+    std::vector<int> ctf_l_nodes, ctf_r_nodes, ctf_sl_faces, ctf_sl_surfsize;
+    std::vector<scalar> ctf_l_forces, ctf_r_forces, ctf_r_axis, ctf_sl_forces;
+    std::vector<char> ctf_r_type;
 };
 }  // namespace
 
@@ -173,6 +174,35 @@ void *ref_blob_create(int n_nodes, const double *pos, double scale_m, int n_elem
 
 void ref_blob_destroy(void *h) { delete static_cast<RefBlob *>(h); }
 
+/* the same arguments as orc_blob_set_rot_ctforces; stored as the storing half of load_ctforces does
+ * (src/Blob.cpp:2668-2730) */
+int ref_blob_set_rot_ctforces(void *h, int n_rot, const int *rot_node, const int *rot_torque, const double *rot_fpd) {
+    RefBlob *b = static_cast<RefBlob *>(h);
+    try {
+        const scalar mdfm1 = 1. / mesoDimensions::force, mdlm1 = 1. / mesoDimensions::length;
+        b->num_r_ctf = n_rot;
+        b->ctf_r_nodes.assign(rot_node, rot_node + n_rot);
+        b->ctf_r_forces.assign(n_rot, 0.0);
+        b->ctf_r_axis.assign(6 * (size_t)n_rot, 0.0);
+        b->ctf_r_type.assign(2 * (size_t)n_rot, 'p');
+        for (int i = 0; i < n_rot; ++i) {
+            const double *q = rot_fpd + 7 * i;
+            arr3 p = {q[1], q[2], q[3]}, d = {q[4], q[5], q[6]};
+            normalize(d);
+            resize(mdlm1, p);
+            b->ctf_r_forces[i] = q[0] * mdfm1;
+            for (int c = 0; c < 3; ++c) {
+                b->ctf_r_axis[6 * i + c] = p[c];
+                b->ctf_r_axis[6 * i + 3 + c] = d[c];
+            }
+            b->ctf_r_type[2 * i + 1] = rot_torque[i] ? 't' : 'f';
+        }
+    } catch (FFEAException &) {
+        return 3;
+    }
+    return 0;
+}
+
 /* the same arguments as orc_blob_set_ctforces, plus the element of each face (face4: element, n0, n1, n2) */
 int ref_blob_set_ctforces(void *h, int n_lin, const int *lin_node, const double *lin_fd, int n_sets,
                           const int *set_size, const int *set_faces, const double *set_fd, int n_faces,
@@ -220,6 +250,23 @@ static void apply_ctforces(RefBlob *b) {
         force[b->ctf_l_nodes[i]][0] += b->ctf_l_forces[3 * i];
         force[b->ctf_l_nodes[i]][1] += b->ctf_l_forces[3 * i + 1];
         force[b->ctf_l_nodes[i]][2] += b->ctf_l_forces[3 * i + 2];
+    }
+    for (int i = 0; i < b->num_r_ctf; i++) {  // CTF 2, axes through a point ('p')
+        arr3 r, f;
+        mesh_node &nd = b->node[b->ctf_r_nodes[i]];
+        intersectingPointToLine(nd.pos, arr_view<scalar, 3>(b->ctf_r_axis, 6 * i),
+                                arr_view<scalar, 3>(b->ctf_r_axis, 6 * i + 3), r);
+        sub(r, nd.pos, r);
+        arr3arr3VectorProduct(r, arr_view<scalar, 3>(b->ctf_r_axis, 6 * i + 3), f);
+        if (b->ctf_r_type[2 * i + 1] == 'f') {
+            resize(b->ctf_r_forces[i], f);
+        } else if (b->ctf_r_type[2 * i + 1] == 't') {
+            const scalar rsize = magnitude(r);
+            resize(b->ctf_r_forces[i] / rsize, f);
+        }
+        force[b->ctf_r_nodes[i]][0] += f[0];
+        force[b->ctf_r_nodes[i]][1] += f[1];
+        force[b->ctf_r_nodes[i]][2] += f[2];
     }
     int auxndx = 0;
     std::vector<scalar> faceAreas;

@@ -71,10 +71,12 @@ def gen_rng():
 
 
 def ctf_case(m, directory, name="ctf"):
-    """Constant-force inputs for a Kuhn cube of side 20 (file units): linear forces on a vertex (twice),
-    on a midpoint and on every node; two sets of surface faces, the top face z = 20 and half of the x = 0
-    face together with three top faces (so three faces carry both sets). Writes ``name``.ctforces and
-    ``name``.surf into ``directory`` and returns their paths."""
+    """Constant-force inputs for a Kuhn cube of side 20 (file units, scale 1e-9 m): linear forces on a vertex
+    (twice), on a midpoint and on every node; rotational forces about the cube's vertical axis ("pf" on a
+    vertex and on every node, "pt" on the same vertex) and about an oblique axis ("pt" on a midpoint); two sets
+    of surface faces, the top face z = 20 and half of the x = 0 face together with three top faces (so three
+    faces carry both sets). Writes ``name``.ctforces and ``name``.surf into ``directory`` and returns their
+    paths."""
     faces = surface_faces(m)
     top = faces_on_plane(m, faces, 2, 20.0)
     side = faces_on_plane(m, faces, 0, 0.0)
@@ -84,6 +86,11 @@ def ctf_case(m, directory, name="ctf"):
     write_ctforces(ctf, linear=[(2e-12, (1.0, 2.0, 3.0), 0, 0, 9), (5e-12, (0.0, 0.0, -1.0), 0, 0, m.n_linear + 7),
                                 (3e-13, (1.0, 0.0, 0.0), 0, 0, "all"), (1e-12, (-1.0, 0.5, 0.0), 0, 0, 9),
                                 (4e-12, (0.0, 1.0, 0.0), 1, 0, 3)],
+                   rotational=[(3e-14, "pf", (1e-8, 1e-8, 0.0), (0.0, 0.0, 2.0), 0, 0, 22),
+                               (1e-12, "pt", (0.0, 0.0, 0.0), (1.0, 1.0, 0.0), 0, 0, m.n_linear + 11),
+                               (2e-14, "pf", (1e-8, 1e-8, 0.0), (0.0, 0.0, 1.0), 0, 0, "all"),
+                               (5e-13, "pt", (1e-8, 1e-8, 0.0), (0.0, 0.0, 1.0), 0, 0, 22),
+                               (1e-12, "pt", (0.0, 0.0, 0.0), (0.0, 1.0, 0.0), 1, 0, 5)],
                    surface=[(2e-11, (0.0, 0.0, 1.0), 0, 0, top),
                             (1e-11, (0.3, -1.0, 0.2), 0, 0, np.concatenate([side[: len(side) // 2], top[:3]])),
                             (1e-11, (1.0, 0.0, 0.0), 1, 0, top)])

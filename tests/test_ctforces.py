@@ -1,9 +1,10 @@
 """Constant forces (Blob::load_ctforces / apply_ctforces, src/Blob.cpp:1676-1741, 2478-2805) on the GPU.
 
 * Against the reference: tests/golden/cube3_*_ctf*.npz come from the reference's own Face and element
-  classes driven through the reference's apply_ctforces order (oracle/ref_driver.cpp), on a Kuhn cube
-  with pins, Stokes drag and noise, linear forces on a vertex (twice), a midpoint and every node, and
-  two overlapping sets of surface faces. Tolerances as the other FP64 parity tests: right-hand side and
+  classes and its intersectingPointToLine, driven through the reference's apply_ctforces order
+  (oracle/ref_driver.cpp), on a Kuhn cube with pins, Stokes drag and noise, linear forces on a vertex
+  (twice), a midpoint and every node, rotational forces ("pf" and "pt", on vertices, a midpoint and every
+  node), and two overlapping sets of surface faces. Tolerances as the other FP64 parity tests: right-hand side and
   RNG state bit-exact; positions bit-exact for the mass-lumped solver, else within 1e-8 of the
   displacement (CG reductions in another order).
 * Mixed precision against FP64 on the same inputs: within 1e-5 of the displacement.
@@ -107,11 +108,10 @@ def test_constant_force_input_errors(gpu, tmp_path):
         b.load_ctforces(path, None, 0)                                   # surface forces need the surface
     expect(False, surface=[(1e-11, (0.0, 0.0, 1.0), 0, 0, [faces.shape[0]])])  # face out of range
     expect(True, surface=[(1e-11, (0.0, 0.0, 1.0), 0, 0, [0, 1])])
-    with open(path, "w") as f:  # a rotational force on this blob
-        f.write("ffea ctforces file\nnum_ctforces 1\nnum_rot_forces 1\nrotational forces:\n"
-                "1e-12 0 0 0 0 0 1 pf 0 0 5\n")
-    with pytest.raises(lib.FFEAError):
-        b.load_ctforces(path, None, 0)
+    expect(True, rotational=[(1e-12, "pt", (0.0, 0.0, 0.0), (0.0, 0.0, 1.0), 0, 0, 5)])
+    expect(False, rotational=[(1e-12, "nt", (0.0, 0.0, 0.0), (0.0, 0.0, 1.0), 0, 0, 5)])  # axis between nodes
+    expect(False, rotational=[(1e-12, "px", (0.0, 0.0, 0.0), (0.0, 0.0, 1.0), 0, 0, 5)])  # neither f nor t
+    expect(False, rotational=[(1e-12, "pf", (0.0, 0.0, 0.0), (0.0, 0.0, 0.0), 0, 0, 5)])  # zero axis
     with open(path, "w") as f:  # header count disagrees with the lines
         f.write("ffea ctforces file\nnum_ctforces 2\nnum_linear_forces 1\nlinear forces:\n1e-12 1 0 0 0 0 3\n")
     with pytest.raises(lib.FFEAError):
