@@ -114,11 +114,6 @@ struct ffea_gpu_batch {
         CK(cudaStreamSynchronize(stream));
         return FFEA_GPU_OK;
     }
-    // the rigid modes of blob b after its host positions changed (they must vanish at its pinned nodes)
-    void refresh_modes(int b) {
-        BlobCgDesc &d = hdesc[b];
-        d.nmodes = rigid_modes(h, p, d.xc, d.modes, d.row0, d.nrows);
-    }
 };
 
 namespace {
@@ -640,9 +635,20 @@ static int batch_set_range(ffea_gpu_batch *bt, int b0, int b1, const double *pos
     if (pos && (rc = put(pos, bt->px, bt->py, bt->pz))) return rc;
     if (vel && (rc = put(vel, bt->vx, bt->vy, bt->vz))) return rc;
     if (pos) {
-        for (int k = r0; k < r0 + nr; ++k)
-            for (int c = 0; c < 3; ++c) h.pos[3 * (size_t)k + c] = pos[3 * (size_t)(h.node_of[k] - n0) + c];
-        for (int b = b0; b < b1; ++b) bt->refresh_modes(b);
+        // each blob's centroid in one pass over its vertex rows; the host copy of the positions is kept for the
+        // pinned rows only (all the rigid modes need)
+        for (int b = b0; b < b1; ++b) {
+            BlobCgDesc &d = bt->hdesc[b];
+            double sum[3] = {0.0, 0.0, 0.0};
+            for (int k = d.row0; k < d.row0 + d.nrows; ++k) {
+                const double *q = pos + 3 * (size_t)(h.node_of[k] - n0);
+                sum[0] += q[0]; sum[1] += q[1]; sum[2] += q[2];
+                if (h.pinned[k])
+                    for (int c = 0; c < 3; ++c) h.pos[3 * (size_t)k + c] = q[c];
+            }
+            for (int c = 0; c < 3; ++c) d.xc[c] = sum[c] / std::max(d.nrows, 1);
+            d.nmodes = rigid_modes_about(h, bt->p, d.xc, d.modes, d.row0, d.nrows);
+        }
         return bt->upload_desc(b1 - b0 == 1 ? b0 : -1);
     }
     return FFEA_GPU_OK;

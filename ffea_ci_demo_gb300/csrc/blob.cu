@@ -683,10 +683,17 @@ struct BlobImpl final : ffea_gpu_blob {
         if (pos && (rc = put(pos, px, py, pz))) return rc;
         if (vel && (rc = put(vel, vx, vy, vz))) return rc;
         if (pos) {
-            // the rigid modes must vanish at the pinned nodes' current positions
-            for (int k = 0; k < N; ++k)
-                for (int c = 0; c < 3; ++c) h.pos[3 * (size_t)k + c] = pos[3 * (size_t)h.node_of[k] + c];
-            nmodes = rigid_modes(h, p, xc, modes);
+            // the rigid modes must vanish at the pinned nodes' current positions, about the new centroid (one
+            // pass over the vertex rows; the host copy of the positions is kept for the pinned rows only)
+            double s[3] = {0.0, 0.0, 0.0};
+            for (int k = 0; k < N; ++k) {
+                const double *q = pos + 3 * (size_t)h.node_of[k];
+                s[0] += q[0]; s[1] += q[1]; s[2] += q[2];
+                if (h.pinned[k])
+                    for (int c = 0; c < 3; ++c) h.pos[3 * (size_t)k + c] = q[c];
+            }
+            for (int c = 0; c < 3; ++c) xc[c] = s[c] / std::max(N, 1);
+            nmodes = rigid_modes_about(h, p, xc, modes, 0, N);
         }
         return FFEA_GPU_OK;
     }

@@ -451,6 +451,12 @@ std::vector<R> cast_vec(const std::vector<double> &v) {
 // space of the viscosity matrix when there is no Stokes drag (mixed-path CG deflation). Returns the
 // mode coefficients (t, omega) row-wise in modes[6*k..6*k+5].
 // Vertex rows [row0, row0 + nrows) (default: all) are one blob of a batch.
+// the rigid modes about a given reference point xc (see rigid_modes); reads only the pinned rows' positions
+inline int rigid_modes_about(const HostModel &h, const ffea_gpu_params &p, const double xc[3], double modes[36],
+                             int row0, int nrows);
+
+// The rigid-body modes the mixed CG deflates, about the centroid xc of rows [row0, row0 + nrows): all six
+// without pins, those that keep every pinned vertex at rest with pins, none with Stokes drag.
 inline int rigid_modes(const HostModel &h, const ffea_gpu_params &p, double xc[3], double modes[36], int row0 = 0,
                        int nrows = -1) {
     if (nrows < 0) nrows = h.N - row0;
@@ -459,6 +465,13 @@ inline int rigid_modes(const HostModel &h, const ffea_gpu_params &p, double xc[3
     for (int a = row0; a < row1; ++a)
         for (int c = 0; c < 3; ++c) xc[c] += h.pos[3 * (size_t)a + c];
     for (int c = 0; c < 3; ++c) xc[c] /= std::max(nrows, 1);
+    return rigid_modes_about(h, p, xc, modes, row0, nrows);
+}
+
+inline int rigid_modes_about(const HostModel &h, const ffea_gpu_params &p, const double xc[3], double modes[36],
+                             int row0, int nrows) {
+    if (nrows < 0) nrows = h.N - row0;
+    const int row1 = row0 + nrows;
     if (p.calc_stokes == 1) return 0;
     // M = sum over pinned vertices of C^T C, C = [I | -[d]x]
     double M[6][6] = {};
