@@ -145,6 +145,10 @@ __global__ void __launch_bounds__(SOLVE_PREP_THREADS)
 
 namespace {
 
+// FP32 matrix bytes up to which the mixed CG_nomass matrix is taken to stay in the GPU's L2 (129 MB, shared with
+// the vectors and the exchange buffers)
+constexpr double L2_MATRIX_BYTES = 64e6;
+
 template <class R>
 struct BlobImpl final : ffea_gpu_blob {
     Arena mem;
@@ -172,6 +176,8 @@ struct BlobImpl final : ffea_gpu_blob {
     int cg_npb = 0;  // rows per block of the owned-rows CG kernels (0: cg_kernel / cg_mixed_kernel)
     int cg_block = 1024;  // threads per CG block
     bool cg_sr = false;   // the mixed CG_nomass solve uses cg_mixed_sr_kernel
+    int cg_poly = 0;      // with a Chebyshev preconditioner of this degree (0: Jacobi)
+    double *cheb = nullptr;  // its lambda_max estimate and the Lanczos record that makes it (CHEB_STATE)
     int *nb_ptr = nullptr, *nb_list = nullptr;  // its blocks' neighbour blocks
     unsigned int *nb_flags = nullptr;           // and their publication counters
     float4 *dpos = nullptr;  // mixed path: node offsets from the reference point
@@ -363,17 +369,33 @@ struct BlobImpl final : ffea_gpu_blob {
         // each block keeps a run of rows in shared memory when they fit (FFEA_GPU_CG_OWN=0 turns this off);
         // the run is a multiple of a warp's rows so that a warp's rows share a SELL slice
         // the mixed CG_nomass solve takes one reduction per iteration (cg_mixed_sr_kernel) when its rows fit
-        // (FFEA_GPU_CG_SR=0 keeps the two-reduction kernel)
+        // (FFEA_GPU_CG_SR=0 keeps the two-reduction kernel, FFEA_GPU_CG_SR=1 takes it whatever the matrix size)
         {
             const char *own = getenv("FFEA_GPU_CG_OWN"), *sr = getenv("FFEA_GPU_CG_SR");
             const int maxrows = (own && own[0] == '0') ? 0 : Launch<R>::cg_own_max_rows(device);
             const int align = 32 / tpn, rows = (N + cg_grid - 1) / cg_grid;
             const int npb = (rows + align - 1) / align * align;
             cg_npb = (maxrows > 0 && npb <= maxrows) ? npb : 0;
-            if (mixed && p.solver == FFEA_GPU_NOMASS_CG && !(sr && sr[0] == '0') && !(own && own[0] == '0')) {
-                const int srrows = Launch<R>::cg_sr_max_rows(device);
-                cg_sr = srrows > 0 && npb <= srrows;
+            // ... while its FP32 matrix (40 B per 3x3 block) stays in L2: once the SpMV streams the matrix from HBM
+            // the two-reduction kernel's iterations are the shorter ones (64^3 cells: 38.7 against 43.5 us)
+            const bool l2_resident = 40.0 * (double)h.nslots <= L2_MATRIX_BYTES;
+            if (mixed && p.solver == FFEA_GPU_NOMASS_CG && !(sr && sr[0] == '0') && !(own && own[0] == '0') &&
+                (l2_resident || (sr && sr[0] == '1'))) {
+                // the polynomial preconditioner's two extra vectors per row must fit as well; else Jacobi
+                const int poly = p.cg_poly == 0 ? FFEA_GPU_CG_POLY_DEFAULT : std::max(p.cg_poly, 0);
+                for (int deg : {poly, 0}) {
+                    const int srrows = Launch<R>::cg_sr_max_rows(device, deg);
+                    if (srrows > 0 && npb <= srrows) {
+                        cg_sr = true;
+                        cg_poly = deg;
+                        break;
+                    }
+                }
                 if (cg_sr) cg_npb = npb;
+            }
+            if (cg_poly > 0) {
+                CK(mem.alloc(&cheb, (size_t)CHEB_STATE));
+                CK(cudaMemset(cheb, 0, CHEB_STATE * sizeof(double)));
             }
             if (cg_sr) {
                 // the blocks each block's SpMV reads z from: owners of the columns of its rows
@@ -503,6 +525,14 @@ struct BlobImpl final : ffea_gpu_blob {
         for (int i = 0; i < 36; ++i) ca.modes[i] = modes[i];
         ca.npb = cg_npb;
         ca.sr = cg_sr && nomass;
+        ca.poly = ca.sr ? cg_poly : 0;
+        ca.cheb = cheb;
+        // a Chebyshev step (SpMV + neighbour exchange) against a whole iteration (SpMV, exchange, grid-wide
+        // reduction): about half while the FP32 matrix (40 B per 3x3 block) stays in L2, more once it streams
+        // from HBM
+        // (FFEA_GPU_CHEB_COST overrides it, for comparison runs)
+        ca.cheb_cost = 40.0 * (double)h.nslots <= L2_MATRIX_BYTES ? 0.5f : 0.9f;
+        if (const char *cc = getenv("FFEA_GPU_CHEB_COST")) ca.cheb_cost = (float)atof(cc);
         if (nb_flags) {
             ca.nb_ptr = nb_ptr; ca.nb_list = nb_list; ca.flags = nb_flags;
             CK(cudaMemsetAsync(nb_flags, 0, (size_t)FLAG_STRIDE * cg_grid * sizeof(unsigned int), stream));
@@ -760,6 +790,17 @@ struct BlobImpl final : ffea_gpu_blob {
         CK(cudaMemcpyAsync(t, phase_ns, sizeof t, cudaMemcpyDeviceToHost, stream));
         CK(cudaStreamSynchronize(stream));
         for (int k = 0; k < n && k < FFEA_GPU_CG_PHASES; ++k) ns[k] = (double)t[k];
+        return FFEA_GPU_OK;
+    }
+
+    int cg_preconditioner(int *degree, double *lambda_max) override {
+        double c = 0.0;
+        if (cheb) {
+            CK(cudaMemcpyAsync(&c, cheb, sizeof(double), cudaMemcpyDeviceToHost, stream));
+            CK(cudaStreamSynchronize(stream));
+        }
+        if (degree) *degree = c > 0.0 ? cg_poly : 0;
+        if (lambda_max) *lambda_max = c > 0.0 ? c : 0.0;
         return FFEA_GPU_OK;
     }
 
@@ -1343,7 +1384,8 @@ struct BlobImpl final : ffea_gpu_blob {
 int check_params(const ffea_gpu_params *p) {
     if (!p) return FFEA_GPU_EINPUT;
     if (p->solver < 0 || p->solver > 2 || (p->precision != FFEA_GPU_FP64 && p->precision != FFEA_GPU_MIXED) ||
-        p->max_iterations_cg < 0 || !(p->dt > 0)) {
+        p->max_iterations_cg < 0 || !(p->dt > 0) ||
+        (p->cg_poly != -1 && p->cg_poly != 0 && p->cg_poly != 2 && p->cg_poly != 4)) {
         g_last_error = "invalid parameters";
         return FFEA_GPU_EINPUT;
     }
@@ -1483,6 +1525,11 @@ int ffea_gpu_blob_cg_profile(ffea_gpu_blob *b, double *ns, int n) {
         return FFEA_GPU_OK;
     }
     return b->cg_profile(ns, n);
+}
+
+int ffea_gpu_blob_cg_preconditioner(ffea_gpu_blob *b, int *degree, double *lambda_max) {
+    if (!b) return FFEA_GPU_EINPUT;
+    return b->cg_preconditioner(degree, lambda_max);
 }
 
 int ffea_gpu_blob_counts(ffea_gpu_blob *b, int *num_nodes, int *num_elements) {

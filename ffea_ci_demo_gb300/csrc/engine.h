@@ -27,8 +27,8 @@ struct Launch {
     // mixed path: the most rows per block cg_mixed_own_kernel can keep in shared memory on `device`
     // (0: not available); a.npb > 0 selects that kernel in cg()
     static int cg_own_max_rows(int device);
-    // the same for cg_mixed_sr_kernel (a.sr selects it); 0 for FP64
-    static int cg_sr_max_rows(int device);
+    // the same for cg_mixed_sr_kernel (a.sr selects it) with a Chebyshev preconditioner of degree poly; 0 for FP64
+    static int cg_sr_max_rows(int device, int poly);
     static cudaError_t euler(const EulerArgs<R> &a, cudaStream_t s);
     // measure_kernel over max(T, N, M) threads in `blocks` blocks, then the final sum into out[6]
     static cudaError_t measure(const MeasureArgs<R> &a, int blocks, double *out, cudaStream_t s);

@@ -26,7 +26,14 @@ cudaError_t Launch<R>::element(const ElemArgs<R> &a, cudaStream_t s) {
 template <class R>
 cudaError_t Launch<R>::assemble(const AsmArgs<R> &a, cudaStream_t s) {
     if (a.N <= 0 || a.nslots <= 0) return cudaSuccess;
-    assemble_kernel<R><<<(unsigned)((a.nslots + ASM_THREADS - 1) / ASM_THREADS), ASM_THREADS, 0, s>>>(a);
+    // three threads per slot while that still fits on the GPU at once (152 SMs x 2048 threads); nslots is a
+    // multiple of 32, so each warp of the split kernel has one block row of 32 slots
+    if (3 * a.nslots <= 152ll * 2048) {
+        const long long threads = 3 * a.nslots;
+        assemble_kernel<R, true><<<(unsigned)((threads + ASM_THREADS - 1) / ASM_THREADS), ASM_THREADS, 0, s>>>(a);
+    } else {
+        assemble_kernel<R, false><<<(unsigned)((a.nslots + ASM_THREADS - 1) / ASM_THREADS), ASM_THREADS, 0, s>>>(a);
+    }
     count_launch();
     return cudaGetLastError();
 }
@@ -94,11 +101,11 @@ int Launch<R>::cg_own_max_rows(int device) {
 }
 
 template <class R>
-int Launch<R>::cg_sr_max_rows(int device) {
+int Launch<R>::cg_sr_max_rows(int device, int poly) {
     if constexpr (std::is_same<R, float>::value)
-        return own_max_rows(cg_mixed_sr_kernel<R>, device, (int)sr_smem_bytes(1));
+        return own_max_rows(cg_mixed_sr_kernel<R>, device, (int)sr_smem_bytes(1, poly));
     else
-        return (void)device, 0;
+        return (void)device, (void)poly, 0;
 }
 
 template <class R>
@@ -111,7 +118,7 @@ cudaError_t Launch<R>::cg(const CgArgs<R> &a, int grid, int threads, cudaStream_
         fn = (const void *)cg_mixed_kernel<R>;
         if (a.npb > 0 && a.sr) {
             fn = (const void *)cg_mixed_sr_kernel<R>;
-            smem = sr_smem_bytes(a.npb);
+            smem = sr_smem_bytes(a.npb, a.poly);
         } else if (a.npb > 0) {
             fn = (const void *)cg_mixed_own_kernel<R>;
             smem = own_smem_bytes(a.npb);

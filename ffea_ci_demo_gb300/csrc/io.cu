@@ -80,6 +80,10 @@ int ffea_gpu_params_assign(ffea_gpu_params *p, const char *key, const char *valu
         if (v == "fp64") p->precision = FFEA_GPU_FP64;
         else if (v == "mixed") p->precision = FFEA_GPU_MIXED;
         else return FFEA_GPU_EINPUT;
+    } else if (k == "cg_poly") {
+        const int v = atoi(value);
+        if (v != -1 && v != 0 && v != 2 && v != 4) return FFEA_GPU_EINPUT;
+        p->cg_poly = v;
     } else {
         return FFEA_GPU_EINPUT;
     }

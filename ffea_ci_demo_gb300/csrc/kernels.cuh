@@ -246,27 +246,34 @@ struct AsmArgs {
 
 constexpr unsigned SRC_IDENTITY = 0xffffffffu;
 
-// One thread per matrix slot (3x3 block): the slot's sources summed from zero in registration order,
-// so each FP64 value rounds as sum_all_sources' does; the diagonal slot of a row also gives the Jacobi
-// inverse. Padding slots past a row's length are never read and are skipped.
-template <class R>
+// The slot's sources are summed from zero in registration order, so each FP64 value rounds as
+// sum_all_sources' does; the diagonal slot of a row also gives the Jacobi inverse. Padding slots past a row's
+// length are never read and are skipped.
+// SPLIT = false: one thread per matrix slot (3x3 block), which reads each source's element geometry once.
+// SPLIT = true: three threads per slot, one per block row (a warp takes one block row of 32 consecutive slots
+// of a slice), for matrices too small to fill the GPU, where the length of each thread's FP64 chain sets the
+// time rather than the geometry reads.
+template <class R, bool SPLIT>
 __global__ void __launch_bounds__(128) assemble_kernel(AsmArgs<R> g) {
+    constexpr int NB = SPLIT ? 1 : 3;  // block rows per thread
     const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (t >= g.nslots || g.st->abort) return;
-    const int s = g.grp_slice[t >> 5];
-    const int lane = (int)(t & 31);
+    const long long slot = SPLIT ? ((t >> 5) / 3) * 32 + (t & 31) : t;
+    const int b0 = SPLIT ? (int)((t >> 5) % 3) : 0;  // first block row
+    if (slot >= g.nslots || g.st->abort) return;
+    const int s = g.grp_slice[slot >> 5];
+    const int lane = (int)(slot & 31);
     const int a = 32 * s + lane;
     if (a >= g.N) return;
-    const int k = (int)((t >> 5) - (g.slice_ptr[s] >> 5));
+    const int k = (int)((slot >> 5) - (g.slice_ptr[s] >> 5));
     if (k >= g.rowlen[a]) return;
-    const long long slot = t;
-    R v[9];
+    R v[3 * NB];
 #pragma unroll
-    for (int c = 0; c < 9; ++c) v[c] = (R)0.0;
+    for (int c = 0; c < 3 * NB; ++c) v[c] = (R)0.0;
     for (int q = g.src_ptr[slot]; q < g.src_ptr[slot + 1]; ++q) {
         const unsigned code = g.src[q];
         if (code == SRC_IDENTITY) {
-            v[0] += (R)1; v[4] += (R)1; v[8] += (R)1;
+#pragma unroll
+            for (int i = 0; i < NB; ++i) v[3 * i + b0 + i] += (R)1;
             continue;
         }
         const int e = (int)(code >> 4), pa = (code >> 2) & 3, pb = code & 3;
@@ -276,24 +283,23 @@ __global__ void __launch_bounds__(128) assemble_kernel(AsmArgs<R> g) {
         for (int m = 0; m < 12; ++m) dpsi[m] = gm[m];
         const R vol = gm[12], A = g.A[e], B = g.B[e];
 #pragma unroll
-        for (int i = 0; i < 3; ++i)
+        for (int i = 0; i < NB; ++i)
 #pragma unroll
-            for (int j = 0; j < 3; ++j) v[3 * i + j] += visc_entry<R>(dpsi, A, B, vol, pa + 4 * i, pb + 4 * j);
+            for (int j = 0; j < 3; ++j) v[3 * i + j] += visc_entry<R>(dpsi, A, B, vol, pa + 4 * (b0 + i), pb + 4 * j);
     }
     if (k == g.diagk[a]) {
-        if (g.drag) {
-            const R dr = (R)g.drag[a];
-            v[0] += dr; v[4] += dr; v[8] += dr;
-        }
-        // calc_inverse_diagonal (src/SparseMatrixFixedPattern.cpp:305-312)
-        g.dinv[4 * a] = (R)1.0 / v[0];
-        g.dinv[4 * a + 1] = (R)1.0 / v[4];
-        g.dinv[4 * a + 2] = (R)1.0 / v[8];
-        if (g.diag) { g.diag[4 * a] = v[0]; g.diag[4 * a + 1] = v[4]; g.diag[4 * a + 2] = v[8]; }
-    }
-    R *vp = g.val + 9 * (size_t)g.slice_ptr[s] + 32 * 9 * (size_t)k + lane;
 #pragma unroll
-    for (int c = 0; c < 9; ++c) vp[32 * c] = v[c];
+        for (int i = 0; i < NB; ++i) {
+            R &d = v[3 * i + b0 + i];
+            if (g.drag) d += (R)g.drag[a];
+            // calc_inverse_diagonal (src/SparseMatrixFixedPattern.cpp:305-312)
+            g.dinv[4 * a + b0 + i] = (R)1.0 / d;
+            if (g.diag) g.diag[4 * a + b0 + i] = d;
+        }
+    }
+    R *vp = g.val + 9 * (size_t)g.slice_ptr[s] + 32 * 9 * (size_t)k + lane + 32 * 3 * b0;
+#pragma unroll
+    for (int c = 0; c < 3 * NB; ++c) vp[32 * c] = v[c];
 }
 
 // ---------------------------------------------------------------------------
@@ -630,6 +636,11 @@ struct CgArgs {
     // one publication counter per block (FLAG_STRIDE words apart, zero at launch)
     const int *nb_ptr, *nb_list;
     unsigned int *flags;
+    // cg_mixed_sr_kernel: degree of the Chebyshev polynomial preconditioner (0: Jacobi alone), its state
+    // (CHEB_STATE doubles, zero at first) and the cost of one Chebyshev step relative to a Jacobi iteration
+    int poly;
+    double *cheb;
+    float cheb_cost;
 };
 
 // p at node b for this iteration: p_new = beta p_old + D^{-1} r (vec3_scale_and_add with the

@@ -45,7 +45,7 @@ class Params(C.Structure):
 
     _fields_ = [("dt", C.c_double), ("kT", C.c_double), ("epsilon2", C.c_double), ("stokes_visc", C.c_double),
                 ("max_iterations_cg", C.c_int), ("calc_noise", C.c_int), ("calc_stokes", C.c_int),
-                ("solver", C.c_int), ("precision", C.c_int), ("reserved", C.c_int)]
+                ("solver", C.c_int), ("precision", C.c_int), ("cg_poly", C.c_int)]
 
 
 class MeshStruct(C.Structure):
@@ -95,6 +95,7 @@ def load():
         "ffea_gpu_blob_counts": (C.c_int, [vp, ip, ip]),
         "ffea_gpu_blob_cg_history": (C.c_int, [vp, dp, C.c_int, ip]),
         "ffea_gpu_blob_cg_profile": (C.c_int, [vp, dp, C.c_int]),
+        "ffea_gpu_blob_cg_preconditioner": (C.c_int, [vp, ip, dp]),
         "ffea_gpu_blob_get_pattern": (C.c_int, [vp, dp, dp, dp, dp, C.POINTER(C.c_longlong)]),
         "ffea_gpu_blob_get_connectivity": (C.c_int, [vp, dp, dp, C.POINTER(C.c_longlong)]),
         "ffea_gpu_blob_get_elements": (C.c_int, [vp, dp, dp, dp]),
@@ -185,8 +186,10 @@ class Blob:
 
     def __init__(self, mesh: Mesh | None = None, *, solver: str = "CG_nomass", precision: str = "fp64",
                  dt: float = 1e-12, kT: float = 4.11e-21, epsilon: float = 1e-10, max_iterations_cg: int = 10000,
-                 calc_noise: int = 1, calc_stokes: int = 0, stokes_visc: float = 1e-3,
+                 calc_noise: int = 1, calc_stokes: int = 0, stokes_visc: float = 1e-3, cg_poly: int = 0,
                  rng_state=(12345,) * 6, _handle=None, _n=None):
+        """cg_poly: preconditioner of the mixed-precision CG_nomass solve (0: default Chebyshev degree 2,
+        -1: Jacobi alone as the reference, 2 or 4: Chebyshev degree); the FP64 path always uses Jacobi."""
         self._lib = load()
         self._h = C.c_void_p()
         if _handle is not None:
@@ -195,7 +198,7 @@ class Blob:
         else:
             params = make_params(solver=solver, precision=precision, dt=dt, kT=kT, epsilon=epsilon,
                                  max_iterations_cg=max_iterations_cg, calc_noise=calc_noise,
-                                 calc_stokes=calc_stokes, stokes_visc=stokes_visc)
+                                 calc_stokes=calc_stokes, stokes_visc=stokes_visc, cg_poly=cg_poly)
             s = mesh.scale / MESO_LENGTH
             self._keep = [np.ascontiguousarray(mesh.pos * s, np.float64),
                           np.ascontiguousarray(mesh.tets, np.int32),
@@ -339,6 +342,12 @@ class Blob:
         buf = np.zeros(len(self.CG_PHASES))
         _check(self._lib.ffea_gpu_blob_cg_profile(self._h, _p(buf), buf.size), "cg_profile")
         return dict(zip(self.CG_PHASES, buf.tolist()))
+
+    def cg_preconditioner(self) -> tuple[int, float]:
+        """(Chebyshev degree of the next CG solve, 0 for Jacobi; its lambda_max(D^-1 V) estimate)."""
+        d, lm = C.c_int(), np.zeros(1)
+        _check(self._lib.ffea_gpu_blob_cg_preconditioner(self._h, C.byref(d), _p(lm)), "cg_preconditioner")
+        return d.value, float(lm[0])
 
     def sizes(self) -> tuple[int, int, int]:
         nl, ne, nb = C.c_int(), C.c_int(), C.c_longlong()

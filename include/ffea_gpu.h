@@ -59,8 +59,15 @@ typedef struct ffea_gpu_params {
     int calc_stokes;  /* 1: Stokes drag 6 pi eta r on every node */
     int solver;       /* FFEA_GPU_NOMASS_CG / FFEA_GPU_CG / FFEA_GPU_MASSLUMPED */
     int precision;    /* FFEA_GPU_FP64 / FFEA_GPU_MIXED */
-    int reserved;
+    /* Preconditioner of the mixed-precision CG_nomass solve (not a reference parameter: the reference and the
+     * FP64 path always precondition with the Jacobi diagonal). 0: the default (FFEA_GPU_CG_POLY_DEFAULT);
+     * -1: Jacobi alone; 2 or 4: a Chebyshev polynomial of that degree in D^-1 V times the Jacobi scaling, which
+     * needs fewer iterations and the same stopping test (|r|^2/|f|^2 < epsilon2). The polynomial applies when
+     * the single-reduction kernel runs (the blob's rows fit in the GPU's shared memory); the blob's first solve
+     * uses Jacobi and estimates the largest eigenvalue of D^-1 V for the later ones. */
+    int cg_poly;
 } ffea_gpu_params;
+#define FFEA_GPU_CG_POLY_DEFAULT 2
 
 /* SimulationParams::SimulationParams() defaults for the hot-path fields
  * (src/SimulationParams.cpp:26-60); solver CG_nomass, precision FP64. */
@@ -171,6 +178,12 @@ int ffea_gpu_blob_cg_history(ffea_gpu_blob *blob, double *res2, int max_entries,
  * (FP64 path only). n_phases is 10. */
 #define FFEA_GPU_CG_PHASES 10
 int ffea_gpu_blob_cg_profile(ffea_gpu_blob *blob, double *phase_ns, int n_phases);
+
+/* The preconditioner the blob's next CG solve uses: *degree is the Chebyshev polynomial's degree (0: Jacobi,
+ * always so on the FP64 path, before the first solve, and when the trial solve found Jacobi cheaper) and
+ * *lambda_max the estimate of the largest eigenvalue of D^-1 V it is built on (0 without one). Each CG
+ * iteration then applies the matrix 1 + degree times. */
+int ffea_gpu_blob_cg_preconditioner(ffea_gpu_blob *blob, int *degree, double *lambda_max);
 
 /* Nodes of the reference numbering (vertices and midpoints) and elements of the blob. */
 int ffea_gpu_blob_counts(ffea_gpu_blob *blob, int *num_nodes, int *num_elements);

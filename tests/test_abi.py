@@ -34,6 +34,11 @@ def test_params_assign_matches_simulationparams(L, oracle_built):
     assert (p.max_iterations_cg, p.calc_noise, p.calc_stokes) == (77, 0, 1)
     assert L.ffea_gpu_params_assign(C.byref(p), b"calc_ssint", b"1") == lib.EINPUT
     assert L.ffea_gpu_params_assign(C.byref(p), b"solver", b"direct") == lib.EINPUT
+    # the mixed CG_nomass preconditioner (an engine key): -1 Jacobi, 0 default, 2 or 4 Chebyshev degree
+    for v in (-1, 0, 2, 4):
+        assert L.ffea_gpu_params_assign(C.byref(p), b"cg_poly", str(v).encode()) == lib.OK and p.cg_poly == v
+    for v in (1, 3, 6):
+        assert L.ffea_gpu_params_assign(C.byref(p), b"cg_poly", str(v).encode()) == lib.EINPUT
 
 
 def test_params_defaults(L):
@@ -62,3 +67,5 @@ def test_blob_create_rejects_bad_input_without_gpu_work(L):
     m.num_nodes, m.num_elements = 0, 0
     assert L.ffea_gpu_blob_create(C.byref(m), C.byref(p), C.byref(h)) == lib.EINPUT
     assert L.ffea_gpu_blob_step(None, 1, None) == lib.EINPUT
+    p.cg_poly = 3  # odd degrees are refused: the preconditioner is positive definite for even ones only
+    assert L.ffea_gpu_blob_create(C.byref(m), C.byref(p), C.byref(h)) == lib.EINPUT

@@ -77,7 +77,8 @@ def test_batch_matches_single_blobs(gpu, oracle_built):
     bt.update(10)
     its, _ = bt.cg_iterations()
     for b, m in enumerate(meshes):
-        s = lib.Blob(m, solver="CG_nomass", precision="mixed", rng_state=substream_states(b + 1)[b], **kw)
+        s = lib.Blob(m, solver="CG_nomass", precision="mixed", cg_poly=-1, rng_state=substream_states(b + 1)[b],
+                     **kw)
         s.set_state(pos=x0[b])
         s.update(10)
         err = np.abs(bt.pos(b) - s.pos()).max() / np.abs(s.pos() - x0[b]).max()

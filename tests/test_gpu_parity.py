@@ -136,11 +136,12 @@ def test_mixed_precision_kT0_error_bound(gpu):
     dict(kT=0.0, calc_noise=0, calc_stokes=1),
 ])
 def test_mixed_precision_iterations_and_error(gpu, kw):
-    """Mixed CG (FP32 matrix, deflated rigid modes) needs the FP64 path's iteration count."""
+    """Mixed CG (FP32 matrix, deflated rigid modes) with the reference's Jacobi preconditioner needs the FP64
+    path's iteration count."""
     m = case_mesh(8, 21)
     out = {}
     for prec in ("fp64", "mixed"):
-        b = gpu_blob(m, 0.02, solver="CG_nomass", precision=prec, dt=1e-12, **kw)
+        b = gpu_blob(m, 0.02, solver="CG_nomass", precision=prec, dt=1e-12, cg_poly=-1, **kw)
         its = []
         for _ in range(5):
             b.update(1)
@@ -148,6 +149,44 @@ def test_mixed_precision_iterations_and_error(gpu, kw):
         out[prec] = (its, b.pos())
     assert all(abs(a - b) <= 2 for a, b in zip(out["fp64"][0], out["mixed"][0])), out
     assert disp_err(out["mixed"][1], out["fp64"][1], sheared(m, 0.02)) < 1e-5
+
+
+@pytest.mark.parametrize("poly", [2, 4])
+def test_chebyshev_preconditioner(gpu, poly):
+    """Mixed CG_nomass with a Chebyshev polynomial preconditioner (degree 2 or 4 in D^-1 V). The blob's first
+    solve is Jacobi's and estimates lambda_max of D^-1 V; the second is the polynomial's trial, kept when it
+    saves work. With thermal noise on a 12^3-cell cube (about 180 Jacobi iterations a step) it is kept and needs
+    at most 0.45x (degree 2) or 0.35x (degree 4) of the iterations; with a Stokes drag (about 26 Jacobi
+    iterations) Jacobi is kept. The trajectory stays within 1e-5 of the FP64 path's displacement, and the blob
+    is reproducible run to run."""
+    m = case_mesh(12, 21)  # 2,197 vertex nodes: nine CG blocks exchanging with their neighbours
+    for kw, kept in ((dict(kT=4.11e-21, calc_noise=1), True), (dict(kT=0.0, calc_noise=0, calc_stokes=1), False)):
+        its, pos = {}, {}
+        for name, prec, cg_poly in (("fp64", "fp64", 0), ("jacobi", "mixed", -1), ("cheb", "mixed", poly),
+                                    ("cheb2", "mixed", poly)):
+            b = gpu_blob(m, 0.02, solver="CG_nomass", precision=prec, dt=1e-12, cg_poly=cg_poly, **kw)
+            its[name] = []
+            for step in range(8):
+                b.update(1)
+                its[name].append(b.cg_iterations()[0])
+                if name == "cheb" and step == 0:
+                    deg, lm = b.cg_preconditioner()
+                    assert deg == poly and 1.5 < lm < 4.0, (deg, lm)  # lambda_max(D^-1 V) of a Kuhn mesh ~2.4
+            pos[name] = b.pos()
+            if prec == "mixed":
+                assert b.cg_preconditioner()[0] == (poly if cg_poly > 0 and kept else 0)
+        print(poly, kw, its)
+        assert its["cheb"][0] == its["jacobi"][0]
+        if kept:
+            bound = {2: 0.45, 4: 0.35}[poly]
+            assert all(c <= bound * j for c, j in zip(its["cheb"][1:], its["jacobi"][1:])), its
+        else:
+            assert its["cheb"][1] < its["jacobi"][1]
+            assert all(abs(c - j) <= 1 for c, j in zip(its["cheb"][2:], its["jacobi"][2:])), its
+        x0 = sheared(m, 0.02)
+        assert disp_err(pos["cheb"], pos["fp64"], x0) < 1e-5
+        assert disp_err(pos["jacobi"], pos["fp64"], x0) < 1e-5
+        assert its["cheb2"] == its["cheb"] and np.array_equal(pos["cheb2"], pos["cheb"])
 
 
 def test_mixed_precision_pinned_nodes(gpu):
