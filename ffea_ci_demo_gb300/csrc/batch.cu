@@ -628,30 +628,30 @@ static int batch_set_range(ffea_gpu_batch *bt, int b0, int b1, const double *pos
         CK(cudaMemcpyAsync(bt->aos + 3 * (size_t)n0, in, 3 * (size_t)n * sizeof(double), cudaMemcpyHostToDevice,
                            bt->stream));
         CK(launch_aos_scatter(bt->aos, bt->d_node_of + r0, nr, dx + r0, dy + r0, dz + r0, bt->stream));
-        CK(cudaStreamSynchronize(bt->stream));
         return FFEA_GPU_OK;
     };
     int rc;
-    if (pos && (rc = put(pos, bt->px, bt->py, bt->pz))) return rc;
     if (vel && (rc = put(vel, bt->vx, bt->vy, bt->vz))) return rc;
-    if (pos) {
-        // each blob's centroid in one pass over its vertex rows; the host copy of the positions is kept for the
-        // pinned rows only (all the rigid modes need)
-        for (int b = b0; b < b1; ++b) {
-            BlobCgDesc &d = bt->hdesc[b];
-            double sum[3] = {0.0, 0.0, 0.0};
-            for (int k = d.row0; k < d.row0 + d.nrows; ++k) {
-                const double *q = pos + 3 * (size_t)(h.node_of[k] - n0);
-                sum[0] += q[0]; sum[1] += q[1]; sum[2] += q[2];
-                if (h.pinned[k])
-                    for (int c = 0; c < 3; ++c) h.pos[3 * (size_t)k + c] = q[c];
-            }
-            for (int c = 0; c < 3; ++c) d.xc[c] = sum[c] / std::max(d.nrows, 1);
-            d.nmodes = rigid_modes_about(h, bt->p, d.xc, d.modes, d.row0, d.nrows);
-        }
-        return bt->upload_desc(b1 - b0 == 1 ? b0 : -1);
+    if (pos && (rc = put(pos, bt->px, bt->py, bt->pz))) return rc;
+    if (!pos) {
+        CK(cudaStreamSynchronize(bt->stream));  // the caller may reuse its arrays on return
+        return FFEA_GPU_OK;
     }
-    return FFEA_GPU_OK;
+    // while the positions travel: each blob's centroid in one pass over its vertex rows; the host copy of the
+    // positions is kept for the pinned rows only (all the rigid modes need)
+    for (int b = b0; b < b1; ++b) {
+        BlobCgDesc &d = bt->hdesc[b];
+        double sum[3] = {0.0, 0.0, 0.0};
+        for (int k = d.row0; k < d.row0 + d.nrows; ++k) {
+            const double *q = pos + 3 * (size_t)(h.node_of[k] - n0);
+            sum[0] += q[0]; sum[1] += q[1]; sum[2] += q[2];
+            if (h.pinned[k])
+                for (int c = 0; c < 3; ++c) h.pos[3 * (size_t)k + c] = q[c];
+        }
+        for (int c = 0; c < 3; ++c) d.xc[c] = sum[c] / std::max(d.nrows, 1);
+        d.nmodes = rigid_modes_about(h, bt->p, d.xc, d.modes, d.row0, d.nrows);
+    }
+    return bt->upload_desc(b1 - b0 == 1 ? b0 : -1);  // ends with a stream synchronisation
 }
 
 int ffea_gpu_batch_get_state(ffea_gpu_batch *bt, int blob, double *pos, double *vel) {

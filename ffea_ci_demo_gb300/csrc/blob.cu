@@ -119,7 +119,6 @@ __global__ void __launch_bounds__(SOLVE_PREP_THREADS)
     if (a == 0) {
         *st = DevStatus{};
         gb->count = 0u;
-        gb->passed = 0u;
         for (int k = 0; k < FFEA_GPU_CG_PHASES; ++k) phase_ns[k] = 0ull;
     }
     double acc[2] = {0.0, 0.0};
@@ -706,15 +705,15 @@ struct BlobImpl final : ffea_gpu_blob {
         auto put = [&](const double *in, double *dx, double *dy, double *dz) -> int {
             CK(cudaMemcpyAsync(aos, in, 3 * (size_t)h.n_all * sizeof(double), cudaMemcpyHostToDevice, stream));
             CK(launch_aos_scatter(aos, d_node_of, N, dx, dy, dz, stream));
-            CK(cudaStreamSynchronize(stream));
             return FFEA_GPU_OK;
         };
         int rc;
-        if (pos && (rc = put(pos, px, py, pz))) return rc;
         if (vel && (rc = put(vel, vx, vy, vz))) return rc;
+        if (pos && (rc = put(pos, px, py, pz))) return rc;
         if (pos) {
-            // the rigid modes must vanish at the pinned nodes' current positions, about the new centroid (one
-            // pass over the vertex rows; the host copy of the positions is kept for the pinned rows only)
+            // while the positions travel: the rigid modes must vanish at the pinned nodes' current positions, about
+            // the new centroid (one pass over the vertex rows; the host copy of the positions is kept for the
+            // pinned rows only)
             double s[3] = {0.0, 0.0, 0.0};
             for (int k = 0; k < N; ++k) {
                 const double *q = pos + 3 * (size_t)h.node_of[k];
@@ -725,6 +724,8 @@ struct BlobImpl final : ffea_gpu_blob {
             for (int c = 0; c < 3; ++c) xc[c] = s[c] / std::max(N, 1);
             nmodes = rigid_modes_about(h, p, xc, modes, 0, N);
         }
+        // the caller may reuse its arrays on return
+        CK(cudaStreamSynchronize(stream));
         return FFEA_GPU_OK;
     }
 

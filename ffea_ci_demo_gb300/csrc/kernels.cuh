@@ -535,7 +535,7 @@ template <class R>
 __global__ void __launch_bounds__(256) gather_kernel(GatherArgs<R> g) {
     __shared__ double smem[64];
     const int a = blockIdx.x * blockDim.x + threadIdx.x;
-    if (a == 0 && g.gb) { g.gb->count = 0u; g.gb->passed = 0u; }
+    if (a == 0 && g.gb) g.gb->count = 0u;
     double acc[2] = {0.0, 0.0};
     const bool live = a < g.N && !g.st->abort;
     if (live) {
@@ -791,7 +791,8 @@ __global__ void __launch_bounds__(1024, 1) cg_kernel(const __grid_constant__ CgA
     grid_sum_d<2>(g.init_partials, g.init_stride, g.n_init, s_sc);
     const double f2 = s_sc[0];
     if (threadIdx.x == 0) { s_delta = s_sc[1]; s_conv = 0; }
-    bool ok = grid_sync(g.gb, st, g.limit_ns);
+    unsigned int bar_ep = 0;  // grid barriers passed
+    bool ok = grid_sync_ep(g.gb, st, g.limit_ns, bar_ep);
     FFEA_MARK(g, tm, 0);
     int it = 0;
     for (; ok && it < g.imax; ++it) {
@@ -812,7 +813,7 @@ __global__ void __launch_bounds__(1024, 1) cg_kernel(const __grid_constant__ CgA
         block_sum_smem<1>(acc1, smem, out1);
         if (threadIdx.x == 0) g.partials[blockIdx.x] = out1[0];
         FFEA_MARK(g, tm, 2);
-        if (!(ok = grid_sync(g.gb, st, g.limit_ns))) break;
+        if (!(ok = grid_sync_ep(g.gb, st, g.limit_ns, bar_ep))) break;
         FFEA_MARK(g, tm, 3);
         grid_sum_d<1>(g.partials, 0, gridDim.x, s_sc);
         if (threadIdx.x == 0) s_alpha = (R)(s_delta / s_sc[0]);
@@ -842,7 +843,7 @@ __global__ void __launch_bounds__(1024, 1) cg_kernel(const __grid_constant__ CgA
             g.partials[2 * g.stride + blockIdx.x] = out2[1];
         }
         FFEA_MARK(g, tm, 6);
-        if (!(ok = grid_sync(g.gb, st, g.limit_ns))) break;
+        if (!(ok = grid_sync_ep(g.gb, st, g.limit_ns, bar_ep))) break;
         FFEA_MARK(g, tm, 7);
         grid_sum_d<2>(g.partials + g.stride, g.stride, gridDim.x, s_sc);
         if (threadIdx.x == 0) {
@@ -865,7 +866,7 @@ __global__ void __launch_bounds__(1024, 1) cg_kernel(const __grid_constant__ CgA
 #pragma unroll
             for (int c = 0; c < 3; ++c) p[4 * a + c] = fma(beta, p[4 * a + c], g.dinv[4 * a + c] * g.r[4 * a + c]);
         }
-        if (!(ok = grid_sync(g.gb, st, g.limit_ns))) break;
+        if (!(ok = grid_sync_ep(g.gb, st, g.limit_ns, bar_ep))) break;
         FFEA_MARK(g, tm, 9);
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -1011,7 +1012,8 @@ __global__ void __launch_bounds__(1024, 1) cg_own_kernel(const __grid_constant__
     grid_sum_d<2>(g.init_partials, g.init_stride, g.n_init, s_sc);
     const double f2 = s_sc[0];
     if (threadIdx.x == 0) { s_delta = s_sc[1]; s_conv = 0; }
-    bool ok = grid_sync(g.gb, st, g.limit_ns);
+    unsigned int bar_ep = 0;  // grid barriers passed
+    bool ok = grid_sync_ep(g.gb, st, g.limit_ns, bar_ep);
     const int tpn = g.tpn, gpb = blockDim.x / tpn, grp = threadIdx.x / tpn, sub = threadIdx.x % tpn;
     const int npass = (nloc + gpb - 1) / gpb;
     FFEA_MARK(g, tm, 0);
@@ -1033,7 +1035,7 @@ __global__ void __launch_bounds__(1024, 1) cg_own_kernel(const __grid_constant__
         block_sum_smem<1>(acc1, smem, out1);
         if (threadIdx.x == 0) g.partials[blockIdx.x] = out1[0];
         FFEA_MARK(g, tm, 2);
-        if (!(ok = grid_sync(g.gb, st, g.limit_ns))) break;
+        if (!(ok = grid_sync_ep(g.gb, st, g.limit_ns, bar_ep))) break;
         FFEA_MARK(g, tm, 3);
         grid_sum_d<1>(g.partials, 0, gridDim.x, s_sc);
         if (threadIdx.x == 0) s_alpha = (R)(s_delta / s_sc[0]);
@@ -1063,7 +1065,7 @@ __global__ void __launch_bounds__(1024, 1) cg_own_kernel(const __grid_constant__
             g.partials[2 * g.stride + blockIdx.x] = out2[1];
         }
         FFEA_MARK(g, tm, 6);
-        if (!(ok = grid_sync(g.gb, st, g.limit_ns))) break;
+        if (!(ok = grid_sync_ep(g.gb, st, g.limit_ns, bar_ep))) break;
         FFEA_MARK(g, tm, 7);
         grid_sum_d<2>(g.partials + g.stride, g.stride, gridDim.x, s_sc);
         if (threadIdx.x == 0) {
@@ -1093,7 +1095,7 @@ __global__ void __launch_bounds__(1024, 1) cg_own_kernel(const __grid_constant__
             p2[2 * a] = make_double2(pv[0], pv[1]);
             p2[2 * a + 1] = make_double2(pv[2], 0.0);
         }
-        if (!(ok = grid_sync(g.gb, st, g.limit_ns))) break;
+        if (!(ok = grid_sync_ep(g.gb, st, g.limit_ns, bar_ep))) break;
         FFEA_MARK(g, tm, 9);
     }
     for (int l = threadIdx.x; l < nloc; l += blockDim.x) {

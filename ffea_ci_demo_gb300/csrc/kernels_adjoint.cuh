@@ -49,7 +49,7 @@ template <class R>
 __global__ void __launch_bounds__(256) adj_gather_kernel(AdjGatherArgs<R> g) {
     __shared__ double smem[ADJ_MOMENTS * 32];
     const int a = blockIdx.x * blockDim.x + threadIdx.x;
-    if (a == 0 && g.gb) { g.gb->count = 0u; g.gb->passed = 0u; }
+    if (a == 0 && g.gb) g.gb->count = 0u;
     double acc[ADJ_MOMENTS];
 #pragma unroll
     for (int i = 0; i < ADJ_MOMENTS; ++i) acc[i] = 0.0;

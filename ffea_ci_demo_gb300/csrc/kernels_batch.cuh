@@ -25,46 +25,6 @@
 
 namespace ffea {
 
-// Barrier of the nblk CTAs of one group: grid_sync with the group's own counter. A one-CTA group
-// needs only __syncthreads (global writes of a block are visible to the block after it).
-__device__ __forceinline__ bool group_sync(GridBarrier *gb, unsigned nblk, DevStatus *st,
-                                           unsigned long long limit_ns) {
-    if (nblk == 1u) {
-        __syncthreads();
-        return true;
-    }
-    __shared__ int s_ok;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        int ok = 1;
-        __threadfence();
-        const unsigned int old = atomicAdd(&gb->count, 1u);
-        const unsigned int k1 = old / nblk + 1u;
-        if (old == k1 * nblk - 1u) {
-            atomicExch(&gb->passed, k1);
-        } else {
-            volatile unsigned int *passed = &gb->passed;
-            const unsigned long long t0 = globaltimer_ns();
-            unsigned int polls = 0;
-            while ((int)(*passed - k1) < 0) {
-                if ((++polls & 255u) == 0u) {
-                    if (globaltimer_ns() - t0 > limit_ns) {
-                        atomicExch(&st->timeout, 1);
-                        atomicExch(&st->abort, 1);
-                        ok = 0;
-                        break;
-                    }
-                    if (*((volatile int *)&st->timeout)) { ok = 0; break; }
-                }
-            }
-        }
-        __threadfence();
-        s_ok = ok;
-    }
-    __syncthreads();
-    return s_ok != 0;
-}
-
 // Rows of one blob split over the warps of its group: the group's W warps take consecutive runs of
 // rppw = min(32 / tpn, ceil(nrows / W)) rows per pass, tpn lanes per row (see FFEA_ROW_LOOP).
 #define BATCH_ROW_LOOP(tpn, row0, nrows, rank, gsz, a, sub, valid)                                   \
@@ -133,7 +93,7 @@ __global__ void __launch_bounds__(BATCH_MAX_THREADS) cg_batch_kernel(const __gri
 #pragma unroll
             for (int i = 0; i < MIXED_GATHER_NP; ++i) spart[i * gsz + rank] = make_float2(o[i].hi, o[i].lo);
     }
-    bool ok = group_sync(gb, gsz, st, g.limit_ns);
+    bool ok = group_sync(gb, (unsigned)gsz, st, g.limit_ns);
     if (!ok) return;
     grid_sum_df<MIXED_GATHER_NP>(spart, gsz, gsz, s_sc);
     const double f2 = s_sc[0];
@@ -164,7 +124,7 @@ __global__ void __launch_bounds__(BATCH_MAX_THREADS) cg_batch_kernel(const __gri
         block_reduce_f<1>(acc0, smemf, o);
         if (threadIdx.x == 0) ipart[rowz * gsz + rank] = make_float2(o[0].hi, o[0].lo);
     }
-    ok = group_sync(gb, gsz, st, g.limit_ns);
+    ok = group_sync(gb, (unsigned)gsz, st, g.limit_ns);
     if (ok) {
         grid_sum_df<1>(ipart + rowz * gsz, 0, gsz, s_sc);
         if (threadIdx.x == 0) s_delta = s_sc[0];
@@ -211,7 +171,7 @@ __global__ void __launch_bounds__(BATCH_MAX_THREADS) cg_batch_kernel(const __gri
 #pragma unroll
                 for (int i = 0; i < MIXED_A_NP; ++i) ipart[i * gsz + rank] = make_float2(o[i].hi, o[i].lo);
         }
-        if (!(ok = group_sync(gb, gsz, st, g.limit_ns))) break;
+        if (!(ok = group_sync(gb, (unsigned)gsz, st, g.limit_ns))) break;
         grid_sum_df<MIXED_A_NP>(ipart, gsz, gsz, s_sc);
         if (threadIdx.x < 32) {
             const int l = threadIdx.x;
@@ -257,7 +217,7 @@ __global__ void __launch_bounds__(BATCH_MAX_THREADS) cg_batch_kernel(const __gri
             if (threadIdx.x == 0)
                 for (int i = 0; i < MIXED_B_NP; ++i) ipart[(MIXED_A_NP + i) * gsz + rank] = make_float2(o[i].hi, o[i].lo);
         }
-        if (!(ok = group_sync(gb, gsz, st, g.limit_ns))) break;
+        if (!(ok = group_sync(gb, (unsigned)gsz, st, g.limit_ns))) break;
         grid_sum_df<MIXED_B_NP>(ipart + MIXED_A_NP * gsz, gsz, gsz, s_sc);
         if (threadIdx.x == 0) {
             s_conv = (f2 == 0.0 || s_sc[0] < g.eps2 * f2);

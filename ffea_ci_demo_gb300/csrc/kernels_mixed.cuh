@@ -52,7 +52,7 @@ template <class R>
 __global__ void __launch_bounds__(256) gather_mixed_kernel(GatherArgs<R> g) {
     __shared__ float2 smem[MIXED_GATHER_NP * 32];
     const int a = blockIdx.x * blockDim.x + threadIdx.x;
-    if (a == 0 && g.gb) { g.gb->count = 0u; g.gb->passed = 0u; }
+    if (a == 0 && g.gb) g.gb->count = 0u;
     df32 acc[MIXED_GATHER_NP];
 #pragma unroll
     for (int i = 0; i < MIXED_GATHER_NP; ++i) acc[i] = df32{0.f, 0.f};
@@ -230,7 +230,8 @@ __global__ void __launch_bounds__(1024, 1) cg_mixed_kernel(const __grid_constant
         block_reduce_f<1>(acc0, smemf, o);
         if (threadIdx.x == 0) partials[row0 * g.stride + blockIdx.x] = make_float2(o[0].hi, o[0].lo);
     }
-    bool ok = grid_sync(g.gb, st, g.limit_ns);
+    unsigned int bar_ep = 0;  // grid barriers passed
+    bool ok = grid_sync_ep(g.gb, st, g.limit_ns, bar_ep);
     if (ok) {
         grid_sum_df<1>(partials + row0 * g.stride, 0, gridDim.x, s_sc);
         if (threadIdx.x == 0) s_delta = s_sc[0];
@@ -275,7 +276,7 @@ __global__ void __launch_bounds__(1024, 1) cg_mixed_kernel(const __grid_constant
                 for (int i = 0; i < MIXED_A_NP; ++i) partials[i * g.stride + blockIdx.x] = make_float2(o[i].hi, o[i].lo);
         }
         FFEA_MARK(g, tm, 2);
-        if (!(ok = grid_sync(g.gb, st, g.limit_ns))) break;
+        if (!(ok = grid_sync_ep(g.gb, st, g.limit_ns, bar_ep))) break;
         FFEA_MARK(g, tm, 3);
         grid_sum_df<MIXED_A_NP>(partials, g.stride, gridDim.x, s_sc);
         // (tau, Omega) = A6 S over six lanes of warp 0; p.V~p = p.q + S . (tau, Omega); alpha = delta / p.V~p
@@ -324,7 +325,7 @@ __global__ void __launch_bounds__(1024, 1) cg_mixed_kernel(const __grid_constant
                     partials[(MIXED_A_NP + i) * g.stride + blockIdx.x] = make_float2(o[i].hi, o[i].lo);
         }
         FFEA_MARK(g, tm, 6);
-        if (!(ok = grid_sync(g.gb, st, g.limit_ns))) break;
+        if (!(ok = grid_sync_ep(g.gb, st, g.limit_ns, bar_ep))) break;
         FFEA_MARK(g, tm, 7);
         grid_sum_df<MIXED_B_NP>(partials + MIXED_A_NP * g.stride, g.stride, gridDim.x, s_sc);
         if (threadIdx.x == 0) {
@@ -575,7 +576,8 @@ __global__ void __launch_bounds__(1024, 1) cg_mixed_own_kernel(const __grid_cons
     }
     const int row0 = MIXED_A_NP + MIXED_B_NP;
     block_reduce_store<1>(acc0, smemf, partials, g.stride, row0);
-    bool ok = grid_sync(g.gb, st, g.limit_ns);
+    unsigned int bar_ep = 0;  // grid barriers passed
+    bool ok = grid_sync_ep(g.gb, st, g.limit_ns, bar_ep);
     if (ok) {
         grid_sum_df8<1>(partials + row0 * g.stride, 0, gridDim.x, s_sc);
         if (threadIdx.x == 0) s_delta = s_sc[0];
@@ -622,7 +624,7 @@ __global__ void __launch_bounds__(1024, 1) cg_mixed_own_kernel(const __grid_cons
         FFEA_MARK(g, tm, 1);
         block_reduce_store<MIXED_A_NP>(acc, smemf, partials, g.stride, 0);
         FFEA_MARK(g, tm, 2);
-        if (!(ok = grid_sync(g.gb, st, g.limit_ns))) break;
+        if (!(ok = grid_sync_ep(g.gb, st, g.limit_ns, bar_ep))) break;
         FFEA_MARK(g, tm, 3);
         grid_sum_df8<MIXED_A_NP>(partials, g.stride, gridDim.x, s_sc);
         if (threadIdx.x < 32) {
@@ -674,7 +676,7 @@ __global__ void __launch_bounds__(1024, 1) cg_mixed_own_kernel(const __grid_cons
         FFEA_MARK(g, tm, 5);
         block_reduce_store<MIXED_B_NP>(acc2, smemf, partials, g.stride, MIXED_A_NP);
         FFEA_MARK(g, tm, 6);
-        if (!(ok = grid_sync(g.gb, st, g.limit_ns))) break;
+        if (!(ok = grid_sync_ep(g.gb, st, g.limit_ns, bar_ep))) break;
         FFEA_MARK(g, tm, 7);
         grid_sum_df8<MIXED_B_NP>(partials + MIXED_A_NP * g.stride, g.stride, gridDim.x, s_sc);
         if (threadIdx.x == 0) {
@@ -879,7 +881,8 @@ __global__ void __launch_bounds__(1024, 1) cg_mixed_sr_kernel(const __grid_const
     const float ith = cheb ? s_ith : 0.f;
     const int tpn = g.tpn, gpb = blockDim.x / tpn, grp = threadIdx.x / tpn, sub = threadIdx.x % tpn;
     const int npass = (nloc + gpb - 1) / gpb;
-    unsigned int ep = 0;  // publication epochs of the neighbour exchanges
+    unsigned int ep = 0;      // publication epochs of the neighbour exchanges
+    unsigned int bar_ep = 0;  // grid barriers passed
     // Chebyshev steps 1..d after step 0 published y0 = D^{-1} r / theta (in y4a) and left D^{-1} r in sw:
     // res -= D^{-1} V y, dd = c1 dd + c2 res, u += dd; each step publishes dd for the next one's SpMV (y4a and
     // y4b alternate; a neighbour has read one before it publishes the next), the last one publishes u as z
@@ -991,7 +994,7 @@ __global__ void __launch_bounds__(1024, 1) cg_mixed_sr_kernel(const __grid_const
         FFEA_MARK(g, tm, 1);
         block_reduce_store<MIXED_SR_NP>(acc, smemf, partials, g.stride, 0);
         FFEA_MARK(g, tm, 2);
-        if (!(ok = grid_sync(g.gb, st, g.limit_ns))) break;
+        if (!(ok = grid_sync_ep(g.gb, st, g.limit_ns, bar_ep))) break;
         FFEA_MARK(g, tm, 3);
         grid_sum_df8<MIXED_SR_NP>(partials, g.stride, gridDim.x, s_sc);
         if (threadIdx.x < 32) {
