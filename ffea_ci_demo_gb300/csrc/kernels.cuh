@@ -886,40 +886,39 @@ __global__ void __launch_bounds__(1024, 1) cg_kernel(const __grid_constant__ CgA
 
 constexpr int FLAG_STRIDE = 32;  // words between two blocks' publication counters (one 128-byte line each)
 
-// Block `blockIdx.x` has written its rows' z for round `epoch`: publish that (a release through the fence
-// and the atomic), then wait (bounded by %globaltimer) until every block owning a column of its rows has
-// published the same round, and order the block's later reads after those writes. Returns false on a
-// timeout (recorded in st) or when another block recorded one.
+// Block `blockIdx.x` has written its rows' z for round `epoch`: publish that (one release store after the
+// block barrier), then wait (bounded by %globaltimer, acquire loads) until every block owning a column of its
+// rows has published the same round; the closing barrier orders the block's later reads after those writes.
+// Returns false on a timeout (recorded in st) or when another block recorded one.
 template <class R>
 __device__ __forceinline__ bool neighbour_sync(const CgArgs<R> &g, unsigned int epoch, DevStatus *st) {
-    __shared__ int s_nok;
     __syncthreads();
-    if (threadIdx.x == 0) {
-        s_nok = 0;
-        __threadfence();
-        atomicExch(g.flags + (size_t)FLAG_STRIDE * blockIdx.x, epoch);
-    }
-    __syncthreads();
+    if (threadIdx.x == 0)
+        asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(g.flags + (size_t)FLAG_STRIDE * blockIdx.x),
+                     "r"(epoch)
+                     : "memory");
+    int bad = 0;
     const int j0 = g.nb_ptr[blockIdx.x], j1 = g.nb_ptr[blockIdx.x + 1];
-    for (int j = j0 + (int)threadIdx.x; j < j1; j += blockDim.x) {
-        const volatile unsigned int *f = g.flags + (size_t)FLAG_STRIDE * g.nb_list[j];
+    for (int j = j0 + (int)threadIdx.x; j < j1 && !bad; j += blockDim.x) {
+        const unsigned int *f = g.flags + (size_t)FLAG_STRIDE * g.nb_list[j];
         const unsigned long long t0 = globaltimer_ns();
         unsigned int polls = 0;
-        while ((int)(*f - epoch) < 0) {
+        for (;;) {
+            unsigned int v;
+            asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(f) : "memory");
+            if ((int)(v - epoch) >= 0) break;
             if ((++polls & 255u) == 0u) {
                 if (globaltimer_ns() - t0 > g.limit_ns) {
                     atomicExch(&st->timeout, 1);
                     atomicExch(&st->abort, 1);
-                    s_nok = 1;
+                    bad = 1;
                     break;
                 }
-                if (*((volatile int *)&st->timeout)) { s_nok = 1; break; }
+                if (*((volatile int *)&st->timeout)) { bad = 1; break; }
             }
         }
-        __threadfence();
     }
-    __syncthreads();
-    return s_nok == 0;
+    return __syncthreads_or(bad) == 0;
 }
 
 // Row a of q = V p for cg_own_kernel (FP64): the direction at neighbour b read as two 16-byte loads; the
