@@ -176,6 +176,7 @@ struct BlobImpl final : ffea_gpu_blob {
     int cg_block = 1024;  // threads per CG block
     bool cg_sr = false;   // the mixed CG_nomass solve uses cg_mixed_sr_kernel
     int cg_poly = 0;      // with a Chebyshev preconditioner of this degree (0: Jacobi)
+    int cg_kc = 0;        // and this many 3x3 blocks of each owned row in shared memory
     double *cheb = nullptr;  // its lambda_max estimate and the Lanczos record that makes it (CHEB_STATE)
     int *nb_ptr = nullptr, *nb_list = nullptr;  // its blocks' neighbour blocks
     unsigned int *nb_flags = nullptr;           // and their publication counters
@@ -392,6 +393,19 @@ struct BlobImpl final : ffea_gpu_blob {
                 }
                 if (cg_sr) cg_npb = npb;
             }
+            if (cg_sr) {
+                // the first blocks of each owned row kept in shared memory for the solve, as many as the rest of
+                // the block's shared memory holds (FFEA_GPU_CG_CACHE=0 turns this off, for comparison runs)
+                const char *cache = getenv("FFEA_GPU_CG_CACHE");
+                const long long avail =
+                    (long long)Launch<R>::cg_sr_smem_limit(device) - (long long)sr_smem_bytes(cg_npb, cg_poly);
+                const long long S = sr_cache_stride(cg_npb, tpn);
+                int maxlen = 0;
+                for (int a = 0; a < N; ++a) maxlen = std::max(maxlen, h.rowlen[a]);
+                cg_kc = (cache && cache[0] == '0') || avail <= 0
+                            ? 0
+                            : (int)std::min<long long>(maxlen, avail / (SR_CACHE_BYTES_PER_BLOCK * S));
+            }
             if (cg_poly > 0) {
                 CK(mem.alloc(&cheb, (size_t)CHEB_STATE));
                 CK(cudaMemset(cheb, 0, CHEB_STATE * sizeof(double)));
@@ -525,6 +539,7 @@ struct BlobImpl final : ffea_gpu_blob {
         ca.npb = cg_npb;
         ca.sr = cg_sr && nomass;
         ca.poly = ca.sr ? cg_poly : 0;
+        ca.kc = ca.sr ? cg_kc : 0;
         ca.cheb = cheb;
         // a Chebyshev step (SpMV + neighbour exchange) against a whole iteration (SpMV, exchange, grid-wide
         // reduction): about half while the FP32 matrix (40 B per 3x3 block) stays in L2, more once it streams

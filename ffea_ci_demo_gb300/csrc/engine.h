@@ -29,6 +29,8 @@ struct Launch {
     static int cg_own_max_rows(int device);
     // the same for cg_mixed_sr_kernel (a.sr selects it) with a Chebyshev preconditioner of degree poly; 0 for FP64
     static int cg_sr_max_rows(int device, int poly);
+    // the dynamic shared memory one cg_mixed_sr_kernel block may take on `device` (0 for FP64)
+    static int cg_sr_smem_limit(int device);
     static cudaError_t euler(const EulerArgs<R> &a, cudaStream_t s);
     // measure_kernel over max(T, N, M) threads in `blocks` blocks, then the final sum into out[6]
     static cudaError_t measure(const MeasureArgs<R> &a, int blocks, double *out, cudaStream_t s);

@@ -109,6 +109,24 @@ int Launch<R>::cg_sr_max_rows(int device, int poly) {
 }
 
 template <class R>
+int Launch<R>::cg_sr_smem_limit(int device) {
+    if constexpr (std::is_same<R, float>::value) {
+        int optin = 0;
+        cudaFuncAttributes fa{};
+        if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device) != cudaSuccess ||
+            cudaFuncGetAttributes(&fa, cg_mixed_sr_kernel<R>) != cudaSuccess)
+            return 0;
+        const int dyn = optin - (int)fa.sharedSizeBytes;
+        if (dyn <= 0 ||
+            cudaFuncSetAttribute(cg_mixed_sr_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn) != cudaSuccess)
+            return 0;
+        return dyn;
+    } else {
+        return (void)device, 0;
+    }
+}
+
+template <class R>
 cudaError_t Launch<R>::cg(const CgArgs<R> &a, int grid, int threads, cudaStream_t s) {
     CgArgs<R> args = a;
     void *params[] = {&args};
@@ -118,7 +136,8 @@ cudaError_t Launch<R>::cg(const CgArgs<R> &a, int grid, int threads, cudaStream_
         fn = (const void *)cg_mixed_kernel<R>;
         if (a.npb > 0 && a.sr) {
             fn = (const void *)cg_mixed_sr_kernel<R>;
-            smem = sr_smem_bytes(a.npb, a.poly);
+            smem = sr_smem_bytes(a.npb, a.poly) +
+                   (a.kc > 0 ? sr_cache_bytes(a.kc, sr_cache_stride(a.npb, a.tpn)) : 0);
         } else if (a.npb > 0) {
             fn = (const void *)cg_mixed_own_kernel<R>;
             smem = own_smem_bytes(a.npb);

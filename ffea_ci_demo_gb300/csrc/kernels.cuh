@@ -641,6 +641,7 @@ struct CgArgs {
     int poly;
     double *cheb;
     float cheb_cost;
+    int kc;               // cg_mixed_sr_kernel: 3x3 blocks per owned row kept in shared memory (0: none)
 };
 
 // p at node b for this iteration: p_new = beta p_old + D^{-1} r (vec3_scale_and_add with the

@@ -718,19 +718,52 @@ __global__ void __launch_bounds__(1024, 1) cg_mixed_own_kernel(const __grid_cons
     }
 }
 
-// Row a of w = V z for cg_mixed_sr_kernel: the preconditioned residual of neighbour b read as one float4;
-// two blocks per trip, products in block order.
+// The first kc 3x3 blocks of each owned row of cg_mixed_sr_kernel, kept in shared memory for the whole solve:
+// values at cv[(9 k + c) S + l], block columns at cc[k S + l] (l the row's index in the block). S is the
+// block's row count padded to S = 32 / tpn (mod 32), so that the tpn lanes of a row, which read blocks k, k + 1,
+// ..., k + tpn - 1 of the rows of one warp, fall on distinct banks.
+struct SrCache {
+    const float *cv;
+    const int *cc;
+    int kc, S;
+};
+
+__host__ __device__ inline int sr_cache_stride(int npb, int tpn) {
+    const int r = tpn > 1 ? 32 / tpn : 0;
+    int S = npb;
+    while ((S & 31) != r) ++S;
+    return S;
+}
+
+#define FFEA_W_FMA(WV, ZV)                                                                   \
+    w0 = fmaf(WV[0], ZV.x, w0); w0 = fmaf(WV[1], ZV.y, w0); w0 = fmaf(WV[2], ZV.z, w0);        \
+    w1 = fmaf(WV[3], ZV.x, w1); w1 = fmaf(WV[4], ZV.y, w1); w1 = fmaf(WV[5], ZV.z, w1);        \
+    w2 = fmaf(WV[6], ZV.x, w2); w2 = fmaf(WV[7], ZV.y, w2); w2 = fmaf(WV[8], ZV.z, w2)
+
+// Row a of w = V z for cg_mixed_sr_kernel: the preconditioned residual of neighbour b read as one float4.
+// Each lane takes blocks k = sub, sub + tpn, ... in order: first those held in shared memory (k < kc), then
+// the rest from the matrix in global memory, two per trip; the products are summed in block order either way,
+// so the row does not depend on kc.
 template <class A>
-__device__ __forceinline__ void spmv_row_w(const A &g, const float4 *z4, int a, int sub, bool valid, float &w0,
-                                           float &w1, float &w2) {
+__device__ __forceinline__ void spmv_row_w(const A &g, const SrCache &c, const float4 *z4, int a, int l, int sub,
+                                           bool valid, float &w0, float &w1, float &w2) {
     w0 = 0.f; w1 = 0.f; w2 = 0.f;
     const int tpn = g.tpn;
     if (valid) {
         const int s = a >> 5, lane = a & 31;
         const int base = __ldg(g.slice_ptr + s);
         const int len = __ldg(g.rowlen + a);
-        const float *v = g.val + 9 * (size_t)base + lane;
+        const int kcl = min(c.kc, len);
         int k = sub;
+#pragma unroll 1
+        for (; k < kcl; k += tpn) {
+            float wk[9];
+#pragma unroll
+            for (int i = 0; i < 9; ++i) wk[i] = c.cv[(9 * k + i) * c.S + l];
+            const float4 z = z4[c.cc[k * c.S + l]];
+            FFEA_W_FMA(wk, z);
+        }
+        const float *v = g.val + 9 * (size_t)base + lane;
 #pragma unroll 1
         for (; k + tpn < len; k += 2 * tpn) {
             const int ba = __ldg(g.bcol + base + 32 * k + lane), bb = __ldg(g.bcol + base + 32 * (k + tpn) + lane);
@@ -742,12 +775,8 @@ __device__ __forceinline__ void spmv_row_w(const A &g, const float4 *z4, int a, 
                 wb[i] = __ldg(vb + 32 * i);
             }
             const float4 za = z4[ba], zb = z4[bb];
-            w0 = fmaf(wa[0], za.x, w0); w0 = fmaf(wa[1], za.y, w0); w0 = fmaf(wa[2], za.z, w0);
-            w1 = fmaf(wa[3], za.x, w1); w1 = fmaf(wa[4], za.y, w1); w1 = fmaf(wa[5], za.z, w1);
-            w2 = fmaf(wa[6], za.x, w2); w2 = fmaf(wa[7], za.y, w2); w2 = fmaf(wa[8], za.z, w2);
-            w0 = fmaf(wb[0], zb.x, w0); w0 = fmaf(wb[1], zb.y, w0); w0 = fmaf(wb[2], zb.z, w0);
-            w1 = fmaf(wb[3], zb.x, w1); w1 = fmaf(wb[4], zb.y, w1); w1 = fmaf(wb[5], zb.z, w1);
-            w2 = fmaf(wb[6], zb.x, w2); w2 = fmaf(wb[7], zb.y, w2); w2 = fmaf(wb[8], zb.z, w2);
+            FFEA_W_FMA(wa, za);
+            FFEA_W_FMA(wb, zb);
         }
         if (k < len) {
             const int b = __ldg(g.bcol + base + 32 * k + lane);
@@ -756,9 +785,7 @@ __device__ __forceinline__ void spmv_row_w(const A &g, const float4 *z4, int a, 
 #pragma unroll
             for (int i = 0; i < 9; ++i) wk[i] = __ldg(vk + 32 * i);
             const float4 z = z4[b];
-            w0 = fmaf(wk[0], z.x, w0); w0 = fmaf(wk[1], z.y, w0); w0 = fmaf(wk[2], z.z, w0);
-            w1 = fmaf(wk[3], z.x, w1); w1 = fmaf(wk[4], z.y, w1); w1 = fmaf(wk[5], z.z, w1);
-            w2 = fmaf(wk[6], z.x, w2); w2 = fmaf(wk[7], z.y, w2); w2 = fmaf(wk[8], z.z, w2);
+            FFEA_W_FMA(wk, z);
         }
     }
     for (int o = 1; o < tpn; o <<= 1) {
@@ -767,6 +794,7 @@ __device__ __forceinline__ void spmv_row_w(const A &g, const float4 *z4, int a, 
         w2 += __shfl_xor_sync(0xffffffffu, w2, o);
     }
 }
+#undef FFEA_W_FMA
 
 // Bytes of dynamic shared memory cg_mixed_sr_kernel needs for npb owned rows: x, r, p, q, w, D^{-1}, D, d, and
 // with a polynomial preconditioner u (the preconditioned residual) and the Chebyshev correction.
@@ -774,6 +802,11 @@ constexpr int SR_FIELDS = 24;
 constexpr int SR_FIELDS_POLY = 30;
 __host__ __device__ constexpr size_t sr_smem_bytes(int npb, int poly) {
     return (size_t)(poly > 0 ? SR_FIELDS_POLY : SR_FIELDS) * npb * sizeof(float);
+}
+// ... plus the matrix cache of kc blocks per row at stride S: nine values and a column each
+constexpr int SR_CACHE_BYTES_PER_BLOCK = 10 * 4;
+__host__ __device__ constexpr size_t sr_cache_bytes(int kc, int S) {
+    return (size_t)SR_CACHE_BYTES_PER_BLOCK * kc * S;
 }
 
 // The Chebyshev preconditioner: degrees 2 and 4 (even degrees keep it positive definite whatever the estimate of
@@ -856,6 +889,25 @@ __global__ void __launch_bounds__(1024, 1) cg_mixed_sr_kernel(const __grid_const
     // polynomial preconditioner: u = M^{-1} r and the Chebyshev correction dd (the residual of the Chebyshev
     // iteration shares w's storage: w is dead between the update and the next SpMV)
     float *su = sn + 24 * npb, *sdd = sn + 27 * npb;
+    // the matrix cache after the row fields, filled once for the solve
+    SrCache mc;
+    mc.kc = g.kc;
+    mc.S = g.kc > 0 ? sr_cache_stride(npb, g.tpn) : 0;
+    {
+        float *cv = sn + (g.poly > 0 ? SR_FIELDS_POLY : SR_FIELDS) * npb;
+        int *cc = reinterpret_cast<int *>(cv + 9 * (size_t)mc.kc * mc.S);
+        for (int t = threadIdx.x; t < mc.kc * nloc; t += blockDim.x) {
+            const int k = t / nloc, l = t - k * nloc, a = a0 + l;
+            if (k >= __ldg(g.rowlen + a)) continue;
+            const int base = __ldg(g.slice_ptr + (a >> 5)), lane = a & 31;
+            const float *vk = g.val + 9 * (size_t)base + lane + (size_t)32 * 9 * k;
+#pragma unroll
+            for (int i = 0; i < 9; ++i) cv[(9 * k + i) * mc.S + l] = __ldg(vk + 32 * i);
+            cc[k * mc.S + l] = __ldg(g.bcol + base + 32 * k + lane);
+        }
+        mc.cv = cv;
+        mc.cc = cc;
+    }
     float4 *z4 = reinterpret_cast<float4 *>(g.q);
     float4 *const y4a = reinterpret_cast<float4 *>(g.pbuf0), *const y4b = reinterpret_cast<float4 *>(g.pbuf1);
     const int poly = g.poly;
@@ -895,7 +947,7 @@ __global__ void __launch_bounds__(1024, 1) cg_mixed_sr_kernel(const __grid_const
                 const int l = ps * gpb + grp;
                 const bool valid = l < nloc;
                 float t[3];
-                spmv_row_w(g, yin, a0 + l, sub, valid, t[0], t[1], t[2]);
+                spmv_row_w(g, mc, yin, a0 + l, l, sub, valid, t[0], t[1], t[2]);
                 if (!valid || sub != 0) continue;
                 float o[3];
 #pragma unroll
@@ -967,7 +1019,7 @@ __global__ void __launch_bounds__(1024, 1) cg_mixed_sr_kernel(const __grid_const
             const int l = ps * gpb + grp;
             const bool valid = l < nloc;
             float w0, w1, w2;
-            spmv_row_w(g, z4, a0 + l, sub, valid, w0, w1, w2);
+            spmv_row_w(g, mc, z4, a0 + l, l, sub, valid, w0, w1, w2);
             if (!valid || sub != 0) continue;
             sw[l] = w0; sw[npb + l] = w1; sw[2 * npb + l] = w2;
             const float r0 = sr[l], r1 = sr[npb + l], r2 = sr[2 * npb + l];
