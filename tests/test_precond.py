@@ -1,0 +1,148 @@
+"""The mixed path's Chebyshev polynomial preconditioner, restated in numpy on the oracle's viscosity matrix (CPU).
+
+cg_mixed_sr_kernel preconditions the CG_nomass solve with M^-1 = P_d(D^-1 V) D^-1, where 1 - lambda P_d(lambda)
+is the Chebyshev polynomial of degree d + 1 on [lambda_max / 30, lambda_max] scaled to 1 at 0, applied as d steps
+of the Chebyshev iteration for V z = r from z = 0. lambda_max comes from the Lanczos matrix of a Jacobi-PCG solve
+(step lengths alpha_i, direction coefficients beta_i). These tests check the algorithm itself on a Kuhn cube's
+matrix from the oracle (the reference's NoMass viscosity matrix, rigid modes shifted as the mixed path does):
+the Lanczos estimate, positive definiteness for even degrees whatever the estimate, and the iteration counts.
+"""
+import numpy as np
+import pytest
+import scipy.sparse as sp
+
+import pyoracle as po
+from gen_golden import case_mesh, sheared
+
+RATIO = 30.0
+
+
+def shifted_system(n=8, seed=21):
+    """V (vertex rows), the projected right-hand side and the shifted operator V + D Z G^-1 Z^T D."""
+    m = case_mesh(n, seed)
+    o = po.OracleBlob(m, solver="CG_nomass", dt=1e-12, kT=4.11e-21, calc_noise=1, calc_stokes=0, threads=1)
+    o.set_pos(sheared(m, 0.02))
+    o.step(1)
+    c = o.csr()
+    nv = m.n_linear
+    rows = np.repeat(np.arange(len(c["key"]) - 1), np.diff(c["key"]))
+    V = sp.csr_matrix((c["val"], (rows, c["col"])), shape=(3 * m.n_nodes, 3 * m.n_nodes))[:3 * nv][:, :3 * nv]
+    V = V.tocsr()
+    f = o.rhs()[:nv].ravel()
+    d = o.pos()[:nv] - o.pos()[:nv].mean(0)
+    Z = np.zeros((3 * nv, 6))
+    for k in range(3):
+        Z[k::3, k] = 1.0
+    Z[1::3, 3], Z[2::3, 3] = -d[:, 2], d[:, 1]
+    Z[0::3, 4], Z[2::3, 4] = d[:, 2], -d[:, 0]
+    Z[0::3, 5], Z[1::3, 5] = -d[:, 1], d[:, 0]
+    D = V.diagonal()
+    DZ = D[:, None] * Z
+    Gi = np.linalg.inv(Z.T @ DZ)
+    f = f - DZ @ (Gi @ (Z.T @ f))
+    return V, D, f, lambda x: V @ x + DZ @ (Gi @ (DZ.T @ x))
+
+
+def chebyshev(V, D, lmax, degree):
+    """z = P_d(D^-1 V) D^-1 r by the kernel's recurrence: y0 = D^-1 r / theta, res = D^-1 r - D^-1 V y0, then
+    dd = c1 dd + c2 res, z += dd, res -= D^-1 V dd."""
+    a, b = lmax / RATIO, lmax
+    theta, delta = (b + a) / 2, (b - a) / 2
+    sigma = theta / delta
+    rho = [1 / sigma]
+    for _ in range(degree):
+        rho.append(1 / (2 * sigma - rho[-1]))
+
+    def apply(r):
+        s = r / D
+        z = s / theta
+        dd = z.copy()
+        res = s - (V @ z) / D
+        for j in range(degree):
+            dd = rho[j + 1] * rho[j] * dd + 2 * rho[j + 1] / delta * res
+            z = z + dd
+            if j + 1 < degree:
+                res = res - (V @ dd) / D
+        return z
+
+    return apply
+
+
+def pcg(A, f, Minv, eps2=1e-20, imax=5000):
+    """Preconditioned CG stopping on |r|^2 < eps2 |f|^2; returns (iterations, step lengths, coefficients)."""
+    x = np.zeros_like(f)
+    r = f.copy()
+    z = Minv(r)
+    p = z.copy()
+    g = r @ z
+    f2 = f @ f
+    al, be = [], [0.0]
+    for it in range(imax):
+        q = A(p)
+        a = g / (p @ q)
+        al.append(a)
+        x += a * p
+        r -= a * q
+        if r @ r < eps2 * f2:
+            return it + 1, al, be
+        z = Minv(r)
+        gn = r @ z
+        be.append(gn / g)
+        p = z + (gn / g) * p
+        g = gn
+    return imax, al, be
+
+
+def lanczos_max(al, be, n=64):
+    n = min(n, len(al))
+    T = np.zeros((n, n))
+    for i in range(n):
+        T[i, i] = 1 / al[i] + (be[i] / al[i - 1] if i > 0 else 0.0)
+        if i + 1 < n:
+            T[i, i + 1] = T[i + 1, i] = np.sqrt(be[i + 1]) / al[i]
+    return float(np.linalg.eigvalsh(T).max())
+
+
+@pytest.fixture(scope="module")
+def system(oracle_built):
+    return shifted_system()
+
+
+def test_lanczos_estimate_of_lambda_max(system):
+    V, D, f, A = system
+    _, al, be = pcg(A, f, lambda r: r / D)
+    est = lanczos_max(al, be)
+    # the largest eigenvalue of D^-1 V (symmetrically scaled), by a dense solve
+    Ds = 1 / np.sqrt(D)
+    true = float(np.linalg.eigvalsh((sp.diags(Ds) @ V @ sp.diags(Ds)).toarray()).max())
+    assert 0.98 * true <= est <= 1.0001 * true
+
+
+@pytest.mark.parametrize("scale", [0.5, 1.05, 3.0])
+def test_even_degrees_stay_positive_definite(system, scale):
+    """M^-1 is symmetric positive definite for degrees 2 and 4 even when lambda_max is under- or overestimated."""
+    V, D, _, _ = system
+    Ds = 1 / np.sqrt(D)
+    lam = np.linalg.eigvalsh((sp.diags(Ds) @ V @ sp.diags(Ds)).toarray())
+    lmax = float(lam.max()) * scale
+    for degree in (2, 4):
+        M = chebyshev(V, D, lmax, degree)
+        Mi = np.column_stack([M(e) for e in np.eye(V.shape[0])[:, :60].T])[:60]
+        assert np.allclose(Mi, Mi.T, rtol=1e-9, atol=1e-12 * np.abs(Mi).max())
+        # the preconditioner's eigenvalues are P_d(lambda) D^-1: P_d > 0 on the whole spectrum of D^-1 V
+        a, b = lmax / RATIO, lmax
+        x = (b + a - 2 * lam) / (b - a)
+        T = np.polynomial.chebyshev.chebval(x, [0] * (degree + 1) + [1])
+        T0 = np.polynomial.chebyshev.chebval((b + a) / (b - a), [0] * (degree + 1) + [1])
+        P = np.where(lam > 1e-12 * b, (1 - T / T0) / np.maximum(lam, 1e-300), 1.0)
+        assert (P > 0).all(), (degree, scale, P.min())
+
+
+def test_chebyshev_cuts_iterations(system):
+    V, D, f, A = system
+    it_j, al, be = pcg(A, f, lambda r: r / D)
+    lmax = 1.05 * lanczos_max(al, be)
+    it2, _, _ = pcg(A, f, chebyshev(V, D, lmax, 2))
+    it4, _, _ = pcg(A, f, chebyshev(V, D, lmax, 4))
+    print("Jacobi", it_j, "Chebyshev 2", it2, "Chebyshev 4", it4)
+    assert it2 <= 0.5 * it_j and it4 <= 0.35 * it_j
