@@ -253,6 +253,62 @@ constexpr unsigned SRC_IDENTITY = 0xffffffffu;
 // SPLIT = true: three threads per slot, one per block row (a warp takes one block row of 32 consecutive slots
 // of a slice), for matrices too small to fill the GPU, where the length of each thread's FP64 chain sets the
 // time rather than the geometry reads.
+template <class R>
+__device__ __forceinline__ R sel3(const R (&x)[3], int i) {
+    return i == 0 ? x[0] : (i == 1 ? x[1] : x[2]);
+}
+
+// visc_entry for the 3x3 block of element nodes (a, b) from their gradients ga = grad psi_a, gb = grad psi_b:
+// entry (i, j) of the block is V[a + 4i][b + 4j]. Each case of visc_entry is symmetric under its mirror
+// (a, i) <-> (b, j) (products commute exactly), so the entry needs no swap and equals visc_entry's bit for bit.
+template <class R>
+__device__ __forceinline__ R visc_block_entry(const R (&ga)[3], const R (&gb)[3], bool same, R A, R B, R vol, int i,
+                                              int j) {
+    if (i == j) {
+        const R t = sel3(ga, i) * sel3(gb, i) * (A + B);
+        const R d2 = (ga[0] * gb[0] + ga[1] * gb[1] + ga[2] * gb[2]);
+        return (t + d2 * A) * vol;
+    }
+    if (same) return ((B + A) * (sel3(ga, i) * sel3(ga, j))) * vol;
+    return (B * (sel3(ga, i) * sel3(gb, j)) + A * (sel3(gb, i) * sel3(ga, j))) * vol;
+}
+
+// One assembly source: the gradients of its two element nodes, the element's volume and viscosity coefficients
+// (nothing for the identity source of a pinned row).
+template <class R>
+__device__ __forceinline__ void asm_load(const AsmArgs<R> &g, unsigned code, R (&ga)[3], R (&gb)[3], R (&vab)[3]) {
+    if (code == SRC_IDENTITY) return;
+    const int e = (int)(code >> 4), pa = (code >> 2) & 3, pb = code & 3;
+    const R *gm = g.geom + 16 * (size_t)e;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        ga[c] = gm[4 * c + pa];
+        gb[c] = gm[4 * c + pb];
+    }
+    vab[0] = gm[12];
+    vab[1] = g.A[e];
+    vab[2] = g.B[e];
+}
+
+// ... added to the thread's NB block rows (from block row b0) of the slot, entries in row-major order
+template <class R, int NB>
+__device__ __forceinline__ void asm_add(R (&v)[3 * NB], unsigned code, const R (&ga)[3], const R (&gb)[3],
+                                        const R (&vab)[3], int b0) {
+    if (code == SRC_IDENTITY) {
+#pragma unroll
+        for (int i = 0; i < NB; ++i)
+#pragma unroll
+            for (int j = 0; j < 3; ++j)
+                if (j == b0 + i) v[3 * i + j] += (R)1;
+        return;
+    }
+    const bool same = ((code >> 2) & 3) == (code & 3);
+#pragma unroll
+    for (int i = 0; i < NB; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) v[3 * i + j] += visc_block_entry<R>(ga, gb, same, vab[1], vab[2], vab[0], b0 + i, j);
+}
+
 template <class R, bool SPLIT>
 __global__ void __launch_bounds__(128) assemble_kernel(AsmArgs<R> g) {
     constexpr int NB = SPLIT ? 1 : 3;  // block rows per thread
@@ -269,33 +325,35 @@ __global__ void __launch_bounds__(128) assemble_kernel(AsmArgs<R> g) {
     R v[3 * NB];
 #pragma unroll
     for (int c = 0; c < 3 * NB; ++c) v[c] = (R)0.0;
-    for (int q = g.src_ptr[slot]; q < g.src_ptr[slot + 1]; ++q) {
-        const unsigned code = g.src[q];
-        if (code == SRC_IDENTITY) {
-#pragma unroll
-            for (int i = 0; i < NB; ++i) v[3 * i + b0 + i] += (R)1;
-            continue;
-        }
-        const int e = (int)(code >> 4), pa = (code >> 2) & 3, pb = code & 3;
-        const R *gm = g.geom + 16 * (size_t)e;
-        R dpsi[12];
-#pragma unroll
-        for (int m = 0; m < 12; ++m) dpsi[m] = gm[m];
-        const R vol = gm[12], A = g.A[e], B = g.B[e];
-#pragma unroll
-        for (int i = 0; i < NB; ++i)
-#pragma unroll
-            for (int j = 0; j < 3; ++j) v[3 * i + j] += visc_entry<R>(dpsi, A, B, vol, pa + 4 * (b0 + i), pb + 4 * j);
+    // two sources per trip: both sources' loads issue before either is summed (the sums keep registration order)
+    const int q1 = g.src_ptr[slot + 1];
+    int q = g.src_ptr[slot];
+    for (; q + 1 < q1; q += 2) {
+        const unsigned c0 = g.src[q], c1 = g.src[q + 1];
+        R a0[3], e0[3], w0[3], a1[3], e1[3], w1[3];
+        asm_load(g, c0, a0, e0, w0);
+        asm_load(g, c1, a1, e1, w1);
+        asm_add<R, NB>(v, c0, a0, e0, w0, b0);
+        asm_add<R, NB>(v, c1, a1, e1, w1, b0);
+    }
+    if (q < q1) {
+        const unsigned c0 = g.src[q];
+        R a0[3], e0[3], w0[3];
+        asm_load(g, c0, a0, e0, w0);
+        asm_add<R, NB>(v, c0, a0, e0, w0, b0);
     }
     if (k == g.diagk[a]) {
 #pragma unroll
-        for (int i = 0; i < NB; ++i) {
-            R &d = v[3 * i + b0 + i];
-            if (g.drag) d += (R)g.drag[a];
-            // calc_inverse_diagonal (src/SparseMatrixFixedPattern.cpp:305-312)
-            g.dinv[4 * a + b0 + i] = (R)1.0 / d;
-            if (g.diag) g.diag[4 * a + b0 + i] = d;
-        }
+        for (int i = 0; i < NB; ++i)
+#pragma unroll
+            for (int j = 0; j < 3; ++j) {
+                if (j != b0 + i) continue;
+                R &d = v[3 * i + j];
+                if (g.drag) d += (R)g.drag[a];
+                // calc_inverse_diagonal (src/SparseMatrixFixedPattern.cpp:305-312)
+                g.dinv[4 * a + j] = (R)1.0 / d;
+                if (g.diag) g.diag[4 * a + j] = d;
+            }
     }
     R *vp = g.val + 9 * (size_t)g.slice_ptr[s] + 32 * 9 * (size_t)k + lane + 32 * 3 * b0;
 #pragma unroll
