@@ -193,7 +193,7 @@ __global__ void __launch_bounds__(128) element_kernel(ElemArgs<R> g) {
             v[4 + a] = (R)g.vy[nd[a]];
             v[8 + a] = (R)g.vz[nd[a]];
         }
-#pragma unroll 1
+#pragma unroll
         for (int i = 0; i < 12; ++i) {
             R s = 0;
 #pragma unroll
