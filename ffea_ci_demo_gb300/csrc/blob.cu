@@ -395,16 +395,19 @@ struct BlobImpl final : ffea_gpu_blob {
             }
             if (cg_sr) {
                 // the first blocks of each owned row kept in shared memory for the solve, as many as the rest of
-                // the block's shared memory holds (FFEA_GPU_CG_CACHE=0 turns this off, for comparison runs)
+                // the block's shared memory holds (FFEA_GPU_CG_CACHE=n caps them at n, 0 turns the cache off, for
+                // comparison runs)
+                // The block's shared memory stops at 168 KB so that L1 (the rest of the SM's 256 KB) keeps the
+                // neighbours' exchanged vectors: on the 40^3 cube 6 cached blocks per row (167 KB) gave 20.8 us per
+                // iteration, the 9 that fit (223 KB) 21.4 us, none 22.3 us.
                 const char *cache = getenv("FFEA_GPU_CG_CACHE");
-                const long long avail =
-                    (long long)Launch<R>::cg_sr_smem_limit(device) - (long long)sr_smem_bytes(cg_npb, cg_poly);
+                const long long avail = std::min<long long>(Launch<R>::cg_sr_smem_limit(device), 168 * 1024) -
+                                        (long long)sr_smem_bytes(cg_npb, cg_poly);
                 const long long S = sr_cache_stride(cg_npb, tpn);
                 int maxlen = 0;
                 for (int a = 0; a < N; ++a) maxlen = std::max(maxlen, h.rowlen[a]);
-                cg_kc = (cache && cache[0] == '0') || avail <= 0
-                            ? 0
-                            : (int)std::min<long long>(maxlen, avail / (SR_CACHE_BYTES_PER_BLOCK * S));
+                cg_kc = avail <= 0 ? 0 : (int)std::min<long long>(maxlen, avail / (SR_CACHE_BYTES_PER_BLOCK * S));
+                if (cache) cg_kc = std::min(cg_kc, std::max(0, atoi(cache)));
             }
             if (cg_poly > 0) {
                 CK(mem.alloc(&cheb, (size_t)CHEB_STATE));
