@@ -74,7 +74,7 @@ constexpr size_t SS_PHASE = SS_PART + ss_round(3 * (size_t)SOLVE_MAX_BLOCKS);
 constexpr size_t SS_STATUS = SS_PHASE + 32;
 constexpr size_t SS_BARRIER = SS_STATUS + 32;
 constexpr size_t SS_TOTAL = SS_BARRIER + 32;
-static_assert(FFEA_GPU_CG_PHASES <= 32 && sizeof(DevStatus) <= 256 && sizeof(GridBarrier) <= 256,
+static_assert(FFEA_GPU_CG_PHASES == CG_PHASES && FFEA_GPU_CG_PHASES <= 32 && sizeof(DevStatus) <= 256 && sizeof(GridBarrier) <= 256,
               "scratch regions too small");
 
 static __device__ __align__(256) double g_solve_scratch[SS_TOTAL];

@@ -818,14 +818,30 @@ __device__ __forceinline__ void spmv_row(const A &g, const R *pold, R beta, bool
 
 constexpr int CG_MAX_THREADS = 1024;
 
-// phase timer of block 0, thread 0: adds the time since the previous mark to phase_ns[k]
+constexpr int CG_PHASES = 10;  // the phase timers' slots (FFEA_GPU_CG_PHASES of the C ABI)
+
+// Phase timers of block 0, thread 0: the time since the previous mark is added to a shared-memory slot k during
+// the solve (a read-modify-write of phase_ns in global memory at every mark would hold block 0 for an L2 round
+// trip each time) and the slots are added to phase_ns when the solve ends.
+#define FFEA_PHASES_BEGIN(t_prev)                                                  \
+    __shared__ unsigned long long s_phase_[CG_PHASES];                    \
+    unsigned long long t_prev = 0ull;                                              \
+    if (blockIdx.x == 0 && threadIdx.x == 0) {                                     \
+        for (int k_ = 0; k_ < CG_PHASES; ++k_) s_phase_[k_] = 0ull;       \
+        t_prev = globaltimer_ns();                                                 \
+    }
 #define FFEA_MARK(g, t_prev, k)                                                   \
     do {                                                                          \
         if (blockIdx.x == 0 && threadIdx.x == 0) {                                \
             const unsigned long long t_now_ = globaltimer_ns();                   \
-            (g).phase_ns[k] += t_now_ - (t_prev);                                 \
+            s_phase_[k] += t_now_ - (t_prev);                                     \
             (t_prev) = t_now_;                                                    \
         }                                                                         \
+    } while (0)
+#define FFEA_PHASES_END(g)                                                        \
+    do {                                                                          \
+        if (blockIdx.x == 0 && threadIdx.x == 0)                                  \
+            for (int k_ = 0; k_ < CG_PHASES; ++k_) (g).phase_ns[k_] += s_phase_[k_]; \
     } while (0)
 
 // FP64 CG: three phases (SpMV, residual update, direction update) with a grid barrier after each;
@@ -840,7 +856,7 @@ __global__ void __launch_bounds__(1024, 1) cg_kernel(const __grid_constant__ CgA
     __shared__ int s_conv;
     DevStatus *st = g.st;
     if (st->abort) return;
-    unsigned long long tm = (blockIdx.x == 0 && threadIdx.x == 0) ? globaltimer_ns() : 0ull;
+    FFEA_PHASES_BEGIN(tm);
     R *p = g.pbuf0;
     // p = z = D^{-1} r  (conjugate_gradient_residual_assume_x_zero, src/NoMassCGSolver.cpp:196-220)
     FFEA_NODE_LOOP(g, a) {
@@ -928,6 +944,7 @@ __global__ void __launch_bounds__(1024, 1) cg_kernel(const __grid_constant__ CgA
         if (!(ok = grid_sync_ep(g.gb, st, g.limit_ns, bar_ep))) break;
         FFEA_MARK(g, tm, 9);
     }
+    FFEA_PHASES_END(g);
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         if (!ok) {
             st->abort = 1;
@@ -1047,7 +1064,7 @@ __global__ void __launch_bounds__(1024, 1) cg_own_kernel(const __grid_constant__
     __shared__ int s_conv;
     DevStatus *st = g.st;
     if (st->abort) return;
-    unsigned long long tm = (blockIdx.x == 0 && threadIdx.x == 0) ? globaltimer_ns() : 0ull;
+    FFEA_PHASES_BEGIN(tm);
     const int npb = g.npb, a0 = blockIdx.x * npb;
     const int nloc = max(0, min(npb, g.N - a0));
     double *sx = snd, *sr = snd + 3 * npb, *sq = snd + 6 * npb, *sp = snd + 9 * npb;
@@ -1164,6 +1181,7 @@ __global__ void __launch_bounds__(1024, 1) cg_own_kernel(const __grid_constant__
             g.r[4 * a + c] = sr[c * npb + l];
         }
     }
+    FFEA_PHASES_END(g);
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         if (!ok) {
             st->abort = 1;

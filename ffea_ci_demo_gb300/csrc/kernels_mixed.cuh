@@ -205,7 +205,7 @@ __global__ void __launch_bounds__(1024, 1) cg_mixed_kernel(const __grid_constant
     DevStatus *st = g.st;
     if (st->abort) return;
     const bool defl = g.nmodes > 0;
-    unsigned long long tm = (blockIdx.x == 0 && threadIdx.x == 0) ? globaltimer_ns() : 0ull;
+    FFEA_PHASES_BEGIN(tm);
     float2 *partials = reinterpret_cast<float2 *>(g.partials);
     // set-up: G = Z^T D Z from the moments M, projected right-hand side
     grid_sum_df<MIXED_GATHER_NP>(reinterpret_cast<const float2 *>(g.init_partials), g.init_stride, g.n_init, s_sc);
@@ -344,6 +344,7 @@ __global__ void __launch_bounds__(1024, 1) cg_mixed_kernel(const __grid_constant
         }
         float *t = pold; pold = pnew; pnew = t;
     }
+    FFEA_PHASES_END(g);
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         if (!ok) {
             st->abort = 1;
@@ -543,7 +544,7 @@ __global__ void __launch_bounds__(1024, 1) cg_mixed_own_kernel(const __grid_cons
     DevStatus *st = g.st;
     if (st->abort) return;
     const bool defl = g.nmodes > 0;
-    unsigned long long tm = (blockIdx.x == 0 && threadIdx.x == 0) ? globaltimer_ns() : 0ull;
+    FFEA_PHASES_BEGIN(tm);
     float2 *partials = reinterpret_cast<float2 *>(g.partials);
     const int npb = g.npb, a0 = blockIdx.x * npb;
     const int nloc = max(0, min(npb, g.N - a0));
@@ -703,6 +704,7 @@ __global__ void __launch_bounds__(1024, 1) cg_mixed_own_kernel(const __grid_cons
             g.r[4 * a + c] = sr[c * npb + l];
         }
     }
+    FFEA_PHASES_END(g);
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         if (!ok) {
             st->abort = 1;
@@ -880,7 +882,7 @@ __global__ void __launch_bounds__(1024, 1) cg_mixed_sr_kernel(const __grid_const
     DevStatus *st = g.st;
     if (st->abort) return;
     const bool defl = g.nmodes > 0;
-    unsigned long long tm = (blockIdx.x == 0 && threadIdx.x == 0) ? globaltimer_ns() : 0ull;
+    FFEA_PHASES_BEGIN(tm);
     float2 *partials = reinterpret_cast<float2 *>(g.partials);
     const int npb = g.npb, a0 = blockIdx.x * npb;
     const int nloc = max(0, min(npb, g.N - a0));
@@ -1146,6 +1148,7 @@ __global__ void __launch_bounds__(1024, 1) cg_mixed_sr_kernel(const __grid_const
             g.r[4 * a + c] = sr[c * npb + l];
         }
     }
+    FFEA_PHASES_END(g);
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         if (!ok) {
             st->abort = 1;
