@@ -635,9 +635,9 @@ def main():
                 "bytes_per_launch_model": model_bytes, "bytes_per_launch_format": fmt_bytes,
                 "achieved_format": fmt_bytes / (cg_ms / 1e3) / 1e9, "ms_per_launch": cg_ms,
                 "cg_iters_per_launch": iters, "matrix_passes_per_launch": passes,
-                "note": "the 40^3 matrix (42 MB as 3x3 SELL blocks) stays in L2 and partly in shared memory across the "
-                        "launch's matrix passes: DRAM moves `traffic` bytes per launch, so a fraction above 1 is "
-                        "on-chip reuse of the model bytes, not DRAM bandwidth",
+                "note": "a matrix that fits in L2 (40 B per 3x3 block: 42 MB at 40^3 cells) stays there, and partly "
+                        "in shared memory, across the launch's matrix passes; DRAM then moves `traffic` bytes per "
+                        "launch (measured at 40^3), and a fraction above 1 is on-chip reuse of the model bytes",
                 "preconditioner": f"chebyshev degree {head['cg_poly']} (lambda_max {head['lambda_max']:.4f})"
                 if head["cg_poly"] else "jacobi"}
     line = {"metric": "node-steps/s", "value": head["value"], "unit": "node-steps/s", "n_gpus": ws,
