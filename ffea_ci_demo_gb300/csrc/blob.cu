@@ -413,8 +413,9 @@ struct BlobImpl final : ffea_gpu_blob {
                 CK(mem.alloc(&cheb, (size_t)CHEB_STATE));
                 CK(cudaMemset(cheb, 0, CHEB_STATE * sizeof(double)));
             }
-            if (cg_sr) {
-                // the blocks each block's SpMV reads z from: owners of the columns of its rows
+            // the FP64 owned-rows CG publishes its search direction the same way (CG_nomass's 3x3 pattern)
+            if (cg_sr || (!mixed && cg_npb > 0 && p.solver == FFEA_GPU_NOMASS_CG)) {
+                // the blocks each block's SpMV reads z (p) from: owners of the columns of its rows
                 std::vector<int> nbp(cg_grid + 1, 0), nbl;
                 std::vector<char> seen(cg_grid, 0);
                 for (int b = 0; b < cg_grid; ++b) {

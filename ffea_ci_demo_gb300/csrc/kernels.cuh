@@ -1087,7 +1087,7 @@ __global__ void __launch_bounds__(1024, 1) cg_own_kernel(const __grid_constant__
     grid_sum_d<2>(g.init_partials, g.init_stride, g.n_init, s_sc);
     const double f2 = s_sc[0];
     if (threadIdx.x == 0) { s_delta = s_sc[1]; s_conv = 0; }
-    unsigned int bar_ep = 0;  // grid barriers passed
+    unsigned int bar_ep = 0, nb_ep = 0;  // grid barriers passed, neighbour publications made
     bool ok = grid_sync_ep(g.gb, st, g.limit_ns, bar_ep);
     const int tpn = g.tpn, gpb = blockDim.x / tpn, grp = threadIdx.x / tpn, sub = threadIdx.x % tpn;
     const int npass = (nloc + gpb - 1) / gpb;
@@ -1170,7 +1170,14 @@ __global__ void __launch_bounds__(1024, 1) cg_own_kernel(const __grid_constant__
             p2[2 * a] = make_double2(pv[0], pv[1]);
             p2[2 * a + 1] = make_double2(pv[2], 0.0);
         }
-        if (!(ok = grid_sync_ep(g.gb, st, g.limit_ns, bar_ep))) break;
+        // the next SpMV reads p only at the rows of the blocks owning its rows' columns: with their lists
+        // (g.flags), wait for those blocks' publication rather than for the whole grid. Every block has finished
+        // this iteration's SpMV (it precedes the two barriers above) before any block overwrites its p.
+        if (g.flags) {
+            if (!(ok = neighbour_sync(g, ++nb_ep, st))) break;
+        } else if (!(ok = grid_sync_ep(g.gb, st, g.limit_ns, bar_ep))) {
+            break;
+        }
         FFEA_MARK(g, tm, 9);
     }
     for (int l = threadIdx.x; l < nloc; l += blockDim.x) {
