@@ -365,6 +365,11 @@ struct BlobImpl final : ffea_gpu_blob {
         const long long lanes = (long long)cg_grid * cg_block;
         tpn = 8;
         while (tpn > 1 && (long long)N * tpn > lanes) tpn >>= 1;
+        // FFEA_GPU_CG_TPN=1, 2, 4 or 8 sets the lanes per matrix row (for comparison runs)
+        if (const char *t = getenv("FFEA_GPU_CG_TPN")) {
+            const int v = atoi(t);
+            if (v == 1 || v == 2 || v == 4 || v == 8) tpn = v;
+        }
         partial_stride = cg_grid;
         // each block keeps a run of rows in shared memory when they fit (FFEA_GPU_CG_OWN=0 turns this off);
         // the run is a multiple of a warp's rows so that a warp's rows share a SELL slice
