@@ -421,9 +421,9 @@ struct BlobImpl final : ffea_gpu_blob {
             // the FP64 owned-rows CG publishes its search direction the same way (CG_nomass's 3x3 pattern)
             if (cg_sr || (!mixed && cg_npb > 0 && p.solver == FFEA_GPU_NOMASS_CG)) {
                 // the blocks each block's SpMV reads z (p) from: owners of the columns of its rows. The pattern is
-                // symmetric (an element couples each pair of its unpinned nodes both ways; a pinned row keeps only its diagonal
-                // and no row has its column), so these
-                // are also the blocks that read from it, which the exchange's buffer reuse relies on.
+                // symmetric (an element couples each pair of its unpinned nodes both ways; a pinned row keeps only
+                // its diagonal and no row has its column), so these are also the blocks that read from it, which
+                // the exchange's buffer reuse relies on.
                 std::vector<int> nbp(cg_grid + 1, 0), nbl;
                 std::vector<char> seen(cg_grid, 0);
                 for (int b = 0; b < cg_grid; ++b) {
