@@ -20,8 +20,9 @@ to the forward window.
 Metric: node-steps/s = vertex nodes x steps / time (whole job, all GPUs).
 Default arm: the mixed-precision GPU path (headline), with the plain FP64
 GPU path timed beside it. `--impl reference` times the reference algorithm on
-the host cores instead (the oracle's C restatement with OpenMP, since the
-reference sources are not on the benchmark machine).
+the host cores instead: the oracle's C restatement with OpenMP (kind "port"),
+because the reference's own sources do not travel to the benchmark machine, so
+its compiled build (oracle/_ref) exists only where the sources are.
 
 Timing: W untimed warm-up steps, then K steps each timed by CUDA events on
 the blob's stream, with 256 MiB of scratch written before every step outside
@@ -172,28 +173,34 @@ def measured_peak() -> tuple[float, str]:
         return 6800.0, "fallback"
 
 
-def profiled_traffic(precision: str):
-    """Per-launch DRAM bytes of cg_kernel from the committed ncu summary, if one exists."""
-    path = os.path.join(ROOT, "profiles", f"cg_kernel_{precision}_cube40.txt")
+def profiled(name: str, key: str):
+    """A figure from a committed ncu summary (profiles/<name>.txt, `key = value` lines), or None."""
+    path = os.path.join(ROOT, "profiles", name + ".txt")
     try:
         for ln in open(path):
-            if ln.startswith("dram_bytes_per_launch_full_size"):
+            if ln.split("=")[0].strip() == key:
                 return float(ln.split("=")[1].split()[0])
     except (OSError, ValueError, IndexError):
         pass
     return None
 
 
-def profiled_batch_traffic_ratio():
-    """DRAM bytes per model byte of cg_batch_kernel, from the committed ncu summary, if one exists."""
-    path = os.path.join(ROOT, "profiles", "cg_batch_kernel_ensemble64.txt")
+def cpu_model() -> str:
+    """The host CPU's model name (lscpu, else /proc/cpuinfo)."""
     try:
-        for ln in open(path):
-            if ln.startswith("dram_bytes_per_model_byte"):
-                return float(ln.split("=")[1].split()[0])
-    except (OSError, ValueError, IndexError):
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for ln in out.splitlines():
+            if ln.startswith("Model name:"):
+                return ln.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
         pass
-    return None
+    try:
+        for ln in open("/proc/cpuinfo"):
+            if ln.lower().startswith(("model name", "cpu part")):
+                return ln.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    return "unknown"
 
 
 _PINNED = []
@@ -226,6 +233,26 @@ def cg_format_bytes_per_iteration(blocks: int, nodes: int, p: int) -> float:
     """Bytes the SELL 3x3-block matrix actually holds per SpMV (values + block columns + row data)
     plus eight passes over padded 4-wide vectors."""
     return blocks * (9 * p + 4) + nodes * 8 + 8 * nodes * 4 * p
+
+
+def cheb_pass_bytes(n: int, p: int) -> float:
+    """One extra matrix pass of the Chebyshev preconditioner by the per-unit model's terms: the matrix
+    (nnz (p + 4) + (R + 1) 4) and two vector passes (2 R p)."""
+    from ffea_ci_demo_gb300.mesh import counts
+
+    c = counts(n)
+    R = 3 * c["N"]
+    return c["nnz_linear"] * (p + 4) + (R + 1) * 4 + 2 * R * p
+
+
+def masslumped_bytes_per_step(n: int, p: int) -> float:
+    """Compulsory bytes of one mass-lumped step by the per-unit model:
+    T (16 + 14 p + 16) + N 48 + 2 (12 T p) + 16 T + 4 (N + 1) + N (24 + 8 + 96)."""
+    from ffea_ci_demo_gb300.mesh import counts
+
+    c = counts(n)
+    T, N = c["T"], c["N"]
+    return T * (16 + 14 * p + 16) + N * 48 + 2 * 12 * T * p + 16 * T + 4 * (N + 1) + N * (24 + 8 + 96)
 
 
 def run_gpu_arm(args, ws, rank, local) -> dict | None:
@@ -262,7 +289,7 @@ def run_gpu_arm(args, ws, rank, local) -> dict | None:
         nl, ne, nb = blob.sizes()
         out[prec] = {"ms": ms, "steps": steps, "value": ws * N * steps / (ms / 1e3), "phase_ms": t["phase_ms"],
                      "cg_iters_per_step": iters / steps, "launches": launches, "clocks": clk.summary(),
-                     "blocks": nb, "cg_poly": deg, "lambda_max": lmax}
+                     "blocks": nb, "cg_poly": deg, "lambda_max": lmax, "cg_kernel": blob.cg_kernel()}
         if prec == args.headline:
             # end to end through the C ABI: every node's host position (the reference's layout, midpoints
             # included, in pinned host memory) in, one step, every position out
@@ -282,19 +309,26 @@ def run_gpu_arm(args, ws, rank, local) -> dict | None:
             out[prec]["e2e"] = {"value": ws * N * k / e2e_s, "unit": "node-steps/s", "h2d_bytes_per_step": nbytes,
                                 "d2h_bytes_per_step": nbytes, "steps": k, "host_memory": mem_kind}
         blob.close()
-    # kT = 0 error of the mixed path against the FP64 path (same initial shear)
+    # kT = 0 error of the mixed path (the timed arithmetic: same kernel, same preconditioner) against the FP64
+    # path from the same initial shear, after error_steps steps; the stated bound is 1e-5 after 1000 steps
     if args.precision == "both" and args.error_steps > 0:
         p0 = apply_shear(mesh, 0.02, seed=3) * (mesh.scale / MESO_LENGTH)
-        res = {}
+        res, how = {}, {}
         for prec in ("fp64", "mixed"):
             b = lib.Blob(mesh, precision=prec, **dict(PHYS, kT=0.0, calc_noise=0))
             b.set_state(pos=p0)
-            b.update(args.error_steps)
+            b.update(min(2, args.error_steps))
+            how[prec] = (b.cg_kernel(), b.cg_preconditioner()[0])
+            b.update(args.error_steps - min(2, args.error_steps))
             res[prec] = b.pos()
             b.close()
         d = np.abs(res["mixed"] - res["fp64"]).max() / np.abs(res["fp64"] - p0).max()
         out["error"] = {"kT0_steps": args.error_steps, "max_abs_disp_err_rel_to_max_disp": float(d),
-                        "reference": "FP64 GPU path (bit-exact element math vs the reference; CG to rounding)"}
+                        "bound": 1e-5, "within_bound": bool(d <= 1e-5),
+                        "mixed_arithmetic": f"{how['mixed'][0]}, chebyshev degree {how['mixed'][1]}"
+                        if how["mixed"][1] else f"{how['mixed'][0]}, jacobi",
+                        "reference": "FP64 GPU path (bit-exact element math vs the reference; CG to rounding; "
+                                     "tied to the oracle at this size by tests/test_headline.py)"}
     # kT > 0: both paths from the same state with the same noise stream; RMS position difference against the
     # RMS displacement, and each path's mean strain energy against equipartition, (3N - 6) kT / 2
     if args.precision == "both" and args.kt_steps > 0:
@@ -377,13 +411,18 @@ def run_batch(args, ws) -> dict:
            "cg_iters_per_blob": {"min": int(last.min()), "mean": float(last.mean()), "max": int(last.max())},
            "launch_config": cfg, "tuned_best_solve_ms": tuned_ms, "gpu_launches": launches,
            "clocks": clk.summary(),
-           "roofline": {"bound": "hbm", "kernel": "whole step (cg_batch_kernel dominant)",
-                        "achieved": model / (ms / 1e3) / 1e9, "peak": peak, "unit": "GB/s",
-                        "frac": model / (ms / 1e3) / 1e9 / peak, "peak_source": peak_kind,
-                        "traffic": (model * ratio) if (ratio := profiled_batch_traffic_ratio()) else None,
-                        "traffic_note": "DRAM bytes per step scaled from the 64-blob ncu capture by model bytes",
-                        "bytes_per_step_model_cg": model, "bytes_per_step_format_cg": fmt,
-                        "achieved_format": fmt / (ms / 1e3) / 1e9}}
+           "roofline": {"bound": "hbm", "kernel": "cg_batch_kernel (CG bytes over the whole step's time)",
+                        "achieved": fmt / (ms / 1e3) / 1e9, "peak": peak, "unit": "GB/s",
+                        "frac": fmt / (ms / 1e3) / 1e9 / peak, "peak_source": peak_kind,
+                        "bytes": "SELL format per CG iteration of each blob x its iterations",
+                        "traffic": (fmt * ratio) if (ratio := profiled("cg_batch_kernel_ensemble64",
+                                                                       "dram_bytes_per_format_byte")) else None,
+                        "traffic_note": "DRAM bytes per step scaled by format bytes from the ncu capture of a timed "
+                                        "launch of the 64-blob ensemble (profiles/cg_batch_kernel_ensemble64.txt)",
+                        "dram_frac_cg_kernel": profiled("cg_batch_kernel_ensemble64", "dram_throughput_pct") / 100
+                        if profiled("cg_batch_kernel_ensemble64", "dram_throughput_pct") else None,
+                        "bytes_per_step_format_cg": fmt, "bytes_per_step_model_cg": model,
+                        "model_equiv_gbs": model / (ms / 1e3) / 1e9}}
     if not args.no_fp64_sample:
         # plain FP64 GPU path, one blob at a time (the reference's order): a stratified sample of the
         # blobs sorted by size, scaled to the whole ensemble
@@ -475,9 +514,13 @@ def run_scale(args) -> dict:
     peak, peak_kind = measured_peak()
     out = {"workload": f"kuhn-cube-{n}: {c['T']} tets, {N} nodes, side {5 * n} nm, kT=4.11e-21 J",
            "cells_per_side": n, "tets": c["T"], "nodes": N}
+    solvers = args.scale_solvers.split(",")
+    precisions = args.scale_precisions.split(",")
     for solver, dt in (("CG_nomass", 1e-12), ("masslumped", args.scale_lumped_dt)):
+        if solver not in solvers:
+            continue
         res = {"dt": dt}
-        for prec in ("mixed", "fp64"):
+        for prec in precisions:
             b = lib.Blob(mesh, precision=prec, **dict(PHYS, solver=solver, dt=dt))
             b.update(2)
             deg = b.cg_preconditioner()[0]
@@ -486,31 +529,59 @@ def run_scale(args) -> dict:
             t = b.update_timed(k, FLUSH_BYTES)
             it = (b.cg_iterations()[1] - it0) / k
             r = {"value": N * k / (t["ms"] / 1e3), "ms_per_step": t["ms"] / k, "cg_iters_per_step": it,
-                 "phase_ms_per_step": {q: v / k for q, v in t["phase_ms"].items()}}
+                 "phase_ms_per_step": {q: v / k for q, v in t["phase_ms"].items()}, "cg_kernel": b.cg_kernel()}
+            p = 4 if prec == "mixed" else 8
             if solver == "CG_nomass":
-                p = 4 if prec == "mixed" else 8
+                # the HBM anchor: at this size the matrix (165 MB mixed in SELL form) no longer fits in L2. The
+                # bytes the format must stream per iteration (40 B per 3x3 block mixed, 76 B FP64, plus eight
+                # vector passes) give the fraction; the per-unit model counts a scalar CSR (8 or 12 B per scalar
+                # nonzero) and is reported as an equivalent rate only
                 cg_ms = t["phase_ms"]["cg"] / k
-                model = it * (1 + deg) * cg_bytes_per_iteration(n, p)
-                r["roofline_cg"] = {"achieved": model / (cg_ms / 1e3) / 1e9, "peak": peak, "unit": "GB/s",
-                                    "frac": model / (cg_ms / 1e3) / 1e9 / peak, "peak_source": peak_kind,
-                                    "preconditioner": f"chebyshev degree {deg}" if deg else "jacobi"}
+                passes = it * (1 + deg)
+                fmt = passes * cg_format_bytes_per_iteration(b.sizes()[2], N, p)
+                model = passes * cg_bytes_per_iteration(n, p)
+                name = f"{b.cg_kernel()}_{prec}_cube{n}"
+                traffic = profiled(name, "dram_bytes_per_launch")
+                r["roofline_cg"] = {
+                    "bound": "hbm", "kernel": b.cg_kernel(), "achieved": fmt / (cg_ms / 1e3) / 1e9, "peak": peak,
+                    "unit": "GB/s", "frac": fmt / (cg_ms / 1e3) / 1e9 / peak, "peak_source": peak_kind,
+                    "bytes": "SELL format per iteration x iterations", "ms_per_launch": cg_ms,
+                    "traffic": traffic, "traffic_source": f"profiles/{name}.txt" if traffic else None,
+                    "dram_frac": (traffic / (cg_ms / 1e3) / 1e9 / peak) if traffic else None,
+                    "model_equiv_gbs": model / (cg_ms / 1e3) / 1e9,
+                    "preconditioner": f"chebyshev degree {deg}" if deg else "jacobi"}
+            else:
+                step_bytes = masslumped_bytes_per_step(n, p)
+                el_ms = t["phase_ms"]["element"] / k
+                r["roofline"] = {"bound": "hbm", "kernel": "whole step (element_kernel dominant)",
+                                 "achieved": step_bytes / (t["ms"] / k / 1e3) / 1e9, "peak": peak, "unit": "GB/s",
+                                 "frac": step_bytes / (t["ms"] / k / 1e3) / 1e9 / peak, "peak_source": peak_kind,
+                                 "bytes_per_step": step_bytes, "element_ms_per_step": el_ms,
+                                 "traffic_element": profiled(f"element_kernel_{prec}_lumped_cube{n}",
+                                                             "dram_bytes_per_launch")}
             res[prec] = r
             b.close()
-        res["speedup_mixed_vs_fp64"] = res["mixed"]["value"] / res["fp64"]["value"]
+        if "mixed" in res and "fp64" in res:
+            res["speedup_mixed_vs_fp64"] = res["mixed"]["value"] / res["fp64"]["value"]
         # kT = 0 error of the mixed path against the FP64 path (same initial shear)
-        p0 = apply_shear(mesh, 0.02, seed=3) * (mesh.scale / MESO_LENGTH)
-        xs = {}
-        for prec in ("fp64", "mixed"):
-            b = lib.Blob(mesh, precision=prec, **dict(PHYS, solver=solver, dt=dt, kT=0.0, calc_noise=0))
-            b.set_state(pos=p0)
-            b.update(args.scale_error_steps)
-            xs[prec] = b.pos()
-            b.close()
-        res["kT0_error"] = {"steps": args.scale_error_steps,
-                            "max_abs_disp_err_rel_to_max_disp":
-                                float(np.abs(xs["mixed"] - xs["fp64"]).max() / np.abs(xs["fp64"] - p0).max())}
+        if args.scale_error_steps > 0:
+            p0 = apply_shear(mesh, 0.02, seed=3) * (mesh.scale / MESO_LENGTH)
+            xs = {}
+            for prec in ("fp64", "mixed"):
+                b = lib.Blob(mesh, precision=prec, **dict(PHYS, solver=solver, dt=dt, kT=0.0, calc_noise=0))
+                b.set_state(pos=p0)
+                b.update(args.scale_error_steps)
+                xs[prec] = b.pos()
+                b.close()
+            res["kT0_error"] = {"steps": args.scale_error_steps,
+                                "max_abs_disp_err_rel_to_max_disp":
+                                    float(np.abs(xs["mixed"] - xs["fp64"]).max() / np.abs(xs["fp64"] - p0).max())}
         out[solver] = res
     return out
+
+
+CPU_FLAGS = "-O3 -ffast-math -fopenmp (the reference's release flags without -march=native: the same build " \
+            "must give the same results on x86 and Arm hosts)"
 
 
 def cpu_sample(n: int, threads: int, budget_s: float, max_steps: int, warmup: int = 1):
@@ -537,7 +608,76 @@ def cpu_sample(n: int, threads: int, budget_s: float, max_steps: int, warmup: in
     return {"value": N * done / dt, "unit": "node-steps/s", "cores": threads, "kind": "port",
             "sample": f"{done} full steps (after {warmup} warm-up) of the {n}^3-cell cube, {N} nodes, "
                       f"{o.total_cg_iters() / max(1, done + warmup):.0f} CG iterations/step",
-            "seconds": dt, "steps": done}
+            "seconds": dt, "steps": done, "cpu_model": cpu_model(), "flags": CPU_FLAGS}
+
+
+def headline_roofline(args, head: dict) -> dict:
+    """Roofline of the headline CG launch. The unit is one CG iteration by the per-unit model,
+    nnz (p + 4) + (R + 1) 4 + 8 R p bytes, so achieved = iterations x that / launch time (CUDA events on the
+    blob's stream) against the measured HBM copy rate. The Chebyshev preconditioner's extra matrix passes are
+    listed apart, at their own bytes (matrix + two vector passes). A matrix that stays in L2 is bounded by L2
+    and synchronisation, not HBM: the `l2` object gives the L2 (lts) throughput and the DRAM bytes that ncu
+    measured on one full-size launch (profiles/)."""
+    peak, peak_kind = measured_peak()
+    p = 4 if args.headline == "mixed" else 8
+    iters = head["cg_iters_per_step"]
+    deg = head["cg_poly"]
+    cg_ms = head["phase_ms"]["cg"] / head["steps"]
+    unit = cg_bytes_per_iteration(args.cells, p)
+    achieved = iters * unit / (cg_ms / 1e3) / 1e9
+    extra = iters * deg * cheb_pass_bytes(args.cells, p)
+    kernel = head["cg_kernel"]
+    prof = f"{kernel}_{args.headline}_cube{args.cells}"
+    traffic = profiled(prof, "dram_bytes_per_launch")
+    l2_resident = head["blocks"] * (9 * p + 4) <= 64e6
+    r = {"bound": "hbm", "kernel": kernel, "achieved": achieved, "peak": peak, "unit": "GB/s",
+         "frac": achieved / peak, "peak_source": peak_kind, "traffic": traffic,
+         "unit_of_work": "one CG iteration (per-unit model bytes)", "bytes_per_unit": unit,
+         "units_per_launch": iters, "ms_per_launch": cg_ms,
+         "preconditioner": f"chebyshev degree {deg} (lambda_max {head['lambda_max']:.4f})" if deg else "jacobi"}
+    if deg:
+        r["chebyshev_passes"] = {"passes_per_launch": iters * deg, "bytes_per_pass": cheb_pass_bytes(args.cells, p),
+                                 "achieved_incl_passes": (iters * unit + extra) / (cg_ms / 1e3) / 1e9}
+    if l2_resident:
+        lts = profiled(prof, "lts_throughput_pct")
+        r["l2"] = {"bound": "l2", "matrix_bytes_sell": head["blocks"] * (9 * p + 4),
+                   "lts_throughput_frac": lts / 100 if lts is not None else None,
+                   "dram_bytes_per_launch": traffic, "source": f"profiles/{prof}.txt",
+                   "note": "the matrix stays in L2 (and partly in shared memory) across the launch's matrix passes; "
+                           "DRAM sees about one read of it per launch after the L2 flush, so the launch is bound by "
+                           "L2 latency and grid synchronisation, and the HBM fraction is a rate, not HBM use"}
+    return r
+
+
+def summary(line: dict) -> dict:
+    """The figures a reader needs first, repeated compactly at the end of the line."""
+    def g(d, *ks):
+        for k in ks:
+            if not isinstance(d, dict) or k not in d:
+                return None
+            d = d[k]
+        return d
+
+    def r3(x):
+        return None if x is None else float(f"{x:.4g}")
+
+    out = {"value": r3(line.get("value")), "e2e": r3(g(line, "e2e", "value")),
+           "ms_per_step": r3(line.get("ms_per_step")), "roofline_frac": r3(g(line, "roofline", "frac")),
+           "l2_frac": r3(g(line, "roofline", "l2", "lts_throughput_frac")),
+           "fp64_value": r3(g(line, "fp64_path", "value")), "mixed_over_fp64": r3(line.get("speedup_vs_fp64_path")),
+           "kT0_err_1000": r3(g(line, "error", "max_abs_disp_err_rel_to_max_disp")),
+           "kT0_err_steps": g(line, "error", "kT0_steps"),
+           "batch_value": r3(g(line, "batched", "value")), "batch_e2e": r3(g(line, "batched", "e2e", "value")),
+           "batch_frac_format": r3(g(line, "batched", "roofline", "frac")),
+           "batch_over_fp64": r3(g(line, "batched", "speedup_vs_fp64_path")),
+           "scale_nomass_mixed": r3(g(line, "scale", "CG_nomass", "mixed", "value")),
+           "scale_nomass_frac": r3(g(line, "scale", "CG_nomass", "mixed", "roofline_cg", "frac")),
+           "scale_lumped_mixed": r3(g(line, "scale", "masslumped", "mixed", "value")),
+           "scale_lumped_frac": r3(g(line, "scale", "masslumped", "mixed", "roofline", "frac")),
+           "adjoint_cost_mixed": r3(g(line, "adjoint", "mixed", "gradient_cost_over_forward")),
+           "adjoint_fd_rel_err": r3(g(line, "adjoint", "fd_check", "rel_err")),
+           "cpu": r3(g(line, "cpu_baseline", "value")), "cpu_1thread": r3(g(line, "cpu_baseline", "value_1_thread"))}
+    return {k: v for k, v in out.items() if v is not None}
 
 
 def main():
@@ -548,11 +688,14 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--precision", choices=["both", "mixed", "fp64"], default="both")
     ap.add_argument("--cells", type=int, default=N_CELLS)
-    ap.add_argument("--error-steps", type=int, default=100)
+    ap.add_argument("--error-steps", type=int, default=1000,
+                    help="kT = 0 steps of the mixed against the FP64 path (the stated bound is for 1000)")
     ap.add_argument("--kt-steps", type=int, default=200, help="kT > 0 comparison of the two paths (0: skip)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", choices=["both", "single", "batch"], default="both",
-                    help="single: the 40^3 blob (headline); batch: the replica ensemble; both: both in one line")
+    ap.add_argument("--no-cpu-1thread", action="store_true", help="skip the 1-thread CPU step")
+    ap.add_argument("--workload", choices=["both", "single", "batch", "scale"], default="both",
+                    help="single: the 40^3 blob (headline); batch: the replica ensemble; scale: the 64^3 cube only "
+                         "(a JSON object, not a bench line; for profiling); both: all in one line")
     ap.add_argument("--blobs", type=int, default=256)
     ap.add_argument("--batch-steps", type=int, default=10,
                     help="timed steps of the replica ensemble (its stiffest blobs are explicitly unstable at "
@@ -569,6 +712,8 @@ def main():
     ap.add_argument("--scale-steps", type=int, default=5)
     ap.add_argument("--scale-error-steps", type=int, default=20)
     ap.add_argument("--scale-lumped-dt", type=float, default=1e-12)
+    ap.add_argument("--scale-solvers", default="CG_nomass,masslumped")
+    ap.add_argument("--scale-precisions", default="mixed,fp64")
     ap.add_argument("--no-adjoint", action="store_true")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
@@ -581,19 +726,23 @@ def main():
             return
         # each step is one full blob step of the same workload, run by the reference algorithm on all host
         # cores; the number of timed steps is capped so that the run stays within a few minutes
-        r = cpu_sample(args.cells, threads, budget_s=150.0, max_steps=args.steps, warmup=min(args.warmup, 1))
+        r = cpu_sample(args.cells, threads, budget_s=150.0, max_steps=args.steps, warmup=args.warmup)
         line = {"metric": "node-steps/s", "value": r["value"], "unit": "node-steps/s", "n_gpus": args.gpus,
-                "steps": r["steps"], "warmup": min(args.warmup, 1), "ms_per_step": 1e3 * r["seconds"] / r["steps"],
+                "steps": r["steps"], "warmup": args.warmup, "ms_per_step": 1e3 * r["seconds"] / r["steps"],
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
                 "data": "synthetic (seeded Kuhn cube)", "config": workload_config(args.cells, "fp64"),
                 "impl": "reference",
-                "cpu_baseline": {k: r[k] for k in ("value", "unit", "cores", "kind", "sample")},
+                "cpu_baseline": {k: r[k] for k in ("value", "unit", "cores", "kind", "sample", "cpu_model", "flags")},
                 "e2e": {"value": r["value"], "unit": "node-steps/s", "h2d_bytes_per_step": 0,
                         "d2h_bytes_per_step": 0}}
         print(json.dumps(line), flush=True)
         return
 
     pick_device(local)
+    if args.workload == "scale":
+        if rank == 0:
+            print(json.dumps({"scale": run_scale(args)}), flush=True)
+        return
     if args.workload == "batch":
         if ws > 1:
             if rank == 0:
@@ -616,38 +765,16 @@ def main():
     if rank != 0:
         return
     head = res[args.headline]
-    peak, peak_kind = measured_peak()
-    p = 4 if args.headline == "mixed" else 8
-    iters = head["cg_iters_per_step"]
-    passes = iters * (1 + head["cg_poly"])  # matrix passes: one per iteration, plus the polynomial's
-    cg_ms = head["phase_ms"]["cg"] / head["steps"]
-    model_bytes = passes * cg_bytes_per_iteration(args.cells, p)
-    fmt_bytes = passes * cg_format_bytes_per_iteration(head["blocks"], (args.cells + 1) ** 3, p)
-    achieved = model_bytes / (cg_ms / 1e3) / 1e9
-    own = not os.environ.get("FFEA_GPU_CG_OWN", "1").startswith("0")
-    sr = own and not os.environ.get("FFEA_GPU_CG_SR", "1").startswith("0")
-    if args.headline == "fp64":
-        cg_name = "cg_own_kernel" if own else "cg_kernel"
-    else:
-        cg_name = "cg_mixed_sr_kernel" if sr else ("cg_mixed_own_kernel" if own else "cg_mixed_kernel")
-    roofline = {"bound": "hbm", "kernel": cg_name, "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "frac": achieved / peak, "peak_source": peak_kind, "traffic": profiled_traffic(args.headline),
-                "bytes_per_launch_model": model_bytes, "bytes_per_launch_format": fmt_bytes,
-                "achieved_format": fmt_bytes / (cg_ms / 1e3) / 1e9, "ms_per_launch": cg_ms,
-                "cg_iters_per_launch": iters, "matrix_passes_per_launch": passes,
-                "note": "a matrix that fits in L2 (40 B per 3x3 block: 42 MB at 40^3 cells) stays there, and partly "
-                        "in shared memory, across the launch's matrix passes; DRAM then moves `traffic` bytes per "
-                        "launch (measured at 40^3), and a fraction above 1 is on-chip reuse of the model bytes",
-                "preconditioner": f"chebyshev degree {head['cg_poly']} (lambda_max {head['lambda_max']:.4f})"
-                if head["cg_poly"] else "jacobi"}
+    line_roofline = headline_roofline(args, head)
     line = {"metric": "node-steps/s", "value": head["value"], "unit": "node-steps/s", "n_gpus": ws,
             "steps": head["steps"], "warmup": args.warmup, "ms_per_step": head["ms"] / head["steps"],
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32+f64" if args.headline == "mixed" else "f64", "data": "synthetic (seeded Kuhn cube)",
             "config": dict(workload_config(args.cells, args.headline), parallelism=f"replicas x{ws}"),
             "clocks": head["clocks"], "e2e": head["e2e"], "gpu_launches": head["launches"],
-            "roofline": roofline, "phase_ms_per_step": {k: v / head["steps"] for k, v in head["phase_ms"].items()},
-            "cg_iters_per_step": iters}
+            "roofline": line_roofline,
+            "phase_ms_per_step": {k: v / head["steps"] for k, v in head["phase_ms"].items()},
+            "cg_iters_per_step": head["cg_iters_per_step"]}
     if "fp64" in res and args.headline != "fp64":
         f = res["fp64"]
         line["fp64_path"] = {"value": f["value"], "ms_per_step": f["ms"] / f["steps"], "steps": f["steps"],
@@ -669,6 +796,11 @@ def main():
         line["cpu_baseline"] = cpu_sample(args.cells, os.cpu_count() or 1, budget_s=20.0, max_steps=3)
         line["cpu_baseline"].pop("seconds")
         line["cpu_baseline"].pop("steps")
+        if not args.no_cpu_1thread:
+            one = cpu_sample(args.cells, 1, budget_s=0.0, max_steps=1, warmup=0)
+            line["cpu_baseline"]["value_1_thread"] = one["value"]
+            line["cpu_baseline"]["sample_1_thread"] = one["sample"]
+    line["summary"] = summary(line)
     print(json.dumps(line), flush=True)
 
 

@@ -84,7 +84,9 @@ std::mutex g_solve_mutex;  // held for a whole call: the array is shared by ever
 double *g_solve_ptr[SOLVE_STATIC_MAX_DEVICES] = {};
 
 // Device address of g_solve_scratch on `device`: looked up once per device, with that device
-// current, and cached. The first lookup also loads this library's module on the device.
+// current, and cached. The first lookup also loads this file's module on the device (CUDA loads
+// modules lazily), which is when the array itself is placed in device memory, so blob creation
+// makes this lookup for every blob that can use the allocation-free solve.
 int solve_scratch(int device, double **out) {
     if (device < 0 || device >= SOLVE_STATIC_MAX_DEVICES) {
         g_last_error = "ffea_gpu_blob_solve_static: device ordinal beyond the scratch table";
@@ -365,27 +367,22 @@ struct BlobImpl final : ffea_gpu_blob {
         const long long lanes = (long long)cg_grid * cg_block;
         tpn = 8;
         while (tpn > 1 && (long long)N * tpn > lanes) tpn >>= 1;
-        // FFEA_GPU_CG_TPN=1, 2, 4 or 8 sets the lanes per matrix row (for comparison runs)
-        if (const char *t = getenv("FFEA_GPU_CG_TPN")) {
-            const int v = atoi(t);
-            if (v == 1 || v == 2 || v == 4 || v == 8) tpn = v;
-        }
         partial_stride = cg_grid;
-        // each block keeps a run of rows in shared memory when they fit (FFEA_GPU_CG_OWN=0 turns this off);
-        // the run is a multiple of a warp's rows so that a warp's rows share a SELL slice
-        // the mixed CG_nomass solve takes one reduction per iteration (cg_mixed_sr_kernel) when its rows fit
-        // (FFEA_GPU_CG_SR=0 keeps the two-reduction kernel, FFEA_GPU_CG_SR=1 takes it whatever the matrix size)
+        // The CG kernel follows from the blob's size alone (no other input selects it):
+        //  - each block keeps a run of rows in shared memory when they fit (cg_own_kernel, cg_mixed_own_kernel);
+        //    the run is a multiple of a warp's rows so that a warp's rows share a SELL slice; else the grid-strided
+        //    cg_kernel / cg_mixed_kernel;
+        //  - the mixed CG_nomass solve takes one reduction per iteration (cg_mixed_sr_kernel) when its rows fit and
+        //    its FP32 matrix stays in L2
         {
-            const char *own = getenv("FFEA_GPU_CG_OWN"), *sr = getenv("FFEA_GPU_CG_SR");
-            const int maxrows = (own && own[0] == '0') ? 0 : Launch<R>::cg_own_max_rows(device);
+            const int maxrows = Launch<R>::cg_own_max_rows(device);
             const int align = 32 / tpn, rows = (N + cg_grid - 1) / cg_grid;
             const int npb = (rows + align - 1) / align * align;
             cg_npb = (maxrows > 0 && npb <= maxrows) ? npb : 0;
             // ... while its FP32 matrix (40 B per 3x3 block) stays in L2: once the SpMV streams the matrix from HBM
             // the two-reduction kernel's iterations are the shorter ones (64^3 cells: 38.7 against 43.5 us)
             const bool l2_resident = 40.0 * (double)h.nslots <= L2_MATRIX_BYTES;
-            if (mixed && p.solver == FFEA_GPU_NOMASS_CG && !(sr && sr[0] == '0') && !(own && own[0] == '0') &&
-                (l2_resident || (sr && sr[0] == '1'))) {
+            if (mixed && p.solver == FFEA_GPU_NOMASS_CG && maxrows > 0 && l2_resident) {
                 // the polynomial preconditioner's two extra vectors per row must fit as well; else Jacobi
                 const int poly = p.cg_poly == 0 ? FFEA_GPU_CG_POLY_DEFAULT : std::max(p.cg_poly, 0);
                 for (int deg : {poly, 0}) {
@@ -400,19 +397,18 @@ struct BlobImpl final : ffea_gpu_blob {
             }
             if (cg_sr) {
                 // the first blocks of each owned row kept in shared memory for the solve, as many as the rest of
-                // the block's shared memory holds (FFEA_GPU_CG_CACHE=n caps them at n, 0 turns the cache off, for
-                // comparison runs)
+                // the block's shared memory holds (ffea_gpu_params::cg_smem_blocks caps them: n > 0 at most n, -1
+                // none; the results do not depend on it)
                 // The block's shared memory stops at 168 KB so that L1 (the rest of the SM's 256 KB) keeps the
                 // neighbours' exchanged vectors: on the 40^3 cube 6 cached blocks per row (167 KB) gave 20.8 us per
                 // iteration, the 9 that fit (223 KB) 21.4 us, none 22.3 us.
-                const char *cache = getenv("FFEA_GPU_CG_CACHE");
                 const long long avail = std::min<long long>(Launch<R>::cg_sr_smem_limit(device), 168 * 1024) -
                                         (long long)sr_smem_bytes(cg_npb, cg_poly);
                 const long long S = sr_cache_stride(cg_npb, tpn);
                 int maxlen = 0;
                 for (int a = 0; a < N; ++a) maxlen = std::max(maxlen, h.rowlen[a]);
                 cg_kc = avail <= 0 ? 0 : (int)std::min<long long>(maxlen, avail / (SR_CACHE_BYTES_PER_BLOCK * S));
-                if (cache) cg_kc = std::min(cg_kc, std::max(0, atoi(cache)));
+                if (p.cg_smem_blocks != 0) cg_kc = std::min(cg_kc, std::max(0, p.cg_smem_blocks));
             }
             if (cg_poly > 0) {
                 CK(mem.alloc(&cheb, (size_t)CHEB_STATE));
@@ -488,6 +484,15 @@ struct BlobImpl final : ffea_gpu_blob {
         if (lrc) return lrc;
         std::vector<uint32_t> rs(rng_host, rng_host + 6);
         CK(mem.upload(&rng_state, rs));
+        // a blob that the allocation-free solve accepts gets the static scratch placed now, and that solve's
+        // kernels loaded (cg_kernel by the occupancy query above), so that its first solve allocates nothing
+        if (!mixed && p.solver != FFEA_GPU_MASSLUMPED && N <= SOLVE_STATIC_MAX_NODES && cg_grid <= SOLVE_MAX_BLOCKS) {
+            double *ss = nullptr;
+            const int src = solve_scratch(device, &ss);
+            if (src) return src;
+            cudaFuncAttributes fa{};
+            CK(cudaFuncGetAttributes(&fa, solve_static_prep_kernel));
+        }
         CK(cudaDeviceSynchronize());
         return FFEA_GPU_OK;
     }
@@ -556,9 +561,7 @@ struct BlobImpl final : ffea_gpu_blob {
         // a Chebyshev step (SpMV + neighbour exchange) against a whole iteration (SpMV, exchange, grid-wide
         // reduction): about half while the FP32 matrix (40 B per 3x3 block) stays in L2, more once it streams
         // from HBM
-        // (FFEA_GPU_CHEB_COST overrides it, for comparison runs)
         ca.cheb_cost = 40.0 * (double)h.nslots <= L2_MATRIX_BYTES ? 0.5f : 0.9f;
-        if (const char *cc = getenv("FFEA_GPU_CHEB_COST")) ca.cheb_cost = (float)atof(cc);
         if (nb_flags) {
             ca.nb_ptr = nb_ptr; ca.nb_list = nb_list; ca.flags = nb_flags;
             CK(cudaMemsetAsync(nb_flags, 0, (size_t)FLAG_STRIDE * cg_grid * sizeof(unsigned int), stream));
@@ -832,6 +835,16 @@ struct BlobImpl final : ffea_gpu_blob {
         return FFEA_GPU_OK;
     }
 
+    const char *cg_kernel_name() const override {
+        if (p.solver == FFEA_GPU_MASSLUMPED) return "none";
+        if constexpr (std::is_same<R, float>::value) {
+            if (cg_npb > 0 && cg_sr && p.solver == FFEA_GPU_NOMASS_CG) return "cg_mixed_sr_kernel";
+            return cg_npb > 0 ? "cg_mixed_own_kernel" : "cg_mixed_kernel";
+        } else {
+            return cg_npb > 0 ? "cg_own_kernel" : "cg_kernel";
+        }
+    }
+
     int get_rhs(double *rhs) override {
         const int N = h.N;
         std::vector<double> hf(4 * (size_t)N);
@@ -852,9 +865,13 @@ struct BlobImpl final : ffea_gpu_blob {
         return FFEA_GPU_OK;
     }
 
-    // Jacobi-PCG solve of the blob's current matrix with every work array in g_solve_scratch:
-    // the same persistent cg_kernel as a step, opened by solve_static_prep_kernel instead of the
-    // gather. Host copies go through the blob's pinned staging buffer; nothing is allocated.
+    // Jacobi-PCG solve of the blob's current matrix with every work array in g_solve_scratch, by the
+    // grid-strided cg_kernel opened by solve_static_prep_kernel instead of the gather. A step of a blob whose
+    // rows fit in shared memory runs cg_own_kernel instead, whose sums run in another order, so the two agree
+    // to rounding, not bit for bit. Host copies go through the blob's pinned staging buffer; nothing is
+    // allocated. The blob's device is current for the call (the caller's is restored), and once a kernel is
+    // queued every return waits for the stream first, so the lock is never released while a kernel of this
+    // call may still use the shared array.
     int solve_static(const double *rhs, double *xout, int *iterations) override {
         if constexpr (std::is_same<R, float>::value) {
             g_last_error = "ffea_gpu_blob_solve_static: FP64 blobs only";
@@ -872,10 +889,22 @@ struct BlobImpl final : ffea_gpu_blob {
                 return FFEA_GPU_EINPUT;
             }
             std::lock_guard<std::mutex> lock(g_solve_mutex);
+            int caller_device = -1;
+            CK(cudaGetDevice(&caller_device));
+            struct RestoreDevice {
+                int d;
+                ~RestoreDevice() { cudaSetDevice(d); }
+            } restore_device{caller_device};
+            if (caller_device != device) CK(cudaSetDevice(device));
             double *s = nullptr;
             int rc = solve_scratch(device, &s);
             if (rc) return rc;
             CK(cudaStreamSynchronize(stream));  // staging may still feed an earlier copy
+            // declared after the lock, so destroyed before it: no early return leaves a kernel running
+            struct SyncOnExit {
+                cudaStream_t st;
+                ~SyncOnExit() { cudaStreamSynchronize(st); }
+            } sync_on_exit{stream};
             for (int k = 0; k < N; ++k)
                 for (int c = 0; c < 3; ++c) staging[3 * (size_t)k + c] = rhs[3 * (size_t)h.node_of[k] + c];
             CK(cudaMemcpyAsync(s + SS_RHS, staging, 3 * (size_t)N * sizeof(double), cudaMemcpyHostToDevice, stream));
@@ -1413,7 +1442,7 @@ int check_params(const ffea_gpu_params *p) {
     if (!p) return FFEA_GPU_EINPUT;
     if (p->solver < 0 || p->solver > 2 || (p->precision != FFEA_GPU_FP64 && p->precision != FFEA_GPU_MIXED) ||
         p->max_iterations_cg < 0 || !(p->dt > 0) ||
-        (p->cg_poly != -1 && p->cg_poly != 0 && p->cg_poly != 2 && p->cg_poly != 4)) {
+        (p->cg_poly != -1 && p->cg_poly != 0 && p->cg_poly != 2 && p->cg_poly != 4) || p->cg_smem_blocks < -1) {
         g_last_error = "invalid parameters";
         return FFEA_GPU_EINPUT;
     }
@@ -1559,6 +1588,8 @@ int ffea_gpu_blob_cg_preconditioner(ffea_gpu_blob *b, int *degree, double *lambd
     if (!b) return FFEA_GPU_EINPUT;
     return b->cg_preconditioner(degree, lambda_max);
 }
+
+const char *ffea_gpu_blob_cg_kernel(ffea_gpu_blob *b) { return b ? b->cg_kernel_name() : "none"; }
 
 int ffea_gpu_blob_counts(ffea_gpu_blob *b, int *num_nodes, int *num_elements) {
     if (!b) return FFEA_GPU_EINPUT;

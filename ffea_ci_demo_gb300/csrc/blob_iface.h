@@ -36,6 +36,7 @@ struct ffea_gpu_blob {
     virtual int cg_history(double *res2, int max_entries, int *count) = 0;
     virtual int cg_profile(double *ns, int n) = 0;
     virtual int cg_preconditioner(int *degree, double *lambda_max) = 0;
+    virtual const char *cg_kernel_name() const = 0;
     virtual int get_matrix_values(std::vector<double> &val_sell) = 0;
     virtual int solve_static(const double *rhs, double *x, int *iterations) = 0;
     virtual int adj_init(int window, int every) = 0;

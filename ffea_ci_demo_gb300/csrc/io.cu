@@ -84,6 +84,10 @@ int ffea_gpu_params_assign(ffea_gpu_params *p, const char *key, const char *valu
         const int v = atoi(value);
         if (v != -1 && v != 0 && v != 2 && v != 4) return FFEA_GPU_EINPUT;
         p->cg_poly = v;
+    } else if (k == "cg_smem_blocks") {
+        const int v = atoi(value);
+        if (v < -1) return FFEA_GPU_EINPUT;
+        p->cg_smem_blocks = v;
     } else {
         return FFEA_GPU_EINPUT;
     }

@@ -14,7 +14,8 @@
 // with its surface file, as Blob::init does (src/Blob.cpp:188-190, read_and_build_system :2266-2290).
 // Everything else outside the path is refused with FFEA_GPU_EINPUT and a message: surface-surface and
 // steric interactions (calc_ssint, calc_steric must be set to 0), electrostatics, kinetics, springs,
-// pre-computed potentials, rotational constant forces, rods, several conformations, STATIC/FROZEN blobs.
+// pre-computed potentials, rotational constant forces about an axis between two nodes (which the reference
+// reads but never applies), rods, several conformations, STATIC/FROZEN blobs.
 //
 // The reference's threads each own a stream; this engine reproduces its single-thread order, in which
 // one stream serves every blob: per step, the elements of blob 0, 1, ... draw 7 numbers each, then

@@ -45,7 +45,8 @@ class Params(C.Structure):
 
     _fields_ = [("dt", C.c_double), ("kT", C.c_double), ("epsilon2", C.c_double), ("stokes_visc", C.c_double),
                 ("max_iterations_cg", C.c_int), ("calc_noise", C.c_int), ("calc_stokes", C.c_int),
-                ("solver", C.c_int), ("precision", C.c_int), ("cg_poly", C.c_int)]
+                ("solver", C.c_int), ("precision", C.c_int), ("cg_poly", C.c_int),
+                ("cg_smem_blocks", C.c_int)]
 
 
 class MeshStruct(C.Structure):
@@ -96,6 +97,7 @@ def load():
         "ffea_gpu_blob_cg_history": (C.c_int, [vp, dp, C.c_int, ip]),
         "ffea_gpu_blob_cg_profile": (C.c_int, [vp, dp, C.c_int]),
         "ffea_gpu_blob_cg_preconditioner": (C.c_int, [vp, ip, dp]),
+        "ffea_gpu_blob_cg_kernel": (C.c_char_p, [vp]),
         "ffea_gpu_blob_get_pattern": (C.c_int, [vp, dp, dp, dp, dp, C.POINTER(C.c_longlong)]),
         "ffea_gpu_blob_get_connectivity": (C.c_int, [vp, dp, dp, C.POINTER(C.c_longlong)]),
         "ffea_gpu_blob_get_elements": (C.c_int, [vp, dp, dp, dp]),
@@ -187,9 +189,11 @@ class Blob:
     def __init__(self, mesh: Mesh | None = None, *, solver: str = "CG_nomass", precision: str = "fp64",
                  dt: float = 1e-12, kT: float = 4.11e-21, epsilon: float = 1e-10, max_iterations_cg: int = 10000,
                  calc_noise: int = 1, calc_stokes: int = 0, stokes_visc: float = 1e-3, cg_poly: int = 0,
-                 rng_state=(12345,) * 6, _handle=None, _n=None):
+                 cg_smem_blocks: int = 0, rng_state=(12345,) * 6, _handle=None, _n=None):
         """cg_poly: preconditioner of the mixed-precision CG_nomass solve (0: default Chebyshev degree 2,
-        -1: Jacobi alone as the reference, 2 or 4: Chebyshev degree); the FP64 path always uses Jacobi."""
+        -1: Jacobi alone as the reference, 2 or 4: Chebyshev degree); the FP64 path always uses Jacobi.
+        cg_smem_blocks: 3x3 matrix blocks per row that the mixed single-reduction CG keeps in shared memory
+        (0: as many as fit, n > 0: at most n, -1: none); results do not depend on it."""
         self._lib = load()
         self._h = C.c_void_p()
         if _handle is not None:
@@ -198,7 +202,8 @@ class Blob:
         else:
             params = make_params(solver=solver, precision=precision, dt=dt, kT=kT, epsilon=epsilon,
                                  max_iterations_cg=max_iterations_cg, calc_noise=calc_noise,
-                                 calc_stokes=calc_stokes, stokes_visc=stokes_visc, cg_poly=cg_poly)
+                                 calc_stokes=calc_stokes, stokes_visc=stokes_visc, cg_poly=cg_poly,
+                                 cg_smem_blocks=cg_smem_blocks)
             s = mesh.scale / MESO_LENGTH
             self._keep = [np.ascontiguousarray(mesh.pos * s, np.float64),
                           np.ascontiguousarray(mesh.tets, np.int32),
@@ -348,6 +353,10 @@ class Blob:
         d, lm = C.c_int(), np.zeros(1)
         _check(self._lib.ffea_gpu_blob_cg_preconditioner(self._h, C.byref(d), _p(lm)), "cg_preconditioner")
         return d.value, float(lm[0])
+
+    def cg_kernel(self) -> str:
+        """Name of the persistent CG kernel this blob's steps launch ("none" for masslumped)."""
+        return self._lib.ffea_gpu_blob_cg_kernel(self._h).decode()
 
     def sizes(self) -> tuple[int, int, int]:
         nl, ne, nb = C.c_int(), C.c_int(), C.c_longlong()

@@ -66,6 +66,11 @@ typedef struct ffea_gpu_params {
      * the single-reduction kernel runs (the blob's rows fit in the GPU's shared memory); the blob's first solve
      * uses Jacobi and estimates the largest eigenvalue of D^-1 V for the later ones. */
     int cg_poly;
+    /* Shared-memory copy of the matrix in the mixed-precision single-reduction CG_nomass kernel (not a reference
+     * parameter): each block keeps the first 3x3 blocks of its owned rows on chip for the whole solve.
+     * 0: as many as fit (the default); n > 0: at most n per row; -1: none. The results do not depend on it
+     * (only where the matrix is read from), so it exists for measurements of the cache's effect. */
+    int cg_smem_blocks;
 } ffea_gpu_params;
 #define FFEA_GPU_CG_POLY_DEFAULT 2
 
@@ -149,10 +154,12 @@ int ffea_gpu_blob_measure(ffea_gpu_blob *blob, double *strain_energy, double *ki
 
 /* Constant forces of the reference's ctforces file for blob `blob_index` (Blob::load_ctforces,
  * src/Blob.cpp:2478-2805; applied as Blob::apply_ctforces, :1676-1743): linear forces on nodes (added
- * before the element forces) and linear surface forces spread over sets of faces of `surface_file`
- * (the blob's .surf; may be NULL without surface forces) in proportion to their current areas (added
- * after the element forces, face by face). Rotational forces return FFEA_GPU_EINPUT. Replaces any
- * constant forces loaded before. */
+ * before the element forces), rotational forces about an axis through a point ("pf", "pt": evaluated at
+ * the nodes' current positions every step, after the linear ones), and linear surface forces spread over
+ * sets of faces of `surface_file` (the blob's .surf; may be NULL without surface forces) in proportion to
+ * their current areas (added after the element forces, face by face). Rotational forces about an axis
+ * between two nodes return FFEA_GPU_EINPUT: the reference reads them but never applies them. Replaces
+ * any constant forces loaded before. */
 int ffea_gpu_blob_load_ctforces(ffea_gpu_blob *blob, const char *ctforces_file, const char *surface_file,
                                 int blob_index);
 
@@ -184,6 +191,13 @@ int ffea_gpu_blob_cg_profile(ffea_gpu_blob *blob, double *phase_ns, int n_phases
  * *lambda_max the estimate of the largest eigenvalue of D^-1 V it is built on (0 without one). Each CG
  * iteration then applies the matrix 1 + degree times. */
 int ffea_gpu_blob_cg_preconditioner(ffea_gpu_blob *blob, int *degree, double *lambda_max);
+
+/* Name of the persistent CG kernel the blob's steps launch, fixed at creation by the blob's size and
+ * precision alone (static string; "none" for masslumped, which solves no system):
+ *   FP64: "cg_own_kernel" (each block keeps its rows on chip) or "cg_kernel" (grid-strided, larger blobs);
+ *   mixed: "cg_mixed_sr_kernel" (CG_nomass, one reduction per iteration, FP32 matrix up to 64 MB so that it
+ *   stays in L2), "cg_mixed_own_kernel" (two reductions, rows on chip) or "cg_mixed_kernel" (grid-strided). */
+const char *ffea_gpu_blob_cg_kernel(ffea_gpu_blob *blob);
 
 /* Nodes of the reference numbering (vertices and midpoints) and elements of the blob. */
 int ffea_gpu_blob_counts(ffea_gpu_blob *blob, int *num_nodes, int *num_elements);
@@ -218,8 +232,11 @@ int ffea_gpu_blob_get_rhs(ffea_gpu_blob *blob, double *rhs);
  *
  * Solves M x = rhs with the blob's current matrix (CG_nomass: the viscosity
  * matrix assembled by the last ffea_gpu_blob_step; CG: the constant mass
- * matrix) by the persistent Jacobi-PCG kernel of a step, from x = 0, with the
- * blob's epsilon and max_iterations_cg. rhs and x hold 3 * num_nodes doubles
+ * matrix) by the grid-strided persistent Jacobi-PCG kernel, from x = 0, with
+ * the blob's epsilon and max_iterations_cg. A step may run another CG kernel
+ * (one whose blocks keep their rows on chip) that sums in another order, so
+ * the two solutions agree to rounding and their iteration counts may differ
+ * by one. rhs and x hold 3 * num_nodes doubles
  * in the layout of ffea_gpu_blob_get_rhs and may be the same array; midpoint
  * rows are identity rows (x = rhs there). *iterations (may be NULL) gets the
  * CG iterations used. Returns FFEA_GPU_ECGMAXIT / FFEA_GPU_ETIMEOUT like a step.
@@ -228,13 +245,16 @@ int ffea_gpu_blob_get_rhs(ffea_gpu_blob *blob, double *rhs);
  * array comes from one static device array of this library, sized for
  * FFEA_GPU_SOLVE_STATIC_MAX_NODES vertex nodes (4.99 MB). Blobs with more
  * vertex nodes, mixed-precision blobs and mass-lumped blobs are rejected with
- * FFEA_GPU_EINPUT and a message in ffea_gpu_last_error. The first call on a
- * device looks the array up (cudaGetSymbolAddress, which also loads the
- * library's module there); make that first call before any stream capture on
- * the device. The array is shared by all calls on a device, so two calls whose
- * kernels overlapped would corrupt each other: each call holds a process-wide
- * lock and waits for its result, so calls from several host threads run one
- * after another. */
+ * FFEA_GPU_EINPUT and a message in ffea_gpu_last_error. The array is placed
+ * on a device (cudaGetSymbolAddress, which loads the library's module there)
+ * by the creation of the first blob that this call accepts, so the first call
+ * allocates nothing either; a caller who fills the GPU's memory should create
+ * its blobs first. The call makes the blob's device current and restores the
+ * caller's on return. The array is shared by all calls on a device, so two
+ * calls whose kernels overlapped would corrupt each other: each call holds a
+ * process-wide lock and waits for its kernels to finish (on success and on
+ * error) before it returns, so calls from several host threads run one after
+ * another. */
 #define FFEA_GPU_SOLVE_STATIC_MAX_NODES 32768
 int ffea_gpu_blob_solve_static(ffea_gpu_blob *blob, const double *rhs, double *x, int *iterations);
 
@@ -326,10 +346,11 @@ int ffea_gpu_batch_tune(ffea_gpu_batch *batch, int solves, double *best_ms);
  *   blob), builds each blob from its structure files, applies centroid /
  *   rotation / velocity and the move into the simulation box, sets the RMSD
  *   reference, seeds the stream from rng_seed (or, with restart = 1, from
- *   checkpoint_in and the trajectory's last complete frame) and opens the
- *   trajectory and measurement files. Features outside the path (calc_ssint,
- *   calc_steric, calc_es, kinetics, springs, preComp, ctforces, rods, several
- *   conformations, STATIC blobs) are refused with FFEA_GPU_EINPUT.
+ *   checkpoint_in and the trajectory's last complete frame), loads each blob's
+ *   constant forces (calc_ctforces = 1) and opens the trajectory and
+ *   measurement files. Features outside the path (calc_ssint, calc_steric,
+ *   calc_es, kinetics, springs, preComp, rods, several conformations, STATIC
+ *   blobs) are refused with FFEA_GPU_EINPUT.
  * run: steps step_initial .. num_steps; every `check` steps the stream state
  *   goes to checkpoint_out before the forces, then the positions to the
  *   trajectory (.ftj) and the measurements (.fm), as the reference writes them.

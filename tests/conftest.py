@@ -1,3 +1,6 @@
+import ctypes as C
+import ctypes.util
+import glob
 import os
 import sys
 
@@ -29,3 +32,29 @@ def gpu():
 
     build.build()
     return lib.load()
+
+
+@pytest.fixture(scope="session")
+def device_free_bytes():
+    """cudaMemGetInfo's free bytes of the current device, through the CUDA runtime the library links."""
+    rt = None
+    for c in ["libcudart.so.13", ctypes.util.find_library("cudart")] + sorted(
+            glob.glob("/usr/local/cuda/lib64/libcudart.so*")):
+        if not c:
+            continue
+        try:
+            rt = C.CDLL(c)
+            break
+        except OSError:
+            continue
+    if rt is None:
+        pytest.skip("libcudart not found")
+    rt.cudaMemGetInfo.argtypes = [C.POINTER(C.c_size_t), C.POINTER(C.c_size_t)]
+    rt.cudaMemGetInfo.restype = C.c_int
+
+    def free() -> int:
+        f, t = C.c_size_t(), C.c_size_t()
+        assert rt.cudaMemGetInfo(C.byref(f), C.byref(t)) == 0
+        return f.value
+
+    return free

@@ -141,3 +141,43 @@ def test_autograd_function(gpu):
     assert mat.grad is not None and x0.grad is not None
     assert torch.isfinite(mat.grad).all() and mat.grad[:, 3].abs().sum() > 0
     assert float(mat.grad[:, 0].abs().sum()) == 0.0  # density does not enter a massless step
+
+
+def test_autograd_frees_device_memory(gpu, device_free_bytes):
+    """The window's blob and checkpoints (its matrix sources alone take 6 MB on this 12^3-cell cube) are freed by
+    a forward that needs no gradient (no_grad, or inputs without requires_grad), by the backward pass, and when a
+    graph whose backward never ran is dropped: three windows of each kind leave the device's free memory within
+    4 MB (the driver's allocation granularity) of where it was."""
+    import gc
+
+    torch = pytest.importorskip("torch")
+    from ffea_ci_demo_gb300.autograd import window
+
+    m = case_mesh(12, 11)
+    kw = dict(dt=1e-12, kT=0.0, calc_noise=0)
+    slack = 4 << 20
+
+    def run(grad: bool):
+        mat = torch.tensor(m.material, dtype=torch.float64, requires_grad=grad)
+        x0 = torch.tensor(sheared(m, 0.02), dtype=torch.float64, requires_grad=grad)
+        return window(m, mat, x0, 6, 3, **kw)
+
+    run(True).sum().backward()  # loads the kernels once
+    gc.collect()
+    base = device_free_bytes()
+    for _ in range(3):
+        with torch.no_grad():
+            run(True)
+    assert device_free_bytes() >= base - slack, "a no_grad forward kept device memory"
+    for _ in range(3):
+        run(False)
+    assert device_free_bytes() >= base - slack, "a forward without differentiable inputs kept device memory"
+    for _ in range(3):
+        run(True).sum().backward()
+    gc.collect()
+    assert device_free_bytes() >= base - slack, "backward left device memory behind"
+    for _ in range(3):
+        xk = run(True)
+        del xk
+    gc.collect()
+    assert device_free_bytes() >= base - slack, "dropping the graph left device memory behind"

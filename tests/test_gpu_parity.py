@@ -189,18 +189,15 @@ def test_chebyshev_preconditioner(gpu, poly):
         assert its["cheb2"] == its["cheb"] and np.array_equal(pos["cheb2"], pos["cheb"])
 
 
-def test_matrix_cache_is_bit_identical(gpu, monkeypatch):
+def test_matrix_cache_is_bit_identical(gpu):
     """The single-reduction CG's shared-memory copy of each owned row's first blocks changes where the matrix is
-    read from, not the arithmetic: a blob without it (FFEA_GPU_CG_CACHE=0, read at creation) and blobs with it
-    capped at two blocks per row or at what fits step to the same bits."""
+    read from, not the arithmetic: a blob without it (cg_smem_blocks = -1) and blobs with it capped at two blocks
+    per row or at what fits (0) step to the same bits."""
     m = case_mesh(12, 21)
     out = []
-    for cache in (None, "0", "2"):
-        if cache is None:
-            monkeypatch.delenv("FFEA_GPU_CG_CACHE", raising=False)
-        else:
-            monkeypatch.setenv("FFEA_GPU_CG_CACHE", cache)
-        b = gpu_blob(m, 0.02, solver="CG_nomass", precision="mixed", dt=1e-12, kT=4.11e-21, calc_noise=1)
+    for cache in (0, -1, 2):
+        b = gpu_blob(m, 0.02, solver="CG_nomass", precision="mixed", dt=1e-12, kT=4.11e-21, calc_noise=1,
+                     cg_smem_blocks=cache)
         b.update(6)
         out.append((b.pos(), b.cg_iterations()[1]))
     for x, it in out[1:]:
