@@ -27,6 +27,14 @@ from gen_golden import case_mesh, sheared
 pytestmark = pytest.mark.gpu
 
 
+def solve_static(L, blob, rhs, out=None):
+    x = np.full_like(rhs, np.nan) if out is None else out
+    it = C.c_int(-1)
+    rc = L.ffea_gpu_blob_solve_static(blob._h, rhs.ctypes.data_as(C.c_void_p), x.ctypes.data_as(C.c_void_p),
+                                      C.byref(it))
+    return rc, x, it.value
+
+
 @pytest.mark.parametrize("solver,dt", [("CG_nomass", 1e-12), ("CG", 1e-14)])
 def test_static_solve_matches_step(gpu, device_free_bytes, solver, dt):
     L = lib.load()
