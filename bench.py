@@ -494,7 +494,62 @@ def run_adjoint(args) -> dict:
                      "finite_gradients": bool(all(np.isfinite(g[k]).all() for k in ("G", "E", "A", "B")))}
         adj.close()
         blob.close()
+    if args.adjoint_fd_steps > 0:
+        out["fd_check"] = adjoint_fd_check(mesh, args.adjoint_fd_steps)
     return out
+
+
+def adjoint_fd_check(mesh, steps: int) -> dict:
+    """Central finite differences of the same loss on a shortened window at kT = 0 (8 sampled per-element
+    parameters, relative step 1e-3, CG tolerance 1e-12 so that the solves' error stays below the differences'),
+    evaluated with the FP64 GPU path (its trajectories follow the reference's to CG rounding), against the FP64
+    and the mixed adjoint; relative error as a vector norm."""
+    import copy
+
+    import numpy as np
+
+    from ffea_ci_demo_gb300 import lib
+    from ffea_ci_demo_gb300.mesh import apply_shear
+
+    kw = dict(PHYS, kT=0.0, calc_noise=0, epsilon=1e-12)
+    rng = np.random.default_rng(7)
+    x0 = apply_shear(mesh, 0.02, seed=3) * (mesh.scale / MESO_LENGTH)
+    target = x0 + rng.normal(0.0, 0.05, size=x0.shape)
+    samples = [(3, 17), (3, 23456), (4, 401), (4, 40000), (1, 999), (1, 31000), (2, 5), (2, 47000)]
+    names = {1: "shear_visc", 2: "bulk_visc", 3: "shear_mod", 4: "bulk_mod"}
+
+    def loss(m):
+        b = lib.Blob(m, precision="fp64", **kw)
+        b.set_state(pos=x0)
+        b.update(steps)
+        d = b.pos() - target
+        b.close()
+        return float((d * d).sum())
+
+    fd = []
+    for c, e in samples:
+        h = 1e-3 * mesh.material[e, c]
+        vals = []
+        for sgn in (1, -1):
+            m = copy.deepcopy(mesh)
+            m.material[e, c] += sgn * h
+            vals.append(loss(m))
+        fd.append((vals[0] - vals[1]) / (2 * h))
+    fd = np.array(fd)
+    res = {"window_steps": steps, "samples": len(samples), "relative_step": 1e-3, "cg_epsilon": 1e-12,
+           "fd_through": "FP64 GPU path, central differences, kT = 0"}
+    for prec in ("fp64", "mixed"):
+        b = lib.Blob(mesh, precision=prec, **kw)
+        b.set_state(pos=x0)
+        adj = lib.Adjoint(b, steps, 5)
+        adj.forward()
+        g = lib.meso_to_si_gradients(adj.backward(2.0 * (b.pos() - target)))
+        got = np.array([g[names[c]][e] for c, e in samples])
+        res[f"rel_err_{prec}"] = float(np.linalg.norm(got - fd) / np.linalg.norm(fd))
+        adj.close()
+        b.close()
+    res["rel_err"] = max(res["rel_err_fp64"], res["rel_err_mixed"])
+    return res
 
 
 def run_scale(args) -> dict:
@@ -707,6 +762,8 @@ def main():
     ap.add_argument("--no-fp64-sample", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--adjoint-steps", type=int, default=200)
+    ap.add_argument("--adjoint-fd-steps", type=int, default=20,
+                    help="window of the adjoint's finite-difference check (0: skip)")
     ap.add_argument("--no-scale", action="store_true")
     ap.add_argument("--scale-cells", type=int, default=64)
     ap.add_argument("--scale-steps", type=int, default=5)

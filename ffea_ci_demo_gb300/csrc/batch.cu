@@ -21,6 +21,7 @@
 #include "../../include/ffea_gpu.h"
 #include "engine.h"
 #include "host_model.h"
+#include "mixed_elements.h"
 
 namespace ffea {
 long long launch_count();
@@ -39,8 +40,9 @@ struct ffea_gpu_batch {
     int device = 0;
     double *px, *py, *pz, *vx, *vy, *vz;
     int4 *tet;
-    float *jinv, *G, *E, *A, *B, *vol0, *ef, *geom;
+    float *jinv, *G, *E, *A, *B, *vol0, *geom;
     double *last_det;
+    MixedElements me;  // FP32 node data, thread-block lists and per-block force sums of the element phase
     int *inc_ptr, *inc, *pinned, *slice_ptr, *rowlen, *bcol, *diagk, *src_ptr, *grp_slice;
     unsigned *src;
     double *drag = nullptr;
@@ -187,8 +189,8 @@ int ffea_gpu_batch::init() {
     CK(mem.upload(&B, cast_vec<float>(h.B)));
     CK(mem.upload(&vol0, cast_vec<float>(h.vol0)));
     CK(mem.upload(&last_det, h.last_det));
-    CK(mem.alloc(&ef, 12 * (size_t)T));
     CK(mem.alloc(&geom, 16 * (size_t)T));
+    CK(me.init(mem, h, false, p.calc_noise == 1, elem_off));
     CK(mem.upload(&inc_ptr, h.inc_ptr));
     CK(mem.upload(&inc, h.inc));
     CK(mem.upload(&pinned, h.pinned));
@@ -321,7 +323,6 @@ int ffea_gpu_batch::launch_forces() {
     ea.jinv = jinv;
     ea.G = G; ea.E = E; ea.A = A; ea.B = B; ea.vol0 = vol0;
     ea.last_det = last_det;
-    ea.ef = ef;
     ea.geom = geom;
     ea.rng_state = rng_states;
     ea.elem_blob = elem_blob;
@@ -329,7 +330,9 @@ int ffea_gpu_batch::launch_forces() {
     ea.chunk_jump = chunk_jump;
     ea.lane_jump = lane_jump;
     ea.st = st;
-    CK(Launch<float>::element(ea, stream));
+    me.fill(ea);
+    CK(me.prep(px, py, pz, vx, vy, vz, rng_states, chunk_jump, stream));
+    CK(MixedLaunch::element(ea, true, stream));
     AsmArgs<float> aa{};
     aa.N = h.N;
     aa.nslots = h.nslots; aa.grp_slice = grp_slice;
@@ -347,7 +350,8 @@ int ffea_gpu_batch::launch_gather() {
     GatherArgs<float> ga{};
     ga.N = h.N;
     ga.mode = 2;
-    ga.inc_ptr = inc_ptr; ga.inc = inc; ga.ef = ef; ga.pinned = pinned;
+    ga.inc_ptr = inc_ptr; ga.inc = inc; ga.ef = nullptr; ga.pinned = pinned;
+    ga.parts = me.parts; ga.part_ptr = me.part_ptr;
     ga.drag = nullptr;
     ga.vx = vx; ga.vy = vy; ga.vz = vz;
     ga.dinv = dinv; ga.f = f; ga.x = x; ga.r = r;

@@ -31,6 +31,7 @@
 #include "ctforces.h"
 #include "host_model.h"
 #include "kernels_mixed.cuh"
+#include "mixed_elements.h"
 
 namespace ffea {
 long long launch_count();
@@ -158,7 +159,7 @@ struct BlobImpl final : ffea_gpu_blob {
     // device arrays
     double *px, *py, *pz, *vx, *vy, *vz;
     int4 *tet;
-    R *jinv, *G, *E, *A, *B, *vol0, *ef, *geom;
+    R *jinv, *G, *E, *A, *B, *vol0, *ef = nullptr, *geom = nullptr;
     double *last_det;
     int *inc_ptr, *inc, *pinned;
     int *slice_ptr, *rowlen, *bcol, *diagk, *src_ptr, *grp_slice;
@@ -183,6 +184,7 @@ struct BlobImpl final : ffea_gpu_blob {
     int *nb_ptr = nullptr, *nb_list = nullptr;  // its blocks' neighbour blocks
     unsigned int *nb_flags = nullptr;           // and their publication counters
     float4 *dpos = nullptr;  // mixed path: node offsets from the reference point
+    MixedElements me;        // mixed path: the element phase's FP32 node data, block lists and block sums
     // measurements: densities, reference positions of vertices and midpoints (SoA), per-block sums
     R *rho = nullptr;
     double *p0 = nullptr, *m0 = nullptr, *meas_part = nullptr, *meas_out = nullptr;
@@ -208,6 +210,11 @@ struct BlobImpl final : ffea_gpu_blob {
     int hist_cap = 0;
     cudaEvent_t ev[FFEA_GPU_NUM_PHASES + 1] = {};
     bool record_phases = false;
+    // The step as a CUDA graph, replayed once per step: [0] plain, [1] with the phase events of step_timed.
+    // Captured on first use. Host state that a step's launches take by value (the rigid modes and centroid,
+    // constant forces, the stream layout) drops them when it changes (invalidate_graphs).
+    cudaGraphExec_t gexec[2] = {nullptr, nullptr};
+    long long graph_launches[2] = {0, 0};
     double *staging = nullptr;  // pinned host buffer, 3*N doubles, for state copies
     // node state in the reference's layout on the device: n_all x 3 doubles, the vertex row of each vertex
     // node, and the source rows of every reference node (vertex (k, k), midpoint (a, b), else (-1, -1))
@@ -224,6 +231,7 @@ struct BlobImpl final : ffea_gpu_blob {
     float2 *adj_part_f = nullptr;
 
     ~BlobImpl() override {
+        invalidate_graphs();
         if (staging) cudaFreeHost(staging);
         for (auto &e : ev)
             if (e) cudaEventDestroy(e);
@@ -231,7 +239,44 @@ struct BlobImpl final : ffea_gpu_blob {
     }
 
     int mark(int k) {
-        if (record_phases) CK(cudaEventRecord(ev[k], stream));
+        // an event record node when the step is being captured
+        if (record_phases) CK(cudaEventRecordWithFlags(ev[k], stream, cudaEventRecordExternal));
+        return FFEA_GPU_OK;
+    }
+
+    void invalidate_graphs() {
+        for (auto &g : gexec)
+            if (g) {
+                cudaGraphExecDestroy(g);
+                g = nullptr;
+            }
+    }
+
+    // one step through its graph (captured from launch_step on first use)
+    int launch_step_graph(int timed) {
+        if (!gexec[timed]) {
+            record_phases = timed != 0;
+            const long long l0 = launch_count();
+            CK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+            const int rc = launch_step();
+            cudaGraph_t graph = nullptr;
+            const cudaError_t e = cudaStreamEndCapture(stream, &graph);
+            record_phases = false;
+            graph_launches[timed] = launch_count() - l0;
+            count_launch((int)-graph_launches[timed]);  // counted on every replay instead
+            if (rc || e != cudaSuccess) {
+                if (graph) cudaGraphDestroy(graph);
+                return rc ? rc : cuda_fail(e, "cudaStreamEndCapture");
+            }
+            const cudaError_t ei = cudaGraphInstantiate(&gexec[timed], graph, 0);
+            cudaGraphDestroy(graph);
+            if (ei != cudaSuccess) {
+                gexec[timed] = nullptr;
+                return cuda_fail(ei, "cudaGraphInstantiate");
+            }
+        }
+        CK(cudaGraphLaunch(gexec[timed], stream));
+        count_launch((int)graph_launches[timed]);
         return FFEA_GPU_OK;
     }
 
@@ -299,8 +344,10 @@ struct BlobImpl final : ffea_gpu_blob {
             CK(mem.alloc(&meas_out, (size_t)MEASURE_NV));
         }
         CK(mem.upload(&last_det, h.last_det));
-        CK(mem.alloc(&ef, 12 * (size_t)T));
-        CK(mem.alloc(&geom, 16 * (size_t)T));
+        // element forces and geometry per element: the FP64 path keeps both (the gather reads the forces in the
+        // reference's order); the mixed path sums forces per thread block and keeps geometry for the assembly only
+        if (!std::is_same<R, float>::value) CK(mem.alloc(&ef, 12 * (size_t)T));
+        if (!std::is_same<R, float>::value || p.solver == FFEA_GPU_NOMASS_CG) CK(mem.alloc(&geom, 16 * (size_t)T));
         CK(mem.upload(&inc_ptr, h.inc_ptr));
         CK(mem.upload(&inc, h.inc));
         CK(mem.upload(&pinned, h.pinned));
@@ -344,6 +391,7 @@ struct BlobImpl final : ffea_gpu_blob {
         if (mixed) {
             CK(mem.alloc(&diag, 4 * (size_t)N));
             CK(mem.alloc(&dpos, (size_t)N));
+            CK(me.init(mem, h, p.solver != FFEA_GPU_NOMASS_CG, p.calc_noise == 1, {}));
         }
         // rigid modes: the mixed CG deflates them; both paths' adjoints project them out
         nmodes = rigid_modes(h, p, xc, modes);
@@ -520,6 +568,24 @@ struct BlobImpl final : ffea_gpu_blob {
         return ea;
     }
 
+    // the element phase: FP64 element_kernel, or (mixed) node_prep_kernel and element_mixed_kernel, which sums
+    // each thread block's forces per vertex for the gather; `recompute` (the adjoint's re-evaluation at stored
+    // positions) needs only the geometry the assembly reads
+    int launch_elements(int recompute) {
+        if constexpr (std::is_same<R, float>::value) {
+            CK(me.prep(px, py, pz, vx, vy, vz, rng_state, chunk_jump, stream));
+            ElemArgs<float> ea = elem_args(recompute);
+            me.fill(ea);
+            ea.ef = nullptr;
+            ea.geom = p.solver == FFEA_GPU_NOMASS_CG ? geom : nullptr;
+            if (recompute) ea.parts = nullptr;
+            CK(MixedLaunch::element(ea, !recompute, stream));
+        } else {
+            CK(Launch<R>::element(elem_args(recompute), stream));
+        }
+        return FFEA_GPU_OK;
+    }
+
     int launch_assemble() {
         AsmArgs<R> aa{};
         aa.N = h.N;
@@ -574,7 +640,7 @@ struct BlobImpl final : ffea_gpu_blob {
         const bool nomass = p.solver == FFEA_GPU_NOMASS_CG;
         int rc = mark(0);
         if (rc) return rc;
-        CK(Launch<R>::element(elem_args(0), stream));
+        if ((rc = launch_elements(0))) return rc;
         if ((rc = mark(1))) return rc;
         if (nomass && (rc = launch_assemble())) return rc;
         if ((rc = mark(2))) return rc;
@@ -582,12 +648,16 @@ struct BlobImpl final : ffea_gpu_blob {
         ga.N = h.N;
         ga.mode = p.solver == FFEA_GPU_MASSLUMPED ? 1 : 0;
         ga.inc_ptr = inc_ptr; ga.inc = inc; ga.ef = ef; ga.pinned = pinned;
+        ga.parts = me.parts; ga.part_ptr = me.part_ptr;
         ga.drag = (!nomass && p.calc_stokes == 1) ? drag : nullptr;
         ga.vx = vx; ga.vy = vy; ga.vz = vz;
         ga.dinv = dinv; ga.f = f; ga.x = x; ga.r = r;
         ga.partials = init_partials; ga.stride = gather_blocks; ga.st = st; ga.gb = gb;
         ga.dpos = dpos; ga.px = px; ga.py = py; ga.pz = pz; ga.diag = diag;
         ga.xc[0] = xc[0]; ga.xc[1] = xc[1]; ga.xc[2] = xc[2];
+        // the mixed mass-lumped step updates positions in the gather (no solve between them)
+        ga.fuse_euler = std::is_same<R, float>::value && p.solver == FFEA_GPU_MASSLUMPED;
+        ga.upx = px; ga.upy = py; ga.upz = pz; ga.uvx = vx; ga.uvy = vy; ga.uvz = vz; ga.dt = p.dt;
         {
             NodeForces &sn = ga.sn;
             sn.noise = sn_chunk_jump != nullptr;
@@ -621,11 +691,13 @@ struct BlobImpl final : ffea_gpu_blob {
         if ((rc = mark(3))) return rc;
         if (p.solver != FFEA_GPU_MASSLUMPED && (rc = launch_cg(init_partials, gather_blocks))) return rc;
         if ((rc = mark(4))) return rc;
-        EulerArgs<R> eu{};
-        eu.N = h.N; eu.nomass = nomass; eu.dt = p.dt; eu.x = x;
-        eu.px = px; eu.py = py; eu.pz = pz; eu.vx = vx; eu.vy = vy; eu.vz = vz;
-        eu.st = st;
-        CK(Launch<R>::euler(eu, stream));
+        if (!ga.fuse_euler) {
+            EulerArgs<R> eu{};
+            eu.N = h.N; eu.nomass = nomass; eu.dt = p.dt; eu.x = x;
+            eu.px = px; eu.py = py; eu.pz = pz; eu.vx = vx; eu.vy = vy; eu.vz = vz;
+            eu.st = st;
+            CK(Launch<R>::euler(eu, stream));
+        }
         CK(launch_finish_step(rng_state, step_jump, st, stream));
         return mark(5);
     }
@@ -654,7 +726,7 @@ struct BlobImpl final : ffea_gpu_blob {
         s.steps_done = 0;
         CK(cudaMemcpyAsync(st, &s, sizeof(DevStatus), cudaMemcpyHostToDevice, stream));
         for (int i = 0; i < nsteps; ++i) {
-            rc = launch_step();
+            rc = launch_step_graph(0);
             if (rc) return rc;
             // the non-finite flag is raised by euler_kernel after the positions moved; stop the step chain
         }
@@ -675,13 +747,12 @@ struct BlobImpl final : ffea_gpu_blob {
         void *scratch = nullptr;
         if (flush_bytes > 0) CK(cudaMalloc(&scratch, (size_t)flush_bytes));
         double tot = 0.0, ph[FFEA_GPU_NUM_PHASES] = {0};
-        record_phases = true;
         for (int i = 0; i < nsteps && rc == FFEA_GPU_OK; ++i) {
             if (scratch) {
                 cudaError_t e = cudaMemsetAsync(scratch, i & 0xff, (size_t)flush_bytes, stream);
                 if (e != cudaSuccess) { rc = cuda_fail(e, "flush"); break; }
             }
-            rc = launch_step();
+            rc = launch_step_graph(1);
             if (rc) break;
             cudaError_t e = cudaEventSynchronize(ev[FFEA_GPU_NUM_PHASES]);
             if (e != cudaSuccess) { rc = cuda_fail(e, "cudaEventSynchronize"); break; }
@@ -693,7 +764,6 @@ struct BlobImpl final : ffea_gpu_blob {
             cudaEventElapsedTime(&ms, ev[0], ev[FFEA_GPU_NUM_PHASES]);
             tot += ms;
         }
-        record_phases = false;
         if (scratch) cudaFree(scratch);
         if (rc) return rc;
         rc = read_status(s);
@@ -753,6 +823,7 @@ struct BlobImpl final : ffea_gpu_blob {
             }
             for (int c = 0; c < 3; ++c) xc[c] = s[c] / std::max(N, 1);
             nmodes = rigid_modes_about(h, p, xc, modes, 0, N);
+            invalidate_graphs();  // the gather and the CG take the centroid and the modes by value
         }
         // the caller may reuse its arrays on return
         CK(cudaStreamSynchronize(stream));
@@ -781,6 +852,11 @@ struct BlobImpl final : ffea_gpu_blob {
     }
 
     int get_elements(double *nf, double *vol, double *visc) override {
+        if constexpr (std::is_same<R, float>::value) {
+            g_last_error = "per-element outputs are kept by the FP64 path only (the mixed path sums each thread "
+                           "block's element forces per vertex)";
+            return FFEA_GPU_EINPUT;
+        }
         const int T = h.T;
         std::vector<R> he(12 * (size_t)T), hg(16 * (size_t)T);
         CK(cudaMemcpyAsync(he.data(), ef, he.size() * sizeof(R), cudaMemcpyDeviceToHost, stream));
@@ -959,6 +1035,7 @@ struct BlobImpl final : ffea_gpu_blob {
     }
 
     int load_ctforces(const char *ctf_file, const char *surf_file, int blob_index) override {
+        invalidate_graphs();
         CtfModel cm;
         std::string err;
         int rc = ffea::host::load_ctforces(ctf_file, surf_file, blob_index, h.n_all, cm, err);
@@ -1116,6 +1193,7 @@ struct BlobImpl final : ffea_gpu_blob {
     // the step's stream advance, and where the Stokes draws start (node i of the reference numbering draws
     // 3 numbers from stokes_base + 3i after the step's state)
     int set_rng_layout(unsigned long long step_draws, unsigned long long stokes_base) override {
+        invalidate_graphs();
         std::vector<MrgJump> sj(1, jump_pow(step_draws));
         CK(cudaMemcpy(step_jump, sj.data(), sizeof(MrgJump), cudaMemcpyHostToDevice));
         if (sn_chunk_jump) {
@@ -1234,8 +1312,9 @@ struct BlobImpl final : ffea_gpu_blob {
     // gtheta += d(dt v)/dtheta^T lambda
     int adj_step(const R *v_step) {
         constexpr bool mixed = std::is_same<R, float>::value;
-        CK(Launch<R>::element(elem_args(1), stream));
-        int rc = launch_assemble();
+        int rc = launch_elements(1);
+        if (rc) return rc;
+        rc = launch_assemble();
         if (rc) return rc;
         AdjGatherArgs<R> ag{};
         ag.N = h.N;

@@ -336,56 +336,71 @@ __host__ __device__ __forceinline__ uint32_t mod_m2(uint64_t x) {
     return (uint32_t)(x >= MRG_M2 ? x - MRG_M2 : x);
 }
 
+// x mod m1 for x < 2^54: 2^32 = 209 (mod m1), so one fold leaves x < 2^22 209 + 2^32 < 2 m1
+__host__ __device__ __forceinline__ uint32_t mod_m1_54(uint64_t x) {
+    x = (x >> 32) * 209ull + (x & 0xffffffffull);
+    return (uint32_t)(x >= MRG_M1 ? x - MRG_M1 : x);
+}
+// x mod m2 for x < 2^54: 2^32 = 22853 (mod m2); the first fold leaves x < 2^37, the second < 2 m2
+__host__ __device__ __forceinline__ uint32_t mod_m2_54(uint64_t x) {
+    x = (x >> 32) * 22853ull + (x & 0xffffffffull);
+    x = (x >> 32) * 22853ull + (x & 0xffffffffull);
+    return (uint32_t)(x >= MRG_M2 ? x - MRG_M2 : x);
+}
+
 // one jump: a pair of 3x3 transition-matrix powers (component 1 mod m1, component 2 mod m2)
 struct MrgJump {
     uint32_t a[9];
     uint32_t b[9];
 };
 
+// o = J s. Each matrix entry is split as a = a_h 2^16 + a_l, so that a s = a_h (2^16 s mod m) + a_l s (mod m):
+// a row is then six products of 16 by 32 bits (< 6 2^48 < 2^51) summed without overflow and reduced once.
 __host__ __device__ __forceinline__ void mrg_apply(const MrgJump &J, const uint32_t s[6], uint32_t o[6]) {
+    uint32_t h[6];
 #pragma unroll
-    for (int i = 0; i < 3; ++i) {
-        uint32_t t = mod_m1((uint64_t)J.a[3 * i] * s[0]);
-        uint32_t u = mod_m1((uint64_t)J.a[3 * i + 1] * s[1]);
-        uint32_t w = mod_m1((uint64_t)J.a[3 * i + 2] * s[2]);
-        uint64_t acc = (uint64_t)t + u;
-        acc = acc >= MRG_M1 ? acc - MRG_M1 : acc;
-        acc += w;
-        o[i] = (uint32_t)(acc >= MRG_M1 ? acc - MRG_M1 : acc);
+    for (int k = 0; k < 3; ++k) {
+        h[k] = mod_m1_54((uint64_t)s[k] << 16);
+        h[3 + k] = mod_m2_54((uint64_t)s[3 + k] << 16);
     }
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
-        uint32_t t = mod_m2((uint64_t)J.b[3 * i] * s[3]);
-        uint32_t u = mod_m2((uint64_t)J.b[3 * i + 1] * s[4]);
-        uint32_t w = mod_m2((uint64_t)J.b[3 * i + 2] * s[5]);
-        uint64_t acc = (uint64_t)t + u;
-        acc = acc >= MRG_M2 ? acc - MRG_M2 : acc;
-        acc += w;
-        o[3 + i] = (uint32_t)(acc >= MRG_M2 ? acc - MRG_M2 : acc);
+        uint64_t acc = 0;
+#pragma unroll
+        for (int k = 0; k < 3; ++k)
+            acc += (uint64_t)(J.a[3 * i + k] >> 16) * h[k] + (uint64_t)(J.a[3 * i + k] & 0xffffu) * s[k];
+        o[i] = mod_m1_54(acc);
     }
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        uint64_t acc = 0;
+#pragma unroll
+        for (int k = 0; k < 3; ++k)
+            acc += (uint64_t)(J.b[3 * i + k] >> 16) * h[3 + k] + (uint64_t)(J.b[3 * i + k] & 0xffffu) * s[3 + k];
+        o[3 + i] = mod_m2_54(acc);
+    }
+}
+
+// One MRG32k3a step (RngStream::U01's recurrences, src/RngStream.cpp:266-289, on integers): advances s and
+// returns p1 - p2 (+ m1 when p1 <= p2), the integer in [1, m1] whose value / (m1 + 1) is the draw.
+// component 1: x_n = 1403580 x_{n-2} - 810728 x_{n-3} (mod m1), formed as 1403580 x_{n-2} + 810728 (m1 - x_{n-3});
+// component 2: x_n = 527612 x_{n-1} - 1370589 x_{n-3} (mod m2), likewise; both sums stay below 2^54.
+__host__ __device__ __forceinline__ uint32_t mrg_step(uint32_t s[6]) {
+    const uint32_t p1 = mod_m1_54(1403580ull * s[1] + 810728ull * (uint64_t)(MRG_M1 - s[0]));
+    s[0] = s[1];
+    s[1] = s[2];
+    s[2] = p1;
+    const uint32_t p2 = mod_m2_54(527612ull * s[5] + 1370589ull * (uint64_t)(MRG_M2 - s[3]));
+    s[3] = s[4];
+    s[4] = s[5];
+    s[5] = p2;
+    return p1 > p2 ? p1 - p2 : p1 - p2 + MRG_M1;
 }
 
 // One MRG32k3a draw in (0,1), formed as RngStream::U01 forms it (src/RngStream.cpp:266-289).
 __host__ __device__ __forceinline__ double mrg_u01(uint32_t s[6]) {
-    // component 1: x_n = 1403580 x_{n-2} - 810728 x_{n-3}  (mod m1)
-    uint32_t t1 = mod_m1(1403580ull * s[1]);
-    uint32_t t2 = mod_m1((uint64_t)(MRG_M1 - 810728u) * s[0]);
-    uint64_t p1 = (uint64_t)t1 + t2;
-    p1 = p1 >= MRG_M1 ? p1 - MRG_M1 : p1;
-    s[0] = s[1];
-    s[1] = s[2];
-    s[2] = (uint32_t)p1;
-    // component 2: x_n = 527612 x_{n-1} - 1370589 x_{n-3}  (mod m2)
-    uint32_t t3 = mod_m2(527612ull * s[5]);
-    uint32_t t4 = mod_m2((uint64_t)(MRG_M2 - 1370589u) * s[3]);
-    uint64_t p2 = (uint64_t)t3 + t4;
-    p2 = p2 >= MRG_M2 ? p2 - MRG_M2 : p2;
-    s[3] = s[4];
-    s[4] = s[5];
-    s[5] = (uint32_t)p2;
     const double norm = 1.0 / (4294967087.0 + 1.0);
-    const double d1 = (double)(uint32_t)p1, d2 = (double)(uint32_t)p2;
-    return (p1 > p2) ? (d1 - d2) * norm : (d1 - d2 + 4294967087.0) * norm;
+    return (double)mrg_step(s) * norm;
 }
 
 // RAND(-.5,.5) of include/tetra_element_linear.h:119

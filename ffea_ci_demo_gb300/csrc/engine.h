@@ -36,6 +36,14 @@ struct Launch {
     static cudaError_t measure(const MeasureArgs<R> &a, int blocks, double *out, cudaStream_t s);
 };
 
+// launchers of the mixed-precision element phase (kernels_element_mixed.cuh; instantiated in engine_mixed.cu)
+struct MixedLaunch {
+    static cudaError_t node_prep(const NodePrepArgs &a, cudaStream_t s);
+    // element_mixed_kernel over a.T elements in blocks of EM_THREADS: per-block vertex sums into a.parts when
+    // `partials`, else per-element forces into a.ef (when set); dpsi and volume into a.geom (when set)
+    static cudaError_t element(const ElemArgs<float> &a, bool partials, cudaStream_t s);
+};
+
 // launchers of the adjoint kernels (kernels_adjoint.cuh)
 template <class R>
 struct AdjLaunch {

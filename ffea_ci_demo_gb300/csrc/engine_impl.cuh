@@ -15,12 +15,17 @@ constexpr int GATHER_THREADS = 256;
 constexpr int CG_THREADS = CG_MAX_THREADS;
 constexpr int EULER_THREADS = 256;
 
+// The FP64 element phase; the mixed path's is MixedLaunch::element (kernels_element_mixed.cuh).
 template <class R>
 cudaError_t Launch<R>::element(const ElemArgs<R> &a, cudaStream_t s) {
-    if (a.T <= 0) return cudaSuccess;
-    element_kernel<R><<<(a.T + ELEM_THREADS - 1) / ELEM_THREADS, ELEM_THREADS, 0, s>>>(a);
-    count_launch();
-    return cudaGetLastError();
+    if constexpr (std::is_same<R, float>::value) {
+        return (void)a, (void)s, cudaErrorNotSupported;
+    } else {
+        if (a.T <= 0) return cudaSuccess;
+        element_kernel<R><<<(a.T + ELEM_THREADS - 1) / ELEM_THREADS, ELEM_THREADS, 0, s>>>(a);
+        count_launch();
+        return cudaGetLastError();
+    }
 }
 
 template <class R>
@@ -149,7 +154,18 @@ cudaError_t Launch<R>::cg(const CgArgs<R> &a, int grid, int threads, cudaStream_
             smem = own_smem_bytes_d(a.npb);
         }
     }
-    cudaError_t e = cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(threads), params, smem, s);
+    // a cooperative launch that stream capture records as a cooperative graph node
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(threads);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    cudaError_t e = cudaLaunchKernelExC(&cfg, fn, params);
     count_launch();
     return e;
 }

@@ -9,6 +9,46 @@ namespace ffea {
 template struct Launch<float>;
 template struct AdjLaunch<float>;
 
+__global__ void __launch_bounds__(256) node_prep_kernel(NodePrepArgs g) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < g.N) {
+        const size_t N = g.N;
+        g.u[i] = make_float4((float)(g.px[i] - g.xr[i]), (float)(g.py[i] - g.xr[N + i]),
+                             (float)(g.pz[i] - g.xr[2 * N + i]), 0.f);
+        if (g.vf) g.vf[i] = make_float4((float)g.vx[i], (float)g.vy[i], (float)g.vz[i], 0.f);
+    }
+    if (i < g.nchunks) {
+        int b = 0, c = i;
+        if (g.chunk_blob) {
+            b = g.chunk_blob[i];
+            c = i - g.chunk_off[b];
+        }
+        uint32_t s[6], o[6];
+#pragma unroll
+        for (int k = 0; k < 6; ++k) s[k] = g.rng_state[6 * (size_t)b + k];
+        mrg_apply(g.chunk_jump[c], s, o);
+#pragma unroll
+        for (int k = 0; k < 6; ++k) g.chunk_state[6 * (size_t)i + k] = o[k];
+    }
+}
+
+cudaError_t MixedLaunch::node_prep(const NodePrepArgs &a, cudaStream_t s) {
+    const int n = a.N > a.nchunks ? a.N : a.nchunks;
+    if (n <= 0) return cudaSuccess;
+    node_prep_kernel<<<(n + 255) / 256, 256, 0, s>>>(a);
+    count_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t MixedLaunch::element(const ElemArgs<float> &a, bool partials, cudaStream_t s) {
+    if (a.T <= 0) return cudaSuccess;
+    const int blocks = (a.T + EM_THREADS - 1) / EM_THREADS;
+    if (partials) element_mixed_kernel<true><<<blocks, EM_THREADS, 0, s>>>(a);
+    else element_mixed_kernel<false><<<blocks, EM_THREADS, 0, s>>>(a);
+    count_launch();
+    return cudaGetLastError();
+}
+
 cudaError_t BatchLaunch::schedule(BlobCgDesc *desc, const int *blob_iters, int nblobs, int ncta, int *cta_blob,
                                   const DevStatus *st, cudaStream_t s) {
     const size_t smem = (size_t)nblobs * (2 * sizeof(double) + sizeof(int));

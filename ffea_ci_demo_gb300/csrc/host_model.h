@@ -227,6 +227,53 @@ inline void build_linearise_events(HostModel &h) {
     for (int a = 0; a < N; ++a) h.lin_ev.insert(h.lin_ev.end(), ev[a].begin(), ev[a].end());
 }
 
+// The mixed element kernel's thread-block lists: for each block of `cta` consecutive elements, its distinct
+// vertices in ascending order (cta_nodes[cta_ptr[c] .. cta_ptr[c + 1])), each element's four vertices as indices
+// into its block's list (loc, 4 per element), and where each (block, vertex) force sum goes: perm[p] for the p-th
+// list entry, such that a vertex's sums lie together, in block order, at [part_ptr[a], part_ptr[a + 1]).
+// The block's own incidence: its 4 x (elements) (element, slot) pairs, coded 4 el + slot with el the element's
+// index in the block, sorted by vertex and, for each vertex, by element (inc_local[4 cta c ..]); the p-th list
+// entry's run starts at inc_start[p] within its block's part and ends where the next entry's starts (the block's
+// last entry at 4 x its elements).
+struct CtaLists {
+    std::vector<int> cta_ptr, cta_nodes, perm, part_ptr;
+    std::vector<uint16_t> loc, inc_local, inc_start;
+};
+
+inline void build_cta_lists(const HostModel &h, int cta, CtaLists &o) {
+    const int T = h.T, N = h.N, nc = (T + cta - 1) / cta;
+    o.cta_ptr.assign(nc + 1, 0);
+    o.cta_nodes.clear();
+    o.inc_local.clear();
+    o.inc_start.clear();
+    o.loc.assign(4 * (size_t)T, 0);
+    std::vector<int> list;
+    for (int c = 0; c < nc; ++c) {
+        const int e0 = c * cta, e1 = std::min(T, e0 + cta);
+        list.assign(h.tet4.begin() + 4 * (size_t)e0, h.tet4.begin() + 4 * (size_t)e1);
+        std::sort(list.begin(), list.end());
+        list.erase(std::unique(list.begin(), list.end()), list.end());
+        for (size_t k = 4 * (size_t)e0; k < 4 * (size_t)e1; ++k)
+            o.loc[k] = (uint16_t)(std::lower_bound(list.begin(), list.end(), h.tet4[k]) - list.begin());
+        // the block's incidence, by vertex then element (a counting sort over the local vertex indices)
+        std::vector<int> cnt(list.size() + 1, 0);
+        for (size_t k = 4 * (size_t)e0; k < 4 * (size_t)e1; ++k) cnt[o.loc[k] + 1]++;
+        for (size_t i = 0; i < list.size(); ++i) cnt[i + 1] += cnt[i];
+        for (size_t i = 0; i < list.size(); ++i) o.inc_start.push_back((uint16_t)cnt[i]);
+        std::vector<uint16_t> blk(4 * (size_t)cta, 0);
+        for (size_t k = 4 * (size_t)e0; k < 4 * (size_t)e1; ++k) blk[cnt[o.loc[k]]++] = (uint16_t)(k - 4 * (size_t)e0);
+        o.inc_local.insert(o.inc_local.end(), blk.begin(), blk.end());
+        o.cta_nodes.insert(o.cta_nodes.end(), list.begin(), list.end());
+        o.cta_ptr[c + 1] = (int)o.cta_nodes.size();
+    }
+    o.part_ptr.assign(N + 1, 0);
+    for (int a : o.cta_nodes) o.part_ptr[a + 1]++;
+    for (int a = 0; a < N; ++a) o.part_ptr[a + 1] += o.part_ptr[a];
+    std::vector<int> fill(o.part_ptr.begin(), o.part_ptr.end() - 1);
+    o.perm.resize(o.cta_nodes.size());
+    for (size_t q = 0; q < o.cta_nodes.size(); ++q) o.perm[q] = fill[o.cta_nodes[q]]++;
+}
+
 inline int build_model(const ffea_gpu_mesh *mesh, const ffea_gpu_params *p, HostModel &h) {
     const int n = mesh->num_nodes, T = mesh->num_elements;
     if (n <= 0 || T <= 0 || mesh->num_pinned < 0 || !mesh->pos || !mesh->tets || !mesh->rho || !mesh->A ||

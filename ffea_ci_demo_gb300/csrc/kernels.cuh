@@ -8,10 +8,12 @@
 // src/SparseMatrixFixedPattern.cpp); only the CG's cross-node reductions are
 // summed in a different (fixed) order.
 //
-// R = float is the mixed path: Jacobian, determinant, inversion check and
-// volume stay FP64; stress, noise scaling, matrix values, SpMV and CG vectors
-// are FP32; dot products and norms are accumulated across nodes in FP64;
-// positions are FP64 accumulators.
+// R = float is the mixed path: stress, noise scaling, matrix values, SpMV and
+// CG vectors are FP32; dot products and norms are accumulated across nodes in
+// FP64; positions are FP64 accumulators. Its element phase is
+// element_mixed_kernel (kernels_element_mixed.cuh), which keeps the Jacobian
+// in FP64 only for near-degenerate elements; element_kernel below is the FP64
+// path's.
 //
 // Layouts (N vertex nodes, T elements):
 //   positions/velocities   SoA double px,py,pz / vx,vy,vz
@@ -48,6 +50,17 @@ struct ElemArgs {
     const MrgJump *lane_jump;      // 32: A^(7*l)
     int recompute;                 // 1: re-evaluation at stored positions (no inversion test, last_det kept)
     DevStatus *st;
+    // mixed path (element_mixed_kernel): node displacements and velocities in FP32 (node_prep_kernel), the thread
+    // blocks' vertex lists, each element's vertices as indices into its block's list, the node-major block sums
+    // and their positions, and the stream state at every 32-element chunk
+    const float4 *u, *vf;
+    const int *cta_ptr, *cta_nodes;
+    const ushort4 *loc;
+    const unsigned short *inc_local, *inc_start;  // each block's incidence, by vertex then element
+    float4 *parts;
+    const int *perm;
+    const uint32_t *chunk_state;   // 6 per 32-element chunk: the stream state at the chunk's first draw
+    const int *chunk_off;          // batch: first chunk of each blob
 };
 
 // V[r][c] of tetra_element_linear::create_viscosity_matrix (src/tetra_element_linear.cpp:298-327)
@@ -569,6 +582,10 @@ struct GatherArgs {
     int mode;             // 0: CG (NoMass or consistent mass), 1: mass-lumped scaling, 2: batch CG (f, r only)
     const int *inc_ptr, *inc;  // element*4 + slot, element order
     const R *ef;
+    // mixed path: the element forces as per-block vertex sums, node-major (parts[part_ptr[a] ..
+    // part_ptr[a + 1]) in block order), in place of inc / ef when set
+    const float4 *parts;
+    const int *part_ptr;
     const int *pinned;
     const double *drag;   // inertial Stokes drag (force -= v * drag) or null
     const double *vx, *vy, *vz;
@@ -587,6 +604,10 @@ struct GatherArgs {
     // Stokes noise (calc_stokes and calc_noise): 3 draws per node of the reference numbering, after the
     // elements' 7T, in node order; a midpoint's force is moved to its edge ends by linearise events
     NodeForces sn;
+    // mixed mass-lumped step: the Euler update (euler_kernel's arithmetic) done by the gather, on these
+    double *upx, *upy, *upz, *uvx, *uvy, *uvz;
+    double dt;
+    int fuse_euler;
 };
 
 template <class R>

@@ -133,7 +133,9 @@ __global__ void __launch_bounds__(BATCH_MAX_THREADS) cg_batch_kernel(const __gri
     const float4 *pold = reinterpret_cast<const float4 *>(g.pbuf0);
     float4 *pnew = reinterpret_cast<float4 *>(g.pbuf1);
     int it = 0;
-    for (; ok && it < g.imax; ++it) {
+    // a zero force (a blob exactly at rest without noise) has the solution x = 0: no iteration
+    if (f2 == 0.0 && threadIdx.x == 0) s_conv = 1;
+    for (; ok && it < g.imax && f2 != 0.0; ++it) {
         const bool first = it == 0;
         const float beta = s_beta;
         // phase A: q = V p with p = z + beta p_old formed on the fly; p.q; moments of D p

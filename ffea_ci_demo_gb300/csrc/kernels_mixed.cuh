@@ -26,6 +26,7 @@
 #pragma once
 
 #include "kernels.cuh"
+#include "kernels_element_mixed.cuh"
 
 namespace ffea {
 
@@ -63,12 +64,21 @@ __global__ void __launch_bounds__(256) gather_mixed_kernel(GatherArgs<R> g) {
             F1 = (float)g.sn.node_ctf[3 * (size_t)a + 1];
             F2 = (float)g.sn.node_ctf[3 * (size_t)a + 2];
         }
-        for (int m = g.inc_ptr[a]; m < g.inc_ptr[a + 1]; ++m) {
-            const int es = g.inc[m];
-            const R *c = g.ef + 12 * (size_t)(es >> 2) + 3 * (es & 3);
-            F0 += c[0];
-            F1 += c[1];
-            F2 += c[2];
+        if (g.parts) {
+            for (int m = g.part_ptr[a]; m < g.part_ptr[a + 1]; ++m) {
+                const float4 q = g.parts[m];
+                F0 += q.x;
+                F1 += q.y;
+                F2 += q.z;
+            }
+        } else {
+            for (int m = g.inc_ptr[a]; m < g.inc_ptr[a + 1]; ++m) {
+                const int es = g.inc[m];
+                const R *c = g.ef + 12 * (size_t)(es >> 2) + 3 * (es & 3);
+                F0 += c[0];
+                F1 += c[1];
+                F2 += c[2];
+            }
         }
         if (g.sn.vface_ptr) {
             float F[3] = {F0, F1, F2};
@@ -90,9 +100,18 @@ __global__ void __launch_bounds__(256) gather_mixed_kernel(GatherArgs<R> g) {
         if (g.pinned[a]) { F0 = 0; F1 = 0; F2 = 0; }
         g.f[4 * a] = F0; g.f[4 * a + 1] = F1; g.f[4 * a + 2] = F2;
         if (g.mode == 1) {
-            g.x[4 * a] = F0 * g.dinv[4 * a];
-            g.x[4 * a + 1] = F1 * g.dinv[4 * a + 1];
-            g.x[4 * a + 2] = F2 * g.dinv[4 * a + 2];
+            const R x0 = F0 * g.dinv[4 * a], x1 = F1 * g.dinv[4 * a + 1], x2 = F2 * g.dinv[4 * a + 2];
+            g.x[4 * a] = x0;
+            g.x[4 * a + 1] = x1;
+            g.x[4 * a + 2] = x2;
+            if (g.fuse_euler) {
+                // euler_integrate (src/Blob.cpp:3249-3279) as euler_kernel does it: v += a dt, p += v dt
+                const double a0 = (double)x0, a1 = (double)x1, a2 = (double)x2;
+                if (!(isfinite(a0) && isfinite(a1) && isfinite(a2))) atomicExch(&g.st->nonfinite, 1);
+                const double v0 = g.uvx[a] + a0 * g.dt, v1 = g.uvy[a] + a1 * g.dt, v2 = g.uvz[a] + a2 * g.dt;
+                g.uvx[a] = v0; g.uvy[a] = v1; g.uvz[a] = v2;
+                g.upx[a] += v0 * g.dt; g.upy[a] += v1 * g.dt; g.upz[a] += v2 * g.dt;
+            }
             return;
         }
         g.r[4 * a] = F0; g.r[4 * a + 1] = F1; g.r[4 * a + 2] = F2;
@@ -240,7 +259,10 @@ __global__ void __launch_bounds__(1024, 1) cg_mixed_kernel(const __grid_constant
     float *pold = g.pbuf0, *pnew = g.pbuf1;
     FFEA_MARK(g, tm, 0);
     int it = 0;
-    for (; ok && it < g.imax; ++it) {
+    // a zero force (a blob exactly at rest without noise) has the solution x = 0: no iteration (the first step
+    // length would be 0/0)
+    if (f2 == 0.0 && threadIdx.x == 0) s_conv = 1;
+    for (; ok && it < g.imax && f2 != 0.0; ++it) {
         const bool first = it == 0;
         const float beta = s_beta;
         // phase A: q = V p with p formed on the fly; p.q; moments of D p for Z^T D p
@@ -590,7 +612,9 @@ __global__ void __launch_bounds__(1024, 1) cg_mixed_own_kernel(const __grid_cons
     const int npass = (nloc + gpb - 1) / gpb;
     FFEA_MARK(g, tm, 0);
     int it = 0;
-    for (; ok && it < g.imax; ++it) {
+    // a zero force (a blob exactly at rest without noise) has the solution x = 0: no iteration
+    if (f2 == 0.0 && threadIdx.x == 0) s_conv = 1;
+    for (; ok && it < g.imax && f2 != 0.0; ++it) {
         const bool first = it == 0;
         const float beta = s_beta;
         // phase A: q = V p over the block's rows (p formed on the fly); p.q; moments of D p

@@ -34,7 +34,8 @@ extern "C" {
 #define FFEA_GPU_EINPUT 3    /* invalid argument, mesh or parameter */
 #define FFEA_GPU_ENOMEM 4    /* device or host allocation failed */
 #define FFEA_GPU_ECUDA 5     /* CUDA runtime error or extension built for another GPU */
-#define FFEA_GPU_ENAN 6      /* non-finite solver output (e.g. zero right-hand side, see the reference's alpha = 0/0) */
+#define FFEA_GPU_ENAN 6      /* non-finite solver output (FP64 path: e.g. an exactly zero right-hand side, as the
+                                reference's alpha = 0/0; the mixed path returns x = 0 for it) */
 #define FFEA_GPU_ETIMEOUT 7  /* a bounded device-side wait gave up */
 #define FFEA_GPU_EFILE 8     /* structure file missing or malformed (FFEAFileException) */
 
