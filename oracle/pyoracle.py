@@ -122,10 +122,8 @@ def ref_lib():
     lib.ref_rng_increased_precis.argtypes = [C.c_void_p, C.c_int]
     lib.ref_rng_get_state.argtypes = [C.c_void_p, _up]
     lib.ref_rng_set_package_seed.argtypes = [_up]
-    lib.ref_blob_create.restype = C.c_void_p
-    lib.ref_blob_create.argtypes = [C.c_int, _dp, C.c_double, C.c_int, _ip, _dp, _dp, C.c_int, _ip,
-                                    C.c_double, C.c_double, C.c_double, C.c_double, C.c_int, C.c_int, C.c_int,
-                                    C.c_int, C.c_int, C.POINTER(C.c_int)]
+    lib.ref_blob_load.restype = C.c_void_p
+    lib.ref_blob_load.argtypes = [C.c_char_p] * 7 + [C.c_double] * 5 + [C.c_int] * 5 + [C.POINTER(C.c_int)]
     lib.ref_blob_destroy.argtypes = [C.c_void_p]
     for name, args in {
         "blob_step": [C.c_void_p, C.c_int],
@@ -142,8 +140,6 @@ def ref_lib():
         "blob_get_inv_mass": [C.c_void_p, _dp],
         "blob_get_rng_state": [C.c_void_p, C.c_int, _up],
         "blob_measure": [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double)],
-        "blob_set_ctforces": [C.c_void_p, C.c_int, _ip, _dp, C.c_int, _ip, _ip, _dp, C.c_int, _ip],
-        "blob_set_rot_ctforces": [C.c_void_p, C.c_int, _ip, _ip, _dp],
     }.items():
         getattr(lib, "ref_" + name).argtypes = args
     lib._typed = True
@@ -375,19 +371,36 @@ class OracleBlob(_BlobBase):
 
 
 class RefBlob(_BlobBase):
-    """The reference's own classes behind the same methods (build container only)."""
+    """The reference's own Blob (Blob::config + Blob::init from structure files, World::run's step) behind the
+    same methods (build container only). The mesh is written to the reference's structure files first (17
+    significant digits, which the reference's readers parse back exactly); ``ctforces`` is a pair (constant-force
+    file, surface file) of the reference's formats, loaded by the reference's own Blob::load_ctforces."""
 
     def __init__(self, mesh, *, solver="CG_nomass", dt=1e-12, kT=4.11e-21, epsilon=1e-10, stokes_visc=1e-3,
-                 max_iterations_cg=10000, calc_noise=1, calc_stokes=0, threads=1, package_seed=(12345,) * 6):
+                 max_iterations_cg=10000, calc_noise=1, calc_stokes=0, threads=1, package_seed=(12345,) * 6,
+                 ctforces=None):
+        import tempfile
+
+        from ffea_ci_demo_gb300.mesh import surface_faces, write_structure, write_surface
+
         self._lib = ref_lib()
         self._p = "ref_"
         if self._lib.ref_rng_set_package_seed(np.asarray(package_seed, np.uint32)) != 0:
             raise ValueError("invalid package seed")
-        st = C.c_int()
-        self._h = self._lib.ref_blob_create(*_mesh_args(mesh), dt, kT, epsilon, stokes_visc, max_iterations_cg,
-                                            calc_noise, calc_stokes, SOLVERS[solver], threads, C.byref(st))
+        with tempfile.TemporaryDirectory() as d:
+            paths = write_structure(mesh, d, "blob")
+            surf = ctforces[1] if ctforces else os.path.join(d, "blob.surf")
+            if not ctforces:
+                write_surface(surf, surface_faces(mesh))
+            enc = lambda x: None if x is None else str(x).encode()  # noqa: E731
+            st = C.c_int()
+            self._h = self._lib.ref_blob_load(enc(paths["node"]), enc(paths["top"]), enc(surf), enc(paths["mat"]),
+                                              enc(paths["stokes"]), enc(paths["pin"]),
+                                              enc(ctforces[0]) if ctforces else None, mesh.scale, dt, kT, epsilon,
+                                              stokes_visc, max_iterations_cg, calc_noise, calc_stokes,
+                                              SOLVERS[solver], threads, C.byref(st))
         if not self._h:
-            raise ValueError(f"ref_blob_create failed (status {st.value})")
+            raise ValueError(f"ref_blob_load failed (status {st.value})")
         self.n_nodes, self.n_elem = mesh.n_nodes, mesh.n_elem
 
     def __del__(self):

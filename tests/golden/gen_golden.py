@@ -5,9 +5,9 @@ Run in a container that has the reference sources (default /root/reference):
     make -C oracle ref
     OMP_NUM_THREADS=1 python tests/golden/gen_golden.py
 
-It drives oracle/_ref/libffea_ref.so (the reference's hot-path classes,
-compiled from its sources by oracle/Makefile) through oracle/pyoracle.py and
-writes small .npz files. OMP_NUM_THREADS=1 is required: the reference's
+It drives oracle/_ref/libffea_ref.so (the reference's own Blob with its
+solvers, compiled from its sources by oracle/Makefile) through
+oracle/pyoracle.py and writes small .npz files. OMP_NUM_THREADS=1 is required: the reference's
 NoMass CG reductions and noise streams are only reproducible single-threaded,
 which is also how the reference's own physics tests run them.
 
@@ -116,11 +116,10 @@ def digest(*arrays):
 
 
 def dump_blob(name, m, pos0, steps, full=True, ctf=None, **kw):
-    b = po.RefBlob(m, **kw)
+    b = po.RefBlob(m, ctforces=ctf, **kw)
     b.set_pos(pos0)
     out = {"n": m.n_nodes, "T": m.n_elem, "steps": steps}
     if ctf is not None:
-        b.set_ctforces(po.read_ctforces(ctf[0], 0, m.n_nodes), po.read_surface(ctf[1]))
         out["ctf_sha256"] = file_digest(*ctf)
     rest = b.rest()
     out["jinv0"] = rest["jinv0"]

@@ -168,3 +168,25 @@ def test_oracle_reports_cg_max_iterations(oracle_built):
     b = po.OracleBlob(m, solver="CG_nomass", dt=1e-12, kT=0.0, calc_noise=0, threads=1, max_iterations_cg=2)
     b.set_pos(sheared(m, 0.02))
     assert b.step(1) == 2  # ORC_ECGMAXIT
+
+
+@pytest.mark.skipif(not os.path.exists(po.REF_LIB), reason="the reference's own build exists only where its sources are")
+@pytest.mark.parametrize("solver,dt,kw", [
+    ("CG_nomass", 1e-12, dict(kT=4.11e-21, calc_noise=1)),
+    ("masslumped", 1e-14, dict(kT=4.11e-21, calc_noise=1, calc_stokes=1)),
+    ("CG", 1e-14, dict(kT=0.0, calc_noise=0)),
+])
+def test_oracle_matches_reference_blob(oracle_built, solver, dt, kw):
+    """Where the reference's sources are, its own Blob (Blob::config/init from structure files, World::run's step;
+    oracle/_ref) and the C restatement step a fresh seeded cube to the same bits: positions, velocities, the
+    last right-hand side and the stream state."""
+    m = case_mesh(2, 31, [3])
+    p = sheared(m, 0.02)
+    r = po.RefBlob(m, solver=solver, dt=dt, threads=1, **kw)
+    o = po.OracleBlob(m, solver=solver, dt=dt, threads=1, **kw)
+    r.set_pos(p)
+    o.set_pos(p)
+    assert r.step(15) == 0 and o.step(15) == 0
+    for get in ("pos", "vel", "rhs"):
+        assert np.array_equal(getattr(r, get)(), getattr(o, get)()), get
+    assert np.array_equal(r.rng_state(), o.rng_state())
