@@ -43,6 +43,14 @@ struct ffea_gpu_batch {
     float *jinv, *G, *E, *A, *B, *vol0, *geom;
     double *last_det;
     MixedElements me;  // FP32 node data, thread-block lists and per-block force sums of the element phase
+    // Stokes noise (calc_stokes with calc_noise): per blob, 3 draws per node of its reference numbering after
+    // its elements' 7 T_b, from its own stream; a midpoint's force reaches the vertices by the linearise replay
+    MrgJump *sn_chunk_jump = nullptr, *sn_lane_jump = nullptr;
+    int *sn_node_orig = nullptr, *sn_mid_orig = nullptr, *sn_lin_ptr = nullptr, *sn_orig_off = nullptr,
+        *sn_chunk_off = nullptr;
+    double *sn_mid_drag = nullptr;
+    int4 *sn_lin_ev = nullptr;
+    float *mid_f = nullptr;
     int *inc_ptr, *inc, *pinned, *slice_ptr, *rowlen, *bcol, *diagk, *src_ptr, *grp_slice;
     unsigned *src;
     double *drag = nullptr;
@@ -242,10 +250,50 @@ int ffea_gpu_batch::init() {
     for (int l = 0; l < 32; ++l) lj[l] = jump_pow(7ull * l);
     CK(mem.upload(&chunk_jump, cj));
     CK(mem.upload(&lane_jump, lj));
+    // a step consumes 7 draws per element of the blob (noise on) and, with Stokes noise, 3 per node of its
+    // reference numbering
+    const bool snoise = p.calc_noise == 1 && p.calc_stokes == 1;
     std::vector<MrgJump> sj(nblobs);
-    for (int b = 0; b < nblobs; ++b)
-        sj[b] = jump_pow(p.calc_noise == 1 ? 7ull * (uint64_t)(elem_off[b + 1] - elem_off[b]) : 0ull);
+    for (int b = 0; b < nblobs; ++b) {
+        const uint64_t draws = p.calc_noise == 1 ? 7ull * (uint64_t)(elem_off[b + 1] - elem_off[b]) : 0ull;
+        const uint64_t sdraws = snoise ? 3ull * (uint64_t)(nall_off[b + 1] - nall_off[b]) : 0ull;
+        sj[b] = jump_pow(draws + sdraws);
+    }
     CK(mem.upload(&step_jumps, sj));
+    if (snoise) {
+        // blob b's node chunk c starts A^(7 T_b + 96 c) after its stream state
+        std::vector<int> choff(nblobs + 1, 0);
+        std::vector<MrgJump> ncj;
+        const Mat3 a96 = mat_pow(MRG_A1, 96, MRG_M1), b96 = mat_pow(MRG_A2, 96, MRG_M2);
+        for (int b = 0; b < nblobs; ++b) {
+            const int nch = (nall_off[b + 1] - nall_off[b] + 31) / 32;
+            const uint64_t base = 7ull * (uint64_t)(elem_off[b + 1] - elem_off[b]);
+            Mat3 ja = mat_pow(MRG_A1, base, MRG_M1), jb = mat_pow(MRG_A2, base, MRG_M2);
+            for (int c = 0; c < nch; ++c) {
+                ncj.push_back(to_jump(ja, jb));
+                ja = mat_mul(a96, ja, MRG_M1);
+                jb = mat_mul(b96, jb, MRG_M2);
+            }
+            choff[b + 1] = choff[b] + nch;
+        }
+        std::vector<MrgJump> nlj(32);
+        for (int l = 0; l < 32; ++l) nlj[l] = jump_pow(3ull * l);
+        CK(mem.upload(&sn_chunk_jump, ncj));
+        CK(mem.upload(&sn_lane_jump, nlj));
+        CK(mem.upload(&sn_chunk_off, choff));
+        CK(mem.upload(&sn_orig_off, nall_off));
+        CK(mem.upload(&sn_node_orig, h.node_of));
+        CK(mem.upload(&sn_mid_orig, h.mid_nodes));
+        std::vector<double> mdrag(h.mid_nodes.size());
+        for (size_t m = 0; m < h.mid_nodes.size(); ++m) mdrag[m] = h.drag_all[h.mid_nodes[m]];
+        CK(mem.upload(&sn_mid_drag, mdrag));
+        CK(mem.upload(&sn_lin_ptr, h.lin_ptr));
+        std::vector<int4> ev(h.lin_ev.size() / 4);
+        for (size_t k = 0; k < ev.size(); ++k)
+            ev[k] = make_int4(h.lin_ev[4 * k], h.lin_ev[4 * k + 1], h.lin_ev[4 * k + 2], -1);
+        CK(mem.upload(&sn_lin_ev, ev));
+        if (!h.mid_nodes.empty()) CK(mem.alloc(&mid_f, 3 * h.mid_nodes.size()));
+    }
     CK(mem.alloc(&st, 1));
     CK(mem.alloc(&gbs, (size_t)nblobs));
     // CG descriptions: rows, rigid modes of each blob; an iteration estimate for the first schedule
@@ -357,6 +405,30 @@ int ffea_gpu_batch::launch_gather() {
     ga.dinv = dinv; ga.f = f; ga.x = x; ga.r = r;
     ga.partials = nullptr; ga.stride = 0; ga.st = st; ga.gb = nullptr;
     ga.dpos = dpos; ga.px = px; ga.py = py; ga.pz = pz; ga.diag = diag;
+    if (sn_chunk_jump) {
+        NodeForces &sn = ga.sn;
+        sn.noise = 1;
+        sn.kT = p.kT;
+        sn.dt = p.dt;
+        sn.rng_state = rng_states;
+        sn.chunk_jump = sn_chunk_jump;
+        sn.lane_jump = sn_lane_jump;
+        sn.node_orig = sn_node_orig;
+        sn.node_drag = drag;
+        sn.mid_orig = sn_mid_orig;
+        sn.mid_drag = sn_mid_drag;
+        sn.lin_ptr = sn_lin_ptr;
+        sn.lin_ev = sn_lin_ev;
+        sn.orig_off = sn_orig_off;
+        sn.chunk_off = sn_chunk_off;
+        sn.nblobs = nblobs;
+        sn.on = 1;
+        // each midpoint's noise once per step (the vertices' linearise replay reads it up to ~20 times)
+        if (mid_f) {
+            CK(Launch<float>::mid_force(sn, (int)h.mid_nodes.size(), mid_f, st, stream));
+            sn.mid_f = mid_f;
+        }
+    }
     const int gthreads = Launch<float>::gather_threads();
     CK(Launch<float>::gather(ga, (h.N + gthreads - 1) / gthreads, stream));
     return FFEA_GPU_OK;
@@ -415,10 +487,6 @@ int check_batch_params(const ffea_gpu_params *p) {
     }
     if (p->solver != FFEA_GPU_NOMASS_CG || p->precision != FFEA_GPU_MIXED) {
         g_last_error = "a batch runs the CG_nomass solver in mixed precision";
-        return FFEA_GPU_EINPUT;
-    }
-    if (p->calc_stokes == 1 && p->calc_noise == 1) {
-        g_last_error = "a batch does not draw Stokes noise (calc_stokes with calc_noise)";
         return FFEA_GPU_EINPUT;
     }
     return FFEA_GPU_OK;

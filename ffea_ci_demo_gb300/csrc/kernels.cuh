@@ -399,17 +399,35 @@ struct NodeForces {
     const int4 *lin_ev;            // up to three live midpoints (-1: already moved) summed into the vertex
     const void *mid_f;             // this step's midpoint forces (3 per midpoint, in the step's precision R) as
                                    // midpoint_force gives them, computed once by mid_force_kernel (or null)
+    // a batch: reference node i belongs to the blob b with orig_off[b] <= i < orig_off[b + 1] (nblobs + 1
+    // entries), draws from rng_state[6 b ..] and its chunk jumps start at chunk_jump[chunk_off[b]] (null: one blob)
+    const int *orig_off;
+    const int *chunk_off;
+    int nblobs;
 };
 
 // force[i] -= RAND(-.5,.5) * sqrt(24 kT drag / dt), three components, for reference node i
-// (Blob::aggregate_forces_and_solve, src/Blob.cpp:3190-3219)
+// (Blob::aggregate_forces_and_solve, src/Blob.cpp:3190-3219); in a batch, i is the node's index in the
+// concatenated numbering and the draws come from its blob's stream
 template <class R>
 __device__ __forceinline__ void stokes_noise_sub(const NodeForces &sn, int i, double drag, R (&F)[3]) {
     uint32_t base[6], s6[6];
+    const uint32_t *rs = sn.rng_state;
+    int li = i, chunk = i >> 5;
+    if (sn.orig_off) {  // a batch: the node's blob, its index in the blob's numbering, the blob's stream
+        int lo = 0, hi = sn.nblobs;
+        while (hi - lo > 1) {
+            const int mid = (lo + hi) >> 1;
+            if (sn.orig_off[mid] <= i) lo = mid; else hi = mid;
+        }
+        li = i - sn.orig_off[lo];
+        chunk = sn.chunk_off[lo] + (li >> 5);
+        rs += 6 * (size_t)lo;
+    }
 #pragma unroll
-    for (int k = 0; k < 6; ++k) s6[k] = sn.rng_state[k];
-    mrg_apply(sn.chunk_jump[i >> 5], s6, base);
-    mrg_apply(sn.lane_jump[i & 31], base, s6);
+    for (int k = 0; k < 6; ++k) s6[k] = rs[k];
+    mrg_apply(sn.chunk_jump[chunk], s6, base);
+    mrg_apply(sn.lane_jump[li & 31], base, s6);
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
         const double r = mrg_rand_half(s6);

@@ -294,7 +294,8 @@ void ffea_gpu_adjoint_destroy(ffea_gpu_adjoint *adj);
  * blob has converged. Mixed precision and the CG_nomass solver only. Blob b's
  * noise comes from substream b of the stream whose state is the package seed
  * 12345 x 6 (RngStream::ResetNextSubstream applied b times), drawn in the
- * reference's single-thread order within the blob.
+ * reference's single-thread order within the blob: 7 per element, then (Stokes
+ * drag with noise) 3 per node of the blob's own numbering.
  * ------------------------------------------------------------------------- */
 typedef struct ffea_gpu_batch ffea_gpu_batch;
 #define FFEA_GPU_BATCH_MAX_BLOBS 2048

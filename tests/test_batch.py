@@ -90,6 +90,39 @@ def test_batch_matches_single_blobs(gpu, oracle_built):
 
 
 @pytest.mark.gpu
+def test_batch_stokes_noise_matches_single_blobs(gpu, oracle_built):
+    """Stokes drag with noise: each blob draws 3 numbers per node of its own numbering after its elements' 7 per
+    element (Blob::aggregate_forces_and_solve, src/Blob.cpp:3190-3219), from its own substream; midpoints' draws
+    reach the vertices through the linearise replay. Same bounds as without Stokes noise."""
+    meshes = [case_mesh(n, s) for n, s in MESHES]
+    kw = dict(dt=1e-12, kT=4.11e-21, calc_noise=1, calc_stokes=1)
+    bt = lib.Batch(meshes, **kw)
+    x0 = [sheared(m, 0.02, seed=11 + b) for b, m in enumerate(meshes)]
+    for b in range(len(meshes)):
+        bt.set_state(b, pos=x0[b])
+    bt.update(1)
+    want = substream_states(len(meshes))
+    for b, m in enumerate(meshes):
+        o = po.OracleRng()
+        o.set_state(want[b])
+        for _ in range(7 * m.n_elem + 3 * m.n_nodes):
+            o.rand_u01()
+        assert np.array_equal(bt.rng_state(b), o.get_state()), b
+    bt.update(9)
+    its, _ = bt.cg_iterations()
+    for b, m in enumerate(meshes):
+        s = lib.Blob(m, solver="CG_nomass", precision="mixed", cg_poly=-1, rng_state=want[b], **kw)
+        s.set_state(pos=x0[b])
+        s.update(10)
+        err = np.abs(bt.pos(b) - s.pos()).max() / np.abs(s.pos() - x0[b]).max()
+        print(f"blob {b}: {m.n_elem} tets, Stokes noise, batch vs single error {err:.2e}, iterations {its[b]} / "
+              f"{s.cg_iterations()[0]}")
+        assert err < 1e-5, b
+        assert abs(int(its[b]) - s.cg_iterations()[0]) <= 2, b
+        assert np.array_equal(bt.rng_state(b), s.rng_state()), b
+
+
+@pytest.mark.gpu
 def test_batch_kT0_error_vs_fp64():
     meshes = [case_mesh(n, s) for n, s in ((4, 1), (6, 12345), (3, 9))]
     kw = dict(dt=1e-12, kT=0.0, calc_noise=0)
