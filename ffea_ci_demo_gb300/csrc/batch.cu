@@ -19,6 +19,8 @@
 #include <vector>
 
 #include "../../include/ffea_gpu.h"
+#include "ctforces.h"
+#include "ctforces_device.h"
 #include "engine.h"
 #include "host_model.h"
 #include "mixed_elements.h"
@@ -51,6 +53,11 @@ struct ffea_gpu_batch {
     double *sn_mid_drag = nullptr;
     int4 *sn_lin_ev = nullptr;
     float *mid_f = nullptr;
+    // constant forces (ffea_gpu_batch_load_ctforces): each blob's model, all of them on the device in the
+    // concatenated numbering, and the linearise replay when only they need it
+    std::vector<CtfModel> ctf_models;
+    CtfDevice ctf;
+    Arena lin_mem;
     int *inc_ptr, *inc, *pinned, *slice_ptr, *rowlen, *bcol, *diagk, *src_ptr, *grp_slice;
     unsigned *src;
     double *drag = nullptr;
@@ -76,6 +83,10 @@ struct ffea_gpu_batch {
     int max_rows = 0, max_elems = 0;
     // launch configuration (ffea_gpu_batch_tune)
     int cg_threads = 256, tpn = 4, ncta = 0, ncta_cap = 0;
+    // launch shapes of the force phase (ffea_gpu_batch_set_shapes): elements per block of the element kernel,
+    // threads per block and slot split of the assembly (0: automatic, 1: three threads per slot, 2: one),
+    // threads per block of the gather
+    int asm_threads = 128, asm_split = 0, gather_threads = 256;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t gexec = nullptr;
     int kernels_per_step = 0;
@@ -91,6 +102,8 @@ struct ffea_gpu_batch {
 
     int init();
     int configure(int threads, int tpn_);
+    int set_shapes(int em, int at, int as, int gt);
+    int time_forces(int reps, double &ms);
     int record_step();
     int capture();
     int launch_forces();
@@ -341,6 +354,42 @@ int ffea_gpu_batch::configure(int threads, int tpn_) {
     return capture();
 }
 
+// the force phase's launch shapes; the step graph is captured again
+int ffea_gpu_batch::set_shapes(int em, int at, int as, int gt) {
+    auto ok = [](int t) { return t == 64 || t == 128 || t == 256; };
+    if (!ok(em) || !ok(at) || !ok(gt) || as < 0 || as > 2) {
+        g_last_error = "invalid batch launch shapes";
+        return FFEA_GPU_EINPUT;
+    }
+    if (em != me.threads) {
+        CK(cudaStreamSynchronize(stream));
+        CK(me.set_threads(h, em));
+    }
+    asm_threads = at;
+    asm_split = as;
+    gather_threads = gt;
+    return capture();
+}
+
+// mean time of the force phase (node preparation, elements, assembly, node forces) over `reps` launches
+// after one warm-up, at the current positions; changes no state the step reads
+int ffea_gpu_batch::time_forces(int reps, double &ms) {
+    double tot = 0.0;
+    for (int k = 0; k <= reps; ++k) {
+        CK(cudaEventRecord(ev0, stream));
+        int rc = launch_forces();
+        if (!rc) rc = launch_gather();
+        if (rc) return rc;
+        CK(cudaEventRecord(ev1, stream));
+        CK(cudaEventSynchronize(ev1));
+        float t = 0.f;
+        CK(cudaEventElapsedTime(&t, ev0, ev1));
+        if (k > 0) tot += t;
+    }
+    ms = tot / reps;
+    return FFEA_GPU_OK;
+}
+
 // one step of every blob, as launched into `stream` (captured by capture())
 int ffea_gpu_batch::record_step() {
     CK(BatchLaunch::schedule(desc, blob_iters, nblobs, ncta, cta_blob, st, stream));
@@ -389,6 +438,8 @@ int ffea_gpu_batch::launch_forces() {
     aa.geom = geom; aa.A = A; aa.B = B;
     aa.drag = (p.calc_stokes == 1) ? drag : nullptr;
     aa.val = val; aa.dinv = dinv; aa.diag = diag; aa.st = st;
+    aa.threads = asm_threads;
+    aa.split = asm_split;
     CK(Launch<float>::assemble(aa, stream));
     return FFEA_GPU_OK;
 }
@@ -405,8 +456,11 @@ int ffea_gpu_batch::launch_gather() {
     ga.dinv = dinv; ga.f = f; ga.x = x; ga.r = r;
     ga.partials = nullptr; ga.stride = 0; ga.st = st; ga.gb = nullptr;
     ga.dpos = dpos; ga.px = px; ga.py = py; ga.pz = pz; ga.diag = diag;
+    NodeForces &sn = ga.sn;
+    ctf.fill(sn);
+    sn.lin_ptr = sn_lin_ptr;
+    sn.lin_ev = sn_lin_ev;
     if (sn_chunk_jump) {
-        NodeForces &sn = ga.sn;
         sn.noise = 1;
         sn.kT = p.kT;
         sn.dt = p.dt;
@@ -417,20 +471,19 @@ int ffea_gpu_batch::launch_gather() {
         sn.node_drag = drag;
         sn.mid_orig = sn_mid_orig;
         sn.mid_drag = sn_mid_drag;
-        sn.lin_ptr = sn_lin_ptr;
-        sn.lin_ev = sn_lin_ev;
         sn.orig_off = sn_orig_off;
         sn.chunk_off = sn_chunk_off;
         sn.nblobs = nblobs;
-        sn.on = 1;
-        // each midpoint's noise once per step (the vertices' linearise replay reads it up to ~20 times)
-        if (mid_f) {
-            CK(Launch<float>::mid_force(sn, (int)h.mid_nodes.size(), mid_f, st, stream));
-            sn.mid_f = mid_f;
-        }
     }
-    const int gthreads = Launch<float>::gather_threads();
-    CK(Launch<float>::gather(ga, (h.N + gthreads - 1) / gthreads, stream));
+    sn.on = sn.noise || sn.lin_ptr != nullptr;
+    CK(ctf.launch(stream));
+    // each midpoint's force once per step (the vertices' linearise replay reads it up to ~20 times)
+    if (sn.lin_ptr && mid_f && (sn.noise || ctf.mid || ctf.mface_ptr)) {
+        CK(Launch<float>::mid_force(sn, (int)h.mid_nodes.size(), mid_f, st, stream));
+        sn.mid_f = mid_f;
+    }
+    ga.threads = gather_threads;
+    CK(Launch<float>::gather(ga, (h.N + gather_threads - 1) / gather_threads, stream));
     return FFEA_GPU_OK;
 }
 
@@ -754,6 +807,40 @@ int ffea_gpu_batch_set_rng_state(ffea_gpu_batch *bt, int blob, const uint32_t s[
     return FFEA_GPU_OK;
 }
 
+int ffea_gpu_batch_load_ctforces(ffea_gpu_batch *bt, int blob, const char *ctf_file, const char *surf_file,
+                                 int blob_index) {
+    if (!bt || blob < 0 || blob >= bt->nblobs || !ctf_file) return FFEA_GPU_EINPUT;
+    const int nb = bt->nblobs;
+    CtfModel cm;
+    std::string err;
+    int rc = load_ctforces(ctf_file, surf_file, blob_index, bt->nall_off[blob + 1] - bt->nall_off[blob], cm, err);
+    if (rc) {
+        g_last_error = err;
+        return rc;
+    }
+    if ((int)bt->ctf_models.size() != nb) {
+        bt->ctf_models.resize(nb);
+        for (int b = 0; b < nb; ++b) empty_ctforces(bt->nall_off[b + 1] - bt->nall_off[b], bt->ctf_models[b]);
+    }
+    bt->ctf_models[blob] = std::move(cm);
+    CtfModel all;
+    concat_ctforces(bt->ctf_models, bt->nall_off, all);
+    CK(cudaStreamSynchronize(bt->stream));
+    CK(bt->ctf.build(bt->h, all, bt->px, bt->py, bt->pz, bt->st));
+    const int M = (int)bt->h.mid_nodes.size();
+    if (bt->ctf.mid_force && !bt->mid_f && M > 0) CK(bt->mem.alloc(&bt->mid_f, 3 * (size_t)M));
+    // midpoints that carry force need the linearisation replay (already there with Stokes noise)
+    if (bt->ctf.mid_force && !bt->sn_lin_ptr) {
+        build_linearise_events(bt->h);
+        CK(bt->lin_mem.upload(&bt->sn_lin_ptr, bt->h.lin_ptr));
+        std::vector<int4> ev(bt->h.lin_ev.size() / 4);
+        for (size_t k = 0; k < ev.size(); ++k)
+            ev[k] = make_int4(bt->h.lin_ev[4 * k], bt->h.lin_ev[4 * k + 1], bt->h.lin_ev[4 * k + 2], -1);
+        CK(bt->lin_mem.upload(&bt->sn_lin_ev, ev));
+    }
+    return bt->capture();
+}
+
 int ffea_gpu_batch_get_rng_state(ffea_gpu_batch *bt, int blob, uint32_t s[6]) {
     if (!bt || blob < 0 || blob >= bt->nblobs || !s) return FFEA_GPU_EINPUT;
     CK(cudaMemcpyAsync(s, bt->rng_states + 6 * (size_t)blob, 6 * sizeof(uint32_t), cudaMemcpyDeviceToHost,
@@ -782,6 +869,22 @@ int ffea_gpu_batch_config(ffea_gpu_batch *bt, int *cg_threads, int *threads_per_
     return FFEA_GPU_OK;
 }
 
+int ffea_gpu_batch_shapes(ffea_gpu_batch *bt, int *element_threads, int *assembly_threads, int *assembly_split,
+                          int *gather_threads) {
+    if (!bt) return FFEA_GPU_EINPUT;
+    if (element_threads) *element_threads = bt->me.threads;
+    if (assembly_threads) *assembly_threads = bt->asm_threads;
+    if (assembly_split) *assembly_split = bt->asm_split;
+    if (gather_threads) *gather_threads = bt->gather_threads;
+    return FFEA_GPU_OK;
+}
+
+int ffea_gpu_batch_set_shapes(ffea_gpu_batch *bt, int element_threads, int assembly_threads, int assembly_split,
+                              int gather_threads) {
+    if (!bt) return FFEA_GPU_EINPUT;
+    return bt->set_shapes(element_threads, assembly_threads, assembly_split, gather_threads);
+}
+
 int ffea_gpu_batch_set_config(ffea_gpu_batch *bt, int cg_threads, int threads_per_row) {
     if (!bt) return FFEA_GPU_EINPUT;
     return bt->configure(cg_threads, threads_per_row);
@@ -793,8 +896,67 @@ int ffea_gpu_batch_tune(ffea_gpu_batch *bt, int solves, double *best_ms) {
     if (rc) return rc;
     DevStatus s0{};
     if ((rc = bt->read_status(s0))) return rc;
-    // forces and matrix of the current positions; no position or RNG update
+    // the force phase's launch shapes, one at a time (coordinate search): elements per block, then the
+    // assembly's threads per block and slot split, then the gather's threads per block
     const int keep_threads = bt->cg_threads, keep_tpn = bt->tpn;
+    const int keep_em = bt->me.threads, keep_at = bt->asm_threads, keep_as = bt->asm_split,
+              keep_gt = bt->gather_threads;
+    auto restore = [&]() {
+        if (bt->me.threads != keep_em) {
+            cudaStreamSynchronize(bt->stream);
+            bt->me.set_threads(bt->h, keep_em);
+        }
+        bt->asm_threads = keep_at;
+        bt->asm_split = keep_as;
+        bt->gather_threads = keep_gt;
+    };
+    {
+        double ms = 0.0, fbest = 1e300;
+        int b_em = keep_em;
+        for (int em : {64, 128, 256}) {
+            if (em != bt->me.threads) {
+                CK(cudaStreamSynchronize(bt->stream));
+                CK(bt->me.set_threads(bt->h, em));
+            }
+            if ((rc = bt->time_forces(solves, ms))) break;
+            if (ms < fbest) { fbest = ms; b_em = em; }
+        }
+        if (!rc && b_em != bt->me.threads) {
+            CK(cudaStreamSynchronize(bt->stream));
+            CK(bt->me.set_threads(bt->h, b_em));
+        }
+        int b_at = keep_at, b_as = keep_as;
+        fbest = 1e300;
+        for (int at : {64, 128, 256}) {
+            for (int as : {1, 2}) {
+                if (rc) break;
+                bt->asm_threads = at;
+                bt->asm_split = as;
+                if ((rc = bt->time_forces(solves, ms))) break;
+                if (ms < fbest) { fbest = ms; b_at = at; b_as = as; }
+            }
+        }
+        bt->asm_threads = b_at;
+        bt->asm_split = b_as;
+        int b_gt = keep_gt;
+        fbest = 1e300;
+        for (int gt : {64, 128, 256}) {
+            if (rc) break;
+            bt->gather_threads = gt;
+            if ((rc = bt->time_forces(solves, ms))) break;
+            if (ms < fbest) { fbest = ms; b_gt = gt; }
+        }
+        bt->gather_threads = b_gt;
+        DevStatus s{};
+        if (!rc) rc = bt->read_status(s);
+        if (!rc) rc = ffea_gpu_batch::status_code(s);
+        if (rc) {
+            restore();
+            bt->configure(keep_threads, keep_tpn);
+            return rc;
+        }
+    }
+    // forces and matrix of the current positions; no position or RNG update
     if ((rc = bt->launch_forces())) return rc;
     auto prepare = [&]() -> int {
         int r2 = bt->launch_gather();
@@ -842,6 +1004,7 @@ int ffea_gpu_batch_tune(ffea_gpu_batch *bt, int solves, double *best_ms) {
         CK(cudaStreamSynchronize(bt->stream));
     }
     if (rc) {
+        restore();
         bt->configure(keep_threads, keep_tpn);
         return rc;
     }

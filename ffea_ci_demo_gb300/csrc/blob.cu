@@ -29,6 +29,7 @@
 #include "engine.h"
 #include "blob_iface.h"
 #include "ctforces.h"
+#include "ctforces_device.h"
 #include "host_model.h"
 #include "kernels_mixed.cuh"
 #include "mixed_elements.h"
@@ -190,18 +191,15 @@ struct BlobImpl final : ffea_gpu_blob {
     double *p0 = nullptr, *m0 = nullptr, *meas_part = nullptr, *meas_out = nullptr;
     int *mid_a = nullptr, *mid_b = nullptr;
     int meas_blocks = 0;
-    // constant forces (ctforces file): per vertex / midpoint linear forces, surface faces and sets
-    Arena ctf_mem;
-    double *ctf_node = nullptr, *ctf_mid = nullptr, *ctf_ff = nullptr;
-    int *vface_ptr = nullptr, *vface = nullptr, *mface_ptr = nullptr, *mface = nullptr;
-    SurfArgs surf{};
-    bool lin_from_ctf = false, has_ctf = false;
+    // constant forces (ctforces file): per vertex / midpoint linear forces, rotational forces, surface sets
+    CtfDevice ctf;
+    Arena lin_mem;  // the linearise replay when only the constant forces need it
+    bool lin_from_ctf = false;
     // Stokes noise (calc_stokes with calc_noise)
     MrgJump *sn_chunk_jump = nullptr, *sn_lane_jump = nullptr;
     int *sn_node_orig = nullptr, *sn_mid_orig = nullptr, *sn_lin_ptr = nullptr;
     double *sn_mid_drag = nullptr;
     R *mid_f = nullptr;  // the step's midpoint forces (3 per midpoint), when any midpoint carries force
-    RotArgs rot{};       // rotational constant forces (nodes, their forces, the arrays they update)
     int4 *sn_lin_ev = nullptr;
     int nmodes = 0;
     double modes[36] = {}, xc[3] = {};
@@ -670,20 +668,15 @@ struct BlobImpl final : ffea_gpu_blob {
             sn.node_drag = drag;
             sn.mid_orig = sn_mid_orig;
             sn.mid_drag = sn_mid_drag;
-            sn.node_ctf = ctf_node;
-            sn.mid_ctf = ctf_mid;
-            sn.vface_ptr = vface_ptr; sn.vface = vface;
-            sn.mface_ptr = mface_ptr; sn.mface = mface;
-            sn.ff = ctf_ff;
+            ctf.fill(sn);
             sn.lin_ptr = sn_lin_ptr;
             sn.lin_ev = sn_lin_ev;
             sn.on = sn.noise || sn.lin_ptr != nullptr;
         }
-        if (rot.nv + rot.nm > 0) CK(launch_rot_forces(rot, stream));
-        if (surf.nsets > 0) CK(launch_surface_forces(surf, stream));
+        CK(ctf.launch(stream));
         // midpoints that carry force: each computed once (the vertices' linearise replay reads it up to ~20 times)
         const int M = (int)h.mid_nodes.size();
-        if (ga.sn.lin_ptr && mid_f && (ga.sn.noise || ctf_mid || mface_ptr)) {
+        if (ga.sn.lin_ptr && mid_f && (ga.sn.noise || ctf.mid || ctf.mface_ptr)) {
             CK(Launch<R>::mid_force(ga.sn, M, mid_f, st, stream));
             ga.sn.mid_f = mid_f;
         }
@@ -1043,150 +1036,22 @@ struct BlobImpl final : ffea_gpu_blob {
             g_last_error = err;
             return rc;
         }
-        const int N = h.N, M = (int)h.mid_nodes.size(), n = h.n_all;
-        std::vector<int> mid_id(n, -1);
-        for (int m = 0; m < M; ++m) mid_id[h.mid_nodes[m]] = m;
-        bool mid_force = false, any_lin = false;
-        std::vector<double> vn(3 * (size_t)N, 0.0), vm(3 * (size_t)std::max(M, 1), 0.0);
-        for (int k = 0; k < N; ++k)
-            for (int c = 0; c < 3; ++c) vn[3 * (size_t)k + c] = cm.lin[3 * (size_t)h.node_of[k] + c];
-        for (int m = 0; m < M; ++m) {
-            for (int c = 0; c < 3; ++c) vm[3 * (size_t)m + c] = cm.lin[3 * (size_t)h.mid_nodes[m] + c];
-            mid_force = mid_force || cm.has_lin[h.mid_nodes[m]] || !cm.rot[h.mid_nodes[m]].empty();
-        }
-        for (int i = 0; i < n; ++i) any_lin = any_lin || cm.has_lin[i] || !cm.rot[i].empty();
-        // rotational forces: the nodes carrying them, in vertex then midpoint order, with their forces in file order
-        std::vector<int> rv_row, rv_ptr(1, 0), rm_idx, rm_ptr(1, 0);
-        std::vector<RotEntry> rent;
-        auto add_rot = [&](int node) {
-            for (const RotCtf &r : cm.rot[node]) {
-                RotEntry e{};
-                e.F = r.F;
-                e.torque = r.torque;
-                for (int c = 0; c < 3; ++c) { e.p[c] = r.p[c]; e.d[c] = r.d[c]; }
-                rent.push_back(e);
-            }
-        };
-        for (int k = 0; k < N; ++k)
-            if (!cm.rot[h.node_of[k]].empty()) {
-                rv_row.push_back(k);
-                add_rot(h.node_of[k]);
-                rv_ptr.push_back((int)rent.size());
-            }
-        for (int m = 0; m < M; ++m)
-            if (!cm.rot[h.mid_nodes[m]].empty()) {
-                rm_idx.push_back(m);
-                add_rot(h.mid_nodes[m]);
-                rm_ptr.push_back((int)rent.size() - rv_ptr.back());
-            }
         if (lin_from_ctf) {  // the replay lived with the previous constant forces
             sn_lin_ptr = nullptr;
             sn_lin_ev = nullptr;
+            lin_mem.clear();
             lin_from_ctf = false;
         }
-        ctf_mem.clear();
-        ctf_node = ctf_mid = ctf_ff = nullptr;
-        vface_ptr = vface = mface_ptr = mface = nullptr;
-        surf = SurfArgs{};
-        rot = RotArgs{};
-        if (any_lin) {
-            CK(ctf_mem.upload(&ctf_node, vn));
-            if (mid_force) CK(ctf_mem.upload(&ctf_mid, vm));
-        }
-        if (!rent.empty()) {
-            // the static linear sums stay as they are; the gather reads copies the rotational kernel rewrites
-            // for its nodes every step
-            double *lin_v = ctf_node, *lin_m = ctf_mid;
-            CK(ctf_mem.upload(&ctf_node, vn));
-            if (mid_force) CK(ctf_mem.upload(&ctf_mid, vm));
-            int *d_vrow, *d_vptr, *d_midx, *d_mptr;
-            RotEntry *d_ent;
-            if (rv_row.empty()) rv_row.push_back(0);
-            if (rm_idx.empty()) rm_idx.push_back(0);
-            CK(ctf_mem.upload(&d_vrow, rv_row));
-            CK(ctf_mem.upload(&d_vptr, rv_ptr));
-            CK(ctf_mem.upload(&d_midx, rm_idx));
-            CK(ctf_mem.upload(&d_mptr, rm_ptr));
-            CK(ctf_mem.upload(&d_ent, rent));
-            rot.nv = (int)rv_ptr.size() - 1;
-            rot.nm = (int)rm_ptr.size() - 1;
-            rot.v_row = d_vrow; rot.v_ptr = d_vptr; rot.m_idx = d_midx; rot.m_ptr = d_mptr;
-            rot.ent = d_ent;
-            rot.ent_m = d_ent + rv_ptr.back();
-            rot.mid_a = mid_a; rot.mid_b = mid_b;
-            rot.px = px; rot.py = py; rot.pz = pz;
-            rot.lin_v = lin_v; rot.lin_m = lin_m;
-            rot.out_v = ctf_node; rot.out_m = ctf_mid;
-            rot.st = st;
-        }
-        const int nsets = (int)cm.set_ptr.size() - 1;
-        if (nsets > 0) {
-            const int nf = (int)cm.face_nodes.size() / 3;
-            std::vector<int2> corner(3 * (size_t)nf);
-            for (int f = 0; f < nf; ++f)
-                for (int k = 0; k < 3; ++k) {
-                    const int x = cm.face_nodes[3 * (size_t)f + k];
-                    corner[3 * (size_t)f + k] = h.lin_of[x] >= 0 ? make_int2(h.lin_of[x], h.lin_of[x])
-                                                                 : make_int2(h.mid_a[mid_id[x]], h.mid_b[mid_id[x]]);
-                }
-            // sets holding each face (set order); faces holding each node (face order), forced faces only
-            std::vector<std::vector<int>> fs(nf), vf(N), mf(M);
-            for (int s2 = 0; s2 < nsets; ++s2)
-                for (int k = cm.set_ptr[s2]; k < cm.set_ptr[s2 + 1]; ++k) fs[cm.set_faces[k]].push_back(s2);
-            for (int f = 0; f < nf; ++f) {
-                if (fs[f].empty()) continue;
-                for (int k = 0; k < 3; ++k) {
-                    const int x = cm.face_nodes[3 * (size_t)f + k];
-                    if (h.lin_of[x] >= 0) vf[h.lin_of[x]].push_back(f);
-                    else { mf[mid_id[x]].push_back(f); mid_force = true; }
-                }
-            }
-            auto csr = [](const std::vector<std::vector<int>> &v, std::vector<int> &ptr, std::vector<int> &idx) {
-                ptr.assign(v.size() + 1, 0);
-                for (size_t i = 0; i < v.size(); ++i) ptr[i + 1] = ptr[i] + (int)v[i].size();
-                idx.clear();
-                for (const auto &x : v) idx.insert(idx.end(), x.begin(), x.end());
-                if (idx.empty()) idx.push_back(0);
-            };
-            std::vector<int> fsp, fsi, vfp, vfi, mfp, mfi;
-            csr(fs, fsp, fsi);
-            csr(vf, vfp, vfi);
-            csr(mf, mfp, mfi);
-            int *d_set_ptr, *d_set_faces, *d_fsp, *d_fsi;
-            int2 *d_corner;
-            double *d_setF, *d_total;
-            CK(ctf_mem.upload(&d_set_ptr, cm.set_ptr));
-            CK(ctf_mem.upload(&d_set_faces, cm.set_faces));
-            CK(ctf_mem.upload(&d_setF, cm.set_force));
-            CK(ctf_mem.upload(&d_corner, corner));
-            CK(ctf_mem.upload(&d_fsp, fsp));
-            CK(ctf_mem.upload(&d_fsi, fsi));
-            CK(ctf_mem.alloc(&d_total, (size_t)nsets));
-            CK(ctf_mem.alloc(&ctf_ff, 3 * (size_t)nf));
-            CK(ctf_mem.upload(&vface_ptr, vfp));
-            CK(ctf_mem.upload(&vface, vfi));
-            if (M > 0) {
-                CK(ctf_mem.upload(&mface_ptr, mfp));
-                CK(ctf_mem.upload(&mface, mfi));
-            }
-            surf.nsets = nsets;
-            surf.nfaces = nf;
-            surf.set_ptr = d_set_ptr; surf.set_faces = d_set_faces; surf.set_force = d_setF;
-            surf.corner = d_corner;
-            surf.face_set_ptr = d_fsp; surf.face_set = d_fsi;
-            surf.px = px; surf.py = py; surf.pz = pz;
-            surf.set_total = d_total; surf.ff = ctf_ff;
-            surf.st = st;
-        }
-        if (mid_force && !mid_f && M > 0) CK(mem.alloc(&mid_f, 3 * (size_t)M));
+        CK(ctf.build(h, cm, px, py, pz, st));
+        const int M = (int)h.mid_nodes.size();
+        if (ctf.mid_force && !mid_f && M > 0) CK(mem.alloc(&mid_f, 3 * (size_t)M));
         // midpoints that carry force need the linearisation replay (already there with Stokes noise)
-        if (mid_force && !sn_lin_ptr) {
+        if (ctf.mid_force && !sn_lin_ptr) {
             build_linearise_events(h);
-            int lrc = upload_linearise(ctf_mem);
+            int lrc = upload_linearise(lin_mem);
             if (lrc) return lrc;
             lin_from_ctf = true;
         }
-        has_ctf = any_lin || nsets > 0;
         return FFEA_GPU_OK;
     }
 
@@ -1221,7 +1086,7 @@ struct BlobImpl final : ffea_gpu_blob {
             g_last_error = "adjoint window and checkpoint interval must be positive";
             return FFEA_GPU_EINPUT;
         }
-        if (has_ctf) {
+        if (ctf.any) {
             g_last_error = "the adjoint does not differentiate constant forces";
             return FFEA_GPU_EINPUT;
         }

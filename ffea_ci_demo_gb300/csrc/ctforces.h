@@ -230,5 +230,36 @@ inline int load_ctforces(const char *ctf_file, const char *surf_file, int blob_i
     return 0;
 }
 
+// A model with no forces on n_all nodes.
+inline void empty_ctforces(int n_all, CtfModel &m) {
+    m = CtfModel{};
+    m.lin.assign(3 * (size_t)n_all, 0.0);
+    m.has_lin.assign(n_all, 0);
+    m.rot.assign(n_all, {});
+    m.set_ptr.assign(1, 0);
+}
+
+// Blob models side by side in one numbering (a replica batch): blob b's node i is node node_off[b] + i, its
+// faces and sets follow those of the blobs before it.
+inline void concat_ctforces(const std::vector<CtfModel> &parts, const std::vector<int> &node_off, CtfModel &out) {
+    empty_ctforces(node_off.back(), out);
+    for (size_t b = 0; b < parts.size(); ++b) {
+        const CtfModel &m = parts[b];
+        const int o = node_off[b], n = node_off[b + 1] - o;
+        const int face0 = (int)out.face_nodes.size() / 3;
+        for (int i = 0; i < n; ++i) {
+            for (int c = 0; c < 3; ++c) out.lin[3 * (size_t)(o + i) + c] = m.lin[3 * (size_t)i + c];
+            out.has_lin[o + i] = m.has_lin[i];
+            out.rot[o + i] = m.rot[i];
+        }
+        for (int x : m.face_nodes) out.face_nodes.push_back(o + x);
+        for (size_t s2 = 0; s2 + 1 < m.set_ptr.size(); ++s2) {
+            for (int k = m.set_ptr[s2]; k < m.set_ptr[s2 + 1]; ++k) out.set_faces.push_back(face0 + m.set_faces[k]);
+            out.set_ptr.push_back((int)out.set_faces.size());
+            for (int c = 0; c < 3; ++c) out.set_force.push_back(m.set_force[3 * s2 + c]);
+        }
+    }
+}
+
 }  // namespace host
 }  // namespace ffea

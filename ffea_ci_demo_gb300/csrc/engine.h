@@ -39,7 +39,7 @@ struct Launch {
 // launchers of the mixed-precision element phase (kernels_element_mixed.cuh; instantiated in engine_mixed.cu)
 struct MixedLaunch {
     static cudaError_t node_prep(const NodePrepArgs &a, cudaStream_t s);
-    // element_mixed_kernel over a.T elements in blocks of EM_THREADS: per-block vertex sums into a.parts when
+    // element_mixed_kernel over a.T elements in blocks of a.em_threads: per-block vertex sums into a.parts when
     // `partials`, else per-element forces into a.ef (when set); dpsi and volume into a.geom (when set)
     static cudaError_t element(const ElemArgs<float> &a, bool partials, cudaStream_t s);
 };

@@ -31,13 +31,16 @@ cudaError_t Launch<R>::element(const ElemArgs<R> &a, cudaStream_t s) {
 template <class R>
 cudaError_t Launch<R>::assemble(const AsmArgs<R> &a, cudaStream_t s) {
     if (a.N <= 0 || a.nslots <= 0) return cudaSuccess;
-    // three threads per slot while that still fits on the GPU at once (152 SMs x 2048 threads); nslots is a
-    // multiple of 32, so each warp of the split kernel has one block row of 32 slots
-    if (3 * a.nslots <= 152ll * 2048) {
+    const int bt = a.threads > 0 ? a.threads : ASM_THREADS;
+    if (!(bt == 64 || bt == 128 || bt == 256)) return cudaErrorInvalidValue;
+    // by default three threads per slot while that still fits on the GPU at once (152 SMs x 2048 threads);
+    // nslots is a multiple of 32, so each warp of the split kernel has one block row of 32 slots
+    const bool split = a.split == 0 ? 3 * a.nslots <= 152ll * 2048 : a.split == 1;
+    if (split) {
         const long long threads = 3 * a.nslots;
-        assemble_kernel<R, true><<<(unsigned)((threads + ASM_THREADS - 1) / ASM_THREADS), ASM_THREADS, 0, s>>>(a);
+        assemble_kernel<R, true><<<(unsigned)((threads + bt - 1) / bt), bt, 0, s>>>(a);
     } else {
-        assemble_kernel<R, false><<<(unsigned)((a.nslots + ASM_THREADS - 1) / ASM_THREADS), ASM_THREADS, 0, s>>>(a);
+        assemble_kernel<R, false><<<(unsigned)((a.nslots + bt - 1) / bt), bt, 0, s>>>(a);
     }
     count_launch();
     return cudaGetLastError();
@@ -48,8 +51,11 @@ int Launch<R>::gather_threads() { return GATHER_THREADS; }
 
 template <class R>
 cudaError_t Launch<R>::gather(const GatherArgs<R> &a, int blocks, cudaStream_t s) {
-    if constexpr (std::is_same<R, float>::value) gather_mixed_kernel<R><<<blocks, GATHER_THREADS, 0, s>>>(a);
-    else gather_kernel<R><<<blocks, GATHER_THREADS, 0, s>>>(a);
+    // modes 0 and 1 reduce over blocks of GATHER_THREADS; the batch's mode 2 takes any of 64, 128, 256
+    const int bt = (a.mode == 2 && a.threads > 0) ? a.threads : GATHER_THREADS;
+    if (!(bt == 64 || bt == 128 || bt == 256)) return cudaErrorInvalidValue;
+    if constexpr (std::is_same<R, float>::value) gather_mixed_kernel<R><<<blocks, bt, 0, s>>>(a);
+    else gather_kernel<R><<<blocks, bt, 0, s>>>(a);
     count_launch();
     return cudaGetLastError();
 }

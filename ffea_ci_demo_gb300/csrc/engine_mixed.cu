@@ -42,9 +42,24 @@ cudaError_t MixedLaunch::node_prep(const NodePrepArgs &a, cudaStream_t s) {
 
 cudaError_t MixedLaunch::element(const ElemArgs<float> &a, bool partials, cudaStream_t s) {
     if (a.T <= 0) return cudaSuccess;
-    const int blocks = (a.T + EM_THREADS - 1) / EM_THREADS;
-    if (partials) element_mixed_kernel<true><<<blocks, EM_THREADS, 0, s>>>(a);
-    else element_mixed_kernel<false><<<blocks, EM_THREADS, 0, s>>>(a);
+    const int nt = a.em_threads > 0 ? a.em_threads : EM_THREADS;
+    const int blocks = (a.T + nt - 1) / nt;
+    switch (nt) {
+    case 64:
+        if (partials) element_mixed_kernel<true, 64><<<blocks, 64, 0, s>>>(a);
+        else element_mixed_kernel<false, 64><<<blocks, 64, 0, s>>>(a);
+        break;
+    case 128:
+        if (partials) element_mixed_kernel<true, 128><<<blocks, 128, 0, s>>>(a);
+        else element_mixed_kernel<false, 128><<<blocks, 128, 0, s>>>(a);
+        break;
+    case 256:
+        if (partials) element_mixed_kernel<true, 256><<<blocks, 256, 0, s>>>(a);
+        else element_mixed_kernel<false, 256><<<blocks, 256, 0, s>>>(a);
+        break;
+    default:
+        return cudaErrorInvalidValue;
+    }
     count_launch();
     return cudaGetLastError();
 }

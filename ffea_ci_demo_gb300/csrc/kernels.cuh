@@ -61,6 +61,7 @@ struct ElemArgs {
     const int *perm;
     const uint32_t *chunk_state;   // 6 per 32-element chunk: the stream state at the chunk's first draw
     const int *chunk_off;          // batch: first chunk of each blob
+    int em_threads;                // elements per thread block, as the block lists were built (0: EM_THREADS)
 };
 
 // V[r][c] of tetra_element_linear::create_viscosity_matrix (src/tetra_element_linear.cpp:298-327)
@@ -255,6 +256,8 @@ struct AsmArgs {
     R *dinv;                // 4*N
     R *diag;                // 4*N diagonal of V (mixed path) or null
     DevStatus *st;
+    int threads;            // threads per block (0: the default); 64, 128 or 256
+    int split;              // 0: three threads per slot while they fit on the GPU at once; 1: three; 2: one
 };
 
 constexpr unsigned SRC_IDENTITY = 0xffffffffu;
@@ -323,7 +326,7 @@ __device__ __forceinline__ void asm_add(R (&v)[3 * NB], unsigned code, const R (
 }
 
 template <class R, bool SPLIT>
-__global__ void __launch_bounds__(128) assemble_kernel(AsmArgs<R> g) {
+__global__ void __launch_bounds__(256) assemble_kernel(AsmArgs<R> g) {
     constexpr int NB = SPLIT ? 1 : 3;  // block rows per thread
     const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     const long long slot = SPLIT ? ((t >> 5) / 3) * 32 + (t & 31) : t;
@@ -626,6 +629,7 @@ struct GatherArgs {
     double *upx, *upy, *upz, *uvx, *uvy, *uvz;
     double dt;
     int fuse_euler;
+    int threads;          // threads per block in mode 2 (0: the default); 64, 128 or 256
 };
 
 template <class R>

@@ -27,8 +27,8 @@
 //   state; node_prep_kernel forms the state at the start of every 32-element chunk once per step and each
 //   element makes one lane jump (A^(7 lane)). The stream states stay bit-exact; RAND(-.5,.5) is formed in
 //   FP32 from the draw's integer, (k - (m1 + 1)/2)/(m1 + 1).
-// * Staging and the deterministic block sum. A thread block of EM_THREADS consecutive elements loads the
-//   distinct vertices of its elements (listed on the host, at most 4 x EM_THREADS) into shared memory once;
+// * Staging and the deterministic block sum. A thread block of NT consecutive elements (EM_THREADS unless tuned)
+//   loads the distinct vertices of its elements (listed on the host, at most 4 NT) into shared memory once;
 //   each element reads its four nodes from there. The block then sums its elements' forces per vertex in
 //   element order (the block's incidence list, sorted on the host) and writes one float4 per (block, vertex)
 //   at the vertex's run of the node-major `parts` array, so the gather adds a vertex's block sums in block
@@ -39,8 +39,10 @@
 
 namespace ffea {
 
+// elements per thread block: the default, and the choices of the batch autotuner (multiples of the 32-element
+// noise chunk)
 constexpr int EM_THREADS = 128;
-constexpr int EM_MAX_NODES = 4 * EM_THREADS;
+constexpr int EM_THREAD_CHOICES[3] = {64, 128, 256};
 constexpr float EM_DEGENERATE = 0.05f;
 
 // RAND(-.5,.5) of include/tetra_element_linear.h:119 in FP32. The MRG32k3a step is RngStream::U01's
@@ -252,22 +254,22 @@ __device__ __forceinline__ bool element_mixed_eval(const ElemArgs<float> &g, int
 
 // PARTIALS: block sums per vertex into g.parts (the step); else per-element forces into g.ef when it is set (or
 // none: recompute for the assembly's geometry only). g.geom, when set, gets dpsi and vol for the assembly.
-template <bool PARTIALS>
-__global__ void __launch_bounds__(EM_THREADS, 8) element_mixed_kernel(ElemArgs<float> g) {
-    __shared__ float4 s_u[EM_MAX_NODES];  // staged displacements; then the elements' forces (12 per element)
-    __shared__ float4 s_v[EM_MAX_NODES];
+template <bool PARTIALS, int NT>
+__global__ void __launch_bounds__(NT, 1024 / NT) element_mixed_kernel(ElemArgs<float> g) {
+    __shared__ float4 s_u[4 * NT];  // staged displacements; then the elements' forces (12 per element)
+    __shared__ float4 s_v[4 * NT];
     __shared__ int s_abort;
-    static_assert(sizeof(s_u) >= EM_THREADS * 12 * sizeof(float), "element forces overlay the staged nodes");
+    static_assert(sizeof(s_u) >= NT * 12 * sizeof(float), "element forces overlay the staged nodes");
     const int tid = threadIdx.x, blk = blockIdx.x;
     if (tid == 0) s_abort = g.st->abort;
     const int n0 = g.cta_ptr[blk], nn = g.cta_ptr[blk + 1] - n0;
     const bool inertial = !g.nomass;
-    for (int i = tid; i < nn; i += EM_THREADS) {
+    for (int i = tid; i < nn; i += NT) {
         const int node = g.cta_nodes[n0 + i];
         s_u[i] = g.u[node];
         if (inertial) s_v[i] = g.vf[node];
     }
-    const int e = blk * EM_THREADS + tid;
+    const int e = blk * NT + tid;
     const bool live = e < g.T;
     const ushort4 l = live ? g.loc[e] : make_ushort4(0, 0, 0, 0);
     __syncthreads();
@@ -312,9 +314,9 @@ __global__ void __launch_bounds__(EM_THREADS, 8) element_mixed_kernel(ElemArgs<f
     __syncthreads();
     // each vertex of the block: its elements' forces in element order, from the block's incidence list
     // (code 4 el + slot, so the force sits at s_f[3 code])
-    const int ne = min(EM_THREADS, g.T - blk * EM_THREADS);
-    const unsigned short *il = g.inc_local + 4 * EM_THREADS * (size_t)blk;
-    for (int i = tid; i < nn; i += EM_THREADS) {
+    const int ne = min(NT, g.T - blk * NT);
+    const unsigned short *il = g.inc_local + 4 * NT * (size_t)blk;
+    for (int i = tid; i < nn; i += NT) {
         const int m0 = g.inc_start[n0 + i], m1 = (i + 1 < nn) ? (int)g.inc_start[n0 + i + 1] : 4 * ne;
         float a0 = 0.f, a1 = 0.f, a2 = 0.f;
         for (int m = m0; m < m1; ++m) {

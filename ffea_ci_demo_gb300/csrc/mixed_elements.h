@@ -19,6 +19,8 @@ struct MixedElements {
     uint32_t *chunk_state = nullptr;     // 6 per 32-element chunk
     int *chunk_blob = nullptr, *chunk_off = nullptr;
     int N = 0, nchunks = 0;
+    int threads = EM_THREADS;  // elements per thread block, as the block lists below were built
+    host::Arena lists;         // the block lists and block sums (rebuilt by set_threads)
 
     // elem_off: first element of each blob and the total at the end (a batch), or empty (one blob, whose
     // chunk c holds elements 32c .. 32c + 31)
@@ -32,20 +34,7 @@ struct MixedElements {
         if ((e = mem.upload(&xr, x)) != cudaSuccess) return e;
         if ((e = mem.alloc(&u, (size_t)N)) != cudaSuccess) return e;
         if (inertial && (e = mem.alloc(&vf, (size_t)N)) != cudaSuccess) return e;
-        host::CtaLists cl;
-        host::build_cta_lists(h, EM_THREADS, cl);
-        std::vector<ushort4> l4(h.T);
-        for (int k = 0; k < h.T; ++k)
-            l4[k] = make_ushort4(cl.loc[4 * (size_t)k], cl.loc[4 * (size_t)k + 1], cl.loc[4 * (size_t)k + 2],
-                                 cl.loc[4 * (size_t)k + 3]);
-        if ((e = mem.upload(&loc, l4)) != cudaSuccess) return e;
-        if ((e = mem.upload(&cta_ptr, cl.cta_ptr)) != cudaSuccess) return e;
-        if ((e = mem.upload(&cta_nodes, cl.cta_nodes)) != cudaSuccess) return e;
-        if ((e = mem.upload(&perm, cl.perm)) != cudaSuccess) return e;
-        if ((e = mem.upload(&part_ptr, cl.part_ptr)) != cudaSuccess) return e;
-        if ((e = mem.upload(&inc_local, cl.inc_local)) != cudaSuccess) return e;
-        if ((e = mem.upload(&inc_start, cl.inc_start)) != cudaSuccess) return e;
-        if ((e = mem.alloc(&parts, cl.cta_nodes.size())) != cudaSuccess) return e;
+        if ((e = set_threads(h, EM_THREADS)) != cudaSuccess) return e;
         nchunks = 0;
         if (noise) {
             if (elem_off.empty()) {
@@ -64,6 +53,31 @@ struct MixedElements {
             }
             if ((e = mem.alloc(&chunk_state, 6 * (size_t)std::max(nchunks, 1))) != cudaSuccess) return e;
         }
+        return cudaSuccess;
+    }
+
+    // block lists for thread blocks of t elements (64, 128 or 256); the device must be idle
+    cudaError_t set_threads(const host::HostModel &h, int t) {
+        if (!(t == 64 || t == 128 || t == 256)) return cudaErrorInvalidValue;
+        lists.clear();
+        loc = nullptr; cta_ptr = cta_nodes = perm = part_ptr = nullptr;
+        inc_local = inc_start = nullptr; parts = nullptr;
+        host::CtaLists cl;
+        host::build_cta_lists(h, t, cl);
+        std::vector<ushort4> l4(h.T);
+        for (int k = 0; k < h.T; ++k)
+            l4[k] = make_ushort4(cl.loc[4 * (size_t)k], cl.loc[4 * (size_t)k + 1], cl.loc[4 * (size_t)k + 2],
+                                 cl.loc[4 * (size_t)k + 3]);
+        cudaError_t e;
+        if ((e = lists.upload(&loc, l4)) != cudaSuccess) return e;
+        if ((e = lists.upload(&cta_ptr, cl.cta_ptr)) != cudaSuccess) return e;
+        if ((e = lists.upload(&cta_nodes, cl.cta_nodes)) != cudaSuccess) return e;
+        if ((e = lists.upload(&perm, cl.perm)) != cudaSuccess) return e;
+        if ((e = lists.upload(&part_ptr, cl.part_ptr)) != cudaSuccess) return e;
+        if ((e = lists.upload(&inc_local, cl.inc_local)) != cudaSuccess) return e;
+        if ((e = lists.upload(&inc_start, cl.inc_start)) != cudaSuccess) return e;
+        if ((e = lists.alloc(&parts, cl.cta_nodes.size())) != cudaSuccess) return e;
+        threads = t;
         return cudaSuccess;
     }
 
@@ -97,6 +111,7 @@ struct MixedElements {
         ea.perm = perm;
         ea.chunk_state = chunk_state;
         ea.chunk_off = chunk_off;
+        ea.em_threads = threads;
     }
 };
 

@@ -123,10 +123,13 @@ def load():
         "ffea_gpu_batch_set_states": (C.c_int, [vp, dp, dp]),
         "ffea_gpu_batch_set_state": (C.c_int, [vp, C.c_int, dp, dp]),
         "ffea_gpu_batch_set_rng_state": (C.c_int, [vp, C.c_int, dp]),
+        "ffea_gpu_batch_load_ctforces": (C.c_int, [vp, C.c_int, C.c_char_p, C.c_char_p, C.c_int]),
         "ffea_gpu_batch_get_rng_state": (C.c_int, [vp, C.c_int, dp]),
         "ffea_gpu_batch_cg_iterations": (C.c_int, [vp, dp, C.POINTER(C.c_longlong)]),
         "ffea_gpu_batch_config": (C.c_int, [vp, ip, ip, ip]),
         "ffea_gpu_batch_set_config": (C.c_int, [vp, C.c_int, C.c_int]),
+        "ffea_gpu_batch_shapes": (C.c_int, [vp, ip, ip, ip, ip]),
+        "ffea_gpu_batch_set_shapes": (C.c_int, [vp, C.c_int, C.c_int, C.c_int, C.c_int]),
         "ffea_gpu_batch_tune": (C.c_int, [vp, C.c_int, C.POINTER(C.c_double)]),
         "ffea_gpu_last_error": (C.c_char_p, []),
         "ffea_gpu_launch_count": (C.c_longlong, []),
@@ -570,6 +573,13 @@ class Batch:
         a = np.ascontiguousarray(s, np.uint32)
         _check(self._lib.ffea_gpu_batch_set_rng_state(self._h, blob, _p(a)), "batch_set_rng_state")
 
+    def load_ctforces(self, blob: int, ctforces_file: str, surface_file: str | None = None,
+                      blob_index: int = 0) -> None:
+        """The reference's constant forces for one blob of the batch (as Blob.load_ctforces)."""
+        _check(self._lib.ffea_gpu_batch_load_ctforces(self._h, int(blob), str(ctforces_file).encode(),
+                                                      None if surface_file is None else str(surface_file).encode(),
+                                                      int(blob_index)), "batch_load_ctforces")
+
     def cg_iterations(self) -> tuple[np.ndarray, int]:
         last = np.zeros(self.n_blobs, np.int32)
         total = C.c_longlong()
@@ -591,14 +601,24 @@ class Batch:
     def config(self) -> dict:
         t, p, c = C.c_int(), C.c_int(), C.c_int()
         _check(self._lib.ffea_gpu_batch_config(self._h, C.byref(t), C.byref(p), C.byref(c)), "batch_config")
-        return {"cg_threads": t.value, "threads_per_row": p.value, "ctas": c.value}
+        e, a, sp, g = C.c_int(), C.c_int(), C.c_int(), C.c_int()
+        _check(self._lib.ffea_gpu_batch_shapes(self._h, C.byref(e), C.byref(a), C.byref(sp), C.byref(g)),
+               "batch_shapes")
+        return {"cg_threads": t.value, "threads_per_row": p.value, "ctas": c.value, "element_threads": e.value,
+                "assembly_threads": a.value, "assembly_split": sp.value, "gather_threads": g.value}
 
     def set_config(self, cg_threads: int, threads_per_row: int) -> None:
         _check(self._lib.ffea_gpu_batch_set_config(self._h, int(cg_threads), int(threads_per_row)),
                "batch_set_config")
 
+    def set_shapes(self, element_threads: int, assembly_threads: int, assembly_split: int,
+                   gather_threads: int) -> None:
+        _check(self._lib.ffea_gpu_batch_set_shapes(self._h, int(element_threads), int(assembly_threads),
+                                                   int(assembly_split), int(gather_threads)), "batch_set_shapes")
+
     def tune(self, solves: int = 2) -> float:
-        """Autotune the CG launch (CTA size, threads per row) on the current forces; returns the best ms."""
+        """Autotune the force phase's launch shapes (elements per block, assembly and gather blocks) and the CG
+        launch (CTA size, threads per row) on the current forces; returns the best CG solve ms."""
         best = C.c_double()
         _check(self._lib.ffea_gpu_batch_tune(self._h, int(solves), C.byref(best)), "batch_tune")
         return best.value

@@ -328,6 +328,12 @@ int ffea_gpu_batch_set_states(ffea_gpu_batch *batch, const double *pos, const do
 int ffea_gpu_batch_set_rng_state(ffea_gpu_batch *batch, int blob, const uint32_t state[6]);
 int ffea_gpu_batch_get_rng_state(ffea_gpu_batch *batch, int blob, uint32_t state[6]);
 
+/* Constant forces of blob `blob` of the batch, read as ffea_gpu_blob_load_ctforces reads them (the
+ * ctforces file's entries for `blob_index`, faces of `surface_file`); each call replaces that blob's
+ * forces only. */
+int ffea_gpu_batch_load_ctforces(ffea_gpu_batch *batch, int blob, const char *ctforces_file,
+                                 const char *surface_file, int blob_index);
+
 /* CG iterations of each blob's last solve (num_blobs entries, may be NULL) and the total since creation. */
 int ffea_gpu_batch_cg_iterations(ffea_gpu_batch *batch, int *last_per_blob, long long *total);
 
@@ -335,9 +341,22 @@ int ffea_gpu_batch_cg_iterations(ffea_gpu_batch *batch, int *last_per_blob, long
 int ffea_gpu_batch_config(ffea_gpu_batch *batch, int *cg_threads, int *threads_per_row, int *ctas);
 int ffea_gpu_batch_set_config(ffea_gpu_batch *batch, int cg_threads, int threads_per_row);
 
-/* Autotuner: times `solves` CG solves of the current forces for every CTA size (128..1024) and
- * threads per row (1, 2, 4, 8) and keeps the fastest; positions, velocities and RNG states are not
- * changed. *best_ms (may be NULL) gets the best mean solve time. */
+/* Launch shapes of the force phase: elements per thread block of the element kernel (64, 128, 256; the
+ * block's vertices are staged in shared memory and its forces summed per vertex there), threads per
+ * block of the assembly (64, 128, 256) and its slot split (0: three threads per matrix slot while they
+ * fit on the GPU at once, 1: three, 2: one), threads per block of the node-force gather (64, 128, 256).
+ * Any shape gives the same trajectory to FP32 rounding (the block sums change grouping). */
+int ffea_gpu_batch_shapes(ffea_gpu_batch *batch, int *element_threads, int *assembly_threads, int *assembly_split,
+                          int *gather_threads);
+int ffea_gpu_batch_set_shapes(ffea_gpu_batch *batch, int element_threads, int assembly_threads,
+                              int assembly_split, int gather_threads);
+
+/* Autotuner. First the force phase (node preparation, elements, assembly, node forces), timed over
+ * `solves` launches per shape and searched one shape at a time: elements per block, then the
+ * assembly's threads and split, then the gather's threads. Then `solves` CG solves of the current
+ * forces for every CTA size (128..1024) and threads per row (1, 2, 4, 8). Keeps the fastest of each;
+ * positions, velocities and RNG states are not changed. *best_ms (may be NULL) gets the best mean solve
+ * time. */
 int ffea_gpu_batch_tune(ffea_gpu_batch *batch, int solves, double *best_ms);
 
 /* ---------------------------------------------------------------------------

@@ -20,7 +20,8 @@ import pytest
 import pyoracle as po
 from ffea_ci_demo_gb300 import build, lib
 from ffea_ci_demo_gb300.lib import MESO_LENGTH
-from gen_golden import case_mesh, sheared
+from ffea_ci_demo_gb300.mesh import write_ctforces
+from gen_golden import case_mesh, ctf_case, sheared
 
 
 def substream_states(n):
@@ -123,6 +124,56 @@ def test_batch_stokes_noise_matches_single_blobs(gpu, oracle_built):
 
 
 @pytest.mark.gpu
+def test_batch_constant_forces_match_single_blobs(gpu, oracle_built, tmp_path):
+    """Constant forces (Blob::apply_ctforces, src/Blob.cpp:1676-1743) per blob of a batch: linear, rotational
+    and surface forces on vertices and midpoints, loaded for blob 0 (the file's blob-0 entries) and blob 1 (the
+    file's blob-1 entries), none on blob 2; Stokes drag and noise on. Each blob follows the single mixed blob
+    given the same files, within the bounds above."""
+    meshes = [case_mesh(3, 7, [0, 1, 5, 66]), case_mesh(4, 21), case_mesh(3, 5)]
+    files = [ctf_case(meshes[0], str(tmp_path), "b0"), ctf_case(meshes[1], str(tmp_path), "b1"), None]
+    kw = dict(dt=1e-12, kT=4.11e-21, calc_noise=1, calc_stokes=1)
+    bt = lib.Batch(meshes, **kw)
+    x0 = [sheared(m, 0.02, seed=5 + b) for b, m in enumerate(meshes)]
+    for b in range(len(meshes)):
+        bt.set_state(b, pos=x0[b])
+        if files[b]:
+            bt.load_ctforces(b, *files[b], blob_index=b)
+    bt.update(10)
+    its, _ = bt.cg_iterations()
+    want = substream_states(len(meshes))
+    for b, m in enumerate(meshes):
+        s = lib.Blob(m, solver="CG_nomass", precision="mixed", cg_poly=-1, rng_state=want[b], **kw)
+        if files[b]:
+            s.load_ctforces(*files[b], blob_index=b)
+        s.set_state(pos=x0[b])
+        s.update(10)
+        err = np.abs(bt.pos(b) - s.pos()).max() / np.abs(s.pos() - x0[b]).max()
+        print(f"blob {b}: constant forces {'yes' if files[b] else 'no'}, batch vs single error {err:.2e}, "
+              f"iterations {its[b]} / {s.cg_iterations()[0]}")
+        assert err < 1e-5, b
+        assert abs(int(its[b]) - s.cg_iterations()[0]) <= 2, b
+        assert np.array_equal(bt.rng_state(b), s.rng_state()), b
+    # replacing one blob's forces leaves the others' in place: a file whose only force is another blob's
+    # takes blob 1's away
+    none = str(tmp_path / "none.ctforces")
+    write_ctforces(none, linear=[(1e-12, (1.0, 0.0, 0.0), 7, 0, 3)])
+    bt.load_ctforces(1, none, blob_index=1)
+    with pytest.raises(lib.FFEAError):
+        bt.load_ctforces(0, str(tmp_path / "missing.ctforces"))
+    start = [(bt.pos(b), bt.rng_state(b)) for b in range(2)]
+    bt.update(5)
+    for b in range(2):
+        s = lib.Blob(meshes[b], solver="CG_nomass", precision="mixed", cg_poly=-1, rng_state=start[b][1], **kw)
+        if b == 0:
+            s.load_ctforces(*files[0], blob_index=0)
+        s.set_state(pos=start[b][0])
+        s.update(5)
+        err = np.abs(bt.pos(b) - s.pos()).max() / np.abs(s.pos() - start[b][0]).max()
+        print(f"blob {b} after replacing blob 1's forces: batch vs single error {err:.2e}")
+        assert err < 1e-5, b
+
+
+@pytest.mark.gpu
 def test_batch_kT0_error_vs_fp64():
     meshes = [case_mesh(n, s) for n, s in ((4, 1), (6, 12345), (3, 9))]
     kw = dict(dt=1e-12, kT=0.0, calc_noise=0)
@@ -169,6 +220,8 @@ def test_batch_tuner_keeps_state():
     best = bt.tune(solves=1)
     cfg = bt.config()
     assert best > 0 and cfg["cg_threads"] in (128, 256, 512, 1024) and cfg["threads_per_row"] in (1, 2, 4, 8)
+    assert cfg["element_threads"] in (64, 128, 256) and cfg["assembly_threads"] in (64, 128, 256)
+    assert cfg["assembly_split"] in (1, 2) and cfg["gather_threads"] in (64, 128, 256)
     for b in range(len(meshes)):
         p, v = bt.state(b)
         assert np.array_equal(p, before[b][0]) and np.array_equal(v, before[b][1])
@@ -182,6 +235,31 @@ def test_batch_tuner_keeps_state():
         p0 = m.pos * (m.scale / MESO_LENGTH)
         d = np.abs(bt.pos(b) - ref.pos(b)).max()
         assert d <= 1e-5 * np.abs(ref.pos(b) - p0).max(), b
+
+
+@pytest.mark.gpu
+def test_batch_launch_shapes_give_one_trajectory():
+    """Every force-phase launch shape (elements per block, assembly block and split, gather block) steps the
+    batch along the default shape's trajectory to FP32 rounding (only the per-block force sums regroup);
+    the RNG states stay bit-exact."""
+    meshes = [case_mesh(n, s) for n, s in MESHES]
+    kw = dict(calc_noise=1, calc_stokes=1)
+    ref = lib.Batch(meshes, **kw)
+    ref.update(6)
+    shapes = [(64, 64, 1, 64), (256, 256, 2, 128), (128, 128, 0, 256), (256, 64, 2, 256)]
+    for sh in shapes:
+        bt = lib.Batch(meshes, **kw)
+        bt.set_shapes(*sh)
+        cfg = bt.config()
+        assert (cfg["element_threads"], cfg["assembly_threads"], cfg["assembly_split"], cfg["gather_threads"]) == sh
+        bt.update(6)
+        for b, m in enumerate(meshes):
+            p0 = m.pos * (m.scale / MESO_LENGTH)
+            d = np.abs(bt.pos(b) - ref.pos(b)).max()
+            assert d <= 1e-5 * np.abs(ref.pos(b) - p0).max(), (sh, b)
+            assert np.array_equal(bt.rng_state(b), ref.rng_state(b)), (sh, b)
+    with pytest.raises(lib.FFEAError):
+        bt.set_shapes(96, 128, 0, 256)
 
 
 @pytest.mark.gpu
