@@ -354,29 +354,27 @@ struct MrgJump {
     uint32_t b[9];
 };
 
-// o = J s. Each matrix entry is split as a = a_h 2^16 + a_l, so that a s = a_h (2^16 s mod m) + a_l s (mod m):
-// a row is then six products of 16 by 32 bits (< 6 2^48 < 2^51) summed without overflow and reduced once.
+// o = J s. Each product a s < 2^64 is folded once before the row sum, hi 2^32 + lo = hi 209 + lo (mod m1) and
+// hi 22853 + lo (mod m2): a row of three folded products stays below 3 (2^47 + 2^32) < 2^54, reduced once.
 __host__ __device__ __forceinline__ void mrg_apply(const MrgJump &J, const uint32_t s[6], uint32_t o[6]) {
-    uint32_t h[6];
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-        h[k] = mod_m1_54((uint64_t)s[k] << 16);
-        h[3 + k] = mod_m2_54((uint64_t)s[3 + k] << 16);
-    }
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
         uint64_t acc = 0;
 #pragma unroll
-        for (int k = 0; k < 3; ++k)
-            acc += (uint64_t)(J.a[3 * i + k] >> 16) * h[k] + (uint64_t)(J.a[3 * i + k] & 0xffffu) * s[k];
+        for (int k = 0; k < 3; ++k) {
+            const uint64_t p = (uint64_t)J.a[3 * i + k] * s[k];
+            acc += (p >> 32) * 209ull + (p & 0xffffffffull);
+        }
         o[i] = mod_m1_54(acc);
     }
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
         uint64_t acc = 0;
 #pragma unroll
-        for (int k = 0; k < 3; ++k)
-            acc += (uint64_t)(J.b[3 * i + k] >> 16) * h[3 + k] + (uint64_t)(J.b[3 * i + k] & 0xffffu) * s[3 + k];
+        for (int k = 0; k < 3; ++k) {
+            const uint64_t p = (uint64_t)J.b[3 * i + k] * s[3 + k];
+            acc += (p >> 32) * 22853ull + (p & 0xffffffffull);
+        }
         o[3 + i] = mod_m2_54(acc);
     }
 }

@@ -38,6 +38,9 @@ struct Launch {
 
 // launchers of the mixed-precision element phase (kernels_element_mixed.cuh; instantiated in engine_mixed.cu)
 struct MixedLaunch {
+    // the element kernels' shared-memory limits on the current device; before the first launch (and outside
+    // stream capture)
+    static cudaError_t init();
     static cudaError_t node_prep(const NodePrepArgs &a, cudaStream_t s);
     // element_mixed_kernel over a.T elements in blocks of a.em_threads: per-block vertex sums into a.parts when
     // `partials`, else per-element forces into a.ef (when set); dpsi and volume into a.geom (when set)

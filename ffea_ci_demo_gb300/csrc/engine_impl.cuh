@@ -54,8 +54,21 @@ cudaError_t Launch<R>::gather(const GatherArgs<R> &a, int blocks, cudaStream_t s
     // modes 0 and 1 reduce over blocks of GATHER_THREADS; the batch's mode 2 takes any of 64, 128, 256
     const int bt = (a.mode == 2 && a.threads > 0) ? a.threads : GATHER_THREADS;
     if (!(bt == 64 || bt == 128 || bt == 256)) return cudaErrorInvalidValue;
-    if constexpr (std::is_same<R, float>::value) gather_mixed_kernel<R><<<blocks, bt, 0, s>>>(a);
-    else gather_kernel<R><<<blocks, bt, 0, s>>>(a);
+    if constexpr (std::is_same<R, float>::value) {
+        const bool nf = a.sn.on || a.sn.node_ctf || a.sn.vface_ptr || a.drag;
+        if (a.mode == 0) {
+            if (nf) gather_mixed_kernel<R, 0, true><<<blocks, bt, 0, s>>>(a);
+            else gather_mixed_kernel<R, 0, false><<<blocks, bt, 0, s>>>(a);
+        } else if (a.mode == 1) {
+            if (nf) gather_mixed_kernel<R, 1, true><<<blocks, bt, 0, s>>>(a);
+            else gather_mixed_kernel<R, 1, false><<<blocks, bt, 0, s>>>(a);
+        } else {
+            if (nf) gather_mixed_kernel<R, 2, true><<<blocks, bt, 0, s>>>(a);
+            else gather_mixed_kernel<R, 2, false><<<blocks, bt, 0, s>>>(a);
+        }
+    } else {
+        gather_kernel<R><<<blocks, bt, 0, s>>>(a);
+    }
     count_launch();
     return cudaGetLastError();
 }

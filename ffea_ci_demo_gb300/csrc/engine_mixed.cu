@@ -40,28 +40,49 @@ cudaError_t MixedLaunch::node_prep(const NodePrepArgs &a, cudaStream_t s) {
     return cudaGetLastError();
 }
 
+namespace {
+
+template <bool PARTIALS, int NT>
+cudaError_t launch_em(const ElemArgs<float> &a, int blocks, size_t smem, cudaStream_t s) {
+    element_mixed_kernel<PARTIALS, NT><<<blocks, NT, smem, s>>>(a);
+    count_launch();
+    return cudaGetLastError();
+}
+
+template <bool PARTIALS, int NT>
+cudaError_t em_attribute() {
+    return cudaFuncSetAttribute(element_mixed_kernel<PARTIALS, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                em_smem_bytes(NT, true, true));
+}
+
+}  // namespace
+
+cudaError_t MixedLaunch::init() {
+    // a block of 256 elements of an inertial solver with noise takes 49,664 bytes, above the default limit
+    cudaError_t e;
+    if ((e = em_attribute<true, 64>()) != cudaSuccess) return e;
+    if ((e = em_attribute<false, 64>()) != cudaSuccess) return e;
+    if ((e = em_attribute<true, 128>()) != cudaSuccess) return e;
+    if ((e = em_attribute<false, 128>()) != cudaSuccess) return e;
+    if ((e = em_attribute<true, 256>()) != cudaSuccess) return e;
+    return em_attribute<false, 256>();
+}
+
 cudaError_t MixedLaunch::element(const ElemArgs<float> &a, bool partials, cudaStream_t s) {
     if (a.T <= 0) return cudaSuccess;
     const int nt = a.em_threads > 0 ? a.em_threads : EM_THREADS;
     const int blocks = (a.T + nt - 1) / nt;
+    const size_t smem = em_smem_bytes(nt, !a.nomass, (partials || a.ef) && a.calc_noise == 1);
     switch (nt) {
     case 64:
-        if (partials) element_mixed_kernel<true, 64><<<blocks, 64, 0, s>>>(a);
-        else element_mixed_kernel<false, 64><<<blocks, 64, 0, s>>>(a);
-        break;
+        return partials ? launch_em<true, 64>(a, blocks, smem, s) : launch_em<false, 64>(a, blocks, smem, s);
     case 128:
-        if (partials) element_mixed_kernel<true, 128><<<blocks, 128, 0, s>>>(a);
-        else element_mixed_kernel<false, 128><<<blocks, 128, 0, s>>>(a);
-        break;
+        return partials ? launch_em<true, 128>(a, blocks, smem, s) : launch_em<false, 128>(a, blocks, smem, s);
     case 256:
-        if (partials) element_mixed_kernel<true, 256><<<blocks, 256, 0, s>>>(a);
-        else element_mixed_kernel<false, 256><<<blocks, 256, 0, s>>>(a);
-        break;
+        return partials ? launch_em<true, 256>(a, blocks, smem, s) : launch_em<false, 256>(a, blocks, smem, s);
     default:
         return cudaErrorInvalidValue;
     }
-    count_launch();
-    return cudaGetLastError();
 }
 
 cudaError_t BatchLaunch::schedule(BlobCgDesc *desc, const int *blob_iters, int nblobs, int ncta, int *cta_blob,

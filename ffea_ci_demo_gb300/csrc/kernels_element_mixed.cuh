@@ -70,34 +70,146 @@ struct NodePrepArgs {
 // (defined in engine_mixed.cu)
 __global__ void __launch_bounds__(256) node_prep_kernel(NodePrepArgs g);
 
-// The stream state at element e's first draw: 7 le draws after its blob's state at the start of the step (le the
-// element's index in its blob), from the state at the start of its 32-element chunk (node_prep_kernel) by one jump
-// of A^(7 (le mod 32)).
-__device__ __forceinline__ void element_stream_state(const ElemArgs<float> &g, int e, uint32_t (&s6)[6]) {
+// The lane jumps A^(7 l), l < 32, in shared memory: 18 words each, padded to 20 so that a quarter warp's 16-byte
+// loads of eight different lanes' jumps fall in distinct banks.
+constexpr int EM_JUMP_WORDS = 20;
+
+// asynchronous global -> shared copies (cp.async, completed by cp_async_wait_all): a block's staging loads are all
+// in flight at once without holding registers
+__device__ __forceinline__ void cp_async4(void *smem, const void *gmem) {
+    const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
+    const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
+__device__ __forceinline__ void stage_lane_jumps(const MrgJump *lane_jump, uint32_t *s_jump, int tid, int nt) {
+    const uint32_t *src = reinterpret_cast<const uint32_t *>(lane_jump);
+    for (int i = tid; i < 32 * 18; i += nt) cp_async4(s_jump + EM_JUMP_WORDS * (i / 18) + i % 18, src + i);
+}
+
+// per-element inputs staged by element_mixed_kernel, EM_EL_ROWS rows of one float per element of the block:
+// J0^-1 (9, row-major), vol0, G, E, A, B
+constexpr int EM_EL_ROWS = 14;
+
+// bytes of dynamic shared memory of an element_mixed_kernel block of nt elements
+__host__ __device__ __forceinline__ int em_smem_bytes(int nt, bool inertial, bool noise) {
+    return (inertial ? 8 : 4) * nt * 16 + EM_EL_ROWS * nt * 4 + 4 * nt * 2 + (noise ? 32 * EM_JUMP_WORDS * 4 : 0);
+}
+
+// Element e's 7 draws of add_fluctuating_stress less one half (RAND(-.5,.5)), in draw order. They start 7 le draws
+// after its blob's state at the start of the step (le the element's index in its blob): from the state at the
+// start of its 32-element chunk (node_prep_kernel) by one jump of A^(7 (le mod 32)) (staged by stage_lane_jumps).
+// (element_chunk_state loads the chunk's state; element_draws makes the draws from it)
+__device__ __forceinline__ int element_chunk_state(const ElemArgs<float> &g, int e, uint32_t (&base)[6]) {
     int le = e, chunk = e >> 5;
     if (g.elem_blob) {
         const int b = g.elem_blob[e];
         le = e - g.elem_off[b];
         chunk = g.chunk_off[b] + (le >> 5);
     }
-    uint32_t base[6];
 #pragma unroll
     for (int k = 0; k < 6; ++k) base[k] = g.chunk_state[6 * (size_t)chunk + k];
-    mrg_apply(g.lane_jump[le & 31], base, s6);
+    return le;
+}
+
+__device__ __forceinline__ void element_draws(const uint32_t (&base)[6], int le, const uint32_t *s_jump,
+                                              float (&rn)[7]) {
+    uint32_t s6[6];
+    MrgJump J;
+    const uint4 *q = reinterpret_cast<const uint4 *>(s_jump + EM_JUMP_WORDS * (le & 31));
+    uint32_t w[20];
+#pragma unroll
+    for (int k = 0; k < 5; ++k) {
+        const uint4 v = q[k];
+        w[4 * k] = v.x; w[4 * k + 1] = v.y; w[4 * k + 2] = v.z; w[4 * k + 3] = v.w;
+    }
+#pragma unroll
+    for (int k = 0; k < 9; ++k) {
+        J.a[k] = w[k];
+        J.b[k] = w[9 + k];
+    }
+    mrg_apply(J, base, s6);
+#pragma unroll
+    for (int k = 0; k < 7; ++k) rn[k] = mrg_rand_half_f(s6);
+}
+
+// The FP64 Jacobian of calculate_jacobian / calc_shape_function_derivatives_and_volume
+// (src/tetra_element_linear.cpp:191-292) for a near-degenerate or inverted element, out of line so that the
+// common FP32 path keeps its registers: dpsi, volume, det K, delta = det K - 1 and M = (J0^-1 J)^T - I, or ok = false
+// (with the inversion flags raised) for an inverted element.
+struct ElemFp64 {
+    float dpsi[12], M[9];
+    float vol, dK, delta;
+    int ok;
+};
+
+static __device__ __noinline__ ElemFp64 element_fp64_jacobian(const ElemArgs<float> &g, int e) {
+    ElemFp64 o;
+    const int4 t = g.tet[e];
+    const double x0 = g.px[t.x], y0 = g.py[t.x], z0 = g.pz[t.x];
+    double J[3][3];
+    J[0][0] = g.px[t.y] - x0; J[0][1] = g.py[t.y] - y0; J[0][2] = g.pz[t.y] - z0;
+    J[1][0] = g.px[t.z] - x0; J[1][1] = g.py[t.z] - y0; J[1][2] = g.pz[t.z] - z0;
+    J[2][0] = g.px[t.w] - x0; J[2][1] = g.py[t.w] - y0; J[2][2] = g.pz[t.w] - z0;
+    double d[12];
+    d[1] = J[2][2] * J[1][1] - J[2][1] * J[1][2];
+    d[2] = J[2][1] * J[0][2] - J[2][2] * J[0][1];
+    d[3] = J[1][2] * J[0][1] - J[1][1] * J[0][2];
+    d[5] = J[2][0] * J[1][2] - J[2][2] * J[1][0];
+    d[6] = J[2][2] * J[0][0] - J[2][0] * J[0][2];
+    d[7] = J[1][0] * J[0][2] - J[1][2] * J[0][0];
+    d[9] = J[2][1] * J[1][0] - J[2][0] * J[1][1];
+    d[10] = J[2][0] * J[0][1] - J[2][1] * J[0][0];
+    d[11] = J[1][1] * J[0][0] - J[1][0] * J[0][1];
+    const double det = J[0][0] * d[1] + J[1][0] * d[2] + J[2][0] * d[3];
+    const double last = g.recompute ? det : g.last_det[e];
+    if (last * det < 0) {
+        atomicAdd(&g.st->inversions, 1);
+        atomicExch(&g.st->abort, 1);
+        o.ok = 0;
+        return o;
+    }
+    o.ok = 1;
+    const double vold = (1.0 / 6.0) * fabs(det);
+    const double idet = 1.0 / det;
+#pragma unroll
+    for (int k = 0; k < 12; ++k)
+        if (k & 3) o.dpsi[k] = (float)(d[k] * idet);
+    o.dpsi[0] = -(o.dpsi[1] + o.dpsi[2] + o.dpsi[3]);
+    o.dpsi[4] = -(o.dpsi[5] + o.dpsi[6] + o.dpsi[7]);
+    o.dpsi[8] = -(o.dpsi[9] + o.dpsi[10] + o.dpsi[11]);
+    o.vol = (float)vold;
+    const size_t T = g.T;
+    o.dK = (float)(vold / (double)g.vol0[e]);
+    o.delta = o.dK - 1.f;
+    // M = (J0^-1 J)^T - I from the FP64 Jacobian
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+        const double j0 = g.jinv[3 * r * T + e], j1 = g.jinv[(3 * r + 1) * T + e], j2 = g.jinv[(3 * r + 2) * T + e];
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+            o.M[3 * c + r] = (float)(j0 * J[0][c] + j1 * J[1][c] + j2 * J[2][c] - (r == c ? 1.0 : 0.0));
+    }
+    return o;
 }
 
 // One element's forces (f[3a + c]: node a, component c; FORCES), shape-function derivatives and volume, with the
-// viscous stress of the nodes' velocities vn when `visc` and the noise drawn from stream state s6; returns false
-// (and raises the inversion flags) for an inverted element.
+// viscous stress of the nodes' velocities vn when `visc` and the thermal stress of the draws rn (element_draws)
+// when noise is on; returns false (and raises the inversion flags) for an inverted element.
+// sel: the element's staged inputs (EM_EL_ROWS rows, `stride` apart).
 template <bool FORCES>
-__device__ __forceinline__ bool element_mixed_eval(const ElemArgs<float> &g, int e, const float4 (&un)[4],
-                                                   bool visc, const float4 (&vn)[4], uint32_t (&s6)[6],
-                                                   float (&f)[12], float (&dpsi)[12], float &vol) {
-    const size_t T = g.T;
+__device__ __forceinline__ bool element_mixed_eval(const ElemArgs<float> &g, int e, const float *sel, int stride,
+                                                   const float4 (&un)[4], bool visc, const float4 (&vn)[4],
+                                                   const float (&rn)[7], float (&f)[12], float (&dpsi)[12],
+                                                   float &vol) {
     float Ji[9];
 #pragma unroll
-    for (int k = 0; k < 9; ++k) Ji[k] = g.jinv[k * T + e];
-    const float vol0 = g.vol0[e];
+    for (int k = 0; k < 9; ++k) Ji[k] = sel[k * stride];
+    const float vol0 = sel[9 * stride];
     // Kd = J0^-1 dU, dU rows = edge displacements u_1 - u_0, u_2 - u_0, u_3 - u_0
     float dU[3][3];
 #pragma unroll
@@ -147,53 +259,20 @@ __device__ __forceinline__ bool element_mixed_eval(const ElemArgs<float> &g, int
 #pragma unroll
             for (int j = 0; j < 3; ++j) M[i][j] = Kd[j][i];
     } else {
-        // near-degenerate or inverted: the FP64 Jacobian of calculate_jacobian / calc_shape_function_derivatives_
-        // and_volume (:191-292), with the inversion test
-        const int4 t = g.tet[e];
-        const double x0 = g.px[t.x], y0 = g.py[t.x], z0 = g.pz[t.x];
-        double J[3][3];
-        J[0][0] = g.px[t.y] - x0; J[0][1] = g.py[t.y] - y0; J[0][2] = g.pz[t.y] - z0;
-        J[1][0] = g.px[t.z] - x0; J[1][1] = g.py[t.z] - y0; J[1][2] = g.pz[t.z] - z0;
-        J[2][0] = g.px[t.w] - x0; J[2][1] = g.py[t.w] - y0; J[2][2] = g.pz[t.w] - z0;
-        double d[12];
-        d[1] = J[2][2] * J[1][1] - J[2][1] * J[1][2];
-        d[2] = J[2][1] * J[0][2] - J[2][2] * J[0][1];
-        d[3] = J[1][2] * J[0][1] - J[1][1] * J[0][2];
-        d[5] = J[2][0] * J[1][2] - J[2][2] * J[1][0];
-        d[6] = J[2][2] * J[0][0] - J[2][0] * J[0][2];
-        d[7] = J[1][0] * J[0][2] - J[1][2] * J[0][0];
-        d[9] = J[2][1] * J[1][0] - J[2][0] * J[1][1];
-        d[10] = J[2][0] * J[0][1] - J[2][1] * J[0][0];
-        d[11] = J[1][1] * J[0][0] - J[1][0] * J[0][1];
-        double det = J[0][0] * d[1] + J[1][0] * d[2] + J[2][0] * d[3];
-        const double last = g.recompute ? det : g.last_det[e];
-        if (last * det < 0) {
-            atomicAdd(&g.st->inversions, 1);
-            atomicExch(&g.st->abort, 1);
-            return false;
-        }
-        const double vold = (1.0 / 6.0) * fabs(det);
-        const double idet = 1.0 / det;
+        // near-degenerate or inverted
+        const ElemFp64 o = element_fp64_jacobian(g, e);
+        if (!o.ok) return false;
 #pragma unroll
-        for (int k = 0; k < 12; ++k)
-            if (k & 3) dpsi[k] = (float)(d[k] * idet);
-        dpsi[0] = -(dpsi[1] + dpsi[2] + dpsi[3]);
-        dpsi[4] = -(dpsi[5] + dpsi[6] + dpsi[7]);
-        dpsi[8] = -(dpsi[9] + dpsi[10] + dpsi[11]);
-        vol = (float)vold;
-        dK = (float)(vold / (double)vol0);
-        delta = dK - 1.f;
+        for (int k = 0; k < 12; ++k) dpsi[k] = o.dpsi[k];
+        vol = o.vol;
+        dK = o.dK;
+        delta = o.delta;
         id = 1.f / dK;
-        // M = (J0^-1 J)^T - I from the FP64 Jacobian
 #pragma unroll
-        for (int r = 0; r < 3; ++r)
-#pragma unroll
-            for (int c = 0; c < 3; ++c)
-                M[c][r] = (float)((double)Ji[3 * r] * J[0][c] + (double)Ji[3 * r + 1] * J[1][c] +
-                                  (double)Ji[3 * r + 2] * J[2][c] - (r == c ? 1.0 : 0.0));
+        for (int k = 0; k < 9; ++k) M[k / 3][k % 3] = o.M[k];
     }
     if (!FORCES) return true;
-    const float G = g.G[e], E = g.E[e], A = g.A[e], B = g.B[e];
+    const float G = sel[10 * stride], E = sel[11 * stride], A = sel[12 * stride], B = sel[13 * stride];
     // elastic stress: (G / det K)(M + M^T + M M^T) + (E - 2G/3) delta (2 + delta) / (2 det K) I
     float S[3][3];
     {
@@ -214,16 +293,15 @@ __device__ __forceinline__ bool element_mixed_eval(const ElemArgs<float> &g, int
     }
     // add_fluctuating_stress :412-431 (draws b, d0, d1, d2, o01, o02, o12)
     if (g.calc_noise == 1) {
-        element_stream_state(g, e, s6);
         const float c = sqrtf((24.f * g.kT) / (vol * g.dt));
-        const float bf = sqrtf(B) * mrg_rand_half_f(s6);
+        const float bf = sqrtf(B) * rn[0];
         const float a2 = sqrtf(2.f * A), a1 = sqrtf(A);
-        S[0][0] += c * (a2 * mrg_rand_half_f(s6) + bf);
-        S[1][1] += c * (a2 * mrg_rand_half_f(s6) + bf);
-        S[2][2] += c * (a2 * mrg_rand_half_f(s6) + bf);
-        const float o01 = c * a1 * mrg_rand_half_f(s6);
-        const float o02 = c * a1 * mrg_rand_half_f(s6);
-        const float o12 = c * a1 * mrg_rand_half_f(s6);
+        S[0][0] += c * (a2 * rn[1] + bf);
+        S[1][1] += c * (a2 * rn[2] + bf);
+        S[2][2] += c * (a2 * rn[3] + bf);
+        const float o01 = c * a1 * rn[4];
+        const float o02 = c * a1 * rn[5];
+        const float o12 = c * a1 * rn[6];
         S[0][1] += o01; S[1][0] += o01;
         S[0][2] += o02; S[2][0] += o02;
         S[1][2] += o12; S[2][1] += o12;
@@ -256,29 +334,58 @@ __device__ __forceinline__ bool element_mixed_eval(const ElemArgs<float> &g, int
 // none: recompute for the assembly's geometry only). g.geom, when set, gets dpsi and vol for the assembly.
 template <bool PARTIALS, int NT>
 __global__ void __launch_bounds__(NT, 1024 / NT) element_mixed_kernel(ElemArgs<float> g) {
-    __shared__ float4 s_u[4 * NT];  // staged displacements; then the elements' forces (12 per element)
-    __shared__ float4 s_v[4 * NT];
+    // dynamic shared memory (em_smem_bytes): staged displacements (4 NT; then the elements' forces, 12 per
+    // element), velocities (4 NT, inertial solvers), the elements' inputs (EM_EL_ROWS x NT), the block's incidence
+    // list (4 NT codes), the lane jumps (noise)
+    extern __shared__ __align__(16) float4 em_smem[];
     __shared__ int s_abort;
-    static_assert(sizeof(s_u) >= NT * 12 * sizeof(float), "element forces overlay the staged nodes");
     const int tid = threadIdx.x, blk = blockIdx.x;
-    if (tid == 0) s_abort = g.st->abort;
-    const int n0 = g.cta_ptr[blk], nn = g.cta_ptr[blk + 1] - n0;
     const bool inertial = !g.nomass;
+    const bool forces = PARTIALS || g.ef != nullptr;
+    const bool noise = forces && g.calc_noise == 1;
+    float4 *s_u = em_smem, *s_v = em_smem + 4 * NT;
+    float *s_el = reinterpret_cast<float *>(em_smem + (inertial ? 8 : 4) * NT);
+    unsigned short *s_il = reinterpret_cast<unsigned short *>(s_el + EM_EL_ROWS * NT);
+    uint32_t *s_jump = reinterpret_cast<uint32_t *>(s_il + 4 * NT);
+    if (tid == 0) s_abort = g.st->abort;
+    if (noise) stage_lane_jumps(g.lane_jump, s_jump, tid, NT);
+    const int n0 = g.cta_ptr[blk], nn = g.cta_ptr[blk + 1] - n0;
     for (int i = tid; i < nn; i += NT) {
         const int node = g.cta_nodes[n0 + i];
-        s_u[i] = g.u[node];
-        if (inertial) s_v[i] = g.vf[node];
+        cp_async16(s_u + i, g.u + node);
+        if (inertial) cp_async16(s_v + i, g.vf + node);
+    }
+    if (PARTIALS) {  // 4 NT codes = NT / 2 chunks of 16 bytes, 16-byte aligned (4 NT 2 bytes per block)
+        const uint4 *src = reinterpret_cast<const uint4 *>(g.inc_local + 4 * NT * (size_t)blk);
+        for (int i = tid; i < NT / 2; i += NT) cp_async16(reinterpret_cast<uint4 *>(s_il) + i, src + i);
     }
     const int e = blk * NT + tid;
     const bool live = e < g.T;
+    if (live) {
+        const size_t T = g.T;
+#pragma unroll
+        for (int k = 0; k < 9; ++k) cp_async4(s_el + k * NT + tid, g.jinv + k * T + e);
+        cp_async4(s_el + 9 * NT + tid, g.vol0 + e);
+        if (forces) {
+            cp_async4(s_el + 10 * NT + tid, g.G + e);
+            cp_async4(s_el + 11 * NT + tid, g.E + e);
+            cp_async4(s_el + 12 * NT + tid, g.A + e);
+            cp_async4(s_el + 13 * NT + tid, g.B + e);
+        }
+    }
     const ushort4 l = live ? g.loc[e] : make_ushort4(0, 0, 0, 0);
+    uint32_t base[6];
+    int le = 0;
+    if (noise && live) le = element_chunk_state(g, e, base);
+    cp_async_wait_all();
     __syncthreads();
     if (s_abort) return;  // uniform: read from shared memory after the barrier
+    // the draws first, while little else is held in registers
+    float rn[7];
+    if (noise && live) element_draws(base, le, s_jump, rn);
     float f[12];
 #pragma unroll
     for (int k = 0; k < 12; ++k) f[k] = 0.f;
-    const bool forces = PARTIALS || g.ef != nullptr;
-    uint32_t s6[6];
     if (live) {
         const float4 un[4] = {s_u[l.x], s_u[l.y], s_u[l.z], s_u[l.w]};
         float4 vb[4] = {};
@@ -286,8 +393,8 @@ __global__ void __launch_bounds__(NT, 1024 / NT) element_mixed_kernel(ElemArgs<f
             vb[0] = s_v[l.x]; vb[1] = s_v[l.y]; vb[2] = s_v[l.z]; vb[3] = s_v[l.w];
         }
         float dpsi[12], vol;
-        const bool ok = forces ? element_mixed_eval<true>(g, e, un, inertial, vb, s6, f, dpsi, vol)
-                               : element_mixed_eval<false>(g, e, un, false, vb, s6, f, dpsi, vol);
+        const bool ok = forces ? element_mixed_eval<true>(g, e, s_el + tid, NT, un, inertial, vb, rn, f, dpsi, vol)
+                               : element_mixed_eval<false>(g, e, s_el + tid, NT, un, false, vb, rn, f, dpsi, vol);
         if (!ok) {
 #pragma unroll
             for (int k = 0; k < 12; ++k) f[k] = 0.f;  // inverted: the step is void; contribute nothing
@@ -315,7 +422,7 @@ __global__ void __launch_bounds__(NT, 1024 / NT) element_mixed_kernel(ElemArgs<f
     // each vertex of the block: its elements' forces in element order, from the block's incidence list
     // (code 4 el + slot, so the force sits at s_f[3 code])
     const int ne = min(NT, g.T - blk * NT);
-    const unsigned short *il = g.inc_local + 4 * NT * (size_t)blk;
+    const unsigned short *il = s_il;
     for (int i = tid; i < nn; i += NT) {
         const int m0 = g.inc_start[n0 + i], m1 = (i + 1 < nn) ? (int)g.inc_start[n0 + i + 1] : 4 * ne;
         float a0 = 0.f, a1 = 0.f, a2 = 0.f;

@@ -48,8 +48,11 @@ __device__ __forceinline__ void phi_cols(float dx, float dy, float dz, float (&p
     phi[5][0] = -dy; phi[5][1] = dx; phi[5][2] = 0;
 }
 
-// mixed-path gather: f (FP64 copy) and r = f (FP32); node offsets; moments for the rigid-mode set-up
-template <class R>
+// mixed-path gather: f (FP64 copy) and r = f (FP32); node offsets; moments for the rigid-mode set-up. MODE is
+// g.mode: 0 (one blob's CG, with the block moments), 1 (mass-lumped), 2 (batch CG); the modes without the block
+// reduction carry none of its registers. NF: some node force besides the elements' (constant forces, inertial
+// Stokes drag, Stokes noise, midpoint forces); without, none of their registers either.
+template <class R, int MODE, bool NF>
 __global__ void __launch_bounds__(256) gather_mixed_kernel(GatherArgs<R> g) {
     __shared__ float2 smem[MIXED_GATHER_NP * 32];
     const int a = blockIdx.x * blockDim.x + threadIdx.x;
@@ -59,7 +62,7 @@ __global__ void __launch_bounds__(256) gather_mixed_kernel(GatherArgs<R> g) {
     for (int i = 0; i < MIXED_GATHER_NP; ++i) acc[i] = df32{0.f, 0.f};
     if (a < g.N && !g.st->abort) {
         float F0 = 0, F1 = 0, F2 = 0;
-        if (g.sn.node_ctf) {
+        if (NF && g.sn.node_ctf) {
             F0 = (float)g.sn.node_ctf[3 * (size_t)a];
             F1 = (float)g.sn.node_ctf[3 * (size_t)a + 1];
             F2 = (float)g.sn.node_ctf[3 * (size_t)a + 2];
@@ -80,18 +83,18 @@ __global__ void __launch_bounds__(256) gather_mixed_kernel(GatherArgs<R> g) {
                 F2 += c[2];
             }
         }
-        if (g.sn.vface_ptr) {
+        if (NF && g.sn.vface_ptr) {
             float F[3] = {F0, F1, F2};
             surface_add<float>(g.sn, g.sn.vface_ptr, g.sn.vface, a, F);
             F0 = F[0]; F1 = F[1]; F2 = F[2];
         }
-        if (g.drag) {
+        if (NF && g.drag) {
             const double dr = g.drag[a];
             F0 -= (float)(g.vx[a] * dr);
             F1 -= (float)(g.vy[a] * dr);
             F2 -= (float)(g.vz[a] * dr);
         }
-        if (g.sn.on) {
+        if (NF && g.sn.on) {
             float F[3] = {F0, F1, F2};
             if (g.sn.noise) stokes_noise_sub<float>(g.sn, g.sn.node_orig[a], g.sn.node_drag[a], F);
             if (g.sn.lin_ptr) midpoint_linearise<float>(g.sn, a, F);
@@ -99,7 +102,7 @@ __global__ void __launch_bounds__(256) gather_mixed_kernel(GatherArgs<R> g) {
         }
         if (g.pinned[a]) { F0 = 0; F1 = 0; F2 = 0; }
         g.f[4 * a] = F0; g.f[4 * a + 1] = F1; g.f[4 * a + 2] = F2;
-        if (g.mode == 1) {
+        if constexpr (MODE == 1) {
             const R x0 = F0 * g.dinv[4 * a], x1 = F1 * g.dinv[4 * a + 1], x2 = F2 * g.dinv[4 * a + 2];
             g.x[4 * a] = x0;
             g.x[4 * a + 1] = x1;
@@ -115,7 +118,7 @@ __global__ void __launch_bounds__(256) gather_mixed_kernel(GatherArgs<R> g) {
             return;
         }
         g.r[4 * a] = F0; g.r[4 * a + 1] = F1; g.r[4 * a + 2] = F2;
-        if (g.mode == 2) return;  // batch: the per-blob CG set-up forms the moments
+        if constexpr (MODE == 2) return;  // batch: the per-blob CG set-up forms the moments
         const float dx = (float)(g.px[a] - g.xc[0]), dy = (float)(g.py[a] - g.xc[1]), dz = (float)(g.pz[a] - g.xc[2]);
         g.dpos[a] = make_float4(dx, dy, dz, 0.f);
         acc[0] = df32{F0 * F0 + F1 * F1 + F2 * F2, 0.f};
@@ -133,7 +136,7 @@ __global__ void __launch_bounds__(256) gather_mixed_kernel(GatherArgs<R> g) {
                     acc[k].hi = phi[i][0] * D[0] * phi[j][0] + phi[i][1] * D[1] * phi[j][1] + phi[i][2] * D[2] * phi[j][2];
         }
     }
-    if (g.mode != 0) return;
+    if constexpr (MODE != 0) return;
     df32 out[MIXED_GATHER_NP];
     block_sum_df<MIXED_GATHER_NP>(acc, smem, out);
     if (threadIdx.x == 0) {

@@ -27,10 +27,11 @@ struct MixedElements {
     cudaError_t init(host::Arena &mem, const host::HostModel &h, bool inertial, bool noise,
                      const std::vector<int> &elem_off) {
         N = h.N;
+        cudaError_t e;
+        if ((e = MixedLaunch::init()) != cudaSuccess) return e;
         std::vector<double> x(3 * (size_t)N);
         for (int k = 0; k < N; ++k)
             for (int c = 0; c < 3; ++c) x[(size_t)c * N + k] = h.pos[3 * (size_t)k + c];
-        cudaError_t e;
         if ((e = mem.upload(&xr, x)) != cudaSuccess) return e;
         if ((e = mem.alloc(&u, (size_t)N)) != cudaSuccess) return e;
         if (inertial && (e = mem.alloc(&vf, (size_t)N)) != cudaSuccess) return e;
