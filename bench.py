@@ -49,6 +49,7 @@ PHYS = dict(solver="CG_nomass", dt=1e-12, kT=4.11e-21, epsilon=1e-10, max_iterat
             calc_stokes=0)
 FLUSH_BYTES = 256 << 20
 MESO_LENGTH = 1.7e-10
+MESO_FORCE = 2.4364705882352941e-11
 
 
 def workload_config(n: int, precision: str) -> dict:
@@ -458,6 +459,89 @@ def run_batch(args, ws) -> dict:
     return out
 
 
+def run_batch_long(args) -> dict:
+    """The replica ensemble over a long run at a stable time step (the stiffest blobs are explicitly unstable at
+    1e-12 s): per-blob equipartition of the strain energy at kT > 0, mean over samples after a burn-in of a fifth
+    of the run, against (3 N_b - 6) kT / 2 (N_b vertices; the blobs carry no pins); and, at kT = 0 from a 2 %
+    shear, the drift of a size-stratified sample of blobs from the FP64 single-blob path over the same steps.
+    The explicit step of the overdamped dynamics holds each internal mode of rate lambda (V^-1 K) at
+    1 / (1 - lambda dt / 2) of its kT / 2, so the ratio exceeds 1 where lambda dt is not small; the same sample
+    of blobs is therefore also run through the FP64 single-blob path (the reference's arithmetic) from the same
+    stream state, whose ratio the batch's must reproduce."""
+    import numpy as np
+
+    from ffea_ci_demo_gb300 import build, lib
+    from ffea_ci_demo_gb300.mesh import apply_shear, ensemble
+
+    build.build()
+    meshes = ensemble(args.blobs)
+    steps, dt, every = args.ensemble_long_steps, args.ensemble_long_dt, 10
+    burn = steps // 5
+    kw = {k: v for k, v in PHYS.items() if k != "solver"}
+    kw["dt"] = dt
+    bt = lib.Batch(meshes, **kw)
+    order = sorted(range(len(meshes)), key=lambda b: meshes[b].n_elem)
+    pick = sorted(set([order[0], order[len(order) // 3], order[2 * len(order) // 3], order[-1]]))
+    rng0 = {b: bt.rng_state(b) for b in pick}
+    t0 = time.perf_counter()
+    samples = []
+    for k in range(0, steps, every):
+        bt.update(every)
+        if k + every > burn:
+            samples.append(bt.strain_energies())
+    run_s = time.perf_counter() - t0
+    bt.close()
+    se = np.array(samples)
+    kt_meso = PHYS["kT"] / (MESO_FORCE * MESO_LENGTH)
+    nv = np.array([m.n_linear for m in meshes])
+    want = kt_meso * (3 * nv - 6) / 2
+    ratio = se.mean(axis=0) / want
+    # one sample's relative spread is sqrt(2 / dof); the run's samples are correlated, so the per-blob z uses
+    # the spread of its own sample means over four quarters of the sampled run
+    q = np.array_split(se, 4, axis=0)
+    qm = np.array([x.mean(axis=0) for x in q]) / want
+    sem = qm.std(axis=0, ddof=1) / 2.0
+    out = {"blobs": len(meshes), "steps": steps, "dt": dt, "burn_in_steps": burn, "sample_every": every,
+           "samples": int(se.shape[0]), "run_s": run_s,
+           "equipartition": {"ensemble_ratio": float(se.mean(axis=0).sum() / want.sum()),
+                             "per_blob_ratio_mean": float(ratio.mean()), "per_blob_ratio_min": float(ratio.min()),
+                             "per_blob_ratio_max": float(ratio.max()),
+                             "per_blob_abs_dev_median": float(np.median(np.abs(ratio - 1))),
+                             "blobs_within_5pct": int((np.abs(ratio - 1) < 0.05).sum()),
+                             "per_blob_sem_median": float(np.median(sem))}}
+    same = {}
+    for b in pick:
+        f = lib.Blob(meshes[b], precision="fp64", rng_state=rng0[b], **dict(PHYS, **kw))
+        fs = []
+        for k in range(0, steps, every):
+            f.update(every)
+            if k + every > burn:
+                fs.append(f.measurements()["strain_energy"])
+        f.close()
+        same[str(b)] = {"tets": meshes[b].n_elem, "ratio_batch": float(ratio[b]),
+                        "ratio_fp64_single_blob": float(np.mean(fs) / want[b])}
+    out["equipartition"]["fp64_same_stream"] = same
+    # kT = 0 drift against the FP64 single-blob path
+    kw0 = dict(kw, kT=0.0, calc_noise=0)
+    bt = lib.Batch(meshes, **kw0)
+    x0 = [apply_shear(m, 0.02, seed=3) * (m.scale / MESO_LENGTH) for m in meshes]
+    bt.set_positions(np.concatenate(x0))
+    bt.update(steps)
+    drift = {}
+    for b in pick:
+        f = lib.Blob(meshes[b], precision="fp64", **dict(PHYS, **kw0))
+        f.set_state(pos=x0[b])
+        f.update(steps)
+        ref = f.pos()
+        drift[str(b)] = {"tets": meshes[b].n_elem,
+                         "max_abs_err_rel_to_max_disp": float(np.abs(bt.pos(b) - ref).max() /
+                                                              np.abs(ref - x0[b]).max())}
+        f.close()
+    bt.close()
+    out["kT0_drift_vs_fp64"] = drift
+    return out
+
+
 def run_adjoint(args) -> dict:
     """Configuration 3: gradient of a 200-step window (checkpoints every 20) of a 20^3-cell cube with
     lognormal per-element moduli, noise frozen (replayed), loss |x_K - target|^2; cost against the
@@ -756,6 +840,10 @@ def main():
                     help="timed steps of the replica ensemble (its stiffest blobs are explicitly unstable at "
                          "dt = 1e-12 s: they invert an element after about 20 steps, in the reference's algorithm "
                          "too, so warm-up + timed steps stay below that)")
+    ap.add_argument("--ensemble-long-steps", type=int, default=0,
+                    help="batch: also run the ensemble this many steps at --ensemble-long-dt for the per-blob "
+                         "equipartition and the kT=0 drift against FP64 (0: skip; 1000 takes about four minutes)")
+    ap.add_argument("--ensemble-long-dt", type=float, default=5e-13)
     ap.add_argument("--no-tune", action="store_true", help="batch: fixed launch configuration (--cg-threads, --tpn)")
     ap.add_argument("--cg-threads", type=int, default=128)
     ap.add_argument("--tpn", type=int, default=1)
@@ -807,6 +895,8 @@ def main():
             return
         args.steps = args.batch_steps
         b = run_batch(args, ws)
+        if args.ensemble_long_steps > 0:
+            b["long_run"] = run_batch_long(args)
         line = {"metric": "node-steps/s", "value": b["value"], "unit": "node-steps/s", "n_gpus": ws,
                 "steps": b["steps"], "warmup": args.warmup, "ms_per_step": b["ms_per_step"],
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",

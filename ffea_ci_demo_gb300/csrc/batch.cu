@@ -841,6 +841,20 @@ int ffea_gpu_batch_load_ctforces(ffea_gpu_batch *bt, int blob, const char *ctf_f
     return bt->capture();
 }
 
+int ffea_gpu_batch_strain_energies(ffea_gpu_batch *bt, double *out) {
+    if (!bt || !out) return FFEA_GPU_EINPUT;
+    double *d = nullptr;
+    CK(cudaMallocAsync(&d, sizeof(double) * bt->nblobs, bt->stream));
+    cudaError_t e = BatchLaunch::strain(bt->tet, bt->px, bt->py, bt->pz, bt->jinv, bt->G, bt->E, bt->vol0, bt->h.T,
+                                        bt->d_elem_off, bt->nblobs, d, bt->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(out, d, sizeof(double) * bt->nblobs, cudaMemcpyDeviceToHost, bt->stream);
+    cudaFreeAsync(d, bt->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(bt->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "batch_strain_energies");
+    return FFEA_GPU_OK;
+}
+
 int ffea_gpu_batch_get_rng_state(ffea_gpu_batch *bt, int blob, uint32_t s[6]) {
     if (!bt || blob < 0 || blob >= bt->nblobs || !s) return FFEA_GPU_EINPUT;
     CK(cudaMemcpyAsync(s, bt->rng_states + 6 * (size_t)blob, 6 * sizeof(uint32_t), cudaMemcpyDeviceToHost,

@@ -211,8 +211,11 @@ struct BlobImpl final : ffea_gpu_blob {
     // The step as a CUDA graph, replayed once per step: [0] plain, [1] with the phase events of step_timed.
     // Captured on first use. Host state that a step's launches take by value (the rigid modes and centroid,
     // constant forces, the stream layout) drops them when it changes (invalidate_graphs).
-    cudaGraphExec_t gexec[2] = {nullptr, nullptr};
-    long long graph_launches[2] = {0, 0};
+    // step graphs: [timed + 2 cont], cont = a step that follows a fused mass-lumped step of the same call (its
+    // FP32 node state was written by that step's gather)
+    cudaGraphExec_t gexec[4] = {nullptr, nullptr, nullptr, nullptr};
+    bool prep_cont = false;  // the step being captured is such a continuation
+    long long graph_launches[4] = {0, 0, 0, 0};
     double *staging = nullptr;  // pinned host buffer, 3*N doubles, for state copies
     // node state in the reference's layout on the device: n_all x 3 doubles, the vertex row of each vertex
     // node, and the source rows of every reference node (vertex (k, k), midpoint (a, b), else (-1, -1))
@@ -250,31 +253,38 @@ struct BlobImpl final : ffea_gpu_blob {
             }
     }
 
-    // one step through its graph (captured from launch_step on first use)
-    int launch_step_graph(int timed) {
-        if (!gexec[timed]) {
+    // the mixed mass-lumped step leaves the next step's FP32 node state behind (its gather updates the positions)
+    bool fused_prep() const { return std::is_same<R, float>::value && p.solver == FFEA_GPU_MASSLUMPED; }
+
+    // one step through its graph (captured from launch_step on first use); `cont`: the previous launch on the
+    // stream was a step of the same call, so a fused step need not form the FP32 node state again
+    int launch_step_graph(int timed, bool cont = false) {
+        const int gi = timed + ((cont && fused_prep()) ? 2 : 0);
+        if (!gexec[gi]) {
             record_phases = timed != 0;
+            prep_cont = gi >= 2;
             const long long l0 = launch_count();
             CK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
             const int rc = launch_step();
             cudaGraph_t graph = nullptr;
             const cudaError_t e = cudaStreamEndCapture(stream, &graph);
             record_phases = false;
-            graph_launches[timed] = launch_count() - l0;
-            count_launch((int)-graph_launches[timed]);  // counted on every replay instead
+            prep_cont = false;
+            graph_launches[gi] = launch_count() - l0;
+            count_launch((int)-graph_launches[gi]);  // counted on every replay instead
             if (rc || e != cudaSuccess) {
                 if (graph) cudaGraphDestroy(graph);
                 return rc ? rc : cuda_fail(e, "cudaStreamEndCapture");
             }
-            const cudaError_t ei = cudaGraphInstantiate(&gexec[timed], graph, 0);
+            const cudaError_t ei = cudaGraphInstantiate(&gexec[gi], graph, 0);
             cudaGraphDestroy(graph);
             if (ei != cudaSuccess) {
-                gexec[timed] = nullptr;
+                gexec[gi] = nullptr;
                 return cuda_fail(ei, "cudaGraphInstantiate");
             }
         }
-        CK(cudaGraphLaunch(gexec[timed], stream));
-        count_launch((int)graph_launches[timed]);
+        CK(cudaGraphLaunch(gexec[gi], stream));
+        count_launch((int)graph_launches[gi]);
         return FFEA_GPU_OK;
     }
 
@@ -571,7 +581,7 @@ struct BlobImpl final : ffea_gpu_blob {
     // positions) needs only the geometry the assembly reads
     int launch_elements(int recompute) {
         if constexpr (std::is_same<R, float>::value) {
-            CK(me.prep(px, py, pz, vx, vy, vz, rng_state, chunk_jump, stream));
+            CK(me.prep(px, py, pz, vx, vy, vz, rng_state, chunk_jump, stream, prep_cont && !recompute));
             ElemArgs<float> ea = elem_args(recompute);
             me.fill(ea);
             ea.ef = nullptr;
@@ -656,6 +666,11 @@ struct BlobImpl final : ffea_gpu_blob {
         // the mixed mass-lumped step updates positions in the gather (no solve between them)
         ga.fuse_euler = std::is_same<R, float>::value && p.solver == FFEA_GPU_MASSLUMPED;
         ga.upx = px; ga.upy = py; ga.upz = pz; ga.uvx = vx; ga.uvy = vy; ga.uvz = vz; ga.dt = p.dt;
+        if (ga.fuse_euler && fused_prep()) {
+            ga.nu = me.u;
+            ga.nvf = me.vf;
+            ga.nxr = me.xr;
+        }
         {
             NodeForces &sn = ga.sn;
             sn.noise = sn_chunk_jump != nullptr;
@@ -719,7 +734,7 @@ struct BlobImpl final : ffea_gpu_blob {
         s.steps_done = 0;
         CK(cudaMemcpyAsync(st, &s, sizeof(DevStatus), cudaMemcpyHostToDevice, stream));
         for (int i = 0; i < nsteps; ++i) {
-            rc = launch_step_graph(0);
+            rc = launch_step_graph(0, i > 0);
             if (rc) return rc;
             // the non-finite flag is raised by euler_kernel after the positions moved; stop the step chain
         }
@@ -745,7 +760,7 @@ struct BlobImpl final : ffea_gpu_blob {
                 cudaError_t e = cudaMemsetAsync(scratch, i & 0xff, (size_t)flush_bytes, stream);
                 if (e != cudaSuccess) { rc = cuda_fail(e, "flush"); break; }
             }
-            rc = launch_step_graph(1);
+            rc = launch_step_graph(1, i > 0);
             if (rc) break;
             cudaError_t e = cudaEventSynchronize(ev[FFEA_GPU_NUM_PHASES]);
             if (e != cudaSuccess) { rc = cuda_fail(e, "cudaEventSynchronize"); break; }

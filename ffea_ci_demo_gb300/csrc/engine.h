@@ -85,6 +85,10 @@ struct BatchLaunch {
     static int cg_max_grid(int device, int threads);
     static cudaError_t finish(uint32_t *rng_states, const MrgJump *step_jumps, int nblobs, DevStatus *st,
                               cudaStream_t s);
+    // every blob's strain energy (batch_strain_kernel) into out[nblobs]
+    static cudaError_t strain(const int4 *tet, const double *px, const double *py, const double *pz,
+                              const float *jinv, const float *G, const float *E, const float *vol0, int T,
+                              const int *elem_off, int nblobs, double *out, cudaStream_t s);
 };
 void count_launch(int n = 1);
 

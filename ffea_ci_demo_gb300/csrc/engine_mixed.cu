@@ -11,7 +11,7 @@ template struct AdjLaunch<float>;
 
 __global__ void __launch_bounds__(256) node_prep_kernel(NodePrepArgs g) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < g.N) {
+    if (i < g.N && !g.skip_nodes) {
         const size_t N = g.N;
         g.u[i] = make_float4((float)(g.px[i] - g.xr[i]), (float)(g.py[i] - g.xr[N + i]),
                              (float)(g.pz[i] - g.xr[2 * N + i]), 0.f);
@@ -33,7 +33,7 @@ __global__ void __launch_bounds__(256) node_prep_kernel(NodePrepArgs g) {
 }
 
 cudaError_t MixedLaunch::node_prep(const NodePrepArgs &a, cudaStream_t s) {
-    const int n = a.N > a.nchunks ? a.N : a.nchunks;
+    const int n = (a.N > a.nchunks && !a.skip_nodes) ? a.N : a.nchunks;
     if (n <= 0) return cudaSuccess;
     node_prep_kernel<<<(n + 255) / 256, 256, 0, s>>>(a);
     count_launch();
@@ -119,6 +119,14 @@ int BatchLaunch::cg_max_grid(int device, int threads) {
 cudaError_t BatchLaunch::finish(uint32_t *rng_states, const MrgJump *step_jumps, int nblobs, DevStatus *st,
                                 cudaStream_t s) {
     batch_finish_kernel<<<(nblobs + 127) / 128, 128, 0, s>>>(rng_states, step_jumps, nblobs, st);
+    count_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t BatchLaunch::strain(const int4 *tet, const double *px, const double *py, const double *pz,
+                                const float *jinv, const float *G, const float *E, const float *vol0, int T,
+                                const int *elem_off, int nblobs, double *out, cudaStream_t s) {
+    batch_strain_kernel<<<nblobs, 256, 0, s>>>(tet, px, py, pz, jinv, G, E, vol0, T, elem_off, out);
     count_launch();
     return cudaGetLastError();
 }

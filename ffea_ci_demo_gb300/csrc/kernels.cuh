@@ -630,6 +630,10 @@ struct GatherArgs {
     double dt;
     int fuse_euler;
     int threads;          // threads per block in mode 2 (0: the default); 64, 128 or 256
+    // with fuse_euler: the next step's FP32 displacements from the rest positions nxr (3 x N, SoA) and velocities
+    // (node_prep_kernel's arithmetic), or null
+    float4 *nu, *nvf;
+    const double *nxr;
 };
 
 template <class R>
@@ -1298,6 +1302,39 @@ struct MeasureArgs {
     double *partials;         // MEASURE_NV rows of gridDim.x
 };
 
+// Twice the elastic energy of element i (the reference's measurement, halved by the caller): with F = J^T J0^-1
+// and the volume ratio t = vol / vol0, vol0 (G (|F|^2 - 3) + C/2 (t^2 - 1) - (C + 2G) ln t), C = E - 2G/3.
+// J and det J as calculate_jacobian forms them from the element's vertex rows t.
+template <class R>
+__device__ __forceinline__ double element_strain_energy2(int4 t, const double *px, const double *py, const double *pz,
+                                                         const R *jinv, size_t T, int i, double Gs, double Es,
+                                                         double v0) {
+    const int nd[4] = {t.x, t.y, t.z, t.w};
+    double J[3][3];
+    for (int r = 0; r < 3; ++r) {
+        J[r][0] = px[nd[r + 1]] - px[nd[0]];
+        J[r][1] = py[nd[r + 1]] - py[nd[0]];
+        J[r][2] = pz[nd[r + 1]] - pz[nd[0]];
+    }
+    const double d1 = J[2][2] * J[1][1] - J[2][1] * J[1][2];
+    const double d2 = J[2][1] * J[0][2] - J[2][2] * J[0][1];
+    const double d3 = J[1][2] * J[0][1] - J[1][1] * J[0][2];
+    const double det = J[0][0] * d1 + J[1][0] * d2 + J[2][0] * d3;
+    const double vol = (1.0 / 6.0) * fabs(det);
+    double F[3][3];
+    for (int a = 0; a < 3; ++a)
+        for (int b = 0; b < 3; ++b) {
+            F[a][b] = 0;
+            for (int k = 0; k < 3; ++k) F[a][b] += J[k][a] * (double)jinv[(size_t)(3 * b + k) * T + i];
+        }
+    const double C = Es - (2.0 / 3.0) * Gs;
+    const double t1 = vol / v0;
+    const double ff = F[0][0] * F[0][0] + F[1][1] * F[1][1] + F[2][2] * F[2][2] + F[0][1] * F[0][1] +
+                      F[1][0] * F[1][0] + F[0][2] * F[0][2] + F[2][0] * F[2][0] + F[1][2] * F[1][2] +
+                      F[2][1] * F[2][1];
+    return v0 * (Gs * (ff - 3) + 0.5 * C * (t1 * t1 - 1) - (C + 2 * Gs) * log(t1));
+}
+
 template <class R>
 __global__ void __launch_bounds__(256) measure_kernel(MeasureArgs<R> g) {
     __shared__ double smem[MEASURE_NV * 32];
@@ -1306,23 +1343,6 @@ __global__ void __launch_bounds__(256) measure_kernel(MeasureArgs<R> g) {
     if (i < g.T) {
         const int4 t = g.tet[i];
         const int nd[4] = {t.x, t.y, t.z, t.w};
-        double J[3][3];
-        for (int r = 0; r < 3; ++r) {
-            J[r][0] = g.px[nd[r + 1]] - g.px[nd[0]];
-            J[r][1] = g.py[nd[r + 1]] - g.py[nd[0]];
-            J[r][2] = g.pz[nd[r + 1]] - g.pz[nd[0]];
-        }
-        const double d1 = J[2][2] * J[1][1] - J[2][1] * J[1][2];
-        const double d2 = J[2][1] * J[0][2] - J[2][2] * J[0][1];
-        const double d3 = J[1][2] * J[0][1] - J[1][1] * J[0][2];
-        const double det = J[0][0] * d1 + J[1][0] * d2 + J[2][0] * d3;
-        const double vol = (1.0 / 6.0) * fabs(det);
-        double F[3][3];
-        for (int a = 0; a < 3; ++a)
-            for (int b = 0; b < 3; ++b) {
-                F[a][b] = 0;
-                for (int k = 0; k < 3; ++k) F[a][b] += J[k][a] * (double)g.jinv[(size_t)(3 * b + k) * g.T + i];
-            }
         const double Gs = g.G[i], Es = g.E[i], v0 = g.vol0[i];
         if (g.inertial) {
             double v[12], tmp[12] = {0};
@@ -1337,12 +1357,7 @@ __global__ void __launch_bounds__(256) measure_kernel(MeasureArgs<R> g) {
             for (int k = 0; k < 12; ++k) s += v[k] * (tmp[k] * m);
             acc[1] = s;
         }
-        const double C = Es - (2.0 / 3.0) * Gs;
-        const double t1 = vol / v0;
-        const double ff = F[0][0] * F[0][0] + F[1][1] * F[1][1] + F[2][2] * F[2][2] + F[0][1] * F[0][1] +
-                          F[1][0] * F[1][0] + F[0][2] * F[0][2] + F[2][0] * F[2][0] + F[1][2] * F[1][2] +
-                          F[2][1] * F[2][1];
-        acc[0] = v0 * (Gs * (ff - 3) + 0.5 * C * (t1 * t1 - 1) - (C + 2 * Gs) * log(t1));
+        acc[0] = element_strain_energy2<R>(t, g.px, g.py, g.pz, g.jinv, g.T, i, Gs, Es, v0);
     }
     if (i < g.N) {
         const double x = g.px[i], y = g.py[i], z = g.pz[i];

@@ -333,4 +333,19 @@ __global__ void batch_finish_kernel(uint32_t *rng_states, const MrgJump *step_ju
     if (b == 0) st->steps_done += 1;
 }
 
+// every blob's strain energy (Blob::make_measurements, src/Blob.cpp:1066-1125) in FP64: one block per blob, its
+// elements' energies summed in a fixed order
+__global__ void __launch_bounds__(256) batch_strain_kernel(const int4 *tet, const double *px, const double *py,
+                                                           const double *pz, const float *jinv, const float *G,
+                                                           const float *E, const float *vol0, int T,
+                                                           const int *elem_off, double *out) {
+    __shared__ double smem[32];
+    const int b = blockIdx.x;
+    double acc[1] = {0.0};
+    for (int i = elem_off[b] + threadIdx.x; i < elem_off[b + 1]; i += blockDim.x)
+        acc[0] += element_strain_energy2<float>(tet[i], px, py, pz, jinv, T, i, G[i], E[i], vol0[i]);
+    block_sum<1>(acc, smem);
+    if (threadIdx.x == 0) out[b] = 0.5 * acc[0];
+}
+
 }  // namespace ffea

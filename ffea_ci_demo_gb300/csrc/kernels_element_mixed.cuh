@@ -64,6 +64,7 @@ struct NodePrepArgs {
     const int *chunk_blob;         // blob of each chunk (null: one blob)
     const int *chunk_off;          // first chunk of each blob (with chunk_blob)
     uint32_t *chunk_state;         // out: 6 per chunk
+    int skip_nodes;                // 1: u and vf already hold this state (the fused mass-lumped gather wrote them)
 };
 
 // u = x - X and the velocities in FP32 for every vertex; the stream state at the start of every 32-element chunk

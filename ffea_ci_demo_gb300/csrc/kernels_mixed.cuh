@@ -113,7 +113,14 @@ __global__ void __launch_bounds__(256) gather_mixed_kernel(GatherArgs<R> g) {
                 if (!(isfinite(a0) && isfinite(a1) && isfinite(a2))) atomicExch(&g.st->nonfinite, 1);
                 const double v0 = g.uvx[a] + a0 * g.dt, v1 = g.uvy[a] + a1 * g.dt, v2 = g.uvz[a] + a2 * g.dt;
                 g.uvx[a] = v0; g.uvy[a] = v1; g.uvz[a] = v2;
-                g.upx[a] += v0 * g.dt; g.upy[a] += v1 * g.dt; g.upz[a] += v2 * g.dt;
+                const double p0 = g.upx[a] + v0 * g.dt, p1 = g.upy[a] + v1 * g.dt, p2 = g.upz[a] + v2 * g.dt;
+                g.upx[a] = p0; g.upy[a] = p1; g.upz[a] = p2;
+                if (g.nu) {
+                    const size_t N = g.N;
+                    g.nu[a] = make_float4((float)(p0 - g.nxr[a]), (float)(p1 - g.nxr[N + a]),
+                                          (float)(p2 - g.nxr[2 * N + a]), 0.f);
+                    g.nvf[a] = make_float4((float)v0, (float)v1, (float)v2, 0.f);
+                }
             }
             return;
         }

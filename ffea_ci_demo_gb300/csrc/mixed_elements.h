@@ -82,10 +82,13 @@ struct MixedElements {
         return cudaSuccess;
     }
 
-    // node_prep_kernel for the state in px..vz and the streams' states (6 per blob)
+    // node_prep_kernel for the state in px..vz and the streams' states (6 per blob); skip_nodes: u and vf already
+    // hold the state (only the chunk states are formed)
     cudaError_t prep(const double *px, const double *py, const double *pz, const double *vx, const double *vy,
-                     const double *vz, const uint32_t *rng_state, const MrgJump *chunk_jump, cudaStream_t s) const {
+                     const double *vz, const uint32_t *rng_state, const MrgJump *chunk_jump, cudaStream_t s,
+                     bool skip_nodes = false) const {
         NodePrepArgs a{};
+        a.skip_nodes = skip_nodes ? 1 : 0;
         a.N = N;
         a.px = px; a.py = py; a.pz = pz; a.vx = vx; a.vy = vy; a.vz = vz;
         a.xr = xr;

@@ -124,6 +124,7 @@ def load():
         "ffea_gpu_batch_set_state": (C.c_int, [vp, C.c_int, dp, dp]),
         "ffea_gpu_batch_set_rng_state": (C.c_int, [vp, C.c_int, dp]),
         "ffea_gpu_batch_load_ctforces": (C.c_int, [vp, C.c_int, C.c_char_p, C.c_char_p, C.c_int]),
+        "ffea_gpu_batch_strain_energies": (C.c_int, [vp, dp]),
         "ffea_gpu_batch_get_rng_state": (C.c_int, [vp, C.c_int, dp]),
         "ffea_gpu_batch_cg_iterations": (C.c_int, [vp, dp, C.POINTER(C.c_longlong)]),
         "ffea_gpu_batch_config": (C.c_int, [vp, ip, ip, ip]),
@@ -572,6 +573,12 @@ class Batch:
     def set_rng_state(self, blob: int, s) -> None:
         a = np.ascontiguousarray(s, np.uint32)
         _check(self._lib.ffea_gpu_batch_set_rng_state(self._h, blob, _p(a)), "batch_set_rng_state")
+
+    def strain_energies(self) -> np.ndarray:
+        """Each blob's strain energy (meso units), as Blob.measurements()["strain_energy"]."""
+        out = np.empty(self.n_blobs)
+        _check(self._lib.ffea_gpu_batch_strain_energies(self._h, _p(out)), "batch_strain_energies")
+        return out
 
     def load_ctforces(self, blob: int, ctforces_file: str, surface_file: str | None = None,
                       blob_index: int = 0) -> None:

@@ -328,6 +328,10 @@ int ffea_gpu_batch_set_states(ffea_gpu_batch *batch, const double *pos, const do
 int ffea_gpu_batch_set_rng_state(ffea_gpu_batch *batch, int blob, const uint32_t state[6]);
 int ffea_gpu_batch_get_rng_state(ffea_gpu_batch *batch, int blob, uint32_t state[6]);
 
+/* Each blob's strain energy (the StrainEnergy of Blob::make_measurements, src/Blob.cpp:1066-1125; meso units)
+ * at the current positions, in FP64: out[num_blobs]. */
+int ffea_gpu_batch_strain_energies(ffea_gpu_batch *batch, double *out);
+
 /* Constant forces of blob `blob` of the batch, read as ffea_gpu_blob_load_ctforces reads them (the
  * ctforces file's entries for `blob_index`, faces of `surface_file`); each call replaces that blob's
  * forces only. */

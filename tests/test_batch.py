@@ -287,3 +287,20 @@ def test_batch_bulk_state_matches_per_blob_calls():
         ref.set_state(b, pos=sheared(m, 0.02))
     ref.update(5)
     assert np.array_equal(bt.positions(), ref.positions())
+
+
+@pytest.mark.gpu
+def test_batch_strain_energies_match_single_blobs():
+    """ffea_gpu_batch_strain_energies: each blob's StrainEnergy of Blob::make_measurements, as the single mixed
+    blob measures it at the same positions (FP64 sums in another order: 1e-12)."""
+    meshes = [case_mesh(n, s) for n, s in MESHES]
+    bt = lib.Batch(meshes, kT=0.0, calc_noise=0)
+    x0 = [sheared(m, 0.02, seed=3 + b) for b, m in enumerate(meshes)]
+    for b in range(len(meshes)):
+        bt.set_state(b, pos=x0[b])
+    se = bt.strain_energies()
+    for b, m in enumerate(meshes):
+        s = lib.Blob(m, solver="CG_nomass", precision="mixed", kT=0.0, calc_noise=0)
+        s.set_state(pos=x0[b])
+        want = s.measurements()["strain_energy"]
+        assert want > 0 and abs(se[b] - want) <= 1e-12 * want, b
