@@ -521,6 +521,22 @@ def run_batch_long(args) -> dict:
         same[str(b)] = {"tets": meshes[b].n_elem, "ratio_batch": float(ratio[b]),
                         "ratio_fp64_single_blob": float(np.mean(fs) / want[b])}
     out["equipartition"]["fp64_same_stream"] = same
+    # the time-step bias on the smallest blob: the same simulated time at smaller steps (mixed single-blob path)
+    b = pick[0]
+    scan = []
+    for div in (1, 2.5, 5, 10):
+        dts = dt / div
+        n_st = int(round(steps * div))
+        f = lib.Blob(meshes[b], precision="mixed", rng_state=rng0[b], **dict(PHYS, **dict(kw, dt=dts)))
+        ev = max(every, int(round(every * div)))
+        fs = []
+        for k in range(0, n_st, ev):
+            f.update(ev)
+            if k + ev > n_st // 5:
+                fs.append(f.measurements()["strain_energy"])
+        f.close()
+        scan.append({"dt": dts, "steps": n_st, "ratio": float(np.mean(fs) / want[b])})
+    out["equipartition"]["dt_scan_smallest_blob"] = {"blob": b, "tets": meshes[b].n_elem, "runs": scan}
     # kT = 0 drift against the FP64 single-blob path
     kw0 = dict(kw, kT=0.0, calc_noise=0)
     bt = lib.Batch(meshes, **kw0)
@@ -669,6 +685,14 @@ def run_scale(args) -> dict:
             it = (b.cg_iterations()[1] - it0) / k
             r = {"value": N * k / (t["ms"] / 1e3), "ms_per_step": t["ms"] / k, "cg_iters_per_step": it,
                  "phase_ms_per_step": {q: v / k for q, v in t["phase_ms"].items()}, "cg_kernel": b.cg_kernel()}
+            if solver == "masslumped":
+                # the value without the phase events (each costs a few microseconds inside a step of about a
+                # tenth of a millisecond): the steps as update() runs them, timed around each graph launch
+                kp = max(k, 20)
+                tp = b.update_timed(kp, FLUSH_BYTES, phases=False)
+                t = {"ms": tp["ms"] * k / kp, "phase_ms": t["phase_ms"]}
+                r.update({"value": N * kp / (tp["ms"] / 1e3), "ms_per_step": tp["ms"] / kp,
+                          "phase_events_ms_per_step": r["ms_per_step"]})
             p = 4 if prec == "mixed" else 8
             if solver == "CG_nomass":
                 # the HBM anchor: at this size the matrix (165 MB mixed in SELL form) no longer fits in L2. The

@@ -760,15 +760,24 @@ struct BlobImpl final : ffea_gpu_blob {
                 cudaError_t e = cudaMemsetAsync(scratch, i & 0xff, (size_t)flush_bytes, stream);
                 if (e != cudaSuccess) { rc = cuda_fail(e, "flush"); break; }
             }
-            rc = launch_step_graph(1, i > 0);
+            if (phase_ms) {
+                rc = launch_step_graph(1, i > 0);
+            } else {  // the untimed graph, events around its launch only
+                cudaError_t e = cudaEventRecord(ev[0], stream);
+                if (e != cudaSuccess) { rc = cuda_fail(e, "cudaEventRecord"); break; }
+                rc = launch_step_graph(0, i > 0);
+                if (!rc && (e = cudaEventRecord(ev[FFEA_GPU_NUM_PHASES], stream)) != cudaSuccess)
+                    rc = cuda_fail(e, "cudaEventRecord");
+            }
             if (rc) break;
             cudaError_t e = cudaEventSynchronize(ev[FFEA_GPU_NUM_PHASES]);
             if (e != cudaSuccess) { rc = cuda_fail(e, "cudaEventSynchronize"); break; }
             float ms = 0.f;
-            for (int k = 0; k < FFEA_GPU_NUM_PHASES; ++k) {
-                cudaEventElapsedTime(&ms, ev[k], ev[k + 1]);
-                ph[k] += ms;
-            }
+            if (phase_ms)
+                for (int k = 0; k < FFEA_GPU_NUM_PHASES; ++k) {
+                    cudaEventElapsedTime(&ms, ev[k], ev[k + 1]);
+                    ph[k] += ms;
+                }
             cudaEventElapsedTime(&ms, ev[0], ev[FFEA_GPU_NUM_PHASES]);
             tot += ms;
         }

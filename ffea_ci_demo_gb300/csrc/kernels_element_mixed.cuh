@@ -236,7 +236,7 @@ __device__ __forceinline__ bool element_mixed_eval(const ElemArgs<float> &g, int
     if (dK > EM_DEGENERATE) {
         // K^-1 = adj(K) / det K, then J^-1 = K^-1 J0^-1: dpsi[4j + a] = (J^-1)[j][a - 1]
         const float k00 = 1.f + Kd[0][0], k11 = 1.f + Kd[1][1], k22 = 1.f + Kd[2][2];
-        id = 1.f / dK;
+        id = __frcp_rn(dK);  // 1 / det K, correctly rounded (the division's value)
         float Ki[3][3];
         Ki[0][0] = (k11 * k22 - Kd[1][2] * Kd[2][1]) * id;
         Ki[0][1] = (Kd[0][2] * Kd[2][1] - Kd[0][1] * k22) * id;

@@ -435,6 +435,60 @@ __device__ __forceinline__ void grid_sum_df8(const float2 *partials, int stride,
     __syncthreads();
 }
 
+// The same row with U blocks per trip (3x3 blocks only): all U blocks' loads (columns, values, z and p) issue
+// before any of their products, so U of the row's dependent DRAM round trips overlap; the products are
+// accumulated in spmv_row_z's order, so the result is identical.
+template <int U, class A>
+__device__ __forceinline__ void spmv_row_zu(const A &g, const float4 *z4, const float4 *p4, float beta, bool first,
+                                            int a, int sub, bool valid, float &q0, float &q1, float &q2) {
+    q0 = 0.f; q1 = 0.f; q2 = 0.f;
+    const int tpn = g.tpn;
+    if (valid) {
+        const int s = a >> 5, lane = a & 31;
+        const int base = __ldg(g.slice_ptr + s);
+        const int len = __ldg(g.rowlen + a);
+        const float *v = g.val + 9 * (size_t)base + lane;
+#pragma unroll 1
+        for (int k = sub; k < len; k += U * tpn) {
+            int bc[U];
+            float w[U][9];
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const int ku = k + u * tpn;
+                const bool in = ku < len;
+                bc[u] = in ? __ldg(g.bcol + base + 32 * ku + lane) : 0;
+                const float *vk = v + (size_t)32 * 9 * ku;
+#pragma unroll
+                for (int i = 0; i < 9; ++i) w[u][i] = in ? __ldg(vk + 32 * i) : 0.f;
+            }
+            float pz[U][3];
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const float4 z = z4[bc[u]];
+                pz[u][0] = z.x; pz[u][1] = z.y; pz[u][2] = z.z;
+                if (!first) {
+                    const float4 po = p4[bc[u]];
+                    pz[u][0] = fmaf(beta, po.x, pz[u][0]);
+                    pz[u][1] = fmaf(beta, po.y, pz[u][1]);
+                    pz[u][2] = fmaf(beta, po.z, pz[u][2]);
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                if (k + u * tpn >= len) break;
+                q0 = fmaf(w[u][0], pz[u][0], q0); q0 = fmaf(w[u][1], pz[u][1], q0); q0 = fmaf(w[u][2], pz[u][2], q0);
+                q1 = fmaf(w[u][3], pz[u][0], q1); q1 = fmaf(w[u][4], pz[u][1], q1); q1 = fmaf(w[u][5], pz[u][2], q1);
+                q2 = fmaf(w[u][6], pz[u][0], q2); q2 = fmaf(w[u][7], pz[u][1], q2); q2 = fmaf(w[u][8], pz[u][2], q2);
+            }
+        }
+    }
+    for (int o = 1; o < tpn; o <<= 1) {
+        q0 += __shfl_xor_sync(0xffffffffu, q0, o);
+        q1 += __shfl_xor_sync(0xffffffffu, q1, o);
+        q2 += __shfl_xor_sync(0xffffffffu, q2, o);
+    }
+}
+
 // Row a of q = V p for cg_mixed_own_kernel and cg_batch_kernel: p at a neighbour b is formed from the preconditioned residual
 // z_b and the previous direction, both stored as float4 per node (two 16-byte loads per neighbour).
 // The same row with two blocks per trip: both blocks' loads (values, columns, z and p) issue before

@@ -261,15 +261,18 @@ class Blob:
         _check(rc, f"step (after {done.value} completed steps)")
         return done.value
 
-    def update_timed(self, nsteps: int, flush_bytes: int = 0) -> dict:
-        """update() with per-step CUDA-event timing on the blob's stream (flush outside the timed window)."""
+    def update_timed(self, nsteps: int, flush_bytes: int = 0, phases: bool = True) -> dict:
+        """update() with per-step CUDA-event timing on the blob's stream (flush outside the timed window).
+        phases: also time each phase (events between the step's kernels, which cost a little themselves);
+        without, the steps run exactly as update() runs them and phase_ms is None."""
         done, ms = C.c_int(0), C.c_double(0)
         ph = np.zeros(5)
         rc = self._lib.ffea_gpu_blob_step_timed(self._h, int(nsteps), int(flush_bytes), C.byref(done), C.byref(ms),
-                                                _p(ph))
+                                                _p(ph) if phases else None)
         _check(rc, f"step_timed (after {done.value} completed steps)")
         return {"steps": done.value, "ms": ms.value,
-                "phase_ms": dict(zip(("element", "assemble", "gather", "cg", "euler"), ph.tolist()))}
+                "phase_ms": dict(zip(("element", "assemble", "gather", "cg", "euler"), ph.tolist())) if phases
+                else None}
 
     def try_update(self, nsteps: int = 1) -> tuple[int, int]:
         """Like update() but returns (status, steps_done) instead of raising."""

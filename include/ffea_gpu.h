@@ -141,7 +141,9 @@ int ffea_gpu_blob_step(ffea_gpu_blob *blob, int nsteps, int *steps_done);
  * Before each step, flush_bytes of scratch device memory are written (outside the
  * timed window) so that each step starts with a cold L2; 0 disables the flush.
  * *step_ms gets the summed device time of the steps; phase_ms (may be NULL) gets
- * FFEA_GPU_NUM_PHASES per-phase sums (events between the kernels of each step). */
+ * FFEA_GPU_NUM_PHASES per-phase sums (events between the kernels of each step). With
+ * phase_ms NULL the steps run without those inner events (each step is timed by
+ * events around its graph launch alone), as ffea_gpu_blob_step runs them. */
 int ffea_gpu_blob_step_timed(ffea_gpu_blob *blob, int nsteps, long long flush_bytes, int *steps_done,
                              double *step_ms, double *phase_ms);
 
