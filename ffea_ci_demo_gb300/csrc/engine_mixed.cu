@@ -111,6 +111,8 @@ cudaError_t BatchLaunch::cg(const BatchCgArgs &a, int grid, int threads, cudaStr
 
 int BatchLaunch::cg_max_grid(int device, int threads) {
     int nsm = 0, per_sm = 0;
+    cudaFuncAttributes fa{};
+    if (cudaFuncGetAttributes(&fa, cg_batch_kernel) != cudaSuccess || threads > fa.maxThreadsPerBlock) return 0;
     if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) return 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, cg_batch_kernel, threads, 0) != cudaSuccess) return 0;
     return nsm * per_sm;

@@ -68,11 +68,17 @@ __global__ void __launch_bounds__(256) gather_mixed_kernel(GatherArgs<R> g) {
             F2 = (float)g.sn.node_ctf[3 * (size_t)a + 2];
         }
         if (g.parts) {
-            for (int m = g.part_ptr[a]; m < g.part_ptr[a + 1]; ++m) {
+            // two block sums per trip, both loads ahead of the adds (the adds keep block order)
+            int m = g.part_ptr[a];
+            const int m1 = g.part_ptr[a + 1];
+            for (; m + 2 <= m1; m += 2) {
+                const float4 q = g.parts[m], q2 = g.parts[m + 1];
+                F0 += q.x; F1 += q.y; F2 += q.z;
+                F0 += q2.x; F1 += q2.y; F2 += q2.z;
+            }
+            if (m < m1) {
                 const float4 q = g.parts[m];
-                F0 += q.x;
-                F1 += q.y;
-                F2 += q.z;
+                F0 += q.x; F1 += q.y; F2 += q.z;
             }
         } else {
             for (int m = g.inc_ptr[a]; m < g.inc_ptr[a + 1]; ++m) {
@@ -103,7 +109,8 @@ __global__ void __launch_bounds__(256) gather_mixed_kernel(GatherArgs<R> g) {
         if (g.pinned[a]) { F0 = 0; F1 = 0; F2 = 0; }
         g.f[4 * a] = F0; g.f[4 * a + 1] = F1; g.f[4 * a + 2] = F2;
         if constexpr (MODE == 1) {
-            const R x0 = F0 * g.dinv[4 * a], x1 = F1 * g.dinv[4 * a + 1], x2 = F2 * g.dinv[4 * a + 2];
+            const float4 di = reinterpret_cast<const float4 *>(g.dinv)[a];
+            const R x0 = F0 * di.x, x1 = F1 * di.y, x2 = F2 * di.z;
             g.x[4 * a] = x0;
             g.x[4 * a + 1] = x1;
             g.x[4 * a + 2] = x2;
