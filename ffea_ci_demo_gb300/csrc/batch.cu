@@ -62,7 +62,6 @@ struct ffea_gpu_batch {
     unsigned *src;
     double *drag = nullptr;
     float *val, *dinv, *diag;
-    double *f;
     float *x, *r, *q, *pbuf0, *pbuf1;
     float4 *zbuf = nullptr;
     float4 *dpos;
@@ -226,7 +225,6 @@ int ffea_gpu_batch::init() {
     CK(mem.alloc(&val, 9 * (size_t)h.nslots));
     CK(mem.alloc(&dinv, 4 * (size_t)N));
     CK(mem.alloc(&diag, 4 * (size_t)N));
-    CK(mem.alloc(&f, 4 * (size_t)N));
     CK(mem.alloc(&x, 4 * (size_t)N));
     CK(mem.alloc(&r, 4 * (size_t)N));
     CK(mem.alloc(&q, 4 * (size_t)N));
@@ -453,7 +451,7 @@ int ffea_gpu_batch::launch_gather() {
     ga.parts = me.parts; ga.part_ptr = me.part_ptr;
     ga.drag = nullptr;
     ga.vx = vx; ga.vy = vy; ga.vz = vz;
-    ga.dinv = dinv; ga.f = f; ga.x = x; ga.r = r;
+    ga.dinv = dinv; ga.x = x; ga.r = r;  // no FP64 copy of the force: the batch CG starts from r
     ga.partials = nullptr; ga.stride = 0; ga.st = st; ga.gb = nullptr;
     ga.dpos = dpos; ga.px = px; ga.py = py; ga.pz = pz; ga.diag = diag;
     NodeForces &sn = ga.sn;

@@ -168,6 +168,7 @@ struct BlobImpl final : ffea_gpu_blob {
     double *drag = nullptr;
     R *val, *dinv;
     double *f;
+    float *f32 = nullptr;  // mixed path: the step's assembled force, as the gather forms it (FP32)
     R *x, *r, *q, *pbuf0, *pbuf1;
     R *diag = nullptr;       // mixed path: diagonal of V
     double *partials, *init_partials;
@@ -387,6 +388,7 @@ struct BlobImpl final : ffea_gpu_blob {
         }
         CK(mem.upload(&dinv, dv));
         CK(mem.alloc(&f, 4 * (size_t)N));
+        if (std::is_same<R, float>::value) CK(mem.alloc(&f32, 4 * (size_t)N));
         CK(mem.alloc(&x, 4 * (size_t)N));
         CK(mem.alloc(&r, 4 * (size_t)N));
         CK(mem.alloc(&pbuf0, 4 * (size_t)N));
@@ -659,7 +661,8 @@ struct BlobImpl final : ffea_gpu_blob {
         ga.parts = me.parts; ga.part_ptr = me.part_ptr;
         ga.drag = (!nomass && p.calc_stokes == 1) ? drag : nullptr;
         ga.vx = vx; ga.vy = vy; ga.vz = vz;
-        ga.dinv = dinv; ga.f = f; ga.x = x; ga.r = r;
+        ga.dinv = dinv; ga.x = x; ga.r = r;
+        if (f32) ga.f32 = f32; else ga.f = f;
         ga.partials = init_partials; ga.stride = gather_blocks; ga.st = st; ga.gb = gb;
         ga.dpos = dpos; ga.px = px; ga.py = py; ga.pz = pz; ga.diag = diag;
         ga.xc[0] = xc[0]; ga.xc[1] = xc[1]; ga.xc[2] = xc[2];
@@ -941,8 +944,15 @@ struct BlobImpl final : ffea_gpu_blob {
     int get_rhs(double *rhs) override {
         const int N = h.N;
         std::vector<double> hf(4 * (size_t)N);
-        CK(cudaMemcpyAsync(hf.data(), f, hf.size() * sizeof(double), cudaMemcpyDeviceToHost, stream));
-        CK(cudaStreamSynchronize(stream));
+        if (f32) {
+            std::vector<float> h32(4 * (size_t)N);
+            CK(cudaMemcpyAsync(h32.data(), f32, h32.size() * sizeof(float), cudaMemcpyDeviceToHost, stream));
+            CK(cudaStreamSynchronize(stream));
+            for (size_t i = 0; i < h32.size(); ++i) hf[i] = h32[i];
+        } else {
+            CK(cudaMemcpyAsync(hf.data(), f, hf.size() * sizeof(double), cudaMemcpyDeviceToHost, stream));
+            CK(cudaStreamSynchronize(stream));
+        }
         for (int i = 0; i < 3 * h.n_all; ++i) rhs[i] = 0.0;
         for (int k = 0; k < N; ++k)
             for (int c = 0; c < 3; ++c) rhs[3 * (size_t)h.node_of[k] + c] = hf[4 * (size_t)k + c];

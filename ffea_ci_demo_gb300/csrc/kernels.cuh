@@ -611,7 +611,8 @@ struct GatherArgs {
     const double *drag;   // inertial Stokes drag (force -= v * drag) or null
     const double *vx, *vy, *vz;
     const R *dinv;        // Jacobi preconditioner (CG) or inverse lumped mass (mode 1)
-    double *f;            // 4*N assembled force (solver input)
+    double *f;            // 4*N assembled force (solver input; the mixed gather: FP64 copy, or null)
+    float *f32;           // mixed gather: the assembled force in FP32 in place of f (4*N), or null
     R *x, *r;
     double *partials;     // [0]: f.f, [stride]: r.z per block (mixed path: moments, float2 pairs)
     int stride;

@@ -107,7 +107,11 @@ __global__ void __launch_bounds__(256) gather_mixed_kernel(GatherArgs<R> g) {
             F0 = F[0]; F1 = F[1]; F2 = F[2];
         }
         if (g.pinned[a]) { F0 = 0; F1 = 0; F2 = 0; }
-        g.f[4 * a] = F0; g.f[4 * a + 1] = F1; g.f[4 * a + 2] = F2;
+        if (g.f32) {
+            g.f32[4 * a] = F0; g.f32[4 * a + 1] = F1; g.f32[4 * a + 2] = F2;
+        } else if (g.f) {
+            g.f[4 * a] = F0; g.f[4 * a + 1] = F1; g.f[4 * a + 2] = F2;
+        }
         if constexpr (MODE == 1) {
             const float4 di = reinterpret_cast<const float4 *>(g.dinv)[a];
             const R x0 = F0 * di.x, x1 = F1 * di.y, x2 = F2 * di.z;
@@ -116,8 +120,8 @@ __global__ void __launch_bounds__(256) gather_mixed_kernel(GatherArgs<R> g) {
             g.x[4 * a + 2] = x2;
             if (g.fuse_euler) {
                 // euler_integrate (src/Blob.cpp:3249-3279) as euler_kernel does it: v += a dt, p += v dt
+                if (!(isfinite(x0) && isfinite(x1) && isfinite(x2))) atomicExch(&g.st->nonfinite, 1);
                 const double a0 = (double)x0, a1 = (double)x1, a2 = (double)x2;
-                if (!(isfinite(a0) && isfinite(a1) && isfinite(a2))) atomicExch(&g.st->nonfinite, 1);
                 const double v0 = g.uvx[a] + a0 * g.dt, v1 = g.uvy[a] + a1 * g.dt, v2 = g.uvz[a] + a2 * g.dt;
                 g.uvx[a] = v0; g.uvy[a] = v1; g.uvz[a] = v2;
                 const double p0 = g.upx[a] + v0 * g.dt, p1 = g.upy[a] + v1 * g.dt, p2 = g.upz[a] + v2 * g.dt;
