@@ -90,9 +90,17 @@ struct ffea_gpu_batch {
     cudaGraphExec_t gexec = nullptr;
     int kernels_per_step = 0;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    // the step with event records around its CG launch (for ffea_gpu_batch_step_timed's CG time), captured on
+    // first use after each capture()
+    cudaGraphExec_t gexec_cg = nullptr;
+    cudaEvent_t evc0 = nullptr, evc1 = nullptr;
+    bool cg_events = false;  // record_step marks the CG launch
 
     ~ffea_gpu_batch() {
         if (gexec) cudaGraphExecDestroy(gexec);
+        if (gexec_cg) cudaGraphExecDestroy(gexec_cg);
+        if (evc0) cudaEventDestroy(evc0);
+        if (evc1) cudaEventDestroy(evc1);
         if (graph) cudaGraphDestroy(graph);
         if (ev0) cudaEventDestroy(ev0);
         if (ev1) cudaEventDestroy(ev1);
@@ -105,6 +113,7 @@ struct ffea_gpu_batch {
     int time_forces(int reps, double &ms);
     int record_step();
     int capture();
+    int capture_cg_timed();
     int launch_forces();
     int launch_gather();
     int launch_cg_only();
@@ -170,6 +179,8 @@ int ffea_gpu_batch::init() {
     CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
     CK(cudaEventCreate(&ev0));
     CK(cudaEventCreate(&ev1));
+    CK(cudaEventCreate(&evc0));
+    CK(cudaEventCreate(&evc1));
     const int N = h.N, T = h.T;
     for (int b = 0; b < nblobs; ++b) {
         max_rows = std::max(max_rows, row_off[b + 1] - row_off[b]);
@@ -393,8 +404,11 @@ int ffea_gpu_batch::record_step() {
     CK(BatchLaunch::schedule(desc, blob_iters, nblobs, ncta, cta_blob, st, stream));
     int rc = launch_forces();
     if (!rc) rc = launch_gather();
-    if (!rc) rc = launch_cg_only();
     if (rc) return rc;
+    if (cg_events) CK(cudaEventRecordWithFlags(evc0, stream, cudaEventRecordExternal));
+    rc = launch_cg_only();
+    if (rc) return rc;
+    if (cg_events) CK(cudaEventRecordWithFlags(evc1, stream, cudaEventRecordExternal));
     EulerArgs<float> eu{};
     eu.N = h.N; eu.nomass = 1; eu.dt = p.dt; eu.x = x;
     eu.px = px; eu.py = py; eu.pz = pz; eu.vx = vx; eu.vy = vy; eu.vz = vz;
@@ -510,6 +524,7 @@ int ffea_gpu_batch::launch_cg_only() {
 }
 
 int ffea_gpu_batch::capture() {
+    if (gexec_cg) { cudaGraphExecDestroy(gexec_cg); gexec_cg = nullptr; }
     if (gexec) { cudaGraphExecDestroy(gexec); gexec = nullptr; }
     if (graph) { cudaGraphDestroy(graph); graph = nullptr; }
     const long long l0 = launch_count();
@@ -526,6 +541,29 @@ int ffea_gpu_batch::capture() {
     kernels_per_step = (int)(launch_count() - l0);
     count_launch(-kernels_per_step);  // counted again on every replay
     CK(cudaGraphInstantiate(&gexec, graph, 0));
+    return FFEA_GPU_OK;
+}
+
+// the same step with event record nodes around its CG launch
+int ffea_gpu_batch::capture_cg_timed() {
+    CK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+    const long long l0 = launch_count();
+    cg_events = true;
+    const int rc = record_step();
+    cg_events = false;
+    count_launch((int)(l0 - launch_count()));
+    cudaGraph_t g = nullptr;
+    const cudaError_t e = cudaStreamEndCapture(stream, &g);
+    if (rc || e != cudaSuccess) {
+        if (g) cudaGraphDestroy(g);
+        return rc ? rc : cuda_fail(e, "cudaStreamEndCapture");
+    }
+    const cudaError_t ei = cudaGraphInstantiate(&gexec_cg, g, 0);
+    cudaGraphDestroy(g);
+    if (ei != cudaSuccess) {
+        gexec_cg = nullptr;
+        return cuda_fail(ei, "cudaGraphInstantiate");
+    }
     return FFEA_GPU_OK;
 }
 
@@ -692,10 +730,13 @@ int ffea_gpu_batch_step(ffea_gpu_batch *bt, int nsteps, int *steps_done) {
 }
 
 int ffea_gpu_batch_step_timed(ffea_gpu_batch *bt, int nsteps, long long flush_bytes, int *steps_done,
-                              double *step_ms) {
+                              double *step_ms, double *cg_ms) {
     if (!bt || nsteps < 0 || flush_bytes < 0) return FFEA_GPU_EINPUT;
     int rc = bt->reset_flags();
     if (rc) return rc;
+    if (cg_ms && !bt->gexec_cg && (rc = bt->capture_cg_timed())) return rc;
+    cudaGraphExec_t ge = cg_ms ? bt->gexec_cg : bt->gexec;
+    double tcg = 0.0;
     void *scratch = nullptr;
     if (flush_bytes > 0) CK(cudaMalloc(&scratch, (size_t)flush_bytes));
     double tot = 0.0;
@@ -703,11 +744,13 @@ int ffea_gpu_batch_step_timed(ffea_gpu_batch *bt, int nsteps, long long flush_by
         cudaError_t e = cudaSuccess;
         if (scratch) e = cudaMemsetAsync(scratch, i & 0xff, (size_t)flush_bytes, bt->stream);
         if (e == cudaSuccess) e = cudaEventRecord(bt->ev0, bt->stream);
-        if (e == cudaSuccess) e = cudaGraphLaunch(bt->gexec, bt->stream);
+        if (e == cudaSuccess) e = cudaGraphLaunch(ge, bt->stream);
         if (e == cudaSuccess) e = cudaEventRecord(bt->ev1, bt->stream);
         if (e == cudaSuccess) e = cudaEventSynchronize(bt->ev1);
-        float ms = 0.f;
+        float ms = 0.f, mc = 0.f;
         if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, bt->ev0, bt->ev1);
+        if (e == cudaSuccess && cg_ms) e = cudaEventElapsedTime(&mc, bt->evc0, bt->evc1);
+        tcg += mc;
         if (e != cudaSuccess) {
             rc = cuda_fail(e, "timed batch step");
             break;
@@ -722,6 +765,7 @@ int ffea_gpu_batch_step_timed(ffea_gpu_batch *bt, int nsteps, long long flush_by
     if (rc) return rc;
     if (steps_done) *steps_done = s.steps_done;
     if (step_ms) *step_ms = tot;
+    if (cg_ms) *cg_ms = tcg;
     return ffea_gpu_batch::status_code(s);
 }
 

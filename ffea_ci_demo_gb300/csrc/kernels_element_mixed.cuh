@@ -92,6 +92,11 @@ __device__ __forceinline__ void stage_lane_jumps(const MrgJump *lane_jump, uint3
     for (int i = tid; i < 32 * 18; i += nt) cp_async4(s_jump + EM_JUMP_WORDS * (i / 18) + i % 18, src + i);
 }
 
+// the elements' forces in shared memory, EM_F_STRIDE floats apart: 13 is coprime to the 32 banks, so a warp's
+// stores of its 32 elements' k-th force component hit 32 different banks
+constexpr int EM_F_STRIDE = 13;
+static_assert(EM_F_STRIDE >= 12 && EM_F_STRIDE <= 16, "the forces overlay the 4 NT staged float4 displacements");
+
 // per-element inputs staged by element_mixed_kernel, EM_EL_ROWS rows of one float per element of the block:
 // J0^-1 (9, row-major), vol0, G, E, A, B
 constexpr int EM_EL_ROWS = 14;
@@ -418,17 +423,18 @@ __global__ void __launch_bounds__(NT, 1024 / NT) element_mixed_kernel(ElemArgs<f
     __syncthreads();  // every element has read its nodes: the staging area now takes the forces
     float *s_f = reinterpret_cast<float *>(s_u);
 #pragma unroll
-    for (int k = 0; k < 12; ++k) s_f[tid * 12 + k] = f[k];
+    for (int k = 0; k < 12; ++k) s_f[tid * EM_F_STRIDE + k] = f[k];
     __syncthreads();
     // each vertex of the block: its elements' forces in element order, from the block's incidence list
-    // (code 4 el + slot, so the force sits at s_f[3 code])
+    // (code 4 el + slot: the force sits at s_f[EM_F_STRIDE el + 3 slot])
     const int ne = min(NT, g.T - blk * NT);
     const unsigned short *il = s_il;
     for (int i = tid; i < nn; i += NT) {
         const int m0 = g.inc_start[n0 + i], m1 = (i + 1 < nn) ? (int)g.inc_start[n0 + i + 1] : 4 * ne;
         float a0 = 0.f, a1 = 0.f, a2 = 0.f;
         for (int m = m0; m < m1; ++m) {
-            const float *c = s_f + 3 * (int)il[m];
+            const int code = il[m];
+            const float *c = s_f + EM_F_STRIDE * (code >> 2) + 3 * (code & 3);
             a0 += c[0];
             a1 += c[1];
             a2 += c[2];

@@ -117,7 +117,8 @@ def load():
         "ffea_gpu_batch_sizes": (C.c_int, [vp, ip, ip, ip, C.POINTER(C.c_longlong)]),
         "ffea_gpu_batch_blob_sizes": (C.c_int, [vp, C.c_int, ip, ip, ip]),
         "ffea_gpu_batch_step": (C.c_int, [vp, C.c_int, ip]),
-        "ffea_gpu_batch_step_timed": (C.c_int, [vp, C.c_int, C.c_longlong, ip, C.POINTER(C.c_double)]),
+        "ffea_gpu_batch_step_timed": (C.c_int, [vp, C.c_int, C.c_longlong, ip, C.POINTER(C.c_double),
+                                      C.POINTER(C.c_double)]),
         "ffea_gpu_batch_get_state": (C.c_int, [vp, C.c_int, dp, dp]),
         "ffea_gpu_batch_get_states": (C.c_int, [vp, dp, dp]),
         "ffea_gpu_batch_set_states": (C.c_int, [vp, dp, dp]),
@@ -534,11 +535,14 @@ class Batch:
         _check(rc, f"batch_step (after {done.value} completed steps)")
         return done.value
 
-    def update_timed(self, nsteps: int, flush_bytes: int = 0) -> dict:
-        done, ms = C.c_int(0), C.c_double(0)
-        rc = self._lib.ffea_gpu_batch_step_timed(self._h, int(nsteps), int(flush_bytes), C.byref(done), C.byref(ms))
+    def update_timed(self, nsteps: int, flush_bytes: int = 0, cg: bool = False) -> dict:
+        """update() timed by CUDA events around each step; cg: also the steps' CG launches (events inside the
+        step), in "cg_ms"."""
+        done, ms, mc = C.c_int(0), C.c_double(0), C.c_double(0)
+        rc = self._lib.ffea_gpu_batch_step_timed(self._h, int(nsteps), int(flush_bytes), C.byref(done), C.byref(ms),
+                                                 C.byref(mc) if cg else None)
         _check(rc, f"batch_step_timed (after {done.value} completed steps)")
-        return {"steps": done.value, "ms": ms.value}
+        return {"steps": done.value, "ms": ms.value, "cg_ms": mc.value if cg else None}
 
     def state(self, blob: int):
         pos = np.empty((self.n_nodes[blob], 3))

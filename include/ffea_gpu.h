@@ -315,9 +315,10 @@ int ffea_gpu_batch_blob_sizes(ffea_gpu_batch *batch, int blob, int *num_nodes, i
 /* nsteps steps of every blob; stops at the first failing step (*steps_done gets the completed steps). */
 int ffea_gpu_batch_step(ffea_gpu_batch *batch, int nsteps, int *steps_done);
 /* Same, each step timed by CUDA events around its graph launch, with flush_bytes of scratch written
- * before every step outside the timed window; *step_ms = summed device time. */
+ * before every step outside the timed window; *step_ms = summed device time. cg_ms (may be NULL): the
+ * summed time of the steps' CG launches (events recorded around it inside the step). */
 int ffea_gpu_batch_step_timed(ffea_gpu_batch *batch, int nsteps, long long flush_bytes, int *steps_done,
-                              double *step_ms);
+                              double *step_ms, double *cg_ms);
 
 /* State of one blob in its own node order (as ffea_gpu_blob_get_state / set_state). */
 int ffea_gpu_batch_get_state(ffea_gpu_batch *batch, int blob, double *pos, double *vel);
