@@ -216,6 +216,23 @@ struct BlobImpl final : ffea_gpu_blob {
     // FP32 node state was written by that step's gather)
     cudaGraphExec_t gexec[4] = {nullptr, nullptr, nullptr, nullptr};
     bool prep_cont = false;  // the step being captured is such a continuation
+    // the mixed mass-lumped step with noise: the next step's chunk jumps A^(224 c + step draws), so that its gather
+    // also forms the next step's chunk states and a continuation step launches no node_prep_kernel
+    MrgJump *next_chunk_jump = nullptr;
+    int upload_next_chunk_jumps(unsigned long long step_draws) {
+        if (!next_chunk_jump) return FFEA_GPU_OK;
+        const int nch = (h.T + 31) / 32;
+        std::vector<MrgJump> v(nch);
+        const Mat3 A224a = mat_pow(MRG_A1, 224, MRG_M1), A224b = mat_pow(MRG_A2, 224, MRG_M2);
+        Mat3 ca = mat_pow(MRG_A1, step_draws, MRG_M1), cb = mat_pow(MRG_A2, step_draws, MRG_M2);
+        for (int c = 0; c < nch; ++c) {
+            v[c] = to_jump(ca, cb);
+            ca = mat_mul(A224a, ca, MRG_M1);
+            cb = mat_mul(A224b, cb, MRG_M2);
+        }
+        CK(cudaMemcpy(next_chunk_jump, v.data(), v.size() * sizeof(MrgJump), cudaMemcpyHostToDevice));
+        return FFEA_GPU_OK;
+    }
     long long graph_launches[4] = {0, 0, 0, 0};
     double *staging = nullptr;  // pinned host buffer, 3*N doubles, for state copies
     // node state in the reference's layout on the device: n_all x 3 doubles, the vertex row of each vertex
@@ -538,6 +555,7 @@ struct BlobImpl final : ffea_gpu_blob {
             int lrc0 = upload_linearise(mem);
             if (lrc0) return lrc0;
         }
+        if (fused_prep() && p.calc_noise == 1) CK(mem.alloc(&next_chunk_jump, (size_t)nchunks));
         int lrc = set_rng_layout(element_draws() + stokes_draws(), element_draws());
         if (lrc) return lrc;
         std::vector<uint32_t> rs(rng_host, rng_host + 6);
@@ -583,7 +601,10 @@ struct BlobImpl final : ffea_gpu_blob {
     // positions) needs only the geometry the assembly reads
     int launch_elements(int recompute) {
         if constexpr (std::is_same<R, float>::value) {
-            CK(me.prep(px, py, pz, vx, vy, vz, rng_state, chunk_jump, stream, prep_cont && !recompute));
+            // a continuation step of the fused mass-lumped path finds its node state and chunk states ready
+            const bool cont = prep_cont && !recompute;
+            if (!cont || (me.nchunks > 0 && !next_chunk_jump))
+                CK(me.prep(px, py, pz, vx, vy, vz, rng_state, chunk_jump, stream, cont));
             ElemArgs<float> ea = elem_args(recompute);
             me.fill(ea);
             ea.ef = nullptr;
@@ -698,7 +719,15 @@ struct BlobImpl final : ffea_gpu_blob {
             CK(Launch<R>::mid_force(ga.sn, M, mid_f, st, stream));
             ga.sn.mid_f = mid_f;
         }
-        CK(Launch<R>::gather(ga, gather_blocks, stream));
+        int gblocks = gather_blocks;
+        if (ga.nu && next_chunk_jump) {
+            ga.ncj = next_chunk_jump;
+            ga.nrng = rng_state;
+            ga.nchunk_state = me.chunk_state;
+            ga.nnchunks = me.nchunks;
+            gblocks = std::max(gblocks, (me.nchunks + Launch<R>::gather_threads() - 1) / Launch<R>::gather_threads());
+        }
+        CK(Launch<R>::gather(ga, gblocks, stream));
         if ((rc = mark(3))) return rc;
         if (p.solver != FFEA_GPU_MASSLUMPED && (rc = launch_cg(init_partials, gather_blocks))) return rc;
         if ((rc = mark(4))) return rc;
@@ -1095,6 +1124,8 @@ struct BlobImpl final : ffea_gpu_blob {
         invalidate_graphs();
         std::vector<MrgJump> sj(1, jump_pow(step_draws));
         CK(cudaMemcpy(step_jump, sj.data(), sizeof(MrgJump), cudaMemcpyHostToDevice));
+        int nrc = upload_next_chunk_jumps(step_draws);
+        if (nrc) return nrc;
         if (sn_chunk_jump) {
             const int nch = (h.n_all + 31) / 32;
             std::vector<MrgJump> ncj(nch);

@@ -635,6 +635,12 @@ struct GatherArgs {
     // (node_prep_kernel's arithmetic), or null
     float4 *nu, *nvf;
     const double *nxr;
+    // with fuse_euler and noise: the next step's stream state at each 32-element chunk, ncj[c] (the chunk's jump
+    // composed with the step's) applied to the step's state nrng (node_prep_kernel's other output), or null
+    const MrgJump *ncj;
+    const uint32_t *nrng;
+    uint32_t *nchunk_state;
+    int nnchunks;
 };
 
 template <class R>

@@ -57,6 +57,16 @@ __global__ void __launch_bounds__(256) gather_mixed_kernel(GatherArgs<R> g) {
     __shared__ float2 smem[MIXED_GATHER_NP * 32];
     const int a = blockIdx.x * blockDim.x + threadIdx.x;
     if (a == 0 && g.gb) g.gb->count = 0u;
+    if constexpr (MODE == 1) {
+        if (g.nchunk_state && a < g.nnchunks) {
+            uint32_t s6[6], o6[6];
+#pragma unroll
+            for (int k = 0; k < 6; ++k) s6[k] = g.nrng[k];
+            mrg_apply(g.ncj[a], s6, o6);
+#pragma unroll
+            for (int k = 0; k < 6; ++k) g.nchunk_state[6 * (size_t)a + k] = o6[k];
+        }
+    }
     df32 acc[MIXED_GATHER_NP];
 #pragma unroll
     for (int i = 0; i < MIXED_GATHER_NP; ++i) acc[i] = df32{0.f, 0.f};
