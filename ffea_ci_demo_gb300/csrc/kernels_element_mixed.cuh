@@ -299,9 +299,11 @@ __device__ __forceinline__ bool element_mixed_eval(const ElemArgs<float> &g, int
     }
     // add_fluctuating_stress :412-431 (draws b, d0, d1, d2, o01, o02, o12)
     if (g.calc_noise == 1) {
-        const float c = sqrtf((24.f * g.kT) / (vol * g.dt));
+        // sqrt(24 kT / (vol dt)) as sqrt(24 kT / dt) / sqrt(vol), and sqrt(2A) as sqrt(2) sqrt(A): the noise
+        // amplitude to a few FP32 ulp with one correctly rounded square root fewer and no division
+        const float c = sqrtf((24.f * g.kT) / g.dt) * rsqrtf(vol);
         const float bf = sqrtf(B) * rn[0];
-        const float a2 = sqrtf(2.f * A), a1 = sqrtf(A);
+        const float a1 = sqrtf(A), a2 = 1.41421356f * a1;
         S[0][0] += c * (a2 * rn[1] + bf);
         S[1][1] += c * (a2 * rn[2] + bf);
         S[2][2] += c * (a2 * rn[3] + bf);
