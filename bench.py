@@ -370,14 +370,24 @@ def batch_bytes_per_iteration(cells: int, p: int) -> tuple[float, float]:
     return float(model), float(fmt)
 
 
-def run_batch(args, ws) -> dict:
-    """Configuration 2: the replica ensemble, all blobs advanced by one graph-captured step."""
+def run_batch(args, ws, rank=0, ranks=None) -> dict:
+    """Configuration 2: the replica ensemble, all blobs advanced by one graph-captured step. With ws ranks, the
+    ensemble is split over them by element count (ffea_ci_demo_gb300.shard) and each rank steps a batch of its own
+    blobs; the time is the slowest rank's and the throughput counts every rank's nodes (strong scaling: the
+    ensemble is fixed)."""
     from ffea_ci_demo_gb300 import build, lib
     from ffea_ci_demo_gb300.mesh import ensemble, ensemble_cells
+    from ffea_ci_demo_gb300.shard import partition_by_elements
 
     build.build()
-    cells = [int(n) for n in ensemble_cells(args.blobs)]
-    meshes = ensemble(args.blobs)
+    cells_all = [int(n) for n in ensemble_cells(args.blobs)]
+    meshes_all = ensemble(args.blobs)
+    mine = partition_by_elements([m.n_elem for m in meshes_all], ws)[rank] if ws > 1 else list(range(args.blobs))
+    meshes = [meshes_all[b] for b in mine]
+    cells = [cells_all[b] for b in mine]
+    nodes_all = sum(m.n_linear for m in meshes_all)
+    barrier = ranks.barrier if ranks else (lambda: None)
+    max_over = ranks.max if ranks else (lambda x: x)
     bt = lib.Batch(meshes, **{k: v for k, v in PHYS.items() if k != "solver"})
     sz = bt.sizes()
     bt.update(args.warmup)
@@ -390,8 +400,11 @@ def run_batch(args, ws) -> dict:
     tot0 = bt.cg_iterations()[1]
     l0 = lib.launch_count()
     k = args.steps
+    barrier()
     with Clocks(os.environ.get("CUDA_VISIBLE_DEVICES", "0")) as clk:
         t = bt.update_timed(k, FLUSH_BYTES, cg=True)
+    barrier()
+    t_all = max_over(t["ms"])
     launches = lib.launch_count() - l0
     last, tot1 = bt.cg_iterations()
     iters_per_step = (tot1 - tot0) / k
@@ -407,8 +420,10 @@ def run_batch(args, ws) -> dict:
     peak, peak_kind = measured_peak()
     out = {"workload": f"ensemble of {args.blobs} Kuhn cubes, cells per side log-uniform in [8,32] (seeded), "
                        f"G ~ U[1e8,1e9] Pa, K = 3.9 G; NoMassCG eps=1e-10, dt=1e-12 s, kT=4.11e-21 J, mixed",
-           "blobs": sz["blobs"], "nodes": sz["nodes"], "tets": sz["elements"], "matrix_blocks": sz["blocks"],
-           "value": ws * sz["nodes"] * k / (t["ms"] / 1e3), "unit": "node-steps/s", "ms_per_step": ms, "steps": k,
+           "blobs": len(meshes_all), "nodes": nodes_all, "tets": sum(m.n_elem for m in meshes_all),
+           "matrix_blocks_this_rank": sz["blocks"],
+           "value": nodes_all * k / (t_all / 1e3), "unit": "node-steps/s", "ms_per_step": t_all / k, "steps": k,
+           "blobs_this_rank": len(mine), "nodes_this_rank": sz["nodes"],
            "warmup": args.warmup, "cg_iters_per_step_all_blobs": iters_per_step,
            "cg_iters_per_blob": {"min": int(last.min()), "mean": float(last.mean()), "max": int(last.max())},
            "launch_config": cfg, "tuned_best_solve_ms": tuned_ms, "gpu_launches": launches,
@@ -428,7 +443,10 @@ def run_batch(args, ws) -> dict:
                         if profiled("cg_batch_kernel_ensemble64", "dram_gbs") else None,
                         "bytes_per_step_format_cg": fmt, "bytes_per_step_model_cg": model,
                         "model_equiv_gbs": model / (ms / 1e3) / 1e9}}
-    if not args.no_fp64_sample:
+    if ws > 1:
+        out["sharding"] = {"ranks": ws, "split": "element counts balanced, longest first (ffea_ci_demo_gb300.shard)",
+                           "collective": "none on the data path (gloo barrier and max of the timing only)"}
+    if not args.no_fp64_sample and ws == 1:
         # plain FP64 GPU path, one blob at a time (the reference's order): a stratified sample of the
         # blobs sorted by size, scaled to the whole ensemble
         order = sorted(range(args.blobs), key=lambda b: cells[b])
@@ -444,7 +462,7 @@ def run_batch(args, ws) -> dict:
                                     "sample_blobs": len(pick), "method": "FP64 single-blob path, blob by blob, "
                                     "stratified sample scaled to all blobs"}
         out["speedup_vs_fp64_path"] = out["value"] / out["fp64_path_sampled"]["value"]
-    if not args.no_e2e:
+    if not args.no_e2e and ws == 1:
         # end to end through the C ABI: every blob's host positions (pinned host memory) in, one step, every
         # blob's positions out
         pos, mem_kind = host_array((sum(m.n_nodes for m in meshes), 3))
@@ -918,21 +936,22 @@ def main():
             print(json.dumps({"scale": run_scale(args)}), flush=True)
         return
     if args.workload == "batch":
-        if ws > 1:
-            if rank == 0:
-                print(json.dumps({"metric": "node-steps/s", "unavailable": "the batch workload runs on one GPU"}))
-            return
         args.steps = args.batch_steps
-        b = run_batch(args, ws)
-        if args.ensemble_long_steps > 0:
+        ranks = Replicas(ws) if ws > 1 else None
+        b = run_batch(args, ws, rank, ranks)
+        if ranks:
+            ranks.close()
+        if rank != 0:
+            return
+        if args.ensemble_long_steps > 0 and ws == 1:
             b["long_run"] = run_batch_long(args)
         line = {"metric": "node-steps/s", "value": b["value"], "unit": "node-steps/s", "n_gpus": ws,
                 "steps": b["steps"], "warmup": args.warmup, "ms_per_step": b["ms_per_step"],
-                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
-                "data": "synthetic (seeded Kuhn-cube ensemble)",
+                "higher_is_better": True, "scaling": "strong" if ws > 1 else "weak", "vs_baseline": None,
+                "dtype": "f32+f64", "data": "synthetic (seeded Kuhn-cube ensemble)",
                 "config": {"workload": b["workload"], "blobs": b["blobs"], "nodes": b["nodes"], "tets": b["tets"],
                            "l2": "flushed before every timed step (256 MiB scratch write)",
-                           "parallelism": "replicas x1"},
+                           "parallelism": f"ensemble sharded x{ws}" if ws > 1 else "replicas x1"},
                 "clocks": b["clocks"], "e2e": b.get("e2e"), "gpu_launches": b["gpu_launches"],
                 "roofline": b["roofline"], "batched": b}
         print(json.dumps(line), flush=True)
