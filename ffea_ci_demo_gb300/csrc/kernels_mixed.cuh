@@ -922,14 +922,16 @@ __host__ __device__ constexpr size_t sr_cache_bytes(int kc, int S) {
 }
 
 // The Chebyshev preconditioner: degrees 2 and 4 (even degrees keep it positive definite whatever the estimate of
-// lambda_max); the interval is [lambda_max / CHEB_RATIO, lambda_max]; the estimate comes from the Lanczos
+// lambda_max); the interval is [lambda_max / cheb_ratio(d), lambda_max]; the estimate comes from the Lanczos
 // matrix of the first CHEB_REC iterations of a Jacobi-preconditioned solve. State (CHEB_STATE doubles):
 // [0] the estimate (0: not yet known, -1: Jacobi kept), [1, 1 + CHEB_REC) step lengths, then as many direction
 // coefficients, then [CHEB_KJ] the iterations of the Jacobi solve while the first polynomial solve (the trial)
 // is pending.
 constexpr int CHEB_MAX = 4;
 constexpr int CHEB_REC = 64;
-constexpr double CHEB_RATIO = 30.0;
+// the interval's width: the degree-4 polynomial gains from a wider one (40^3 Kuhn cube, CG per step: ratio 30
+// 4.24 ms, 60 4.10, 120 4.04, 250 4.06), the degree-2 one hardly (30 4.17, 60 4.14, 120 4.17 ms)
+__host__ __device__ constexpr double cheb_ratio(int degree) { return degree > 2 ? 120.0 : 30.0; }
 constexpr double CHEB_MARGIN = 1.05;
 constexpr int CHEB_KJ = 1 + 2 * CHEB_REC;
 constexpr int CHEB_STATE = CHEB_KJ + 1;
@@ -1027,7 +1029,7 @@ __global__ void __launch_bounds__(1024, 1) cg_mixed_sr_kernel(const __grid_const
     const bool cheb = lmax > 0.0;              // Chebyshev this solve
     const bool rec = poly > 0 && lmax == 0.0;  // Jacobi this solve, recording the Lanczos coefficients
     if (cheb && threadIdx.x == 0) {
-        const double b = lmax, a = lmax / CHEB_RATIO, theta = 0.5 * (b + a), delta = 0.5 * (b - a);
+        const double b = lmax, a = lmax / cheb_ratio(poly), theta = 0.5 * (b + a), delta = 0.5 * (b - a);
         const double sigma = theta / delta;
         double rho = 1.0 / sigma;
         for (int j = 0; j < poly; ++j) {

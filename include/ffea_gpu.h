@@ -73,7 +73,7 @@ typedef struct ffea_gpu_params {
      * (only where the matrix is read from), so it exists for measurements of the cache's effect. */
     int cg_smem_blocks;
 } ffea_gpu_params;
-#define FFEA_GPU_CG_POLY_DEFAULT 2
+#define FFEA_GPU_CG_POLY_DEFAULT 4
 
 /* SimulationParams::SimulationParams() defaults for the hot-path fields
  * (src/SimulationParams.cpp:26-60); solver CG_nomass, precision FP64. */

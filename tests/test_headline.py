@@ -9,7 +9,7 @@ the benchmark times, with CG_nomass at epsilon 1e-10, dt = 1e-12 s, run at kT = 
   right-hand side is bit-exact; after 3 steps the positions agree within 1e-8 of the displacement (both CGs
   stop at |r|^2/|f|^2 < 1e-20 and sum in different orders).
 * Mixed path with the arithmetic the benchmark times (single-reduction CG kernel, Chebyshev preconditioner
-  of degree 2 after the first two solves) against the FP64 GPU path after 1000 steps: the stated bound,
+  of the default degree after the first two solves) against the FP64 GPU path after 1000 steps: the stated bound,
   max |x_mixed - x_fp64| <= 1e-5 * max |x_fp64 - x_0|.
 
 Reference: NoMassCGSolver::solve (src/NoMassCGSolver.cpp:156-188), Blob::update_internal_forces and
@@ -68,9 +68,9 @@ def test_headline_mixed_1000_steps_within_bound(gpu, headline):
         b.set_state(pos=x0)
         b.update(2)
         if prec == "mixed":
-            # the benchmark's arithmetic: single-reduction kernel with the degree-2 polynomial
+            # the benchmark's arithmetic: single-reduction kernel with the default polynomial
             assert b.cg_kernel() == "cg_mixed_sr_kernel"
-            assert b.cg_preconditioner()[0] == 2
+            assert b.cg_preconditioner()[0] == lib.CG_POLY_DEFAULT
         b.update(998)
         res[prec] = (b.pos(), b.cg_iterations()[1])
         b.close()

@@ -1,7 +1,8 @@
 """The mixed path's Chebyshev polynomial preconditioner, restated in numpy on the oracle's viscosity matrix (CPU).
 
 cg_mixed_sr_kernel preconditions the CG_nomass solve with M^-1 = P_d(D^-1 V) D^-1, where 1 - lambda P_d(lambda)
-is the Chebyshev polynomial of degree d + 1 on [lambda_max / 30, lambda_max] scaled to 1 at 0, applied as d steps
+is the Chebyshev polynomial of degree d + 1 on [lambda_max / r_d, lambda_max] (r_2 = 30, r_4 = 120) scaled to 1 at
+0, applied as d steps
 of the Chebyshev iteration for V z = r from z = 0. lambda_max comes from the Lanczos matrix of a Jacobi-PCG solve
 (step lengths alpha_i, direction coefficients beta_i). These tests check the algorithm itself on a Kuhn cube's
 matrix from the oracle (the reference's NoMass viscosity matrix, rigid modes shifted as the mixed path does):
@@ -14,7 +15,9 @@ import scipy.sparse as sp
 import pyoracle as po
 from gen_golden import case_mesh, sheared
 
-RATIO = 30.0
+def ratio(degree):
+    """The interval's width: the kernel's cheb_ratio."""
+    return 120.0 if degree > 2 else 30.0
 
 
 def shifted_system(n=8, seed=21):
@@ -46,7 +49,7 @@ def shifted_system(n=8, seed=21):
 def chebyshev(V, D, lmax, degree):
     """z = P_d(D^-1 V) D^-1 r by the kernel's recurrence: y0 = D^-1 r / theta, res = D^-1 r - D^-1 V y0, then
     dd = c1 dd + c2 res, z += dd, res -= D^-1 V dd."""
-    a, b = lmax / RATIO, lmax
+    a, b = lmax / ratio(degree), lmax
     theta, delta = (b + a) / 2, (b - a) / 2
     sigma = theta / delta
     rho = [1 / sigma]
@@ -130,7 +133,7 @@ def test_even_degrees_stay_positive_definite(system, scale):
         Mi = np.column_stack([M(e) for e in np.eye(V.shape[0])[:, :60].T])[:60]
         assert np.allclose(Mi, Mi.T, rtol=1e-9, atol=1e-12 * np.abs(Mi).max())
         # the preconditioner's eigenvalues are P_d(lambda) D^-1: P_d > 0 on the whole spectrum of D^-1 V
-        a, b = lmax / RATIO, lmax
+        a, b = lmax / ratio(degree), lmax
         x = (b + a - 2 * lam) / (b - a)
         T = np.polynomial.chebyshev.chebval(x, [0] * (degree + 1) + [1])
         T0 = np.polynomial.chebyshev.chebval((b + a) / (b - a), [0] * (degree + 1) + [1])
