@@ -864,11 +864,19 @@ int ffea_gpu_batch_load_ctforces(ffea_gpu_batch *bt, int blob, const char *ctf_f
         bt->ctf_models.resize(nb);
         for (int b = 0; b < nb; ++b) empty_ctforces(bt->nall_off[b + 1] - bt->nall_off[b], bt->ctf_models[b]);
     }
-    bt->ctf_models[blob] = std::move(cm);
+    std::swap(bt->ctf_models[blob], cm);  // cm now holds the blob's previous forces
     CtfModel all;
     concat_ctforces(bt->ctf_models, bt->nall_off, all);
     CK(cudaStreamSynchronize(bt->stream));
-    CK(bt->ctf.build(bt->h, all, bt->px, bt->py, bt->pz, bt->st));
+    const cudaError_t be = bt->ctf.build(bt->h, all, bt->px, bt->py, bt->pz, bt->st);
+    if (be != cudaSuccess) {
+        // keep the batch consistent: the previous forces back on the device, the step graph re-captured
+        std::swap(bt->ctf_models[blob], cm);
+        concat_ctforces(bt->ctf_models, bt->nall_off, all);
+        bt->ctf.build(bt->h, all, bt->px, bt->py, bt->pz, bt->st);
+        bt->capture();
+        return cuda_fail(be, "batch_load_ctforces");
+    }
     const int M = (int)bt->h.mid_nodes.size();
     if (bt->ctf.mid_force && !bt->mid_f && M > 0) CK(bt->mem.alloc(&bt->mid_f, 3 * (size_t)M));
     // midpoints that carry force need the linearisation replay (already there with Stokes noise)

@@ -30,9 +30,18 @@ struct CtfDevice {
         mid_force = any = false;
     }
 
-    // cm over h's reference numbering (h.n_all nodes); px..pz the device positions the per-step kernels read
+    // cm over h's reference numbering (h.n_all nodes); px..pz the device positions the per-step kernels read. On
+    // an error nothing is left half built: the device holds no constant forces.
     cudaError_t build(const host::HostModel &h, const host::CtfModel &cm, const double *px, const double *py,
                       const double *pz, const DevStatus *st) {
+        const cudaError_t e = build_arrays(h, cm, px, py, pz, st);
+        if (e != cudaSuccess) release();
+        return e;
+    }
+
+  private:
+    cudaError_t build_arrays(const host::HostModel &h, const host::CtfModel &cm, const double *px, const double *py,
+                             const double *pz, const DevStatus *st) {
         release();
         const int N = h.N, M = (int)h.mid_nodes.size(), n = h.n_all;
         std::vector<int> mid_id(n, -1);
@@ -169,6 +178,7 @@ struct CtfDevice {
         return cudaSuccess;
     }
 
+  public:
     void fill(NodeForces &sn) const {
         sn.node_ctf = node;
         sn.mid_ctf = mid;
