@@ -172,7 +172,12 @@ struct BlobImpl final : ffea_gpu_blob {
     R *x, *r, *q, *pbuf0, *pbuf1;
     R *diag = nullptr;       // mixed path: diagonal of V
     double *partials, *init_partials;
-    uint32_t *rng_state;
+    // the stream state. The fused mass-lumped step keeps two buffers: a step reads the current one and its gather
+    // writes the next state into the other (no closing kernel), so the current buffer alternates step by step
+    // (rng_cur, kept on the host; the step graphs are captured per buffer)
+    uint32_t *rng_bufs[2] = {nullptr, nullptr};
+    int rng_cur = 0;
+    uint32_t *rng_state() const { return rng_bufs[rng_cur]; }
     MrgJump *chunk_jump, *lane_jump, *step_jump;
     DevStatus *st;
     GridBarrier *gb;
@@ -214,7 +219,7 @@ struct BlobImpl final : ffea_gpu_blob {
     // constant forces, the stream layout) drops them when it changes (invalidate_graphs).
     // step graphs: [timed + 2 cont], cont = a step that follows a fused mass-lumped step of the same call (its
     // FP32 node state was written by that step's gather)
-    cudaGraphExec_t gexec[4] = {nullptr, nullptr, nullptr, nullptr};
+    cudaGraphExec_t gexec[8] = {};
     bool prep_cont = false;  // the step being captured is such a continuation
     // the mixed mass-lumped step with noise: the next step's chunk jumps A^(224 c + step draws), so that its gather
     // also forms the next step's chunk states and a continuation step launches no node_prep_kernel
@@ -233,7 +238,7 @@ struct BlobImpl final : ffea_gpu_blob {
         CK(cudaMemcpy(next_chunk_jump, v.data(), v.size() * sizeof(MrgJump), cudaMemcpyHostToDevice));
         return FFEA_GPU_OK;
     }
-    long long graph_launches[4] = {0, 0, 0, 0};
+    long long graph_launches[8] = {};
     double *staging = nullptr;  // pinned host buffer, 3*N doubles, for state copies
     // node state in the reference's layout on the device: n_all x 3 doubles, the vertex row of each vertex
     // node, and the source rows of every reference node (vertex (k, k), midpoint (a, b), else (-1, -1))
@@ -277,7 +282,7 @@ struct BlobImpl final : ffea_gpu_blob {
     // one step through its graph (captured from launch_step on first use); `cont`: the previous launch on the
     // stream was a step of the same call, so a fused step need not form the FP32 node state again
     int launch_step_graph(int timed, bool cont = false) {
-        const int gi = timed + ((cont && fused_prep()) ? 2 : 0);
+        const int gi = timed + ((cont && fused_prep()) ? 2 : 0) + 4 * rng_cur;
         if (!gexec[gi]) {
             record_phases = timed != 0;
             prep_cont = gi >= 2;
@@ -559,7 +564,8 @@ struct BlobImpl final : ffea_gpu_blob {
         int lrc = set_rng_layout(element_draws() + stokes_draws(), element_draws());
         if (lrc) return lrc;
         std::vector<uint32_t> rs(rng_host, rng_host + 6);
-        CK(mem.upload(&rng_state, rs));
+        CK(mem.upload(&rng_bufs[0], rs));
+        if (fused_prep()) CK(mem.alloc(&rng_bufs[1], 6));
         // a blob that the allocation-free solve accepts gets the static scratch placed now, and that solve's
         // kernels loaded (cg_kernel by the occupancy query above), so that its first solve allocates nothing
         if (!mixed && p.solver != FFEA_GPU_MASSLUMPED && N <= SOLVE_STATIC_MAX_NODES && cg_grid <= SOLVE_MAX_BLOCKS) {
@@ -588,7 +594,7 @@ struct BlobImpl final : ffea_gpu_blob {
         ea.last_det = last_det;
         ea.ef = ef;
         ea.geom = geom;
-        ea.rng_state = rng_state;
+        ea.rng_state = rng_state();
         ea.chunk_jump = chunk_jump;
         ea.lane_jump = lane_jump;
         ea.recompute = recompute;
@@ -604,7 +610,7 @@ struct BlobImpl final : ffea_gpu_blob {
             // a continuation step of the fused mass-lumped path finds its node state and chunk states ready
             const bool cont = prep_cont && !recompute;
             if (!cont || (me.nchunks > 0 && !next_chunk_jump))
-                CK(me.prep(px, py, pz, vx, vy, vz, rng_state, chunk_jump, stream, cont));
+                CK(me.prep(px, py, pz, vx, vy, vz, rng_state(), chunk_jump, stream, cont));
             ElemArgs<float> ea = elem_args(recompute);
             me.fill(ea);
             ea.ef = nullptr;
@@ -694,13 +700,17 @@ struct BlobImpl final : ffea_gpu_blob {
             ga.nu = me.u;
             ga.nvf = me.vf;
             ga.nxr = me.xr;
+            // the gather closes the step: the next stream state into the other buffer
+            ga.nrng = rng_state();
+            ga.fin_jump = step_jump;
+            ga.fin_next = rng_bufs[rng_cur ^ 1];
         }
         {
             NodeForces &sn = ga.sn;
             sn.noise = sn_chunk_jump != nullptr;
             sn.kT = p.kT;
             sn.dt = p.dt;
-            sn.rng_state = rng_state;
+            sn.rng_state = rng_state();
             sn.chunk_jump = sn_chunk_jump;
             sn.lane_jump = sn_lane_jump;
             sn.node_orig = sn_node_orig;
@@ -722,7 +732,7 @@ struct BlobImpl final : ffea_gpu_blob {
         int gblocks = gather_blocks;
         if (ga.nu && next_chunk_jump) {
             ga.ncj = next_chunk_jump;
-            ga.nrng = rng_state;
+            ga.nrng = rng_state();
             ga.nchunk_state = me.chunk_state;
             ga.nnchunks = me.nchunks;
             gblocks = std::max(gblocks, (me.nchunks + Launch<R>::gather_threads() - 1) / Launch<R>::gather_threads());
@@ -738,7 +748,7 @@ struct BlobImpl final : ffea_gpu_blob {
             eu.st = st;
             CK(Launch<R>::euler(eu, stream));
         }
-        CK(launch_finish_step(rng_state, step_jump, st, stream));
+        if (!ga.fin_next) CK(launch_finish_step(rng_state(), step_jump, st, stream));
         return mark(5);
     }
 
@@ -765,15 +775,35 @@ struct BlobImpl final : ffea_gpu_blob {
         s.inversions = s.cg_fail = s.nonfinite = s.timeout = s.abort = 0;
         s.steps_done = 0;
         CK(cudaMemcpyAsync(st, &s, sizeof(DevStatus), cudaMemcpyHostToDevice, stream));
+        const int cur0 = rng_cur;
         for (int i = 0; i < nsteps; ++i) {
             rc = launch_step_graph(0, i > 0);
-            if (rc) return rc;
-            // the non-finite flag is raised by euler_kernel after the positions moved; stop the step chain
+            if (rc) {
+                settle_rng(cur0);
+                return rc;
+            }
+            if (rng_bufs[1]) rng_cur ^= 1;
         }
         rc = read_status(s);
         if (rc) return rc;
+        settle_rng(cur0, s.steps_done);
         if (done) *done = s.steps_done;
         return status_code(s);
+    }
+
+    // after a call's steps: with two stream buffers the current one follows the completed steps (a step that did
+    // not complete wrote no next state); -1: read the count from the device
+    void settle_rng(int cur0, int steps_done = -1) {
+        if (!rng_bufs[1]) return;
+        if (steps_done < 0) {
+            DevStatus s{};
+            if (read_status(s)) {
+                rng_cur = cur0;
+                return;
+            }
+            steps_done = s.steps_done;
+        }
+        rng_cur = (cur0 + steps_done) & 1;
     }
 
     int step_timed(int nsteps, long long flush_bytes, int *done, double *step_ms, double *phase_ms) override {
@@ -787,6 +817,7 @@ struct BlobImpl final : ffea_gpu_blob {
         void *scratch = nullptr;
         if (flush_bytes > 0) CK(cudaMalloc(&scratch, (size_t)flush_bytes));
         double tot = 0.0, ph[FFEA_GPU_NUM_PHASES] = {0};
+        const int cur0 = rng_cur;
         for (int i = 0; i < nsteps && rc == FFEA_GPU_OK; ++i) {
             if (scratch) {
                 cudaError_t e = cudaMemsetAsync(scratch, i & 0xff, (size_t)flush_bytes, stream);
@@ -802,6 +833,7 @@ struct BlobImpl final : ffea_gpu_blob {
                     rc = cuda_fail(e, "cudaEventRecord");
             }
             if (rc) break;
+            if (rng_bufs[1]) rng_cur ^= 1;
             cudaError_t e = cudaEventSynchronize(ev[FFEA_GPU_NUM_PHASES]);
             if (e != cudaSuccess) { rc = cuda_fail(e, "cudaEventSynchronize"); break; }
             float ms = 0.f;
@@ -814,9 +846,13 @@ struct BlobImpl final : ffea_gpu_blob {
             tot += ms;
         }
         if (scratch) cudaFree(scratch);
-        if (rc) return rc;
+        if (rc) {
+            settle_rng(cur0);
+            return rc;
+        }
         rc = read_status(s);
         if (rc) return rc;
+        settle_rng(cur0, s.steps_done);
         if (done) *done = s.steps_done;
         if (step_ms) *step_ms = tot;
         if (phase_ms)
@@ -880,13 +916,13 @@ struct BlobImpl final : ffea_gpu_blob {
     }
 
     int set_rng(const uint32_t s[6]) override {
-        CK(cudaMemcpyAsync(rng_state, s, 6 * sizeof(uint32_t), cudaMemcpyHostToDevice, stream));
+        CK(cudaMemcpyAsync(rng_state(), s, 6 * sizeof(uint32_t), cudaMemcpyHostToDevice, stream));
         CK(cudaStreamSynchronize(stream));
         return FFEA_GPU_OK;
     }
 
     int get_rng(uint32_t s[6]) override {
-        CK(cudaMemcpyAsync(s, rng_state, 6 * sizeof(uint32_t), cudaMemcpyDeviceToHost, stream));
+        CK(cudaMemcpyAsync(s, rng_state(), 6 * sizeof(uint32_t), cudaMemcpyDeviceToHost, stream));
         CK(cudaStreamSynchronize(stream));
         return FFEA_GPU_OK;
     }
@@ -1192,7 +1228,7 @@ struct BlobImpl final : ffea_gpu_blob {
         CK(cudaMemcpyAsync(pos3, px, N * sizeof(double), cudaMemcpyDeviceToDevice, stream));
         CK(cudaMemcpyAsync(pos3 + N, py, N * sizeof(double), cudaMemcpyDeviceToDevice, stream));
         CK(cudaMemcpyAsync(pos3 + 2 * N, pz, N * sizeof(double), cudaMemcpyDeviceToDevice, stream));
-        if (rng) CK(cudaMemcpyAsync(rng, rng_state, 6 * sizeof(uint32_t), cudaMemcpyDeviceToDevice, stream));
+        if (rng) CK(cudaMemcpyAsync(rng, rng_state(), 6 * sizeof(uint32_t), cudaMemcpyDeviceToDevice, stream));
         if (det) CK(cudaMemcpyAsync(det, last_det, h.T * sizeof(double), cudaMemcpyDeviceToDevice, stream));
         return FFEA_GPU_OK;
     }
@@ -1202,7 +1238,7 @@ struct BlobImpl final : ffea_gpu_blob {
         CK(cudaMemcpyAsync(px, pos3, N * sizeof(double), cudaMemcpyDeviceToDevice, stream));
         CK(cudaMemcpyAsync(py, pos3 + N, N * sizeof(double), cudaMemcpyDeviceToDevice, stream));
         CK(cudaMemcpyAsync(pz, pos3 + 2 * N, N * sizeof(double), cudaMemcpyDeviceToDevice, stream));
-        if (rng) CK(cudaMemcpyAsync(rng_state, rng, 6 * sizeof(uint32_t), cudaMemcpyDeviceToDevice, stream));
+        if (rng) CK(cudaMemcpyAsync(rng_state(), rng, 6 * sizeof(uint32_t), cudaMemcpyDeviceToDevice, stream));
         if (det) CK(cudaMemcpyAsync(last_det, det, h.T * sizeof(double), cudaMemcpyDeviceToDevice, stream));
         return FFEA_GPU_OK;
     }
@@ -1298,7 +1334,7 @@ struct BlobImpl final : ffea_gpu_blob {
         ae.tet = tet;
         ae.px = px; ae.py = py; ae.pz = pz;
         ae.jinv = jinv; ae.G = G; ae.E = E; ae.A = A; ae.B = B; ae.vol0 = vol0;
-        ae.rng_state = rng_state; ae.chunk_jump = chunk_jump; ae.lane_jump = lane_jump;
+        ae.rng_state = rng_state(); ae.chunk_jump = chunk_jump; ae.lane_jump = lane_jump;
         ae.mu = x;
         ae.v = v_step;
         ae.nmodes = nmodes;

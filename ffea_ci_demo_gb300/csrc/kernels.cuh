@@ -641,6 +641,11 @@ struct GatherArgs {
     const uint32_t *nrng;
     uint32_t *nchunk_state;
     int nnchunks;
+    // with fuse_euler: the step closed here (finish_step_kernel's work) unless aborted: fin_jump applied to the step's
+    // stream state nrng into fin_next (the other of two buffers, so no thread reads what is written) and the step
+    // counted; or null
+    const MrgJump *fin_jump;
+    uint32_t *fin_next;
 };
 
 template <class R>

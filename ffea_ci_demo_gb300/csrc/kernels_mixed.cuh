@@ -59,6 +59,15 @@ __global__ void __launch_bounds__(256, (MODE == 1 && !NF) ? 8 : 1) gather_mixed_
     const int a = blockIdx.x * blockDim.x + threadIdx.x;
     if (a == 0 && g.gb) g.gb->count = 0u;
     if constexpr (MODE == 1) {
+        if (g.fin_next && a == 0 && !g.st->abort) {
+            uint32_t s6[6], o6[6];
+#pragma unroll
+            for (int k = 0; k < 6; ++k) s6[k] = g.nrng[k];
+            mrg_apply(*g.fin_jump, s6, o6);
+#pragma unroll
+            for (int k = 0; k < 6; ++k) g.fin_next[k] = o6[k];
+            g.st->steps_done += 1;
+        }
         if (g.nchunk_state && a < g.nnchunks) {
             uint32_t s6[6], o6[6];
 #pragma unroll
