@@ -710,7 +710,7 @@ def run_scale(args) -> dict:
             if solver == "masslumped":
                 # the value without the phase events (each costs a few microseconds inside a step of about a
                 # tenth of a millisecond): the steps as update() runs them, timed around each graph launch
-                kp = max(k, 20)
+                kp = max(k, 50)
                 tp = b.update_timed(kp, FLUSH_BYTES, phases=False)
                 t = {"ms": tp["ms"] * k / kp, "phase_ms": t["phase_ms"]}
                 r.update({"value": N * kp / (tp["ms"] / 1e3), "ms_per_step": tp["ms"] / kp,

@@ -285,7 +285,7 @@ struct BlobImpl final : ffea_gpu_blob {
         const int gi = timed + ((cont && fused_prep()) ? 2 : 0) + 4 * rng_cur;
         if (!gexec[gi]) {
             record_phases = timed != 0;
-            prep_cont = gi >= 2;
+            prep_cont = (gi & 2) != 0;
             const long long l0 = launch_count();
             CK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
             const int rc = launch_step();
