@@ -302,7 +302,9 @@ void ffea_gpu_adjoint_destroy(ffea_gpu_adjoint *adj);
 typedef struct ffea_gpu_batch ffea_gpu_batch;
 #define FFEA_GPU_BATCH_MAX_BLOBS 2048
 
-/* meshes[b] as for ffea_gpu_blob_create; params shared by every blob. */
+/* meshes[b] as for ffea_gpu_blob_create; params shared by every blob. Every blob needs a CTA of the CG launch
+ * resident at once, so num_blobs is also bounded by the GPU's resident CTAs of 128 threads (1,216 on a GB300);
+ * above either bound FFEA_GPU_EINPUT. */
 int ffea_gpu_batch_create(const ffea_gpu_mesh *meshes, int num_blobs, const ffea_gpu_params *params,
                           ffea_gpu_batch **out);
 void ffea_gpu_batch_destroy(ffea_gpu_batch *batch);

@@ -304,3 +304,63 @@ def test_batch_strain_energies_match_single_blobs():
         s.set_state(pos=x0[b])
         want = s.measurements()["strain_energy"]
         assert want > 0 and abs(se[b] - want) <= 1e-12 * want, b
+
+
+@pytest.mark.gpu
+def test_batch_ragged_edge_cases(gpu, oracle_built):
+    """Ragged batches: a batch of one blob, and a batch mixing a one-element blob, a blob with pinned nodes and an
+    ordinary one, Stokes drag and noise on; each blob follows the single mixed blob from the same stream state."""
+    from test_mixed_elements import one_tet
+
+    kw = dict(dt=1e-12, kT=4.11e-21, calc_noise=1, calc_stokes=1)
+    for meshes in ([case_mesh(4, 7)], [one_tet(), case_mesh(3, 4, [0, 1, 5]), case_mesh(5, 2)]):
+        bt = lib.Batch(meshes, **kw)
+        x0 = [sheared(m, 0.02, seed=21 + b) for b, m in enumerate(meshes)]
+        want = substream_states(len(meshes))
+        for b in range(len(meshes)):
+            bt.set_state(b, pos=x0[b])
+        bt.update(6)
+        for b, m in enumerate(meshes):
+            s = lib.Blob(m, solver="CG_nomass", precision="mixed", cg_poly=-1, rng_state=want[b], **kw)
+            s.set_state(pos=x0[b])
+            s.update(6)
+            scale = np.abs(s.pos() - x0[b]).max()
+            assert scale > 0, b
+            assert np.abs(bt.pos(b) - s.pos()).max() <= 1e-5 * scale, (len(meshes), b)
+            assert np.array_equal(bt.rng_state(b), s.rng_state()), (len(meshes), b)
+        if len(meshes) > 1:
+            p = bt.pos(1)
+            assert np.array_equal(p[[0, 1, 5]], x0[1][[0, 1, 5]])
+
+
+@pytest.mark.gpu
+def test_batch_largest_and_refused_counts(gpu):
+    """The most blobs a batch takes: one CG CTA per blob resident at once (the grid of 128-thread CTAs). That many
+    small blobs step together, each as its single blob does; one more, and more than FFEA_GPU_BATCH_MAX_BLOBS, are
+    refused with EINPUT."""
+    import ctypes as C
+
+    probe = lib.Batch([case_mesh(2, 1)], kT=0.0, calc_noise=0)
+    probe.set_config(128, 1)
+    cap = probe.config()["ctas"]
+    probe.close()
+    meshes = [case_mesh(2, 1000 + b) for b in range(cap)]
+    bt = lib.Batch(meshes, kT=0.0, calc_noise=0)
+    assert bt.config()["ctas"] >= cap
+    x0 = [sheared(m, 0.02, seed=b) for b, m in enumerate(meshes)]
+    bt.set_positions(np.concatenate(x0))
+    bt.update(3)
+    for b in (0, cap // 2, cap - 1):
+        s = lib.Blob(meshes[b], solver="CG_nomass", precision="fp64", kT=0.0, calc_noise=0)
+        s.set_state(pos=x0[b])
+        s.update(3)
+        assert np.abs(bt.pos(b) - s.pos()).max() <= 1e-5 * np.abs(s.pos() - x0[b]).max(), b
+    bt.close()
+    L = lib.load()
+    for n in (cap + 1, 2049):
+        many = [case_mesh(2, 7)] * n
+        keep: list = []
+        arr = (lib.MeshStruct * n)(*[lib._mesh_struct(m, keep) for m in many])
+        p = lib.make_params(solver="CG_nomass", precision="mixed")
+        h = C.c_void_p()
+        assert L.ffea_gpu_batch_create(C.cast(arr, C.c_void_p), n, C.byref(p), C.byref(h)) == lib.EINPUT, n
