@@ -145,7 +145,7 @@ __global__ void __launch_bounds__(BATCH_MAX_THREADS) cg_batch_kernel(const __gri
         {
             BATCH_ROW_LOOP(g.tpn, row0, nrows, rank, gsz, a, sub, valid) {
                 float q0, q1, q2;
-                spmv_row_zu<2>(g, g.z, pold, beta, first, a, sub, valid, q0, q1, q2);
+                spmv_row_zu<3>(g, g.z, pold, beta, first, a, sub, valid, q0, q1, q2);
                 if (!valid || sub != 0) continue;
                 const float4 z = g.z[a];
                 float p0 = z.x, p1 = z.y, p2 = z.z;
