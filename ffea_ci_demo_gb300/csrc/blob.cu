@@ -1487,7 +1487,7 @@ int check_params(const ffea_gpu_params *p) {
     if (!p) return FFEA_GPU_EINPUT;
     if (p->solver < 0 || p->solver > 2 || (p->precision != FFEA_GPU_FP64 && p->precision != FFEA_GPU_MIXED) ||
         p->max_iterations_cg < 0 || !(p->dt > 0) ||
-        (p->cg_poly != -1 && p->cg_poly != 0 && p->cg_poly != 2 && p->cg_poly != 4) || p->cg_smem_blocks < -1) {
+        (p->cg_poly < -1 || p->cg_poly > CHEB_MAX || (p->cg_poly > 0 && p->cg_poly % 2 != 0)) || p->cg_smem_blocks < -1) {
         g_last_error = "invalid parameters";
         return FFEA_GPU_EINPUT;
     }

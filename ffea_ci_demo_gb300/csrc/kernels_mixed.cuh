@@ -930,16 +930,16 @@ __host__ __device__ constexpr size_t sr_cache_bytes(int kc, int S) {
     return (size_t)SR_CACHE_BYTES_PER_BLOCK * kc * S;
 }
 
-// The Chebyshev preconditioner: degrees 2 and 4 (even degrees keep it positive definite whatever the estimate of
-// lambda_max); the interval is [lambda_max / cheb_ratio(d), lambda_max]; the estimate comes from the Lanczos
-// matrix of the first CHEB_REC iterations of a Jacobi-preconditioned solve. State (CHEB_STATE doubles):
+// The Chebyshev preconditioner: degrees 2, 4, 6 and 8 (even degrees keep it positive definite whatever the
+// estimate of lambda_max); the interval is [lambda_max / cheb_ratio(d), lambda_max]; the estimate comes from the
+// Lanczos matrix of the first CHEB_REC iterations of a Jacobi-preconditioned solve. State (CHEB_STATE doubles):
 // [0] the estimate (0: not yet known, -1: Jacobi kept), [1, 1 + CHEB_REC) step lengths, then as many direction
 // coefficients, then [CHEB_KJ] the iterations of the Jacobi solve while the first polynomial solve (the trial)
 // is pending.
-constexpr int CHEB_MAX = 4;
+constexpr int CHEB_MAX = 8;
 constexpr int CHEB_REC = 64;
-// the interval's width: the degree-4 polynomial gains from a wider one (40^3 Kuhn cube, CG per step: ratio 30
-// 4.24 ms, 60 4.10, 120 4.04, 250 4.06), the degree-2 one hardly (30 4.17, 60 4.14, 120 4.17 ms)
+// the interval's width: degrees 4 and up gain from a wider one (40^3 Kuhn cube, degree 4, CG per step: ratio 30
+// 4.24 ms, 60 4.10, 120 4.04, 250 4.06), degree 2 hardly (30 4.17, 60 4.14, 120 4.17 ms)
 __host__ __device__ constexpr double cheb_ratio(int degree) { return degree > 2 ? 120.0 : 30.0; }
 constexpr double CHEB_MARGIN = 1.05;
 constexpr int CHEB_KJ = 1 + 2 * CHEB_REC;
@@ -983,11 +983,16 @@ static __device__ __noinline__ double lanczos_lambda_max(const double *al, const
 // those of the other mixed CG kernels; in FP32 they agree to rounding and converge in the same number of
 // iterations.
 // Polynomial preconditioning (g.poly = d > 0, once lambda_max of D^{-1} V is known): M^{-1} = P_d(D^{-1} V) D^{-1},
-// with 1 - lambda P_d(lambda) the Chebyshev polynomial of degree d + 1 on [lambda_max / 30, lambda_max], scaled
-// to 1 at 0. z is built by d steps of the Chebyshev iteration for V z = r from z = 0 (d SpMVs, each exchanging
-// its input vector with the neighbour blocks only), which cut the number of iterations, and with it the number
-// of grid-wide reductions, by 2.4x (d = 2) to 3.6x (d = 4) on Kuhn cubes. The preconditioner is built from V
-// without the rigid-mode shift: it is positive definite on the whole spectrum for even d.
+// with 1 - lambda P_d(lambda) the Chebyshev polynomial of degree d + 1 on [lambda_max / cheb_ratio(d),
+// lambda_max], scaled to 1 at 0. z is built by d steps of the Chebyshev iteration for V z = r from z = 0 (d SpMVs,
+// each exchanging its input vector with the neighbour blocks only), which cut the number of iterations, and with
+// it the number of grid-wide reductions, by 2.8x (d = 2) to 7.7x (d = 8) on the 40^3 Kuhn cube. The
+// preconditioner is built from V without the rigid-mode shift: it is positive definite on the whole spectrum for
+// even d, and maps a D-weighted rigid mode D Z c to P_d(0) Z c. The shift D Z A6 Z^T D is therefore scaled by
+// 1 / P_d(0) while the polynomial applies, which puts the rigid modes' eigenvalue of M^{-1} V~ at 1, inside the
+// cluster of the others (unscaled they sit at P_d(0), 15.7 for d = 4 on the 40^3 cube, which then needed 132
+// iterations a step instead of 110). The scale changes the shifted operator only on the rigid modes, where the
+// projected right-hand side has no component, so the solution is the same: the one with Z^T D x = 0.
 template <class R>
 __global__ void __launch_bounds__(1024, 1) cg_mixed_sr_kernel(const __grid_constant__ CgArgs<R> g) {
     static_assert(sizeof(R) == sizeof(float), "the single-reduction CG is the mixed path's");
@@ -999,6 +1004,7 @@ __global__ void __launch_bounds__(1024, 1) cg_mixed_sr_kernel(const __grid_const
     __shared__ double s_g, s_pq;      // r.z and p.q~ of the previous iteration
     __shared__ float s_alpha, s_beta, s_tau[3], s_Om[3], s_dummy;
     __shared__ float s_c1[CHEB_MAX], s_c2[CHEB_MAX], s_ith;
+    __shared__ double s_shift;        // scale of the rigid-mode shift: 1 / P_d(0) with the polynomial, else 1
     __shared__ int s_conv, s_stop;
     DevStatus *st = g.st;
     if (st->abort) return;
@@ -1040,15 +1046,20 @@ __global__ void __launch_bounds__(1024, 1) cg_mixed_sr_kernel(const __grid_const
     if (cheb && threadIdx.x == 0) {
         const double b = lmax, a = lmax / cheb_ratio(poly), theta = 0.5 * (b + a), delta = 0.5 * (b - a);
         const double sigma = theta / delta;
-        double rho = 1.0 / sigma;
+        // the same recurrence at lambda = 0, where the residual stays D^{-1} r, gives P_d(0)
+        double rho = 1.0 / sigma, p0 = 1.0 / theta, d0 = p0;
         for (int j = 0; j < poly; ++j) {
             const double rn = 1.0 / (2.0 * sigma - rho);
             s_c1[j] = (float)(rn * rho);
             s_c2[j] = (float)(2.0 * rn / delta);
+            d0 = rn * rho * d0 + 2.0 * rn / delta;
+            p0 += d0;
             rho = rn;
         }
         s_ith = (float)(1.0 / theta);
+        s_shift = 1.0 / p0;
     }
+    if (!cheb && threadIdx.x == 0) s_shift = 1.0;
     grid_sum_df8<MIXED_GATHER_NP>(reinterpret_cast<const float2 *>(g.init_partials), g.init_stride, g.n_init, s_sc);
     const double f2 = s_sc[0];
     mixed_setup(g, s_sc, s_A6, s_tau, s_Om, &s_dummy, &s_conv);
@@ -1174,11 +1185,12 @@ __global__ void __launch_bounds__(1024, 1) cg_mixed_sr_kernel(const __grid_const
         grid_sum_df8<MIXED_SR_NP>(partials, g.stride, gridDim.x, s_sc);
         if (threadIdx.x < 32) {
             const int ln = threadIdx.x;
-            // c = A6 m(z): the rigid-mode coefficients of D Z A6 Z^T D z, over six lanes
+            // c = s A6 m(z): the rigid-mode coefficients of s D Z A6 Z^T D z, over six lanes
             double c = 0.0;
             if (defl && ln < 6) {
 #pragma unroll
                 for (int qq = 0; qq < 6; ++qq) c += s_A6[6 * ln + qq] * s_sc[5 + qq];
+                c *= s_shift;
             }
             double mzc = (ln < 6) ? s_sc[5 + ln] * c : 0.0;   // m(z).c
             double mpc = (ln < 6) ? s_mp[ln] * c : 0.0;       // m(p_old).c

@@ -28,7 +28,7 @@ OK, EINVERTED, ECGMAXIT, EINPUT, ENOMEM, ECUDA, ENAN, ETIMEOUT, EFILE = range(9)
 SOLVERS = {"CG_nomass": 0, "CG": 1, "masslumped": 2}
 PRECISIONS = {"fp64": 0, "mixed": 1}
 MESO_LENGTH = 1.7e-10
-CG_POLY_DEFAULT = 4  # FFEA_GPU_CG_POLY_DEFAULT: the mixed CG_nomass solve's default Chebyshev degree
+CG_POLY_DEFAULT = 6  # FFEA_GPU_CG_POLY_DEFAULT: the mixed CG_nomass solve's default Chebyshev degree
 
 
 class FFEAError(RuntimeError):
@@ -196,8 +196,8 @@ class Blob:
                  dt: float = 1e-12, kT: float = 4.11e-21, epsilon: float = 1e-10, max_iterations_cg: int = 10000,
                  calc_noise: int = 1, calc_stokes: int = 0, stokes_visc: float = 1e-3, cg_poly: int = 0,
                  cg_smem_blocks: int = 0, rng_state=(12345,) * 6, _handle=None, _n=None):
-        """cg_poly: preconditioner of the mixed-precision CG_nomass solve (0: default Chebyshev degree 4,
-        -1: Jacobi alone as the reference, 2 or 4: Chebyshev degree); the FP64 path always uses Jacobi.
+        """cg_poly: preconditioner of the mixed-precision CG_nomass solve (0: default Chebyshev degree 6,
+        -1: Jacobi alone as the reference, 2, 4, 6 or 8: Chebyshev degree); the FP64 path always uses Jacobi.
         cg_smem_blocks: 3x3 matrix blocks per row that the mixed single-reduction CG keeps in shared memory
         (0: as many as fit, n > 0: at most n, -1: none); results do not depend on it."""
         self._lib = load()

@@ -62,8 +62,8 @@ typedef struct ffea_gpu_params {
     int precision;    /* FFEA_GPU_FP64 / FFEA_GPU_MIXED */
     /* Preconditioner of the mixed-precision CG_nomass solve (not a reference parameter: the reference and the
      * FP64 path always precondition with the Jacobi diagonal). 0: the default (FFEA_GPU_CG_POLY_DEFAULT);
-     * -1: Jacobi alone; 2 or 4: a Chebyshev polynomial of that degree in D^-1 V times the Jacobi scaling, which
-     * needs fewer iterations and the same stopping test (|r|^2/|f|^2 < epsilon2). The polynomial applies when
+     * -1: Jacobi alone; 2, 4, 6 or 8: a Chebyshev polynomial of that degree in D^-1 V times the Jacobi scaling,
+     * which needs fewer iterations and the same stopping test (|r|^2/|f|^2 < epsilon2). The polynomial applies when
      * the single-reduction kernel runs (the blob's rows fit in the GPU's shared memory); the blob's first solve
      * uses Jacobi and estimates the largest eigenvalue of D^-1 V for the later ones. */
     int cg_poly;
@@ -73,7 +73,7 @@ typedef struct ffea_gpu_params {
      * (only where the matrix is read from), so it exists for measurements of the cache's effect. */
     int cg_smem_blocks;
 } ffea_gpu_params;
-#define FFEA_GPU_CG_POLY_DEFAULT 4
+#define FFEA_GPU_CG_POLY_DEFAULT 6
 
 /* SimulationParams::SimulationParams() defaults for the hot-path fields
  * (src/SimulationParams.cpp:26-60); solver CG_nomass, precision FP64. */

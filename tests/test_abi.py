@@ -34,10 +34,10 @@ def test_params_assign_matches_simulationparams(L, oracle_built):
     assert (p.max_iterations_cg, p.calc_noise, p.calc_stokes) == (77, 0, 1)
     assert L.ffea_gpu_params_assign(C.byref(p), b"calc_ssint", b"1") == lib.EINPUT
     assert L.ffea_gpu_params_assign(C.byref(p), b"solver", b"direct") == lib.EINPUT
-    # the mixed CG_nomass preconditioner (an engine key): -1 Jacobi, 0 default, 2 or 4 Chebyshev degree
-    for v in (-1, 0, 2, 4):
+    # the mixed CG_nomass preconditioner (an engine key): -1 Jacobi, 0 default, 2, 4, 6 or 8 Chebyshev degree
+    for v in (-1, 0, 2, 4, 6, 8):
         assert L.ffea_gpu_params_assign(C.byref(p), b"cg_poly", str(v).encode()) == lib.OK and p.cg_poly == v
-    for v in (1, 3, 6):
+    for v in (-2, 1, 3, 5, 10):
         assert L.ffea_gpu_params_assign(C.byref(p), b"cg_poly", str(v).encode()) == lib.EINPUT
 
 
