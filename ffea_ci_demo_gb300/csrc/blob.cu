@@ -220,6 +220,9 @@ struct BlobImpl final : ffea_gpu_blob {
     // step graphs: [timed + 2 cont], cont = a step that follows a fused mass-lumped step of the same call (its
     // FP32 node state was written by that step's gather)
     cudaGraphExec_t gexec[8] = {};
+    // graphs whose launches' by-value arguments changed (set_state's centroid and rigid modes) but not their
+    // launches: re-captured on next use and updated in place, which costs less than a new instantiation
+    bool refresh[8] = {};
     bool prep_cont = false;  // the step being captured is such a continuation
     // the mixed mass-lumped step with noise: the next step's chunk jumps A^(224 c + step draws), so that its gather
     // also forms the next step's chunk states and a continuation step launches no node_prep_kernel
@@ -274,6 +277,7 @@ struct BlobImpl final : ffea_gpu_blob {
                 cudaGraphExecDestroy(g);
                 g = nullptr;
             }
+        for (auto &r : refresh) r = false;
     }
 
     // the mixed mass-lumped step leaves the next step's FP32 node state behind (its gather updates the positions)
@@ -283,7 +287,7 @@ struct BlobImpl final : ffea_gpu_blob {
     // stream was a step of the same call, so a fused step need not form the FP32 node state again
     int launch_step_graph(int timed, bool cont = false) {
         const int gi = timed + ((cont && fused_prep()) ? 2 : 0) + 4 * rng_cur;
-        if (!gexec[gi]) {
+        if (!gexec[gi] || refresh[gi]) {
             record_phases = timed != 0;
             prep_cont = (gi & 2) != 0;
             const long long l0 = launch_count();
@@ -299,7 +303,19 @@ struct BlobImpl final : ffea_gpu_blob {
                 if (graph) cudaGraphDestroy(graph);
                 return rc ? rc : cuda_fail(e, "cudaStreamEndCapture");
             }
-            const cudaError_t ei = cudaGraphInstantiate(&gexec[gi], graph, 0);
+            refresh[gi] = false;
+            if (gexec[gi]) {
+                // the same launches with new arguments: update the instantiated graph; if the update is refused,
+                // instantiate anew (the refusal is not a sticky error, but it is cleared from the last-error slot)
+                cudaGraphExecUpdateResultInfo info{};
+                if (cudaGraphExecUpdate(gexec[gi], graph, &info) != cudaSuccess) {
+                    (void)cudaGetLastError();
+                    cudaGraphExecDestroy(gexec[gi]);
+                    gexec[gi] = nullptr;
+                }
+            }
+            cudaError_t ei = cudaSuccess;
+            if (!gexec[gi]) ei = cudaGraphInstantiate(&gexec[gi], graph, 0);
             cudaGraphDestroy(graph);
             if (ei != cudaSuccess) {
                 gexec[gi] = nullptr;
@@ -908,7 +924,8 @@ struct BlobImpl final : ffea_gpu_blob {
             }
             for (int c = 0; c < 3; ++c) xc[c] = s[c] / std::max(N, 1);
             nmodes = rigid_modes_about(h, p, xc, modes, 0, N);
-            invalidate_graphs();  // the gather and the CG take the centroid and the modes by value
+            // the gather and the CG take the centroid and the modes by value
+            for (auto &r : refresh) r = true;
         }
         // the caller may reuse its arrays on return
         CK(cudaStreamSynchronize(stream));
