@@ -1,10 +1,9 @@
 """The mixed path's Chebyshev polynomial preconditioner, restated in numpy on the oracle's viscosity matrix (CPU).
 
 cg_mixed_sr_kernel preconditions the CG_nomass solve with M^-1 = P_d(D^-1 V) D^-1, where 1 - lambda P_d(lambda)
-is the Chebyshev polynomial of degree d + 1 on [lambda_max / r_d, lambda_max] (r_2 = 30, r_4 = 120) scaled to 1 at
-0, applied as d steps
-of the Chebyshev iteration for V z = r from z = 0. lambda_max comes from the Lanczos matrix of a Jacobi-PCG solve
-(step lengths alpha_i, direction coefficients beta_i). These tests check the algorithm itself on a Kuhn cube's
+is the Chebyshev polynomial of degree d + 1 on [lambda_max / r_d, lambda_max] (r_2 = 30, r_d = 120 for d >= 4)
+scaled to 1 at 0, applied as d steps of the Chebyshev iteration for V z = r from z = 0. lambda_max comes from the
+Lanczos matrix of a Jacobi-PCG solve (step lengths alpha_i, direction coefficients beta_i). These tests check the algorithm itself on a Kuhn cube's
 matrix from the oracle (the reference's NoMass viscosity matrix, rigid modes shifted as the mixed path does):
 the Lanczos estimate, positive definiteness for even degrees whatever the estimate, the scale 1 / P_d(0) of the
 rigid-mode shift while the polynomial applies, and the iteration counts.
@@ -141,12 +140,12 @@ def test_lanczos_estimate_of_lambda_max(system):
 
 @pytest.mark.parametrize("scale", [0.5, 1.05, 3.0])
 def test_even_degrees_stay_positive_definite(system, scale):
-    """M^-1 is symmetric positive definite for degrees 2 and 4 even when lambda_max is under- or overestimated."""
+    """M^-1 is symmetric positive definite for even degrees even when lambda_max is under- or overestimated."""
     V, D, _, _, _ = system
     Ds = 1 / np.sqrt(D)
     lam = np.linalg.eigvalsh((sp.diags(Ds) @ V @ sp.diags(Ds)).toarray())
     lmax = float(lam.max()) * scale
-    for degree in (2, 4):
+    for degree in (2, 4, 6, 8):
         M = chebyshev(V, D, lmax, degree)
         Mi = np.column_stack([M(e) for e in np.eye(V.shape[0])[:, :60].T])[:60]
         assert np.allclose(Mi, Mi.T, rtol=1e-9, atol=1e-12 * np.abs(Mi).max())
@@ -192,10 +191,10 @@ def test_chebyshev_cuts_iterations(system):
     it_j, al, be = pcg(A(1.0), f, lambda r: r / D)
     lmax = 1.05 * lanczos_max(al, be)
     its, its_unscaled = {}, {}
-    for degree in (2, 4, 8):
+    for degree in (2, 4, 6, 8):
         M, p0 = chebyshev(V, D, lmax, degree), p_at_zero(lmax, degree)
         its[degree] = pcg(A(1.0 / p0), f, M)[0]
         its_unscaled[degree] = pcg(A(1.0), f, M)[0]
     print("Jacobi", it_j, "Chebyshev (shift scaled by 1/P(0))", its, "unscaled", its_unscaled)
-    assert its[2] <= 0.4 * it_j and its[4] <= 0.25 * it_j and its[8] <= 0.15 * it_j
+    assert its[2] <= 0.4 * it_j and its[4] <= 0.25 * it_j and its[6] <= 0.2 * it_j and its[8] <= 0.15 * it_j
     assert all(its[d] <= its_unscaled[d] for d in its)
