@@ -1500,11 +1500,15 @@ struct BlobImpl final : ffea_gpu_blob {
     }
 };
 
+static_assert(FFEA_GPU_CG_POLY_MAX == CHEB_MAX, "the CG kernel holds the coefficients of every accepted degree");
+static_assert(FFEA_GPU_CG_POLY_DEFAULT > 0 && FFEA_GPU_CG_POLY_DEFAULT <= CHEB_MAX && FFEA_GPU_CG_POLY_DEFAULT % 2 == 0,
+              "the default Chebyshev degree is an accepted one");
+
 int check_params(const ffea_gpu_params *p) {
     if (!p) return FFEA_GPU_EINPUT;
     if (p->solver < 0 || p->solver > 2 || (p->precision != FFEA_GPU_FP64 && p->precision != FFEA_GPU_MIXED) ||
         p->max_iterations_cg < 0 || !(p->dt > 0) ||
-        (p->cg_poly < -1 || p->cg_poly > CHEB_MAX || (p->cg_poly > 0 && p->cg_poly % 2 != 0)) || p->cg_smem_blocks < -1) {
+        (p->cg_poly < -1 || p->cg_poly > FFEA_GPU_CG_POLY_MAX || (p->cg_poly > 0 && p->cg_poly % 2 != 0)) || p->cg_smem_blocks < -1) {
         g_last_error = "invalid parameters";
         return FFEA_GPU_EINPUT;
     }

@@ -82,7 +82,7 @@ int ffea_gpu_params_assign(ffea_gpu_params *p, const char *key, const char *valu
         else return FFEA_GPU_EINPUT;
     } else if (k == "cg_poly") {
         const int v = atoi(value);
-        if (v < -1 || v > 8 || (v > 0 && v % 2 != 0)) return FFEA_GPU_EINPUT;
+        if (v < -1 || v > FFEA_GPU_CG_POLY_MAX || (v > 0 && v % 2 != 0)) return FFEA_GPU_EINPUT;
         p->cg_poly = v;
     } else if (k == "cg_smem_blocks") {
         const int v = atoi(value);

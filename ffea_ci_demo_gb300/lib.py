@@ -29,6 +29,7 @@ SOLVERS = {"CG_nomass": 0, "CG": 1, "masslumped": 2}
 PRECISIONS = {"fp64": 0, "mixed": 1}
 MESO_LENGTH = 1.7e-10
 CG_POLY_DEFAULT = 6  # FFEA_GPU_CG_POLY_DEFAULT: the mixed CG_nomass solve's default Chebyshev degree
+CG_POLY_MAX = 8  # FFEA_GPU_CG_POLY_MAX: the highest degree cg_poly accepts (even degrees only)
 
 
 class FFEAError(RuntimeError):

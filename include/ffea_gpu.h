@@ -74,6 +74,7 @@ typedef struct ffea_gpu_params {
     int cg_smem_blocks;
 } ffea_gpu_params;
 #define FFEA_GPU_CG_POLY_DEFAULT 6
+#define FFEA_GPU_CG_POLY_MAX 8  /* the highest Chebyshev degree cg_poly accepts (even degrees only) */
 
 /* SimulationParams::SimulationParams() defaults for the hot-path fields
  * (src/SimulationParams.cpp:26-60); solver CG_nomass, precision FP64. */

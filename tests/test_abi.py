@@ -69,3 +69,14 @@ def test_blob_create_rejects_bad_input_without_gpu_work(L):
     assert L.ffea_gpu_blob_step(None, 1, None) == lib.EINPUT
     p.cg_poly = 3  # odd degrees are refused: the preconditioner is positive definite for even ones only
     assert L.ffea_gpu_blob_create(C.byref(m), C.byref(p), C.byref(h)) == lib.EINPUT
+
+
+def test_binding_constants_match_the_header():
+    """The binding's status codes and preconditioner constants are the header's #defines."""
+    import re
+    src = open(lib.HEADER).read()
+    defs = {k: int(v) for k, v in re.findall(r"^#define\s+(FFEA_GPU_\w+)\s+(-?\d+)", src, re.M)}
+    assert defs["FFEA_GPU_CG_POLY_DEFAULT"] == lib.CG_POLY_DEFAULT
+    assert defs["FFEA_GPU_CG_POLY_MAX"] == lib.CG_POLY_MAX
+    for name in ("OK", "EINVERTED", "ECGMAXIT", "EINPUT", "ENOMEM", "ECUDA", "ENAN", "ETIMEOUT", "EFILE"):
+        assert defs["FFEA_GPU_" + name] == getattr(lib, name), name
